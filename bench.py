@@ -1,0 +1,380 @@
+"""Benchmark: force-layout point-iterations/s on one GB300.
+
+Workload (default): stochastic block model, 1,000,000 points in 200
+communities with Zipf(1.2) sizes, mean degree 10 (~5M links, 90% intra),
+positions uniform in [0, 8192)^2, spaceSize 8192, repulsion 0.1, gravity 0.25,
+friction 0.85, linkSpring 1.0, linkDistance 2.0, decay 5000 — synthetic,
+seeded.  One step = one simulation tick (Graph.step()) over the whole graph.
+
+  value  point-iterations/s = live points x ticks / device time, inputs
+         resident in HBM, CUDA events on the engine's stream, max over ranks.
+  e2e    the same metric through the C ABI with host buffers: each step is
+         cgl_step(1) (uploads the tick's alpha and seed, 8 bytes) followed by
+         cgl_get_point_positions into pinned host memory (8 bytes per point),
+         timed by the host clock (the reference's benchmark story flushes
+         steps with the same readback, repulsion-benchmark.ts:80-86).
+  --impl reference  times the oracle (the CPU restatement of the reference's
+         per-tick algorithm; the reference itself is TypeScript/WebGL and
+         cannot run here) on all host cores, same workload and metric.
+
+Multi-GPU (torchrun): replicas only — each rank lays out its own copy of the
+graph, no collective on the data path; value sums the ranks.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from graph_gb300 import _abi, generators  # noqa: E402
+
+METRIC = "point-iterations/s"
+UNIT = "point-iter/s"
+
+
+# ------------------------------------------------------------------ workload --
+def make_workload(name, seed=1):
+    if name == "sbm1m":
+        n = 1_000_000
+        links = generators.sbm_zipf(n, 200, 1.2, 10, 0.9, seed=seed)
+        pos = generators.uniform_positions(n, 0, 8192, seed)
+        fields = dict(space_size=8192, simulation_repulsion=0.1, simulation_gravity=0.25, simulation_friction=0.85,
+                      simulation_link_spring=1.0, simulation_link_distance=2.0, simulation_decay=5000,
+                      random_seed=seed)
+        desc = "SBM 1,000,000 points / 200 Zipf(1.2) communities / mean degree 10 / spaceSize 8192"
+    elif name == "ba10k":
+        n = 10_000
+        links = generators.barabasi_albert(n, 5, seed)
+        pos = generators.centred_square(n, 4096, seed)
+        fields = dict(space_size=4096, simulation_repulsion=0.1, simulation_gravity=0.25, simulation_friction=0.85,
+                      simulation_link_spring=1.0, simulation_link_distance=2.0, simulation_decay=5000,
+                      random_seed=seed)
+        desc = "Barabasi-Albert 10,000 points m=5 / spaceSize 4096"
+    else:
+        raise SystemExit("unknown workload %r" % name)
+    return pos, links, fields, desc
+
+
+# Algorithmic bytes per launch of each stage (bytes each stage must move at
+# minimum; HBM-resident arrays counted once per pass, L2-resident cell data
+# counted once per tick in `cells`).  n = live points, m = link entries per
+# direction, c = finest cells, cl = cells of all levels.
+def stage_bytes(stage, n, m, c, cl):
+    return {
+        "prepass": 29 * n,          # pos R 8 + flags 1 + pos W 8 + key W 4 + rank W 4 + histogram RMW 4
+        "center": 21 * n,
+        "scan": 16 * c,             # counts R twice, cell_start W, counts zeroed
+        "scatter": 32 * n,          # key 4 + rank 4 + pos 8 + cell_start 4 R; sorted idx 4 + pos 8 W
+        "cells": 12 * n + 16 * cl + 8 * c,
+        "manybody": 29 * n,         # sorted idx 4 + pos 8, jitter 8, flags 1 R; pos 8 W
+        "link_in": 21 * n + 24 * m,  # rowptr 4, own pos 8, flags 1 R, pos 8 W; entry 16 + neighbour pos 8
+        "link_out": 21 * n + 24 * m,
+        "collision_grid": 13 * n,
+        "collision_force": 21 * n,
+    }[stage]
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def load_traffic(stage):
+    """DRAM bytes per launch of `stage` from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "traffic_sbm1m.json")
+    try:
+        with open(path) as f:
+            t = json.load(f)
+        return t.get(stage)
+    except Exception:
+        return None
+
+
+# ------------------------------------------------------------------- clocks --
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits", "-lms", "100",
+                 "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+        time.sleep(0.3)
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU side --
+def time_oracle(pos, links, fields, budget_s, max_ticks, warmup=1):
+    """Oracle ticks on all host cores; returns (point-iter/s, ticks timed, seconds, cores)."""
+    from oracle import OracleEngine
+    o = OracleEngine(**fields)
+    o.set_point_positions(pos)
+    o.set_links(links)
+    o.render()
+    o.start(1.0)
+    for _ in range(warmup):
+        o.step(1)
+    t0 = time.perf_counter()
+    o.step(1)
+    t1 = time.perf_counter() - t0
+    ticks = 1
+    more = int(min(max_ticks - 1, max(0, budget_s / max(t1, 1e-6) - 1)))
+    t0 = time.perf_counter()
+    if more > 0:
+        o.step(more)
+    t = t1 + (time.perf_counter() - t0)
+    ticks += max(more, 0)
+    live = o.layout().live_points
+    o.close()
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return live * ticks / t, ticks, t, cores
+
+
+def cpu_model():
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                if ln.lower().startswith("model name"):
+                    return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.machine()
+
+
+# ------------------------------------------------------------------- main --
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="sbm1m", choices=["sbm1m", "ba10k"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of oracle ticks for cpu_baseline")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        run_reference(args)
+        return
+
+    import torch
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    pos, links, fields, desc = make_workload(args.workload, seed=1 + rank)
+    from graph_gb300.engine import Engine
+    eng = Engine(**dict(fields, device=local_rank))
+    eng.set_point_positions(pos)
+    eng.set_links(links)
+    eng.render()
+    eng.start(1.0)
+    lay = eng.layout()
+    live = lay.live_points
+    stream = torch.cuda.Stream()
+    eng.set_stream(stream.cuda_stream)
+
+    eng.step(args.warmup)
+    eng.synchronize()
+
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    eng.step(args.steps)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = live * args.steps * world / (ms / 1e3)
+
+    # per-stage device times (events between the tick's kernels, no graph)
+    stages = eng.profile_stages(20)
+    m = lay.link_entries_in
+    c = lay.finest_grid ** 2
+    cl = sum((4 << l) ** 2 for l in range(lay.levels))
+    dom = max(stages, key=lambda k: stages[k])
+    dom_ms = stages[dom]
+    alg = stage_bytes(dom, live, m, c, cl)
+    peak, peak_kind = load_peaks()
+    achieved = alg / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
+    per_stage = {k: round(v * 1e3, 2) for k, v in stages.items() if v > 0}
+    stage_gbs = {k: round(stage_bytes(k, live, m, c, cl) / (stages[k] / 1e3) / 1e9, 1)
+                 for k in stages if stages[k] > 0}
+
+    # end to end through the C ABI with host buffers
+    pinned = torch.empty(2 * lay.points_number, dtype=torch.float32, pin_memory=True)
+    host = pinned.numpy()
+    e2e_steps = max(10, min(args.steps, 200))
+    eng.step(1)
+    eng.get_point_positions_into(host)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        eng.step(1)
+        eng.get_point_positions_into(host)
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = live * e2e_steps * world / e2e_s
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, ticks, secs, cores = time_oracle(pos, links, fields, args.cpu_budget, 50)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": "%d ticks of the same %s workload on the oracle (C++ restatement, OpenMP, %s), %.1f s"
+                         % (ticks, args.workload, cpu_model(), secs)}
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": desc, "points": int(lay.points_number), "links": int(lay.links_number),
+                       "link_entries_per_direction": int(m), "finest_grid": int(lay.finest_grid),
+                       "levels": int(lay.levels), "step": "one simulation tick (Graph.step)",
+                       "l2": "inputs larger than L2 (per-tick working set ~%d MB > 129 MB)"
+                             % int((29 * live + 24 * 2 * m + 60 * live) / 1e6),
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": load_traffic(dom),
+                         "algorithmic_bytes": alg, "launch_ms": dom_ms, "peak_source": peak_kind},
+            "stage_us": per_stage,
+            "stage_alg_gbs": stage_gbs,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8,
+                    "d2h_bytes_per_step": 8 * int(lay.points_number), "steps": e2e_steps},
+            "gpu_launches": int(lay.kernels_per_tick) * args.steps,
+            "clocks": clk,
+        }
+        print(json.dumps(out))
+    eng.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    pos, links, fields, desc = make_workload(args.workload, seed=1)
+    budget = 150.0
+    from oracle import OracleEngine
+    o = OracleEngine(**fields)
+    o.set_point_positions(pos)
+    o.set_links(links)
+    o.render()
+    o.start(1.0)
+    live = o.layout().live_points
+    t0 = time.perf_counter()
+    warm = 0
+    while warm < args.warmup and (warm == 0 or time.perf_counter() - t0 < budget / 4):
+        o.step(1)
+        warm += 1
+    t_start = time.perf_counter()
+    ticks = 0
+    while ticks < args.steps:
+        o.step(1)
+        ticks += 1
+        if time.perf_counter() - t_start > budget / 2:
+            break
+    secs = time.perf_counter() - t_start
+    value = live * ticks / secs
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    sample = ("%d of %d requested ticks (after %d warm-up) of the %s workload on the oracle port "
+              "(C++ restatement of the reference's per-tick algorithm, OpenMP on %s); the reference itself "
+              "is TypeScript + WebGL2 and cannot execute on this machine" % (ticks, args.steps, warm, desc,
+                                                                           cpu_model()))
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": ticks, "warmup": warm, "ms_per_step": secs * 1e3 / ticks, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": desc, "step": "one simulation tick (Graph.step)"},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    o.close()
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,954 @@
+// engine.cu — host side of the GB300 force-layout engine: the C ABI of
+// include/cgl.h, data ingest (Graph.render), the simulation state machine
+// (Store, Graph.start/stop/pause/unpause/step) and tick scheduling on one CUDA
+// stream, one captured CUDA graph per tick topology.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "../../include/cgl.h"
+#include "kernels.cuh"
+
+using namespace cgl;
+
+namespace {
+
+constexpr double kAlphaMin = 0.001;   // ALPHA_MIN (Store/index.ts:8)
+constexpr uint32_t kParamChunk = 4096; // ticks per parameter upload
+
+// SplitMix64 draw k (0-based) of seed s; u = top 53 bits / 2^53.
+inline uint64_t splitmix_draw(uint64_t seed, uint64_t k) {
+  uint64_t z = seed + (k + 1) * 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace
+
+struct cgl_engine {
+  cgl_config cfg{};
+  bool destroyed = false;
+  std::string err;
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+
+  // staged input (copied at set_*, applied at render)
+  bool have_pos_input = false, have_link_input = false, have_strength = false, have_sizes = false;
+  std::vector<float> in_pos, in_links, in_strength, in_sizes;
+  bool pinned_set = false;
+  std::vector<double> pinned_input;
+  bool pos_dirty = false, links_dirty = false, sizes_dirty = false;
+
+  // applied data
+  uint64_t N = 0, E = 0;
+  uint32_t T = 0, W = 0;
+  bool has_strength = false;
+  std::vector<float> data_sizes;
+  bool has_data_sizes = false;
+  std::vector<uint8_t> absent, pinned;
+  uint64_t live = 0;
+  uint64_t entries = 0;
+  uint32_t max_deg_in = 0, max_deg_out = 0;
+  bool mb_ready = false;
+  int Gf = 0, L = 0, tile = 0;
+  int fixed_bits = 0;
+  FixedScale fx{};
+
+  // collision
+  bool collision_ready = false;
+  int cgrid = 0;
+  float ccell = 0.f;
+
+  // simulation state (Store)
+  double adjusted_space = 4096;
+  double alpha = 1.0;
+  double progress = 0.0;
+  bool running = false;
+  uint64_t rng_seed = 0, rng_ctr = 0;
+  uint64_t tick = 0;
+
+  // device state
+  size_t dev_bytes = 0;
+  DevBuf b_pos, b_pos_alt, b_flags, b_jitter, b_key, b_rank, b_sorted_idx, b_sorted_pos;
+  DevBuf b_counts, b_cell_start, b_block_sums, b_tickets, b_rec, b_acc, b_centroid;
+  DevBuf b_params, b_tick_ctr;
+  DevBuf b_rowptr_in, b_rowptr_out, b_ent_in, b_ent_out;
+  DevBuf b_size, b_cgrid_acc, b_cgrid;
+  DeviceView view{};
+  uint32_t level_off[10] = {};
+  uint32_t acc_off[10] = {};
+
+  TickParams* h_params = nullptr;          // pinned staging
+  cudaEvent_t params_copied = nullptr;
+  bool params_pending = false;
+
+  cudaGraphExec_t graph = nullptr;
+  bool graph_dirty = true;
+  bool use_graph = true;
+
+  double rnd(double mn, double mx) {
+    double u = (double)(splitmix_draw(rng_seed, rng_ctr++) >> 11) * 0x1.0p-53;
+    return mn + (mx - mn) * u;
+  }
+};
+
+namespace {
+
+cgl_status fail(cgl_engine* e, cgl_status st, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (e) e->err = buf;
+  return st;
+}
+
+#define CU(call)                                                                              \
+  do {                                                                                        \
+    cudaError_t _err = (call);                                                                \
+    if (_err != cudaSuccess)                                                                  \
+      return fail(e, _err == cudaErrorMemoryAllocation ? CGL_OOM : CGL_CUDA_ERROR, "%s: %s (%s:%d)", \
+                  #call, cudaGetErrorString(_err), __FILE__, __LINE__);                       \
+  } while (0)
+
+cgl_status dev_reserve(cgl_engine* e, DevBuf& b, size_t bytes, bool zero) {
+  if (bytes == 0) bytes = 16;
+  if (b.bytes >= bytes) {
+    if (zero) CU(cudaMemsetAsync(b.p, 0, bytes, e->stream));
+    return CGL_OK;
+  }
+  const double budget = e->cfg.hbm_budget_bytes;
+  if (budget > 0 && (double)(e->dev_bytes - b.bytes + bytes) > budget)
+    return fail(e, CGL_OOM, "device memory budget %.0f bytes exceeded (need %zu more)", budget, bytes - b.bytes);
+  if (b.p) {
+    CU(cudaStreamSynchronize(e->stream));
+    CU(cudaFree(b.p));
+    e->dev_bytes -= b.bytes;
+    b.p = nullptr;
+    b.bytes = 0;
+  }
+  CU(cudaMalloc(&b.p, bytes));
+  b.bytes = bytes;
+  e->dev_bytes += bytes;
+  if (zero) CU(cudaMemsetAsync(b.p, 0, bytes, e->stream));
+  return CGL_OK;
+}
+
+void dev_free_all(cgl_engine* e) {
+  DevBuf* all[] = {&e->b_pos, &e->b_pos_alt, &e->b_flags, &e->b_jitter, &e->b_key, &e->b_rank,
+                   &e->b_sorted_idx, &e->b_sorted_pos, &e->b_counts, &e->b_cell_start, &e->b_block_sums,
+                   &e->b_tickets, &e->b_rec, &e->b_acc, &e->b_centroid, &e->b_params, &e->b_tick_ctr,
+                   &e->b_rowptr_in, &e->b_rowptr_out, &e->b_ent_in, &e->b_ent_out, &e->b_size,
+                   &e->b_cgrid_acc, &e->b_cgrid};
+  for (DevBuf* b : all) {
+    if (b->p) cudaFree(b->p);
+    b->p = nullptr;
+    b->bytes = 0;
+  }
+  e->dev_bytes = 0;
+}
+
+void adjust_space_size(cgl_engine* e) {
+  // Store.adjustSpaceSize (Store/index.ts:209-233)
+  double s = e->cfg.space_size;
+  if (!(s > 0) || !std::isfinite(s)) s = 4096;
+  if (s < 2) s = 2;
+  const double m = e->cfg.max_texture_dimension;
+  if (m > 0 && std::isfinite(m) && m >= 2 && s >= m) s = std::max(m / 2, 2.0);
+  e->adjusted_space = s;
+}
+
+bool is_point_index(double v, uint64_t n) {
+  // GraphData.isPointIndex (GraphData/index.ts:286-289)
+  return std::isfinite(v) && v == std::floor(v) && v >= 0 && v < (double)n;
+}
+
+int ceil_log2_u64(uint64_t v) { int k = 0; while ((1ull << k) < v) ++k; return k; }
+
+void setup_fixed(cgl_engine* e) {
+  // Exact cell sums: coordinates saturate at B = smallest power of two >= 2*S,
+  // scaled by 2^F with F = 62 - ceil(log2 N) - log2 B (N * B * 2^F <= 2^62).
+  const float S = (float)e->adjusted_space;
+  int lb = 0;
+  while (std::ldexp(1.0, lb) < 2.0 * (double)S) ++lb;
+  const int ln = ceil_log2_u64(e->N < 1 ? 1 : e->N);
+  int F = 62 - ln - lb;
+  if (F > 60) F = 60;
+  e->fixed_bits = F;
+  e->fx.bound = (float)std::ldexp(1.0, lb);
+  e->fx.scale = std::ldexp(1.0f, F);
+  e->fx.inv = std::ldexp(1.0f, -F);
+}
+
+float resolved_size(const cgl_engine* e, uint64_t i) {
+  // GraphData.getResolvedPointSize (GraphData/index.ts:189-194); EXIT_DEFAULT_SIZE = 0
+  if (e->has_data_sizes && i < e->data_sizes.size()) {
+    const float r = e->data_sizes[i];
+    if (!std::isnan(r)) return r;
+  }
+  if (e->absent[i]) return 0.f;
+  return (float)e->cfg.point_default_size;
+}
+
+void refresh_view(cgl_engine* e) {
+  DeviceView& d = e->view;
+  d.n = (uint32_t)e->N;
+  d.pos = (float2*)e->b_pos.p;
+  d.pos_alt = (float2*)e->b_pos_alt.p;
+  d.flags = (const uint8_t*)e->b_flags.p;
+  d.jitter = (const float2*)e->b_jitter.p;
+  d.key = (uint32_t*)e->b_key.p;
+  d.rank = (uint32_t*)e->b_rank.p;
+  d.sorted_idx = (uint32_t*)e->b_sorted_idx.p;
+  d.sorted_pos = (float2*)e->b_sorted_pos.p;
+  d.counts = (uint32_t*)e->b_counts.p;
+  d.cell_start = (uint32_t*)e->b_cell_start.p;
+  d.block_sums = (uint32_t*)e->b_block_sums.p;
+  d.scan_ticket = (uint32_t*)e->b_tickets.p;
+  d.cells_ticket = d.scan_ticket ? d.scan_ticket + 1 : nullptr;
+  d.rec = (float4*)e->b_rec.p;
+  d.acc = (long long*)e->b_acc.p;
+  std::memcpy(d.level_off, e->level_off, sizeof(d.level_off));
+  std::memcpy(d.acc_off, e->acc_off, sizeof(d.acc_off));
+  d.centroid = (long long*)e->b_centroid.p;
+  d.tick_params = (const TickParams*)e->b_params.p;
+  d.tick_ctr = (uint32_t*)e->b_tick_ctr.p;
+  d.rowptr_in = (const uint32_t*)e->b_rowptr_in.p;
+  d.ent_in = (const uint4*)e->b_ent_in.p;
+  d.rowptr_out = (const uint32_t*)e->b_rowptr_out.p;
+  d.ent_out = (const uint4*)e->b_ent_out.p;
+  d.size = (const float*)e->b_size.p;
+  d.cgrid_acc = (long long*)e->b_cgrid_acc.p;
+  d.cgrid = (float4*)e->b_cgrid.p;
+}
+
+SimScalars make_scalars(const cgl_engine* e) {
+  SimScalars s{};
+  s.space = (float)e->adjusted_space;
+  s.friction = (float)e->cfg.simulation_friction;
+  s.gravity = (float)e->cfg.simulation_gravity;
+  s.center = (float)e->cfg.simulation_center;
+  s.repulsion = (float)e->cfg.simulation_repulsion;
+  s.link_spring = (float)e->cfg.simulation_link_spring;
+  s.link_distance = (float)e->cfg.simulation_link_distance;
+  s.link_r0 = (float)e->cfg.simulation_link_dist_random_variation_range[0];
+  s.link_r1 = (float)e->cfg.simulation_link_dist_random_variation_range[1];
+  s.coll_strength = (float)e->cfg.simulation_collision;
+  const double cr = e->cfg.simulation_collision_radius;
+  s.coll_radius = std::isnan(cr) ? 0.f : (float)cr;
+  s.coll_padding = (float)e->cfg.simulation_collision_padding;
+  s.coll_cell = e->ccell;
+  s.coll_grid = e->cgrid;
+  s.gf = e->Gf;
+  s.levels = e->L;
+  s.tile = e->tile;
+  s.csf = e->Gf ? (float)(e->adjusted_space / e->Gf) : 1.f;
+  s.fx = e->fx;
+  return s;
+}
+
+// ------------------------------------------------------------------ tick --
+struct TickPlan {
+  bool grav, cent, mb, link_in, link_out, coll;
+};
+
+TickPlan plan_tick(const cgl_engine* e) {
+  const uint32_t m = e->cfg.stage_mask;
+  TickPlan p{};
+  p.grav = e->cfg.simulation_gravity != 0 && (m & CGL_STAGE_GRAVITY) && e->N > 0;
+  p.cent = e->cfg.simulation_center != 0 && (m & CGL_STAGE_CENTER) && e->N > 0;
+  p.mb = (m & CGL_STAGE_MANYBODY) && e->mb_ready && e->N > 0;
+  const bool links = e->W > 0 && e->N > 0;
+  p.link_in = links && (m & CGL_STAGE_LINK_IN);
+  p.link_out = links && (m & CGL_STAGE_LINK_OUT);
+  p.coll = e->cfg.simulation_collision != 0 && (m & CGL_STAGE_COLLISION) && e->N > 0;
+  return p;
+}
+
+// Enqueue one tick.  ev (optional) = 2 events per stage for profiling.
+cgl_status enqueue_tick(cgl_engine* e, cudaStream_t st, cudaEvent_t* ev) {
+  const TickPlan p = plan_tick(e);
+  const SimScalars s = make_scalars(e);
+  const DeviceView& d = e->view;
+  auto mark = [&](int stage, int which) {
+    if (ev) cudaEventRecord(ev[2 * stage + which], st);
+  };
+  if (p.cent) CU(cudaMemsetAsync(d.centroid, 0, 3 * sizeof(long long), st));
+  uint32_t mode = 0;
+  if (p.grav) mode |= kPreGravity;
+  if (p.cent) mode |= kPreCentroid;
+  else if (p.mb) mode |= kPreBin;
+  mark(0, 0);
+  if (mode) launch_prepass(d, s, mode, st);
+  mark(0, 1);
+  mark(1, 0);
+  if (p.cent) launch_center(d, s, p.mb, st);
+  mark(1, 1);
+  if (p.mb) {
+    mark(2, 0); launch_scan(d, s, st); mark(2, 1);
+    mark(3, 0); launch_scatter(d, s, st); mark(3, 1);
+    mark(4, 0); launch_cells(d, s, st); mark(4, 1);
+    mark(5, 0); launch_manybody(d, s, st); mark(5, 1);
+  }
+  if (p.link_in || p.link_out) {
+    mark(6, 0);
+    if (p.link_in) launch_link(d, s, 0, false, st);
+    mark(6, 1);
+    mark(7, 0);
+    if (p.link_out) launch_link(d, s, 1, p.link_in, st);
+    mark(7, 1);
+    if (!(p.link_in && p.link_out))
+      CU(cudaMemcpyAsync(d.pos, d.pos_alt, e->N * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+  }
+  if (p.coll) {
+    mark(8, 0); launch_collision_grid(d, s, st); mark(8, 1);
+    mark(9, 0); launch_collision_force(d, s, st); mark(9, 1);
+  }
+  launch_tick_end(d, st);
+  CU(cudaGetLastError());
+  return CGL_OK;
+}
+
+cgl_status collision_create(cgl_engine* e) {
+  // ForceCollision.create (ForceCollision/index.ts:61-148)
+  double max_size = e->cfg.point_default_size;
+  std::vector<float> sizes(e->N);
+  for (uint64_t i = 0; i < e->N; ++i) {
+    sizes[i] = resolved_size(e, i);
+    if (e->has_data_sizes) max_size = std::max(max_size, (double)sizes[i]);
+  }
+  const double cr = std::isnan(e->cfg.simulation_collision_radius) ? 0 : e->cfg.simulation_collision_radius;
+  const double pad = e->cfg.simulation_collision_padding;
+  const double eff = (cr > 0 ? cr : max_size * 0.5) + pad;
+  const double cell = std::max(eff * 2, 8.0);
+  const int grid = (int)std::min(512.0, std::max(1.0, std::floor(e->adjusted_space / cell)));
+  e->cgrid = grid;
+  e->ccell = (float)(e->adjusted_space / grid);
+  const size_t cells = 4 * (size_t)grid * grid;
+  cgl_status st;
+  if ((st = dev_reserve(e, e->b_size, e->N * sizeof(float), false))) return st;
+  if ((st = dev_reserve(e, e->b_cgrid_acc, cells * 4 * sizeof(long long), true))) return st;
+  if ((st = dev_reserve(e, e->b_cgrid, cells * sizeof(float4), false))) return st;
+  if (e->N) CU(cudaMemcpyAsync(e->b_size.p, sizes.data(), e->N * sizeof(float), cudaMemcpyHostToDevice, e->stream));
+  CU(cudaStreamSynchronize(e->stream));
+  e->collision_ready = true;
+  refresh_view(e);
+  return CGL_OK;
+}
+
+cgl_status prepare_tick(cgl_engine* e) {
+  const TickPlan p = plan_tick(e);
+  if (p.coll && !e->collision_ready) {
+    cgl_status st = collision_create(e);
+    if (st) return st;
+    e->graph_dirty = true;
+  }
+  if (!e->use_graph) return CGL_OK;
+  if (!e->graph_dirty && e->graph) return CGL_OK;
+  if (e->graph) { cudaGraphExecDestroy(e->graph); e->graph = nullptr; }
+  cudaGraph_t g = nullptr;
+  CU(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+  cgl_status st = enqueue_tick(e, e->stream, nullptr);
+  cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+  if (st) { if (g) cudaGraphDestroy(g); return st; }
+  if (ce != cudaSuccess) return fail(e, CGL_CUDA_ERROR, "graph capture: %s", cudaGetErrorString(ce));
+  ce = cudaGraphInstantiate(&e->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (ce != cudaSuccess) { e->graph = nullptr; return fail(e, CGL_CUDA_ERROR, "graph instantiate: %s", cudaGetErrorString(ce)); }
+  e->graph_dirty = false;
+  return CGL_OK;
+}
+
+// Host side of one tick: the f32 alpha uniform and the peel seed draw
+// (ForceManyBody/index.ts:521), then Store.addAlpha (Store/index.ts:328-332).
+TickParams host_tick(cgl_engine* e, bool draws_seed) {
+  TickParams tp;
+  tp.alpha = (float)e->alpha;
+  tp.seed_bits = 0;
+  if (draws_seed) {
+    const float seed = (float)e->rnd(0, 1);
+    std::memcpy(&tp.seed_bits, &seed, 4);
+  }
+  e->alpha += (0 - e->alpha) * (1 - std::pow(kAlphaMin, 1 / e->cfg.simulation_decay));
+  e->progress = std::sqrt(std::min(1.0, kAlphaMin / e->alpha));
+  e->tick++;
+  return tp;
+}
+
+cgl_status run_ticks(cgl_engine* e, uint32_t ticks, cudaEvent_t* ev, double* stage_ms) {
+  if (ticks == 0) return CGL_OK;
+  cgl_status st = prepare_tick(e);
+  if (st) return st;
+  const bool seed = plan_tick(e).mb;
+  uint32_t done = 0;
+  while (done < ticks) {
+    const uint32_t n = std::min(kParamChunk, ticks - done);
+    if (e->params_pending) { CU(cudaEventSynchronize(e->params_copied)); e->params_pending = false; }
+    for (uint32_t t = 0; t < n; ++t) e->h_params[t] = host_tick(e, seed);
+    CU(cudaMemcpyAsync(e->b_params.p, e->h_params, n * sizeof(TickParams), cudaMemcpyHostToDevice, e->stream));
+    CU(cudaEventRecord(e->params_copied, e->stream));
+    e->params_pending = true;
+    CU(cudaMemsetAsync(e->b_tick_ctr.p, 0, sizeof(uint32_t), e->stream));
+    for (uint32_t t = 0; t < n; ++t) {
+      if (ev) {
+        st = enqueue_tick(e, e->stream, ev);
+        if (st) return st;
+        CU(cudaStreamSynchronize(e->stream));
+        for (int k = 0; k < CGL_NUM_STAGE_TIMES; ++k) {
+          float ms = 0.f;
+          if (cudaEventElapsedTime(&ms, ev[2 * k], ev[2 * k + 1]) == cudaSuccess) stage_ms[k] += ms;
+        }
+        cudaGetLastError();
+      } else if (e->use_graph) {
+        CU(cudaGraphLaunch(e->graph, e->stream));
+      } else {
+        st = enqueue_tick(e, e->stream, nullptr);
+        if (st) return st;
+      }
+    }
+    done += n;
+  }
+  return CGL_OK;
+}
+
+cgl_status apply_pinned(cgl_engine* e) {
+  // Points.updatePinnedStatus (Points/index.ts:1264-1277) -> device flags
+  e->pinned.assign(e->N, 0);
+  if (e->pinned_set)
+    for (double v : e->pinned_input)
+      if (v >= 0 && v < (double)e->N && v == std::floor(v)) e->pinned[(size_t)v] = 1;
+  if (!e->N) return CGL_OK;
+  std::vector<uint8_t> flags(e->N);
+  for (uint64_t i = 0; i < e->N; ++i) flags[i] = (e->pinned[i] ? kPinned : 0) | (e->absent[i] ? kAbsent : 0);
+  CU(cudaMemcpyAsync(e->b_flags.p, flags.data(), e->N, cudaMemcpyHostToDevice, e->stream));
+  CU(cudaStreamSynchronize(e->stream));
+  return CGL_OK;
+}
+
+// ForceLink.create for one direction (ForceLink/index.ts:40-83): CSR stable in
+// link-index order, bias / strength in FP64 rounded to f32, one random draw
+// per entry in CSR order.
+void build_csr(cgl_engine* e, const std::vector<float>& links, bool incoming, const std::vector<uint32_t>& deg,
+               std::vector<uint32_t>& rowptr, std::vector<uint4>& ent, uint32_t& max_deg) {
+  const uint64_t N = e->N, E = e->E;
+  rowptr.assign(N + 1, 0);
+  std::vector<uint8_t> valid(E, 0);
+  for (uint64_t i = 0; i < E; ++i) {
+    const double s = links[2 * i], t = links[2 * i + 1];
+    if (!is_point_index(s, N) || !is_point_index(t, N)) continue;
+    valid[i] = 1;
+    const uint32_t p = (uint32_t)(incoming ? s : t);
+    rowptr[p + 1]++;
+  }
+  max_deg = 0;
+  for (uint64_t p = 0; p < N; ++p) {
+    max_deg = std::max(max_deg, rowptr[p + 1]);
+    rowptr[p + 1] += rowptr[p];
+  }
+  const uint32_t M = rowptr[N];
+  ent.assign(M, make_uint4(0, 0, 0, 0));
+  std::vector<uint32_t> lidx(M);
+  std::vector<uint32_t> cur(rowptr.begin(), rowptr.end() - 1);
+  for (uint64_t i = 0; i < E; ++i) {
+    if (!valid[i]) continue;
+    const uint32_t s = (uint32_t)links[2 * i], t = (uint32_t)links[2 * i + 1];
+    const uint32_t p = incoming ? s : t, q = incoming ? t : s;
+    const uint32_t at = cur[p]++;
+    ent[at].x = q;
+    lidx[at] = (uint32_t)i;
+  }
+  for (uint64_t p = 0; p < N; ++p) {
+    for (uint32_t at = rowptr[p]; at < rowptr[p + 1]; ++at) {
+      const uint32_t q = ent[at].x;
+      const double degree = deg[q], connected = deg[p];
+      const double sum = degree + connected;
+      const double bias = sum != 0 ? degree / sum : 0.5;
+      const double mind = std::min(degree, connected);
+      double strength;
+      const double si = e->has_strength ? (double)e->in_strength[lidx[at]] : 0.0;
+      if (!e->has_strength || !std::isfinite(si) || si < 0) strength = 1.0 / std::max(mind, 1.0);
+      else strength = si;
+      strength = std::sqrt(strength);
+      const float fb = (float)bias, fs = (float)strength, fr = (float)e->rnd(0, 1);
+      std::memcpy(&ent[at].y, &fr, 4);
+      std::memcpy(&ent[at].z, &fb, 4);
+      std::memcpy(&ent[at].w, &fs, 4);
+      if (e->absent[q]) ent[at].x = kAbsentTarget;   // skipped at run time (force-spring.ts:71-74)
+    }
+  }
+}
+
+cgl_status do_render(cgl_engine* e, double alpha) {
+  // GraphData.update (GraphData/index.ts:443-462)
+  const uint64_t N = e->have_pos_input ? e->in_pos.size() / 2 : 0;
+  const uint64_t E = e->have_link_input ? e->in_links.size() / 2 : 0;
+  if (N == 0 && E == 0) return CGL_OK;   // empty render (src/index.ts:941-955)
+  if (N > (1ull << 24)) return fail(e, CGL_INVALID_ARG, "%llu points: point indices must stay exact in f32 (max 2^24)", (unsigned long long)N);
+  if (E > 0xFFFFFFF0ull) return fail(e, CGL_INVALID_ARG, "too many links");
+  const bool pos_changed = e->pos_dirty;
+  const bool links_changed = e->links_dirty || pos_changed;
+  cgl_status st;
+  if (pos_changed) e->N = N;
+  e->E = E;
+  e->has_strength = e->have_strength && e->in_strength.size() == E;
+  e->has_data_sizes = e->have_sizes;
+  e->data_sizes = e->in_sizes;
+  // Graph.update (src/index.ts:1987-1994)
+  e->T = (uint32_t)std::ceil(std::sqrt((double)e->N));
+  e->W = (uint32_t)std::ceil(std::sqrt((double)e->E * 2));
+  const size_t n = e->N;
+  if (pos_changed) {
+    e->graph_dirty = true;
+    // Points.updatePositions (Points/index.ts:390-592)
+    std::vector<float> pos(2 * n);
+    e->absent.assign(n, 0);
+    e->live = 0;
+    for (size_t i = 0; i < n; ++i) {
+      const float x = e->in_pos[2 * i], y = e->in_pos[2 * i + 1];
+      const bool ab = std::isnan(x) || std::isnan(y);
+      e->absent[i] = ab;
+      e->live += !ab;
+      pos[2 * i] = ab ? NAN : x;
+      pos[2 * i + 1] = ab ? NAN : y;
+    }
+    if ((st = dev_reserve(e, e->b_pos, n * sizeof(float2), false))) return st;
+    if ((st = dev_reserve(e, e->b_pos_alt, n * sizeof(float2), false))) return st;
+    if ((st = dev_reserve(e, e->b_flags, n, false))) return st;
+    if ((st = dev_reserve(e, e->b_jitter, n * sizeof(float2), false))) return st;
+    if ((st = dev_reserve(e, e->b_key, n * sizeof(uint32_t), false))) return st;
+    if ((st = dev_reserve(e, e->b_rank, n * sizeof(uint32_t), false))) return st;
+    if ((st = dev_reserve(e, e->b_sorted_idx, n * sizeof(uint32_t), false))) return st;
+    if ((st = dev_reserve(e, e->b_sorted_pos, n * sizeof(float2), false))) return st;
+    if (n) CU(cudaMemcpyAsync(e->b_pos.p, pos.data(), n * sizeof(float2), cudaMemcpyHostToDevice, e->stream));
+    CU(cudaStreamSynchronize(e->stream));
+    refresh_view(e);
+    if ((st = apply_pinned(e))) return st;
+    setup_fixed(e);
+    // ForceManyBody.create (ForceManyBody/index.ts:124-185): pyramid sizes and
+    // the jitter texture (2 draws per texel of pointsTextureSize^2, :133-138)
+    e->mb_ready = false;
+    if (e->T) {
+      const double target = 2 * std::sqrt((double)e->N);
+      const double g = std::min((double)kMaxGrid, std::max(8.0, std::pow(2.0, std::ceil(std::log2(target)))));
+      e->Gf = (int)g;
+      e->L = (int)std::log2(g) - 1;
+      e->tile = std::min(16, e->Gf);
+      uint32_t off = 0;
+      for (int l = 0; l < e->L; ++l) { e->level_off[l] = off; off += (uint32_t)((4 << l) * (4 << l)); }
+      uint32_t aoff = 0;
+      for (int l = 0; l < e->L; ++l) { e->acc_off[l] = aoff; aoff += (uint32_t)((4 << l) * (4 << l)); }
+      const uint32_t cells = (uint32_t)(e->Gf * e->Gf);
+      if ((st = dev_reserve(e, e->b_counts, cells * sizeof(uint32_t), true))) return st;
+      if ((st = dev_reserve(e, e->b_cell_start, (cells + 1) * sizeof(uint32_t), false))) return st;
+      if ((st = dev_reserve(e, e->b_block_sums, (scan_blocks(cells) + 1) * sizeof(uint32_t), false))) return st;
+      if ((st = dev_reserve(e, e->b_tickets, 4 * sizeof(uint32_t), true))) return st;
+      if ((st = dev_reserve(e, e->b_rec, off * sizeof(float4), true))) return st;
+      if ((st = dev_reserve(e, e->b_acc, 3 * (size_t)aoff * sizeof(long long), true))) return st;
+      if ((st = dev_reserve(e, e->b_centroid, 3 * sizeof(long long), true))) return st;
+      std::vector<float2> jit(n);
+      const uint64_t texels = (uint64_t)e->T * e->T;
+      for (uint64_t t = 0; t < texels; ++t) {
+        const float jx = (float)(e->rnd(-1, 1) * 0.00001);
+        const float jy = (float)(e->rnd(-1, 1) * 0.00001);
+        if (t < n) jit[t] = make_float2(jx, jy);
+      }
+      if (n) CU(cudaMemcpyAsync(e->b_jitter.p, jit.data(), n * sizeof(float2), cudaMemcpyHostToDevice, e->stream));
+      CU(cudaStreamSynchronize(e->stream));
+      e->mb_ready = true;
+    }
+    e->collision_ready = false;
+  }
+  if (e->sizes_dirty) e->collision_ready = false;
+  if (links_changed) {
+    e->graph_dirty = true;
+    // ForceLink.create(INCOMING) then (OUTGOING) (src/index.ts:1663-1666)
+    std::vector<uint32_t> rp_in, rp_out;
+    std::vector<uint4> en_in, en_out;
+    e->max_deg_in = e->max_deg_out = 0;
+    if (e->T && e->W) {
+      std::vector<uint32_t> deg(n, 0);
+      for (uint64_t i = 0; i < E; ++i) {
+        const double s = e->in_links[2 * i], t = e->in_links[2 * i + 1];
+        if (is_point_index(s, n) && is_point_index(t, n)) { deg[(size_t)s]++; deg[(size_t)t]++; }
+      }
+      build_csr(e, e->in_links, true, deg, rp_in, en_in, e->max_deg_in);
+      build_csr(e, e->in_links, false, deg, rp_out, en_out, e->max_deg_out);
+    } else {
+      rp_in.assign(n + 1, 0);
+      rp_out.assign(n + 1, 0);
+    }
+    e->entries = en_in.size();
+    if ((st = dev_reserve(e, e->b_rowptr_in, (n + 1) * sizeof(uint32_t), false))) return st;
+    if ((st = dev_reserve(e, e->b_rowptr_out, (n + 1) * sizeof(uint32_t), false))) return st;
+    if ((st = dev_reserve(e, e->b_ent_in, en_in.size() * sizeof(uint4), false))) return st;
+    if ((st = dev_reserve(e, e->b_ent_out, en_out.size() * sizeof(uint4), false))) return st;
+    CU(cudaMemcpyAsync(e->b_rowptr_in.p, rp_in.data(), (n + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, e->stream));
+    CU(cudaMemcpyAsync(e->b_rowptr_out.p, rp_out.data(), (n + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, e->stream));
+    if (!en_in.empty())
+      CU(cudaMemcpyAsync(e->b_ent_in.p, en_in.data(), en_in.size() * sizeof(uint4), cudaMemcpyHostToDevice, e->stream));
+    if (!en_out.empty())
+      CU(cudaMemcpyAsync(e->b_ent_out.p, en_out.data(), en_out.size() * sizeof(uint4), cudaMemcpyHostToDevice, e->stream));
+    CU(cudaStreamSynchronize(e->stream));
+  }
+  refresh_view(e);
+  e->pos_dirty = e->links_dirty = e->sizes_dirty = false;
+  if (!std::isnan(alpha)) e->alpha = alpha;
+  return CGL_OK;
+}
+
+}  // namespace
+
+// ================================================================ C ABI ====
+extern "C" {
+
+void cgl_config_defaults(cgl_config* c) {
+  // src/variables.ts:10,15,19,69-82,147-148
+  std::memset(c, 0, sizeof(*c));
+  c->space_size = 4096;
+  c->simulation_decay = 5000;
+  c->simulation_gravity = 0.25;
+  c->simulation_center = 0;
+  c->simulation_repulsion = 1.0;
+  c->simulation_repulsion_theta = 1.15;
+  c->simulation_link_spring = 1;
+  c->simulation_link_distance = 10;
+  c->simulation_link_dist_random_variation_range[0] = 1;
+  c->simulation_link_dist_random_variation_range[1] = 1.2;
+  c->simulation_friction = 0.85;
+  c->simulation_collision = 0;
+  c->simulation_collision_radius = NAN;
+  c->simulation_collision_padding = 0;
+  c->point_default_size = 4;
+  c->enable_simulation = 1;
+  c->has_random_seed = 0;
+  c->random_seed = 0;
+  c->max_texture_dimension = 0;
+  c->stage_mask = CGL_STAGE_ALL;
+  c->device = 0;
+  c->hbm_budget_bytes = 0;
+}
+
+cgl_status cgl_create(const cgl_config* cfg, cgl_engine** out) {
+  if (!cfg || !out) return CGL_INVALID_ARG;
+  *out = nullptr;
+  cgl_engine* e = new cgl_engine();
+  e->cfg = *cfg;
+  e->device = cfg->device;
+  if (cfg->has_random_seed) e->rng_seed = cfg->random_seed;
+  else { std::random_device rd; e->rng_seed = ((uint64_t)rd() << 32) ^ rd(); }
+  adjust_space_size(e);
+  const char* g = getenv("CGL_NO_GRAPH");
+  e->use_graph = !(g && g[0] == '1');
+  cudaError_t ce = cudaSetDevice(e->device);
+  if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking);
+  if (ce == cudaSuccess) ce = cudaMallocHost((void**)&e->h_params, kParamChunk * sizeof(TickParams));
+  if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->params_copied, cudaEventDisableTiming);
+  if (ce != cudaSuccess) {
+    cudaGetLastError();
+    static thread_local std::string create_err;
+    create_err = cudaGetErrorString(ce);
+    if (e->own_stream) cudaStreamDestroy(e->own_stream);
+    if (e->h_params) cudaFreeHost(e->h_params);
+    delete e;
+    return ce == cudaErrorMemoryAllocation ? CGL_OOM : CGL_CUDA_ERROR;
+  }
+  e->stream = e->own_stream;
+  cgl_status st;
+  if ((st = dev_reserve(e, e->b_params, kParamChunk * sizeof(TickParams), true)) ||
+      (st = dev_reserve(e, e->b_tick_ctr, sizeof(uint32_t), true))) {
+    cgl_destroy(e);
+    return st;
+  }
+  refresh_view(e);
+  *out = e;
+  return CGL_OK;
+}
+
+cgl_status cgl_destroy(cgl_engine* e) {
+  if (!e) return CGL_INVALID_ARG;
+  cudaSetDevice(e->device);
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  if (e->graph) cudaGraphExecDestroy(e->graph);
+  dev_free_all(e);
+  if (e->params_copied) cudaEventDestroy(e->params_copied);
+  if (e->h_params) cudaFreeHost(e->h_params);
+  if (e->own_stream) cudaStreamDestroy(e->own_stream);
+  delete e;
+  return CGL_OK;
+}
+
+#define CHECK_E(e)                                  \
+  do {                                              \
+    if (!(e)) return CGL_INVALID_ARG;               \
+    if ((e)->destroyed) return CGL_DESTROYED;       \
+    (e)->err.clear();                               \
+    if (cudaSetDevice((e)->device) != cudaSuccess) return fail(e, CGL_CUDA_ERROR, "cudaSetDevice"); \
+  } while (0)
+
+cgl_status cgl_set_config(cgl_engine* e, const cgl_config* cfg) {
+  CHECK_E(e);
+  if (!cfg) return CGL_INVALID_ARG;
+  const cgl_config prev = e->cfg;
+  e->cfg = *cfg;
+  e->cfg.has_random_seed = prev.has_random_seed;   // init-only (src/index.ts:1720-1724)
+  e->cfg.random_seed = prev.random_seed;
+  e->cfg.device = prev.device;
+  e->graph_dirty = true;
+  if (prev.space_size != e->cfg.space_size) {
+    // src/index.ts:1844-1851
+    adjust_space_size(e);
+    e->collision_ready = false;
+    if (e->N) setup_fixed(e);
+    e->alpha = e->running ? e->alpha : 0;
+  }
+  return CGL_OK;
+}
+
+cgl_status cgl_get_config(cgl_engine* e, cgl_config* out) {
+  CHECK_E(e);
+  if (!out) return CGL_INVALID_ARG;
+  *out = e->cfg;
+  return CGL_OK;
+}
+
+cgl_status cgl_set_point_positions(cgl_engine* e, const float* xy, uint64_t n) {
+  CHECK_E(e);
+  if (!xy && n) return CGL_INVALID_ARG;
+  cgl_status st = CGL_OK;
+  if (n % 2) {
+    n -= 1;
+    st = fail(e, CGL_WARNING, "Invalid point positions length: %llu. The trailing value was ignored.",
+              (unsigned long long)(n + 1));
+  }
+  e->in_pos.assign(xy, xy + n);
+  e->have_pos_input = true;
+  e->pos_dirty = e->links_dirty = e->sizes_dirty = true;
+  return st;
+}
+
+cgl_status cgl_set_links(cgl_engine* e, const float* st_, uint64_t n) {
+  CHECK_E(e);
+  if (!st_ && n) return CGL_INVALID_ARG;
+  cgl_status st = CGL_OK;
+  if (n % 2) {
+    n -= 1;
+    st = fail(e, CGL_WARNING, "Invalid links length: %llu. The trailing value was ignored.", (unsigned long long)(n + 1));
+  }
+  e->in_links.assign(st_, st_ + n);
+  e->have_link_input = true;
+  e->links_dirty = true;
+  return st;
+}
+
+cgl_status cgl_set_link_strength(cgl_engine* e, const float* v, uint64_t n) {
+  CHECK_E(e);
+  if (!v || n == 0) { e->in_strength.clear(); e->have_strength = false; }
+  else { e->in_strength.assign(v, v + n); e->have_strength = true; }
+  e->links_dirty = true;
+  return CGL_OK;
+}
+
+cgl_status cgl_set_point_sizes(cgl_engine* e, const float* v, uint64_t n) {
+  CHECK_E(e);
+  if (!v) { e->in_sizes.clear(); e->have_sizes = false; }
+  else { e->in_sizes.assign(v, v + n); e->have_sizes = true; }
+  e->sizes_dirty = true;
+  return CGL_OK;
+}
+
+cgl_status cgl_set_pinned_points(cgl_engine* e, const double* idx, uint64_t n) {
+  CHECK_E(e);
+  e->pinned_set = idx && n > 0;
+  if (e->pinned_set) e->pinned_input.assign(idx, idx + n);
+  else e->pinned_input.clear();
+  if (e->N) return apply_pinned(e);
+  return CGL_OK;
+}
+
+cgl_status cgl_render(cgl_engine* e, double alpha) {
+  CHECK_E(e);
+  return do_render(e, alpha);
+}
+
+cgl_status cgl_start(cgl_engine* e, double alpha) {
+  CHECK_E(e);
+  if (!e->cfg.enable_simulation || e->N == 0) return CGL_OK;
+  e->running = true;
+  e->progress = 0;
+  e->alpha = alpha;
+  return CGL_OK;
+}
+
+cgl_status cgl_stop(cgl_engine* e) {
+  CHECK_E(e);
+  e->running = false;
+  e->progress = 0;
+  e->alpha = 0;
+  return CGL_OK;
+}
+
+cgl_status cgl_pause(cgl_engine* e) {
+  CHECK_E(e);
+  e->running = false;
+  return CGL_OK;
+}
+
+cgl_status cgl_unpause(cgl_engine* e) {
+  CHECK_E(e);
+  if (e->cfg.enable_simulation) e->running = true;
+  return CGL_OK;
+}
+
+cgl_status cgl_step(cgl_engine* e, uint32_t ticks) {
+  CHECK_E(e);
+  if (!e->cfg.enable_simulation || e->T == 0) return CGL_OK;
+  return run_ticks(e, ticks, nullptr, nullptr);
+}
+
+cgl_status cgl_run(cgl_engine* e, uint32_t max_ticks, uint32_t* ticks_done) {
+  CHECK_E(e);
+  uint32_t n = 0;
+  if (e->cfg.enable_simulation && e->T && e->running) {
+    // alpha evolves on the host only, so the tick count is known up front
+    double a = e->alpha;
+    const double f = 1 - std::pow(kAlphaMin, 1 / e->cfg.simulation_decay);
+    while (n < max_ticks && !(a < kAlphaMin)) { a += (0 - a) * f; ++n; }
+    cgl_status st = run_ticks(e, n, nullptr, nullptr);
+    if (st) return st;
+    if (n < max_ticks && e->alpha < kAlphaMin) { e->running = false; e->progress = 1; }
+  }
+  if (ticks_done) *ticks_done = n;
+  return CGL_OK;
+}
+
+cgl_status cgl_get_point_positions(cgl_engine* e, float* out, uint64_t cap) {
+  CHECK_E(e);
+  if (cap < 2 * e->N || (!out && e->N)) return fail(e, CGL_INVALID_ARG, "output holds %llu floats, need %llu",
+                                                      (unsigned long long)cap, (unsigned long long)(2 * e->N));
+  if (!e->N) return CGL_OK;
+  CU(cudaMemcpyAsync(out, e->b_pos.p, e->N * sizeof(float2), cudaMemcpyDeviceToHost, e->stream));
+  CU(cudaStreamSynchronize(e->stream));
+  return CGL_OK;
+}
+
+cgl_status cgl_get_state(cgl_engine* e, cgl_state* s) {
+  if (!e || !s) return CGL_INVALID_ARG;
+  std::memset(s, 0, sizeof(*s));
+  s->destroyed = e->destroyed;
+  s->alpha = e->alpha;
+  s->progress = e->progress;
+  s->is_simulation_running = e->running;
+  s->tick = e->tick;
+  s->points_number = e->N;
+  s->links_number = e->E;
+  s->rng_draws = e->rng_ctr;
+  return CGL_OK;
+}
+
+const char* cgl_last_error(cgl_engine* e) { return e ? e->err.c_str() : "null engine"; }
+
+cgl_status cgl_set_stream(cgl_engine* e, void* cuda_stream) {
+  CHECK_E(e);
+  CU(cudaStreamSynchronize(e->stream));
+  e->stream = cuda_stream ? (cudaStream_t)cuda_stream : e->own_stream;
+  return CGL_OK;
+}
+
+cgl_status cgl_synchronize(cgl_engine* e) {
+  CHECK_E(e);
+  CU(cudaStreamSynchronize(e->stream));
+  return CGL_OK;
+}
+
+cgl_status cgl_profile_stages(cgl_engine* e, uint32_t ticks, double* ms_out) {
+  CHECK_E(e);
+  if (!ms_out) return CGL_INVALID_ARG;
+  for (int k = 0; k < CGL_NUM_STAGE_TIMES; ++k) ms_out[k] = 0;
+  if (!e->cfg.enable_simulation || e->T == 0 || ticks == 0) return CGL_OK;
+  cudaEvent_t ev[2 * CGL_NUM_STAGE_TIMES];
+  for (auto& x : ev) CU(cudaEventCreate(&x));
+  cgl_status st = run_ticks(e, ticks, ev, ms_out);
+  for (auto& x : ev) cudaEventDestroy(x);
+  if (st) return st;
+  for (int k = 0; k < CGL_NUM_STAGE_TIMES; ++k) ms_out[k] /= ticks;
+  return CGL_OK;
+}
+
+cgl_status cgl_get_layout(cgl_engine* e, cgl_layout* o) {
+  CHECK_E(e);
+  if (!o) return CGL_INVALID_ARG;
+  std::memset(o, 0, sizeof(*o));
+  o->points_number = e->N;
+  o->live_points = e->live;
+  o->links_number = e->E;
+  o->link_entries_in = e->entries;
+  o->points_texture_size = e->T;
+  o->finest_grid = (uint32_t)e->Gf;
+  o->levels = (uint32_t)e->L;
+  o->max_degree_in = e->max_deg_in;
+  o->max_degree_out = e->max_deg_out;
+  o->fixed_point_bits = e->fixed_bits;
+  o->fixed_point_bound = e->fx.bound;
+  o->collision_grid = (uint32_t)e->cgrid;
+  o->collision_cell_size = e->ccell;
+  o->device_bytes = e->dev_bytes;
+  const TickPlan p = plan_tick(e);
+  uint32_t k = 1;                                      // tick end
+  if (p.grav || p.cent || p.mb) k += 1;                // prepass
+  if (p.cent) k += 1;
+  if (p.mb) k += 5;                                    // scan (2), scatter, cells, manybody
+  k += (uint32_t)p.link_in + (uint32_t)p.link_out;
+  if (p.coll) k += 3;                                  // grid, convert, force
+  o->kernels_per_tick = k;
+  return CGL_OK;
+}
+
+cgl_status cgl_debug_get_cells(cgl_engine* e, uint32_t level, float* out, uint64_t cap) {
+  CHECK_E(e);
+  if (!e->mb_ready || level >= (uint32_t)e->L) return fail(e, CGL_INVALID_ARG, "no level %u", level);
+  const uint64_t cells = (uint64_t)(4u << level) * (4u << level);
+  if (cap < 4 * cells) return CGL_INVALID_ARG;
+  CU(cudaMemcpyAsync(out, (float4*)e->b_rec.p + e->level_off[level], cells * sizeof(float4), cudaMemcpyDeviceToHost,
+                     e->stream));
+  CU(cudaStreamSynchronize(e->stream));
+  return CGL_OK;
+}
+
+cgl_status cgl_debug_get_slots(cgl_engine* e, int32_t* out, uint64_t cap) {
+  CHECK_E(e);
+  if (!e->mb_ready) return CGL_INVALID_ARG;
+  const uint64_t cells = (uint64_t)e->Gf * e->Gf;
+  if (cap < kSlots * cells) return CGL_INVALID_ARG;
+  std::vector<float4> fine(cells);
+  std::vector<uint32_t> start(cells + 1);
+  std::vector<uint32_t> sidx(e->live);
+  CU(cudaMemcpyAsync(fine.data(), (float4*)e->b_rec.p + e->level_off[e->L - 1], cells * sizeof(float4),
+                     cudaMemcpyDeviceToHost, e->stream));
+  CU(cudaMemcpyAsync(start.data(), e->b_cell_start.p, (cells + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream));
+  if (e->live)
+    CU(cudaMemcpyAsync(sidx.data(), e->b_sorted_idx.p, e->live * sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream));
+  CU(cudaStreamSynchronize(e->stream));
+  for (uint64_t c = 0; c < cells; ++c) {
+    const int ns = (int)fine[c].w;
+    for (int q = 0; q < kSlots; ++q)
+      out[c * kSlots + q] = (q < ns && start[c] + q < e->live) ? (int32_t)sidx[start[c] + q] : -1;
+  }
+  return CGL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,713 @@
+// kernels.cu — per-tick force kernels of the GB300 force-layout engine.
+//
+// One tick (Graph.runSimulationStep, src/index.ts:2006-2099) is:
+//   prepass      gravity + update (force-gravity.frag, update-position.frag),
+//                optional centroid sums (calculate-centermass.vert), and the
+//                finest-cell histogram of the many-body binning
+//   center       ForceCenter (force-center.frag) + update + binning   [if on]
+//   scan         exclusive scan of the finest-cell histogram
+//   scatter      counting-sort scatter of live points into cell order
+//   cells        per finest cell: exact sums, the 8-slot near-field peel
+//                (build-nearfield-slots.vert), and the pyramid of coarser
+//                levels (calculate-level.vert for every level)
+//   manybody     level passes + near field + update (force-level.frag,
+//                force-nearfield.frag, update-position.frag)
+//   link in/out  spring force over each direction's link lists + update
+//                (force-spring.ts)
+//   collision    4 offset grids + spatial collision force + update
+//                (build-grid.vert, force-collision-spatial.frag)
+// Kernels read the tick's alpha and peel seed from device memory so that one
+// captured CUDA graph serves every tick.
+#include "kernels.cuh"
+
+namespace cgl {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+__device__ __forceinline__ TickParams tick_params(const DeviceView& d) {
+  return d.tick_params[*d.tick_ctr];
+}
+
+__device__ __forceinline__ long long warp_sum_ll(long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-reduce three integer sums and add them to dst[0..2] (one atomic each).
+__device__ void block_add3(long long a, long long b, long long c, long long* dst) {
+  __shared__ long long sm[3][kBlock / 32];
+  a = warp_sum_ll(a); b = warp_sum_ll(b); c = warp_sum_ll(c);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) { sm[0][w] = a; sm[1][w] = b; sm[2][w] = c; }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+    a = lane < nw ? sm[0][lane] : 0; b = lane < nw ? sm[1][lane] : 0; c = lane < nw ? sm[2][lane] : 0;
+    a = warp_sum_ll(a); b = warp_sum_ll(b); c = warp_sum_ll(c);
+    if (lane == 0) {
+      atomicAdd((unsigned long long*)&dst[0], (unsigned long long)a);
+      atomicAdd((unsigned long long*)&dst[1], (unsigned long long)b);
+      atomicAdd((unsigned long long*)&dst[2], (unsigned long long)c);
+    }
+  }
+}
+
+__device__ __forceinline__ void bin_point(const DeviceView& d, const SimScalars& s, uint32_t i, float2 p) {
+  const int cx = cell_index(p.x, s.csf, s.gf), cy = cell_index(p.y, s.csf, s.gf);
+  const uint32_t key = (uint32_t)(cy * s.gf + cx);
+  d.key[i] = key;
+  d.rank[i] = atomicAdd(&d.counts[key], 1u);
+}
+
+// ---------------------------------------------------------------- prepass --
+template <uint32_t MODE>
+__global__ void __launch_bounds__(kBlock) k_prepass(DeviceView d, SimScalars s) {
+  const TickParams tp = tick_params(d);
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  long long sx = 0, sy = 0, sn = 0;
+  if (i < d.n) {
+    const uint8_t f = d.flags[i];
+    float2 p = d.pos[i];
+    if (MODE & kPreGravity) {
+      // force-gravity.frag:24-40
+      const float c = __fmul_rn(s.space, 0.5f);
+      const float dx = __fsub_rn(c, p.x), dy = __fsub_rn(c, p.y);
+      const float dist = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
+      float vx = 0.f, vy = 0.f;
+      if (dist > 0.f) {
+        const float add = __fmul_rn(__fmul_rn(__fmul_rn(tp.alpha, s.gravity), dist), 0.1f);
+        vx = __fadd_rn(vx, __fmul_rn(add, __fdiv_rn(dx, dist)));
+        vy = __fadd_rn(vy, __fmul_rn(add, __fdiv_rn(dy, dist)));
+      }
+      if (!(f & (kPinned | kAbsent))) {
+        p = integrate(p, vx, vy, s.friction, s.space);
+        d.pos[i] = p;
+      }
+    }
+    if (!(f & kAbsent)) {
+      if (MODE & kPreCentroid) { sx = to_fixed(p.x, s.fx); sy = to_fixed(p.y, s.fx); sn = 1; }
+      if (MODE & kPreBin) bin_point(d, s, i, p);
+    } else if (MODE & kPreBin) {
+      d.key[i] = kNoCell;
+    }
+  }
+  if (MODE & kPreCentroid) block_add3(sx, sy, sn, d.centroid);
+}
+
+// ----------------------------------------------------------------- center --
+template <bool BIN>
+__global__ void __launch_bounds__(kBlock) k_center(DeviceView d, SimScalars s) {
+  // ForceCenter.run (ForceCenter/index.ts:149-199), force-center.frag:22-36
+  const TickParams tp = tick_params(d);
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n) return;
+  const float sx = from_fixed(d.centroid[0], s.fx), sy = from_fixed(d.centroid[1], s.fx);
+  const float cnt = (float)d.centroid[2];
+  const float cmx = __fdiv_rn(sx, cnt), cmy = __fdiv_rn(sy, cnt);
+  const uint8_t f = d.flags[i];
+  float2 p = d.pos[i];
+  const float dx = __fsub_rn(cmx, p.x), dy = __fsub_rn(cmy, p.y);
+  const float dist = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
+  float vx = 0.f, vy = 0.f;
+  if (dist > 0.f) {
+    const float add = __fmul_rn(__fmul_rn(__fmul_rn(tp.alpha, s.center), dist), 0.01f);
+    vx = __fadd_rn(vx, __fmul_rn(add, __fdiv_rn(dx, dist)));
+    vy = __fadd_rn(vy, __fmul_rn(add, __fdiv_rn(dy, dist)));
+  }
+  if (!(f & (kPinned | kAbsent))) {
+    p = integrate(p, vx, vy, s.friction, s.space);
+    d.pos[i] = p;
+  }
+  if (BIN) {
+    if (!(f & kAbsent)) bin_point(d, s, i, p);
+    else d.key[i] = kNoCell;
+  }
+}
+
+// ------------------------------------------------------------------- scan --
+constexpr int kScanItems = 4;
+constexpr int kScanChunk = kBlock * kScanItems;   // cells per scan block
+
+__device__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total) {
+  __shared__ uint32_t warp_tot[kBlock / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    uint32_t t = lane < (kBlock / 32) ? warp_tot[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    if (lane < (kBlock / 32)) warp_tot[lane] = t;
+  }
+  __syncthreads();
+  const uint32_t before = w > 0 ? warp_tot[w - 1] : 0;
+  *total = warp_tot[kBlock / 32 - 1];
+  __syncthreads();
+  return before + x - v;
+}
+
+__global__ void __launch_bounds__(kBlock) k_scan_reduce(DeviceView d, uint32_t cells) {
+  const uint32_t base = blockIdx.x * kScanChunk;
+  uint32_t sum = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    uint32_t c = base + k * kBlock + threadIdx.x;
+    if (c < cells) sum += d.counts[c];
+  }
+  uint32_t total;
+  block_exclusive_scan(sum, &total);
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    d.block_sums[blockIdx.x] = total;
+    __threadfence();
+    last = atomicAdd(d.scan_ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  // Last block: exclusive scan of the block totals (gridDim.x <= kScanChunk).
+  __threadfence();
+  uint32_t v[kScanItems];
+  uint32_t run = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    uint32_t b = threadIdx.x * kScanItems + k;
+    v[k] = b < gridDim.x ? __ldcg(&d.block_sums[b]) : 0;
+    run += v[k];
+  }
+  uint32_t grand;
+  uint32_t off = block_exclusive_scan(run, &grand);
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    uint32_t b = threadIdx.x * kScanItems + k;
+    if (b < gridDim.x) d.block_sums[b] = off;
+    off += v[k];
+  }
+  if (threadIdx.x == 0) {
+    d.block_sums[gridDim.x] = grand;
+    *d.scan_ticket = 0;
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_scan_down(DeviceView d, uint32_t cells) {
+  const uint32_t base = blockIdx.x * kScanChunk + threadIdx.x * kScanItems;
+  uint32_t v[kScanItems];
+  uint32_t run = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    uint32_t c = base + k;
+    v[k] = c < cells ? d.counts[c] : 0;
+    run += v[k];
+  }
+  uint32_t total;
+  uint32_t off = block_exclusive_scan(run, &total) + __ldcg(&d.block_sums[blockIdx.x]);
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    uint32_t c = base + k;
+    if (c < cells) {
+      d.cell_start[c] = off;
+      d.counts[c] = 0;   // histogram ready for the next tick
+    }
+    off += v[k];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) d.cell_start[cells] = __ldcg(&d.block_sums[gridDim.x]);
+}
+
+// ---------------------------------------------------------------- scatter --
+__global__ void __launch_bounds__(kBlock) k_scatter(DeviceView d) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n) return;
+  const uint32_t k = d.key[i];
+  if (k == kNoCell) return;
+  const uint32_t dst = d.cell_start[k] + d.rank[i];
+  d.sorted_idx[dst] = i;
+  d.sorted_pos[dst] = d.pos[i];
+}
+
+// ------------------------------------------------------------------ cells --
+// One thread per finest cell, one CTA per tile x tile block of cells.
+__global__ void k_cells(DeviceView d, SimScalars s) {
+  extern __shared__ long long sm[];   // 3 * tile * tile
+  const TickParams tp = tick_params(d);
+  const int T = s.tile;
+  const int tiles_row = s.gf / T;
+  const int tile_x = blockIdx.x % tiles_row, tile_y = blockIdx.x / tiles_row;
+  const int tx = threadIdx.x % T, ty = threadIdx.x / T;
+  const int cx = tile_x * T + tx, cy = tile_y * T + ty;
+  const uint32_t c = (uint32_t)(cy * s.gf + cx);
+  const uint32_t b = d.cell_start[c], e = d.cell_start[c + 1];
+
+  // exact sums and the 8 smallest distinct peel hashes (build-nearfield-slots.vert)
+  long long ax = 0, ay = 0;
+  unsigned long long best[kSlots];
+  uint32_t at[kSlots];
+#pragma unroll
+  for (int q = 0; q < kSlots; ++q) { best[q] = ~0ull; at[q] = 0; }
+  for (uint32_t j = b; j < e; ++j) {
+    const float2 p = d.sorted_pos[j];
+    ax += to_fixed(p.x, s.fx);
+    ay += to_fixed(p.y, s.fx);
+    const uint32_t idx = d.sorted_idx[j];
+    const uint32_t hb = __float_as_uint(peel_hash(idx, tp.seed_bits));
+    unsigned long long key = ((unsigned long long)hb << 32) | idx;
+    bool dup = false;
+#pragma unroll
+    for (int q = 0; q < kSlots; ++q) {
+      if ((uint32_t)(best[q] >> 32) == hb && best[q] != ~0ull) {
+        dup = true;
+        if (key < best[q]) { best[q] = key; at[q] = j; }
+      }
+    }
+    if (!dup && key < best[kSlots - 1]) {
+      uint32_t apos = j;
+#pragma unroll
+      for (int q = 0; q < kSlots; ++q) {
+        if (key < best[q]) {
+          unsigned long long tk = best[q]; best[q] = key; key = tk;
+          uint32_t ta = at[q]; at[q] = apos; apos = ta;
+        }
+      }
+    }
+  }
+  int ns = 0;
+#pragma unroll
+  for (int q = 0; q < kSlots; ++q) ns += best[q] != ~0ull;
+  // move the slots to the head of the segment, in hash order
+#pragma unroll
+  for (int q = 0; q < kSlots; ++q) {
+    if (q < ns) {
+      const uint32_t tq = b + q, pq = at[q];
+      if (pq != tq) {
+        const uint32_t i0 = d.sorted_idx[tq], i1 = d.sorted_idx[pq];
+        const float2 p0 = d.sorted_pos[tq], p1 = d.sorted_pos[pq];
+        d.sorted_idx[tq] = i1; d.sorted_pos[tq] = p1;
+        d.sorted_idx[pq] = i0; d.sorted_pos[pq] = p0;
+#pragma unroll
+        for (int r = q + 1; r < kSlots; ++r)
+          if (at[r] == tq) at[r] = pq;
+      }
+    }
+  }
+  const uint32_t cnt = e - b;
+  {
+    float4 r = make_float4(0.f, 0.f, 0.f, (float)ns);
+    if (cnt > 0) {
+      const float cf = (float)cnt;
+      r.x = __fdiv_rn(from_fixed(ax, s.fx), cf);
+      r.y = __fdiv_rn(from_fixed(ay, s.fx), cf);
+      r.z = cf;
+    }
+    d.rec[d.level_off[s.levels - 1] + c] = r;
+  }
+
+  // coarser levels inside the tile
+  long long* smx = sm;
+  long long* smy = sm + T * T;
+  long long* smn = sm + 2 * T * T;
+  smx[threadIdx.x] = ax; smy[threadIdx.x] = ay; smn[threadIdx.x] = cnt;
+  __syncthreads();
+  int g = T;
+  int lv = s.levels - 1;
+  while (g > 1 && lv > 0) {
+    g >>= 1;
+    --lv;
+    long long vx = 0, vy = 0, vn = 0;
+    const bool active = tx < g && ty < g;
+    if (active) {
+      const int i00 = (2 * ty) * T + 2 * tx;
+      vx = smx[i00] + smx[i00 + 1] + smx[i00 + T] + smx[i00 + T + 1];
+      vy = smy[i00] + smy[i00 + 1] + smy[i00 + T] + smy[i00 + T + 1];
+      vn = smn[i00] + smn[i00 + 1] + smn[i00 + T] + smn[i00 + T + 1];
+    }
+    __syncthreads();
+    if (active) {
+      smx[ty * T + tx] = vx; smy[ty * T + tx] = vy; smn[ty * T + tx] = vn;
+      const int G = 4 << lv;
+      const int gx = tile_x * g + tx, gy = tile_y * g + ty;
+      float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (vn > 0) {
+        const float cf = (float)vn;
+        r.x = __fdiv_rn(from_fixed(vx, s.fx), cf);
+        r.y = __fdiv_rn(from_fixed(vy, s.fx), cf);
+        r.z = cf;
+      }
+      d.rec[d.level_off[lv] + gy * G + gx] = r;
+    }
+    __syncthreads();
+  }
+  if (lv == 0) return;   // the tile reached the coarsest level: no tile is partial
+  // levels coarser than the tile: integer atomics, finished by the last CTA
+  if (threadIdx.x == 0) {
+    const long long tx_ = smx[0], ty_ = smy[0], tn_ = smn[0];
+    for (int l = lv - 1; l >= 0; --l) {
+      const int sh = lv - l;
+      const int G = 4 << l;
+      const int gx = tile_x >> sh, gy = tile_y >> sh;
+      long long* a = d.acc + 3 * (size_t)(d.acc_off[l] + gy * G + gx);
+      atomicAdd((unsigned long long*)&a[0], (unsigned long long)tx_);
+      atomicAdd((unsigned long long*)&a[1], (unsigned long long)ty_);
+      atomicAdd((unsigned long long*)&a[2], (unsigned long long)tn_);
+    }
+  }
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(d.cells_ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const uint32_t total_cells = d.acc_off[lv];
+  for (uint32_t k = threadIdx.x; k < total_cells; k += blockDim.x) {
+    int l = 0;
+    while (l + 1 < lv && d.acc_off[l + 1] <= k) ++l;
+    const uint32_t cl = k - d.acc_off[l];
+    long long* a = d.acc + 3 * (size_t)k;
+    const long long vx = __ldcg(&a[0]), vy = __ldcg(&a[1]), vn = __ldcg(&a[2]);
+    float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (vn > 0) {
+      const float cf = (float)vn;
+      r.x = __fdiv_rn(from_fixed(vx, s.fx), cf);
+      r.y = __fdiv_rn(from_fixed(vy, s.fx), cf);
+      r.z = cf;
+    }
+    d.rec[d.level_off[l] + cl] = r;
+    a[0] = 0; a[1] = 0; a[2] = 0;
+  }
+  if (threadIdx.x == 0) *d.cells_ticket = 0;
+}
+
+// --------------------------------------------------------------- manybody --
+__global__ void __launch_bounds__(kBlock) k_manybody(DeviceView d, SimScalars s) {
+  const TickParams tp = tick_params(d);
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t total = d.cell_start[s.gf * s.gf];
+  if (j >= total) return;
+  const uint32_t i = d.sorted_idx[j];
+  const float2 p = d.sorted_pos[j];
+  const float px = p.x, py = p.y;
+  const int gf = s.gf, L = s.levels;
+  const int fcx = cell_index(px, s.csf, gf), fcy = cell_index(py, s.csf, gf);
+  const float k = __fmul_rn(tp.alpha, s.repulsion);
+  float vx = 0.f, vy = 0.f;
+  for (int l = 0; l < L; ++l) {
+    const int G = 4 << l;
+    const int sh = L - 1 - l;
+    const int pcx = fcx >> sh, pcy = fcy >> sh;
+    const float4* lv = d.rec + d.level_off[l];
+    float lx = 0.f, ly = 0.f;
+    if (l == 0) {   // force-level.frag:70-79
+#pragma unroll
+      for (int jj = 0; jj < 4; ++jj)
+#pragma unroll
+        for (int ii = 0; ii < 4; ++ii) {
+          if (max(abs(ii - pcx), abs(jj - pcy)) <= 1) continue;
+          cell_velocity(__ldg(&lv[jj * 4 + ii]), px, py, k, lx, ly);
+        }
+    } else {        // force-level.frag:80-95
+      const int bx = (pcx / 2) * 2 - 2, by = (pcy / 2) * 2 - 2;
+#pragma unroll
+      for (int jj = 0; jj < 6; ++jj)
+#pragma unroll
+        for (int ii = 0; ii < 6; ++ii) {
+          const int cx = bx + ii, cy = by + jj;
+          if (cx < 0 || cy < 0 || cx >= G || cy >= G) continue;
+          if (max(abs(cx - pcx), abs(cy - pcy)) <= 1) continue;
+          cell_velocity(__ldg(&lv[cy * G + cx]), px, py, k, lx, ly);
+        }
+    }
+    vx = __fadd_rn(vx, lx);
+    vy = __fadd_rn(vy, ly);
+  }
+  // near field (force-nearfield.frag:199-263)
+  const float2 rj = d.jitter[i];
+  const float self = (float)i;
+  const float4* fine = d.rec + d.level_off[L - 1];
+  float nx = 0.f, ny = 0.f;
+#pragma unroll
+  for (int jj = -1; jj <= 1; ++jj)
+#pragma unroll
+    for (int ii = -1; ii <= 1; ++ii) {
+      const int cx = fcx + ii, cy = fcy + jj;
+      if (cx < 0 || cy < 0 || cx >= gf || cy >= gf) continue;
+      const uint32_t c = (uint32_t)(cy * gf + cx);
+      const float4 r = __ldg(&fine[c]);
+      const float others = __fsub_rn(r.z, (ii == 0 && jj == 0) ? 1.0f : 0.0f);
+      if (others <= 0.f) continue;
+      const int ns = (int)r.w;
+      const uint32_t b = __ldg(&d.cell_start[c]);
+      float sx = 0.f, sy = 0.f, sampled = 0.f;
+      for (int q = 0; q < kSlots; ++q) {
+        if (q >= ns) { sx = __fadd_rn(sx, 0.f); sy = __fadd_rn(sy, 0.f); continue; }
+        const uint32_t oi = __ldg(&d.sorted_idx[b + q]);
+        if ((float)oi == self) { sx = __fadd_rn(sx, 0.f); sy = __fadd_rn(sy, 0.f); continue; }
+        const float2 o = __ldg(&d.sorted_pos[b + q]);
+        sampled = __fadd_rn(sampled, 1.0f);
+        pair_velocity(px, py, o.x, o.y, rj.x, rj.y, k, sx, sy);
+      }
+      if (sampled > 0.f) {
+        const float w = __fdiv_rn(others, sampled);
+        nx = __fadd_rn(nx, __fmul_rn(w, sx));
+        ny = __fadd_rn(ny, __fmul_rn(w, sy));
+      }
+    }
+  nx = __fadd_rn(nx, __fmul_rn(nx, rj.x));
+  ny = __fadd_rn(ny, __fmul_rn(ny, rj.y));
+  const float max_step = __fmul_rn(2.0f, s.csf);
+  const float speed = __fsqrt_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)));
+  if (speed > max_step) {
+    const float sc = __fdiv_rn(max_step, speed);
+    nx = __fmul_rn(nx, sc);
+    ny = __fmul_rn(ny, sc);
+  }
+  vx = __fadd_rn(vx, nx);
+  vy = __fadd_rn(vy, ny);
+  if (!(d.flags[i] & kPinned)) d.pos[i] = integrate(p, vx, vy, s.friction, s.space);
+}
+
+// ------------------------------------------------------------------- link --
+__global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, const uint32_t* __restrict__ rowptr,
+                                                 const uint4* __restrict__ ent, const float2* __restrict__ src,
+                                                 float2* __restrict__ dst) {
+  // ForceLink.run (ForceLink/index.ts:221-263), force-spring.ts:38-96
+  const TickParams tp = tick_params(d);
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= d.n) return;
+  const float2 pp = src[p];
+  const uint8_t f = d.flags[p];
+  if (f & kAbsent) { dst[p] = pp; return; }
+  const float sa = __fmul_rn(s.link_spring, tp.alpha);
+  const float span = __fsub_rn(s.link_r1, s.link_r0);
+  float vx = 0.f, vy = 0.f;
+  const uint32_t e0 = rowptr[p], e1 = rowptr[p + 1];
+  for (uint32_t at = e0; at < e1; ++at) {
+    const uint4 en = __ldg(&ent[at]);
+    if (en.x == kAbsentTarget) continue;
+    float dd = __fadd_rn(__fmul_rn(__uint_as_float(en.y), span), s.link_r0);
+    dd = __fmul_rn(dd, s.link_distance);
+    const float2 q = __ldg(&src[en.x]);
+    float x = __fsub_rn(q.x, __fadd_rn(pp.x, vx));
+    float y = __fsub_rn(q.y, __fadd_rn(pp.y, vy));
+    float l = __fsqrt_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)));
+    l = gmax(l, __fmul_rn(dd, 0.99f));
+    l = __fdiv_rn(__fsub_rn(l, dd), l);
+    l = __fmul_rn(l, sa);
+    l = __fmul_rn(l, __uint_as_float(en.w));
+    l = __fmul_rn(l, __uint_as_float(en.z));
+    x = __fmul_rn(x, l);
+    y = __fmul_rn(y, l);
+    vx = __fadd_rn(vx, x);
+    vy = __fadd_rn(vy, y);
+  }
+  dst[p] = (f & kPinned) ? pp : integrate(pp, vx, vy, s.friction, s.space);
+}
+
+// -------------------------------------------------------------- collision --
+__device__ __forceinline__ float coll_bin(float p, float o, float cs, float gm1) {
+  const float off = __fadd_rn(p, __fmul_rn(o, cs));
+  float c = gclamp(floorf(__fdiv_rn(off, cs)), 0.f, gm1);
+  if (!(c == c)) c = 0.f;
+  return c;
+}
+
+__constant__ float kOffX[4] = {0.f, 0.5f, 0.f, 0.5f};
+__constant__ float kOffY[4] = {0.f, 0.f, 0.5f, 0.5f};
+
+__global__ void __launch_bounds__(kBlock) k_coll_grid(DeviceView d, SimScalars s) {
+  // build-grid.vert:28-62 for the 4 offsets (ForceCollision/index.ts:19-24)
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n) return;
+  if (d.flags[i] & kAbsent) return;
+  const float2 p = d.pos[i];
+  const float sz = d.size[i];
+  const float gm1 = (float)s.coll_grid - 1.0f;
+  const long long fx = to_fixed(p.x, s.fx), fy = to_fixed(p.y, s.fx), fs = to_fixed(sz, s.fx);
+  const uint32_t G2 = (uint32_t)(s.coll_grid * s.coll_grid);
+#pragma unroll
+  for (int g = 0; g < 4; ++g) {
+    const int cx = (int)coll_bin(p.x, kOffX[g], s.coll_cell, gm1);
+    const int cy = (int)coll_bin(p.y, kOffY[g], s.coll_cell, gm1);
+    long long* a = d.cgrid_acc + 4 * ((size_t)g * G2 + (uint32_t)(cy * s.coll_grid + cx));
+    atomicAdd((unsigned long long*)&a[0], (unsigned long long)fx);
+    atomicAdd((unsigned long long*)&a[1], (unsigned long long)fy);
+    atomicAdd((unsigned long long*)&a[2], (unsigned long long)fs);
+    atomicAdd((unsigned long long*)&a[3], 1ull);
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_coll_convert(DeviceView d, SimScalars s) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t total = 4u * (uint32_t)(s.coll_grid * s.coll_grid);
+  if (k >= total) return;
+  long long* a = d.cgrid_acc + 4 * (size_t)k;
+  d.cgrid[k] = make_float4(from_fixed(a[0], s.fx), from_fixed(a[1], s.fx), from_fixed(a[2], s.fx), (float)a[3]);
+  a[0] = 0; a[1] = 0; a[2] = 0; a[3] = 0;
+}
+
+__global__ void __launch_bounds__(kBlock) k_coll_force(DeviceView d, SimScalars s) {
+  // force-collision-spatial.frag:103-168, 4 passes blended, then update
+  const TickParams tp = tick_params(d);
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n) return;
+  const uint8_t f = d.flags[i];
+  if (f & kAbsent) return;
+  const float2 p = d.pos[i];
+  const float cs = s.coll_cell;
+  const int G = s.coll_grid;
+  const float Gf = (float)G;
+  const float gm1 = Gf - 1.0f;
+  const uint32_t G2 = (uint32_t)(G * G);
+  const float cur = (float)i;
+  const float csz = d.size[i];
+  const float cr = s.coll_radius, pad = s.coll_padding;
+  const float R = __fadd_rn(cr > 0.f ? cr : __fmul_rn(csz, 0.5f), pad);
+  float vx = 0.f, vy = 0.f;
+  if (!(cur < 0.f || cur >= (float)d.n)) {
+    for (int g = 0; g < 4; ++g) {
+      const float mx = coll_bin(p.x, kOffX[g], cs, gm1);
+      const float my = coll_bin(p.y, kOffY[g], cs, gm1);
+      const float4* grid = d.cgrid + (size_t)g * G2;
+      float total = 0.f, gx = 0.f, gy = 0.f;
+      for (int dx = -1; dx <= 1; ++dx)
+        for (int dy = -1; dy <= 1; ++dy) {
+          const float ncx = __fadd_rn(mx, (float)dx), ncy = __fadd_rn(my, (float)dy);
+          if (ncx < 0.f || ncx >= Gf || ncy < 0.f || ncy >= Gf) continue;
+          const float4 cd = __ldg(&grid[(int)ncy * G + (int)ncx]);
+          const float cnt = cd.w;
+          if (cnt < 0.5f) continue;
+          float ec = cnt, spx = cd.x, spy = cd.y, ss = cd.z;
+          if (dx == 0 && dy == 0) {
+            ec = __fsub_rn(cnt, 1.0f);
+            spx = __fsub_rn(spx, p.x); spy = __fsub_rn(spy, p.y); ss = __fsub_rn(ss, csz);
+          }
+          if (ec < 0.5f) continue;
+          total = __fadd_rn(total, ec);
+          const float avx = __fdiv_rn(spx, ec), avy = __fdiv_rn(spy, ec);
+          const float avs = __fdiv_rn(ss, ec);
+          const float oR = __fadd_rn(cr > 0.f ? cr : __fmul_rn(avs, 0.5f), pad);
+          const float comb = __fadd_rn(R, oR);
+          const float ddx = __fsub_rn(p.x, avx), ddy = __fsub_rn(p.y, avy);
+          const float dist = __fsqrt_rn(__fadd_rn(__fmul_rn(ddx, ddx), __fmul_rn(ddy, ddy)));
+          if (dist < comb && dist > 0.001f) {
+            const float ov = __fdiv_rn(__fsub_rn(comb, dist), comb);
+            const float soft = __fmul_rn(__fmul_rn(__fsqrt_rn(ov), comb), 0.5f);
+            const float dirx = __fdiv_rn(ddx, dist), diry = __fdiv_rn(ddy, dist);
+            float fo = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(tp.alpha, s.coll_strength), soft), 0.25f), ec);
+            fo = gmin(fo, __fmul_rn(comb, 0.5f));
+            gx = __fadd_rn(gx, __fmul_rn(fo, dirx));
+            gy = __fadd_rn(gy, __fmul_rn(fo, diry));
+          } else if (dist <= 0.001f && ec > 0.f) {
+            const float ang = __fmul_rn(cur, 0.618033988749895f);
+            const float fo = gmin(__fmul_rn(__fmul_rn(__fmul_rn(tp.alpha, s.coll_strength), comb), 0.1f),
+                                  __fmul_rn(comb, 0.3f));
+            float sn, cn;
+            portable_sincos(ang, &sn, &cn);
+            const float fe = __fmul_rn(fo, ec);
+            gx = __fadd_rn(gx, __fmul_rn(fe, cn));
+            gy = __fadd_rn(gy, __fmul_rn(fe, sn));
+          }
+        }
+      if (total > 2.0f) {
+        const float dmp = __fdiv_rn(2.0f, total);
+        gx = __fmul_rn(gx, dmp); gy = __fmul_rn(gy, dmp);
+      }
+      const float maxc = __fmul_rn(R, 0.1f);
+      const float corr = __fsqrt_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)));
+      if (corr > maxc) {
+        const float sc = __fdiv_rn(maxc, corr);
+        gx = __fmul_rn(gx, sc); gy = __fmul_rn(gy, sc);
+      }
+      vx = __fadd_rn(vx, gx);
+      vy = __fadd_rn(vy, gy);
+    }
+  }
+  if (!(f & kPinned)) d.pos[i] = integrate(p, vx, vy, s.friction, s.space);
+}
+
+__global__ void k_tick_end(DeviceView d) { *d.tick_ctr += 1; }
+
+inline uint32_t blocks_for(uint32_t n) { return (n + kBlock - 1) / kBlock; }
+
+}  // namespace
+
+uint32_t scan_blocks(uint32_t cells) { return (cells + kScanChunk - 1) / kScanChunk; }
+
+void launch_prepass(const DeviceView& d, const SimScalars& s, uint32_t mode, cudaStream_t st) {
+  const uint32_t nb = blocks_for(d.n);
+  if (nb == 0) return;
+  switch (mode) {
+    case kPreGravity: k_prepass<kPreGravity><<<nb, kBlock, 0, st>>>(d, s); break;
+    case kPreGravity | kPreBin: k_prepass<kPreGravity | kPreBin><<<nb, kBlock, 0, st>>>(d, s); break;
+    case kPreGravity | kPreCentroid: k_prepass<kPreGravity | kPreCentroid><<<nb, kBlock, 0, st>>>(d, s); break;
+    case kPreCentroid: k_prepass<kPreCentroid><<<nb, kBlock, 0, st>>>(d, s); break;
+    case kPreBin: k_prepass<kPreBin><<<nb, kBlock, 0, st>>>(d, s); break;
+    default: break;
+  }
+}
+
+void launch_center(const DeviceView& d, const SimScalars& s, bool bin, cudaStream_t st) {
+  const uint32_t nb = blocks_for(d.n);
+  if (nb == 0) return;
+  if (bin) k_center<true><<<nb, kBlock, 0, st>>>(d, s);
+  else k_center<false><<<nb, kBlock, 0, st>>>(d, s);
+}
+
+void launch_scan(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
+  const uint32_t cells = (uint32_t)(s.gf * s.gf);
+  const uint32_t nb = scan_blocks(cells);
+  k_scan_reduce<<<nb, kBlock, 0, st>>>(d, cells);
+  k_scan_down<<<nb, kBlock, 0, st>>>(d, cells);
+}
+
+void launch_scatter(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
+  (void)s;
+  const uint32_t nb = blocks_for(d.n);
+  if (nb) k_scatter<<<nb, kBlock, 0, st>>>(d);
+}
+
+void launch_cells(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
+  const int tiles = (s.gf / s.tile) * (s.gf / s.tile);
+  const size_t smem = 3 * sizeof(long long) * s.tile * s.tile;
+  k_cells<<<tiles, s.tile * s.tile, smem, st>>>(d, s);
+}
+
+void launch_manybody(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
+  const uint32_t nb = blocks_for(d.n);
+  if (nb) k_manybody<<<nb, kBlock, 0, st>>>(d, s);
+}
+
+void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool swap_back, cudaStream_t st) {
+  const uint32_t nb = blocks_for(d.n);
+  if (!nb) return;
+  const uint32_t* rp = direction == 0 ? d.rowptr_in : d.rowptr_out;
+  const uint4* en = direction == 0 ? d.ent_in : d.ent_out;
+  if (!swap_back) k_link<<<nb, kBlock, 0, st>>>(d, s, rp, en, d.pos, d.pos_alt);
+  else k_link<<<nb, kBlock, 0, st>>>(d, s, rp, en, d.pos_alt, d.pos);
+}
+
+void launch_collision_grid(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
+  const uint32_t nb = blocks_for(d.n);
+  if (nb) k_coll_grid<<<nb, kBlock, 0, st>>>(d, s);
+  const uint32_t cells = 4u * (uint32_t)(s.coll_grid * s.coll_grid);
+  k_coll_convert<<<blocks_for(cells), kBlock, 0, st>>>(d, s);
+}
+
+void launch_collision_force(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
+  const uint32_t nb = blocks_for(d.n);
+  if (nb) k_coll_force<<<nb, kBlock, 0, st>>>(d, s);
+}
+
+void launch_tick_end(const DeviceView& d, cudaStream_t st) { k_tick_end<<<1, 1, 0, st>>>(d); }
+
+}  // namespace cgl

@@ -1,0 +1,88 @@
+// kernels.cuh — launch interface of the per-tick kernels (kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "common.cuh"
+
+namespace cgl {
+
+// Per-tick scalars computed on the host (alpha in FP64 -> f32 uniform, the
+// near-field peel seed draw), read on the device at tick_params[*tick_ctr].
+struct TickParams {
+  float alpha;
+  uint32_t seed_bits;
+};
+
+// Device state of one engine: structure-of-arrays in HBM.
+struct DeviceView {
+  uint32_t n;                 // points (original index space)
+  float2* pos;                // current positions [n]
+  float2* pos_alt;            // ping-pong target of the link passes [n]
+  const uint8_t* flags;       // kPinned | kAbsent [n]
+  const float2* jitter;       // per-point random vector (ForceManyBody/index.ts:133-138) [n]
+  uint32_t* key;              // finest cell of each point, kNoCell if absent [n]
+  uint32_t* rank;             // rank within its cell from the histogram atomics [n]
+  uint32_t* sorted_idx;       // points grouped by finest cell; head of each cell = slots in hash order [n]
+  float2* sorted_pos;         // positions in the same order (snapshot for the many-body pass) [n]
+  uint32_t* counts;           // finest-cell histogram [G^2] (zeroed by the scan)
+  uint32_t* cell_start;       // exclusive scan [G^2 + 1]
+  uint32_t* block_sums;       // scan partials
+  uint32_t* scan_ticket;      // last-block ticket of the scan
+  float4* rec;                // cell records of all levels (cx, cy, count, nslot)
+  uint32_t level_off[10];     // offset of level l in rec
+  long long* acc;             // coarse-level integer sums (x, y, count) per cell, levels < tile level
+  uint32_t acc_off[10];       // offset (in cells) of level l in acc
+  uint32_t* cells_ticket;     // last-block ticket of the cell kernel
+  long long* centroid;        // x, y, count sums for ForceCenter
+  const TickParams* tick_params;
+  uint32_t* tick_ctr;
+  // link CSR (two directions)
+  const uint32_t* rowptr_in;
+  const uint4* ent_in;        // (col, rnd bits, bias bits, strength bits)
+  const uint32_t* rowptr_out;
+  const uint4* ent_out;
+  // collision
+  const float* size;          // resolved point sizes [n]
+  long long* cgrid_acc;       // 4 grids x G_c^2 x (x, y, size, count)
+  float4* cgrid;              // 4 grids x G_c^2 (sx, sy, ssize, count)
+};
+
+struct SimScalars {
+  float space;                // adjustedSpaceSize (f32 uniform)
+  float friction;
+  float gravity;
+  float center;
+  float repulsion;
+  float link_spring;
+  float link_distance;
+  float link_r0, link_r1;     // linkDistRandomVariationRange
+  float coll_strength;
+  float coll_radius;          // 0 when undefined
+  float coll_padding;
+  float coll_cell;            // collision cell size (f32 uniform)
+  int coll_grid;
+  int gf;                     // finest grid
+  int levels;
+  int tile;                   // cell-kernel tile edge
+  float csf;                  // finest cell size
+  FixedScale fx;
+};
+
+enum PrepassMode : uint32_t { kPreGravity = 1, kPreCentroid = 2, kPreBin = 4 };
+
+void launch_prepass(const DeviceView& d, const SimScalars& s, uint32_t mode, cudaStream_t st);
+void launch_center(const DeviceView& d, const SimScalars& s, bool bin, cudaStream_t st);
+void launch_scan(const DeviceView& d, const SimScalars& s, cudaStream_t st);
+void launch_scatter(const DeviceView& d, const SimScalars& s, cudaStream_t st);
+void launch_cells(const DeviceView& d, const SimScalars& s, cudaStream_t st);
+void launch_manybody(const DeviceView& d, const SimScalars& s, cudaStream_t st);
+// direction 0 = incoming (reads pos, writes pos_alt), 1 = outgoing (pos_alt -> pos)
+void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool swap_back, cudaStream_t st);
+void launch_collision_grid(const DeviceView& d, const SimScalars& s, cudaStream_t st);
+void launch_collision_force(const DeviceView& d, const SimScalars& s, cudaStream_t st);
+void launch_tick_end(const DeviceView& d, cudaStream_t st);
+
+uint32_t scan_blocks(uint32_t cells);
+
+}  // namespace cgl

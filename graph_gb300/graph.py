@@ -1,0 +1,227 @@
+"""`Graph` — the reference's simulation surface over the GB300 engine.
+
+Mirrors cosmos.gl's `Graph` (src/index.ts) for the parts that drive the force
+simulation: setPointPositions / setLinks / setLinkStrength / setPointSizes /
+setPinnedPoints / render / start / stop / pause / unpause / step /
+getPointPositions / progress / isSimulationRunning / setConfig /
+setConfigPartial / destroy, and the onSimulation* callbacks.  Rendering,
+zoom, hover and picking stay in the browser and are not part of this class.
+
+As in the reference, setters stage their array BY REFERENCE and the data is
+read when `render()` runs (src/index.ts:548-574, GraphData/index.ts:123-127);
+every method is a silent no-op after `destroy()`.
+"""
+import math
+
+import numpy as np
+
+from . import _abi
+from .engine import Engine
+
+ALPHA_MIN = 0.001
+
+_CALLBACKS = ("onSimulationStart", "onSimulationTick", "onSimulationEnd", "onSimulationPause",
+              "onSimulationUnpause")
+
+
+def _to_fields(config):
+    fields = {}
+    for k, v in (config or {}).items():
+        if k in _CALLBACKS:
+            continue
+        f = _abi.CAMEL_TO_FIELD.get(k)
+        if f is None:
+            continue   # visual keys of the reference are accepted and ignored here
+        if f == "simulation_collision_radius" and v is None:
+            v = math.nan
+        if f == "enable_simulation":
+            v = 1 if v else 0
+        fields[f] = v
+    return fields
+
+
+class Graph:
+    def __init__(self, config=None, device=0):
+        config = dict(config or {})
+        self._callbacks = {k: config.get(k) for k in _CALLBACKS}
+        self._config = dict(config)
+        fields = _to_fields(config)
+        seed = fields.pop("random_seed", None)
+        cfg = _abi.make_config(device=device, **fields)
+        if seed is not None:
+            cfg.has_random_seed = 1
+            cfg.random_seed = _abi.seed_to_u64(seed)
+        self._engine = Engine(cfg)
+        self._destroyed = False
+        self._staged = {}
+
+    # --- config (src/index.ts:500-530) -------------------------------------
+    def _apply(self, merged):
+        self._callbacks = {k: merged.get(k) for k in _CALLBACKS}
+        fields = _to_fields(merged)
+        fields.pop("random_seed", None)
+        cfg = _abi.make_config(**fields)
+        self._engine.set_config(cfg)
+        self._config = merged
+
+    def setConfig(self, config):
+        if self._destroyed:
+            return
+        merged = dict(config or {})
+        if "randomSeed" in self._config:
+            merged["randomSeed"] = self._config["randomSeed"]
+        self._apply(merged)
+
+    def setConfigPartial(self, config):
+        if self._destroyed:
+            return
+        merged = dict(self._config)
+        for k, v in (config or {}).items():
+            if k == "randomSeed":
+                continue
+            if v is None:
+                merged.pop(k, None)   # explicit undefined resets to the default (config.ts:866-881)
+            else:
+                merged[k] = v
+        self._apply(merged)
+
+    @property
+    def config(self):
+        return dict(self._config)
+
+    # --- data (staged by reference, read at render) -------------------------
+    def setPointPositions(self, pointPositions, dontRescale=None):
+        if self._destroyed:
+            return
+        self._staged["positions"] = pointPositions
+
+    def setLinks(self, links):
+        if self._destroyed:
+            return
+        self._staged["links"] = links
+
+    def setLinkStrength(self, linkStrength):
+        if self._destroyed:
+            return
+        self._staged["strength"] = linkStrength
+
+    def setPointSizes(self, pointSizes):
+        if self._destroyed:
+            return
+        self._staged["sizes"] = pointSizes
+
+    def setPinnedPoints(self, pinnedIndices):
+        if self._destroyed:
+            return
+        idx = None if pinnedIndices is None or len(pinnedIndices) == 0 else pinnedIndices
+        self._engine.set_pinned_points(idx)
+
+    def render(self, simulationAlpha=None, transitionDuration=None):
+        if self._destroyed:
+            return
+        s = self._staged
+        if "positions" in s:
+            self._engine.set_point_positions(s.pop("positions"))
+        if "links" in s:
+            self._engine.set_links(s.pop("links"))
+        if "strength" in s:
+            self._engine.set_link_strength(s.pop("strength"))
+        if "sizes" in s:
+            self._engine.set_point_sizes(s.pop("sizes"))
+        self._engine.render(simulationAlpha)
+
+    # --- control (src/index.ts:1457-1540) ------------------------------------
+    def _cb(self, name, *args):
+        fn = self._callbacks.get(name)
+        if fn:
+            fn(*args)
+
+    def start(self, alpha=1.0):
+        if self._destroyed:
+            return
+        before = self._engine.state()
+        self._engine.start(alpha)
+        after = self._engine.state()
+        if after.is_simulation_running and not before.is_simulation_running:
+            self._cb("onSimulationStart")
+
+    def stop(self):
+        if self._destroyed:
+            return
+        s = self._engine.state()
+        was_active = s.is_simulation_running or s.alpha > 0 or s.progress > 0
+        self._engine.stop()
+        if was_active:
+            self._cb("onSimulationEnd")
+
+    def pause(self):
+        if self._destroyed:
+            return
+        if not self._engine.state().is_simulation_running:
+            return
+        self._engine.pause()
+        self._cb("onSimulationPause")
+
+    def unpause(self):
+        if self._destroyed:
+            return
+        if self._engine.state().is_simulation_running:
+            return
+        self._engine.unpause()
+        if self._engine.state().is_simulation_running:
+            self._cb("onSimulationUnpause")
+
+    def step(self, ticks=1):
+        """Graph.step(); `ticks` > 1 runs that many steps in one call."""
+        if self._destroyed:
+            return
+        if self._callbacks.get("onSimulationTick"):
+            for _ in range(int(ticks)):
+                self._engine.step(1)
+                self._cb("onSimulationTick", self._engine.state().alpha, None, None)
+        else:
+            self._engine.step(int(ticks))
+
+    def run(self, maxTicks):
+        """The animation-frame loop: tick while running, end once alpha < ALPHA_MIN."""
+        if self._destroyed:
+            return 0
+        was_running = self._engine.state().is_simulation_running
+        if self._callbacks.get("onSimulationTick"):
+            n = 0
+            while n < maxTicks:
+                done = self._engine.run(1)
+                if done == 0:
+                    break
+                n += 1
+                self._cb("onSimulationTick", self._engine.state().alpha, None, None)
+        else:
+            n = self._engine.run(int(maxTicks))
+        if was_running and not self._engine.state().is_simulation_running:
+            self._cb("onSimulationEnd")
+        return n
+
+    # --- read-back -------------------------------------------------------------
+    def getPointPositions(self):
+        """Positions as float32 [x0, y0, x1, y1, ...]; absent points read NaN."""
+        if self._destroyed:
+            return np.zeros(0, dtype=np.float32)
+        return self._engine.get_point_positions()
+
+    @property
+    def progress(self):
+        return 0.0 if self._destroyed else self._engine.state().progress
+
+    @property
+    def isSimulationRunning(self):
+        return False if self._destroyed else bool(self._engine.state().is_simulation_running)
+
+    @property
+    def engine(self):
+        return self._engine
+
+    def destroy(self):
+        if self._destroyed:
+            return
+        self._destroyed = True
+        self._engine.close()

@@ -1,0 +1,210 @@
+/*
+ * cgl.h — C ABI of the GB300 force-layout engine (headless cosmos.gl simulation).
+ *
+ * The engine replaces the per-tick force simulation behind cosmos.gl's `Graph`
+ * simulation surface.  Each entry point below names the reference interface it
+ * replaces (cosmos.gl `@cosmos.gl/graph` v3.4.1, paths relative to the project
+ * root).  The reference has no native FFI: its host is TypeScript calling
+ * luma.gl/WebGL2.  The binding a maintainer adds on the reference side is an
+ * N-API addon that forwards `Graph` methods to these functions.
+ *
+ * Conventions
+ *  - Plain pointers and sizes only.  Input arrays are COPIED at the call
+ *    (the reference stores them by reference and reads them at `render()`;
+ *    the data still takes effect only at `cgl_render`, as in the reference).
+ *  - Output buffers are caller-allocated host memory.
+ *  - Every call returns a cgl_status.  The reference never throws from these
+ *    methods; non-OK statuses here correspond to its console warnings/no-ops
+ *    (see cgl_last_error for the text).
+ *  - One engine handle = one CUDA stream on one device.  A handle is not
+ *    thread-safe; different handles are independent.
+ */
+#ifndef CGL_H
+#define CGL_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CGL_ABI_VERSION 1u
+
+typedef enum cgl_status {
+  CGL_OK = 0,
+  CGL_INVALID_ARG = 1,     /* bad argument; the call had no effect */
+  CGL_OOM = 2,             /* device allocation refused (HBM budget or cudaMalloc) */
+  CGL_CUDA_ERROR = 3,      /* a CUDA runtime call failed; text in cgl_last_error */
+  CGL_DEVICE_TIMEOUT = 4,  /* a bounded device-side wait gave up (status word set) */
+  CGL_DESTROYED = 5,       /* handle already destroyed (reference: silent no-op) */
+  CGL_WARNING = 6          /* call applied with an adjustment (odd length truncated, ...) */
+} cgl_status;
+
+/* Bits of cgl_config.stage_mask: which forces a tick runs (all by default).
+ * Used by stage-level parity tests; the reference always runs every enabled force. */
+enum {
+  CGL_STAGE_GRAVITY = 1u << 0,
+  CGL_STAGE_CENTER = 1u << 1,
+  CGL_STAGE_MANYBODY = 1u << 2,
+  CGL_STAGE_LINK_IN = 1u << 3,
+  CGL_STAGE_LINK_OUT = 1u << 4,
+  CGL_STAGE_COLLISION = 1u << 5,
+  CGL_STAGE_ALL = 0x3Fu
+};
+
+/* Simulation configuration.  Field meanings and defaults follow the reference:
+ * src/config.ts:56 (spaceSize), :369-456 (simulation*), :771 (randomSeed);
+ * defaults src/variables.ts:10,15,19,69-82,147-148.  Fill with
+ * cgl_config_defaults() and override.  "undefined" in the reference maps to
+ * NaN for simulation_collision_radius and to has_random_seed = 0. */
+typedef struct cgl_config {
+  double space_size;                         /* spaceSize, default 4096 */
+  double simulation_decay;                   /* default 5000 */
+  double simulation_gravity;                 /* default 0.25 */
+  double simulation_center;                  /* default 0 */
+  double simulation_repulsion;               /* default 1.0 */
+  double simulation_repulsion_theta;         /* default 1.15; accepted and ignored (deprecated no-op in the reference, config.ts) */
+  double simulation_link_spring;             /* default 1 */
+  double simulation_link_distance;           /* default 10 */
+  double simulation_link_dist_random_variation_range[2]; /* default [1, 1.2] */
+  double simulation_friction;                /* default 0.85 */
+  double simulation_collision;               /* default 0 (off) */
+  double simulation_collision_radius;        /* default NaN (= undefined: radius from point sizes) */
+  double simulation_collision_padding;       /* default 0 */
+  double point_default_size;                 /* default 4 (collision radius source) */
+  int32_t enable_simulation;                 /* default 1 */
+  int32_t has_random_seed;                   /* 0 = reference's unseeded generator (engine seeds from entropy) */
+  uint64_t random_seed;                      /* randomSeed; init-only, as in the reference */
+  double max_texture_dimension;              /* WebGL maxTextureDimension2D used by Store.adjustSpaceSize; 0 = no limit */
+  uint32_t stage_mask;                       /* CGL_STAGE_* bits, default CGL_STAGE_ALL */
+  int32_t device;                            /* CUDA device ordinal, default 0 */
+  double hbm_budget_bytes;                   /* device-memory admission budget for this handle; 0 = unlimited */
+} cgl_config;
+
+typedef struct cgl_state {
+  double alpha;               /* Store.alpha (FP64 on the host, as in JS) */
+  double progress;            /* Graph.progress = simulationProgress */
+  int32_t is_simulation_running;
+  int32_t destroyed;
+  uint64_t tick;              /* ticks run since create */
+  uint64_t points_number;     /* applied point count (after render) */
+  uint64_t links_number;      /* applied link count, including links skipped for invalid endpoints */
+  uint64_t rng_draws;         /* random draws consumed so far */
+} cgl_state;
+
+typedef struct cgl_engine cgl_engine;
+
+/* Fill *cfg with the reference's defaults (src/variables.ts). */
+void cgl_config_defaults(cgl_config* cfg);
+
+/* new Graph(div, config) — src/index.ts:167-464.  Selects the device, applies
+ * Store.adjustSpaceSize (Store/index.ts:209-233) and the random seed (:452). */
+cgl_status cgl_create(const cgl_config* cfg, cgl_engine** out);
+
+/* Graph.destroy() — src/index.ts:1545.  Frees all device memory. */
+cgl_status cgl_destroy(cgl_engine* e);
+
+/* Graph.setConfig(config) — src/index.ts:500-509 (full replacement; randomSeed is
+ * init-only and preserved, :1720-1724; a spaceSize change re-runs update, :1844-1851).
+ * Partial updates (setConfigPartial, :519) are merged by the host shim. */
+cgl_status cgl_set_config(cgl_engine* e, const cgl_config* cfg);
+cgl_status cgl_get_config(cgl_engine* e, cgl_config* out);
+
+/* Graph.setPointPositions(Float32Array) — src/index.ts:548-574.  xy = [x0,y0,x1,y1,...];
+ * a NaN in either coordinate marks the point absent (helper.ts:157-159).  An odd
+ * length drops the trailing value with CGL_WARNING (GraphData/index.ts:117-120). */
+cgl_status cgl_set_point_positions(cgl_engine* e, const float* xy, uint64_t n_floats);
+
+/* Graph.setLinks(Float32Array) — src/index.ts:723-734.  st = [s0,t0,s1,t1,...] of
+ * point indices as floats; links with an invalid endpoint are skipped but keep
+ * their index (GraphData/index.ts:534-547).  Odd length: CGL_WARNING (:296-299). */
+cgl_status cgl_set_links(cgl_engine* e, const float* st, uint64_t n_floats);
+
+/* Graph.setLinkStrength(Float32Array) — src/index.ts:836-841.  NULL/0 clears. */
+cgl_status cgl_set_link_strength(cgl_engine* e, const float* strength, uint64_t n);
+
+/* Graph.setPointSizes(Float32Array) — src/index.ts (setPointSizes); sizes feed the
+ * collision radius (ForceCollision/index.ts:68-74, GraphData/index.ts:189-194). */
+cgl_status cgl_set_point_sizes(cgl_engine* e, const float* sizes, uint64_t n);
+
+/* Graph.setPinnedPoints(number[] | null) — src/index.ts:912-918; applied at once
+ * (Points/index.ts:1264-1304).  Non-integer or out-of-range indices are ignored. */
+cgl_status cgl_set_pinned_points(cgl_engine* e, const double* indices, uint64_t n);
+
+/* Graph.render(simulationAlpha?) — src/index.ts:936-1003: ingests staged data
+ * (GraphData.update :443-462, Graph.update :1987-1994, Graph.create :1635-1688).
+ * alpha = NaN keeps the current alpha. */
+cgl_status cgl_render(cgl_engine* e, double alpha);
+
+/* Graph.start(alpha = 1) — src/index.ts:1457-1476. */
+cgl_status cgl_start(cgl_engine* e, double alpha);
+/* Graph.stop() — src/index.ts:1482-1489. */
+cgl_status cgl_stop(cgl_engine* e);
+/* Graph.pause() — src/index.ts:1496-1502. */
+cgl_status cgl_pause(cgl_engine* e);
+/* Graph.unpause() — src/index.ts:1510-1521. */
+cgl_status cgl_unpause(cgl_engine* e);
+
+/* Graph.step() × ticks — src/index.ts:1528-1540 → runSimulationStep(true)
+ * (:2006-2099).  Runs even when paused.  Asynchronous on the engine stream. */
+cgl_status cgl_step(cgl_engine* e, uint32_t ticks);
+
+/* The requestAnimationFrame loop (frame() :2152-2177 → renderFrame :2237-2278):
+ * while running, end the simulation when alpha < ALPHA_MIN before a tick
+ * (:2164-2169, end() :2335-2339), else run a tick; at most max_ticks ticks. */
+cgl_status cgl_run(cgl_engine* e, uint32_t max_ticks, uint32_t* ticks_done);
+
+/* Graph.getPointPositions() — src/index.ts:1106-1129; absent points read NaN.
+ * out_xy holds 2 * points_number floats.  Synchronises the engine stream. */
+cgl_status cgl_get_point_positions(cgl_engine* e, float* out_xy, uint64_t capacity_floats);
+
+/* Graph.progress / Graph.isSimulationRunning — src/index.ts:469, :477. */
+cgl_status cgl_get_state(cgl_engine* e, cgl_state* out);
+
+/* Text of the last error or warning on this handle ("" if none). */
+const char* cgl_last_error(cgl_engine* e);
+
+/* --- Engine extensions (no counterpart in the reference) ------------------- */
+
+/* Run the engine's kernels on a caller-owned cudaStream_t (NULL = engine's own). */
+cgl_status cgl_set_stream(cgl_engine* e, void* cuda_stream);
+/* Block until all queued work on the engine stream finished. */
+cgl_status cgl_synchronize(cgl_engine* e);
+/* Average device time per tick stage over `ticks` profiled ticks, in ms, via CUDA
+ * events between stages (no CUDA graph).  Stage order: see CGL_NUM_STAGE_TIMES. */
+#define CGL_NUM_STAGE_TIMES 10
+cgl_status cgl_profile_stages(cgl_engine* e, uint32_t ticks, double* ms_out /*[CGL_NUM_STAGE_TIMES]*/);
+
+/* Static layout facts of the applied data (for tests, benches and byte models). */
+typedef struct cgl_layout {
+  uint64_t points_number;      /* N */
+  uint64_t live_points;        /* N minus absent points */
+  uint64_t links_number;       /* E as given (pairs) */
+  uint64_t link_entries_in;    /* valid links in the incoming CSR (== outgoing) */
+  uint32_t points_texture_size;/* T = ceil(sqrt(N)) */
+  uint32_t finest_grid;        /* G_f */
+  uint32_t levels;             /* L */
+  uint32_t max_degree_in;      /* longest link list, incoming direction */
+  uint32_t max_degree_out;
+  int32_t fixed_point_bits;    /* F: cell sums are exact integers in units of 2^-F */
+  float fixed_point_bound;     /* |coordinate| saturates at this bound inside cell sums */
+  uint32_t collision_grid;     /* collision grid size (0 until collision first runs) */
+  float collision_cell_size;
+  uint64_t device_bytes;       /* device memory held by the handle */
+  uint32_t kernels_per_tick;   /* kernel launches one tick makes with the current data and config */
+  uint32_t reserved;
+} cgl_layout;
+cgl_status cgl_get_layout(cgl_engine* e, cgl_layout* out);
+
+/* Test hooks: state retained from the last tick's many-body pass. */
+/* level l in [0, L): 4 floats per cell (centroid x, centroid y, count, slots), row-major. */
+cgl_status cgl_debug_get_cells(cgl_engine* e, uint32_t level, float* out, uint64_t capacity_floats);
+/* finest level: 8 point indices per cell in slot (hash) order, -1 = empty slot. */
+cgl_status cgl_debug_get_slots(cgl_engine* e, int32_t* out, uint64_t capacity);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CGL_H */

@@ -1,0 +1,70 @@
+"""CPU tests of the C ABI library: it builds, loads, exports every declared
+symbol, and its defaults match the reference.  No compute calls (no GPU here)."""
+import ctypes as C
+import math
+import os
+import re
+
+import pytest
+
+from graph_gb300 import _abi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "cgl.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(cgl_[a-z_0-9]+)\s*\(", src)))
+
+
+def test_header_declares_the_simulation_surface():
+    names = declared_functions()
+    for fn in ["cgl_create", "cgl_destroy", "cgl_set_config", "cgl_set_point_positions", "cgl_set_links",
+               "cgl_set_link_strength", "cgl_set_point_sizes", "cgl_set_pinned_points", "cgl_render",
+               "cgl_start", "cgl_stop", "cgl_pause", "cgl_unpause", "cgl_step", "cgl_run",
+               "cgl_get_point_positions", "cgl_get_state", "cgl_last_error"]:
+        assert fn in names
+
+
+def test_library_exports_every_declared_symbol(engine_lib):
+    missing = [fn for fn in declared_functions() if not hasattr(engine_lib, fn)]
+    assert not missing, missing
+
+
+def test_config_defaults_match_reference(engine_lib):
+    c = _abi.Config()
+    engine_lib.cgl_config_defaults(C.byref(c))
+    got = _abi.config_to_dict(c)
+    for k, v in _abi.DEFAULTS.items():
+        if isinstance(v, float) and math.isnan(v):
+            assert math.isnan(got[k]), k
+        elif k == "simulation_link_dist_random_variation_range":
+            assert tuple(got[k]) == tuple(v)
+        else:
+            assert got[k] == v, k
+
+
+def test_struct_sizes_match_header():
+    # natural C layout: doubles and uint64 aligned to 8
+    assert C.sizeof(_abi.Config) == 160
+    assert C.sizeof(_abi.State) == 56
+    assert C.sizeof(_abi.Layout) == 88
+
+
+def test_create_without_gpu_fails_loudly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from graph_gb300.engine import Engine
+    from graph_gb300._calls import StatusError
+    with pytest.raises(StatusError):
+        Engine(random_seed=1)
+
+
+def test_seed_mapping():
+    assert _abi.seed_to_u64(5) == 5
+    assert _abi.seed_to_u64(-1) == (1 << 64) - 1
+    assert _abi.seed_to_u64("abc") == _abi.seed_to_u64("abc") != _abi.seed_to_u64("abd")
+    assert _abi.seed_to_u64(2.0) == 2
