@@ -211,6 +211,9 @@ def main():
     ap.add_argument("--workload", default="sbm1m", choices=["sbm1m", "ba10k"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of oracle ticks for cpu_baseline")
+    ap.add_argument("--save-positions", default=None, help="write the final positions (.npy) for profiling runs")
+    ap.add_argument("--positions-from", default=None, help="start from saved positions (.npy) instead of the seeded ones")
+    ap.add_argument("--quick", action="store_true", help="timed ticks only: no stage profile, e2e or CPU baseline")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -233,6 +236,9 @@ def main():
         dist.init_process_group("nccl")
 
     pos, links, fields, desc = make_workload(args.workload, seed=1 + rank)
+    if args.positions_from:
+        pos = np.load(args.positions_from).astype(np.float32)
+        desc += " (evolved positions from %s)" % os.path.basename(args.positions_from)
     from graph_gb300.engine import Engine
     eng = Engine(**dict(fields, device=local_rank))
     eng.set_point_positions(pos)
@@ -268,6 +274,14 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = live * args.steps * world / (ms / 1e3)
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "steps": args.steps,
+                              "ms_per_step": ms / args.steps, "quick": True, "config": {"workload": desc}}))
+        if args.save_positions and rank == 0:
+            np.save(args.save_positions, eng.get_point_positions())
+        eng.close()
+        return
 
     # per-stage device times (events between the tick's kernels, no graph)
     stages = eng.profile_stages(20)
@@ -332,6 +346,8 @@ def main():
             "clocks": clk,
         }
         print(json.dumps(out))
+        if args.save_positions:
+            np.save(args.save_positions, eng.get_point_positions())
     eng.close()
     if dist:
         dist.destroy_process_group()

@@ -85,6 +85,7 @@ struct cgl_engine {
   size_t dev_bytes = 0;
   DevBuf b_pos, b_pos_alt, b_flags, b_jitter, b_key, b_rank, b_sorted_idx, b_sorted_pos;
   DevBuf b_counts, b_cell_start, b_block_sums, b_tickets, b_rec, b_acc, b_centroid;
+  DevBuf b_big_list, b_big_count, b_big_sx, b_big_sy, b_big_ns;
   DevBuf b_params, b_tick_ctr;
   DevBuf b_rowptr_in, b_rowptr_out, b_ent_in, b_ent_out;
   DevBuf b_size, b_cgrid_acc, b_cgrid;
@@ -154,7 +155,8 @@ void dev_free_all(cgl_engine* e) {
                    &e->b_sorted_idx, &e->b_sorted_pos, &e->b_counts, &e->b_cell_start, &e->b_block_sums,
                    &e->b_tickets, &e->b_rec, &e->b_acc, &e->b_centroid, &e->b_params, &e->b_tick_ctr,
                    &e->b_rowptr_in, &e->b_rowptr_out, &e->b_ent_in, &e->b_ent_out, &e->b_size,
-                   &e->b_cgrid_acc, &e->b_cgrid};
+                   &e->b_cgrid_acc, &e->b_cgrid, &e->b_big_list, &e->b_big_count,
+                   &e->b_big_sx, &e->b_big_sy, &e->b_big_ns};
   for (DevBuf* b : all) {
     if (b->p) cudaFree(b->p);
     b->p = nullptr;
@@ -221,6 +223,11 @@ void refresh_view(cgl_engine* e) {
   d.block_sums = (uint32_t*)e->b_block_sums.p;
   d.scan_ticket = (uint32_t*)e->b_tickets.p;
   d.cells_ticket = d.scan_ticket ? d.scan_ticket + 1 : nullptr;
+  d.big_list = (uint32_t*)e->b_big_list.p;
+  d.big_count = (uint32_t*)e->b_big_count.p;
+  d.big_sx = (long long*)e->b_big_sx.p;
+  d.big_sy = (long long*)e->b_big_sy.p;
+  d.big_ns = (uint32_t*)e->b_big_ns.p;
   d.rec = (float4*)e->b_rec.p;
   d.acc = (long long*)e->b_acc.p;
   std::memcpy(d.level_off, e->level_off, sizeof(d.level_off));
@@ -289,6 +296,7 @@ cgl_status enqueue_tick(cgl_engine* e, cudaStream_t st, cudaEvent_t* ev) {
     if (ev) cudaEventRecord(ev[2 * stage + which], st);
   };
   if (p.cent) CU(cudaMemsetAsync(d.centroid, 0, 3 * sizeof(long long), st));
+  if (p.mb) CU(cudaMemsetAsync(d.big_count, 0, 2 * sizeof(uint32_t), st));
   uint32_t mode = 0;
   if (p.grav) mode |= kPreGravity;
   if (p.cent) mode |= kPreCentroid;
@@ -560,6 +568,11 @@ cgl_status do_render(cgl_engine* e, double alpha) {
       if ((st = dev_reserve(e, e->b_rec, off * sizeof(float4), true))) return st;
       if ((st = dev_reserve(e, e->b_acc, 3 * (size_t)aoff * sizeof(long long), true))) return st;
       if ((st = dev_reserve(e, e->b_centroid, 3 * sizeof(long long), true))) return st;
+      if ((st = dev_reserve(e, e->b_big_list, 2 * (size_t)cells * sizeof(uint32_t), false))) return st;
+      if ((st = dev_reserve(e, e->b_big_count, 2 * sizeof(uint32_t), true))) return st;
+      if ((st = dev_reserve(e, e->b_big_sx, cells * sizeof(long long), false))) return st;
+      if ((st = dev_reserve(e, e->b_big_sy, cells * sizeof(long long), false))) return st;
+      if ((st = dev_reserve(e, e->b_big_ns, cells * sizeof(uint32_t), false))) return st;
       std::vector<float2> jit(n);
       const uint64_t texels = (uint64_t)e->T * e->T;
       for (uint64_t t = 0; t < texels; ++t) {
@@ -911,7 +924,7 @@ cgl_status cgl_get_layout(cgl_engine* e, cgl_layout* o) {
   uint32_t k = 1;                                      // tick end
   if (p.grav || p.cent || p.mb) k += 1;                // prepass
   if (p.cent) k += 1;
-  if (p.mb) k += 5;                                    // scan (2), scatter, cells, manybody
+  if (p.mb) k += 6;                                    // scan (2), scatter, big cells, cells, manybody
   k += (uint32_t)p.link_in + (uint32_t)p.link_out;
   if (p.coll) k += 3;                                  // grid, convert, force
   o->kernels_per_tick = k;

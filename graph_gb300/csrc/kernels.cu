@@ -218,6 +218,8 @@ __global__ void __launch_bounds__(kBlock) k_scan_down(DeviceView d, uint32_t cel
     if (c < cells) {
       d.cell_start[c] = off;
       d.counts[c] = 0;   // histogram ready for the next tick
+      if (v[k] > kBigCell) d.big_list[atomicAdd(&d.big_count[0], 1u)] = c;
+      else if (v[k] > kSmallCell) d.big_list[cells + atomicAdd(&d.big_count[1], 1u)] = c;
     }
     off += v[k];
   }
@@ -236,54 +238,34 @@ __global__ void __launch_bounds__(kBlock) k_scatter(DeviceView d) {
 }
 
 // ------------------------------------------------------------------ cells --
-// One thread per finest cell, one CTA per tile x tile block of cells.
-__global__ void k_cells(DeviceView d, SimScalars s) {
-  extern __shared__ long long sm[];   // 3 * tile * tile
-  const TickParams tp = tick_params(d);
-  const int T = s.tile;
-  const int tiles_row = s.gf / T;
-  const int tile_x = blockIdx.x % tiles_row, tile_y = blockIdx.x / tiles_row;
-  const int tx = threadIdx.x % T, ty = threadIdx.x / T;
-  const int cx = tile_x * T + tx, cy = tile_y * T + ty;
-  const uint32_t c = (uint32_t)(cy * s.gf + cx);
-  const uint32_t b = d.cell_start[c], e = d.cell_start[c + 1];
-
-  // exact sums and the 8 smallest distinct peel hashes (build-nearfield-slots.vert)
-  long long ax = 0, ay = 0;
-  unsigned long long best[kSlots];
-  uint32_t at[kSlots];
+// Insert (hash bits, index) into a sorted list of the 8 smallest DISTINCT
+// hashes, each kept with its lowest index (the peel's tie rule,
+// build-nearfield-slots.vert:146-162); `at` tracks segment positions.
+__device__ __forceinline__ void top8_insert(unsigned long long (&best)[kSlots], uint32_t (&at)[kSlots],
+                                            unsigned long long key, uint32_t pos) {
+  const uint32_t hb = (uint32_t)(key >> 32);
+  bool dup = false;
 #pragma unroll
-  for (int q = 0; q < kSlots; ++q) { best[q] = ~0ull; at[q] = 0; }
-  for (uint32_t j = b; j < e; ++j) {
-    const float2 p = d.sorted_pos[j];
-    ax += to_fixed(p.x, s.fx);
-    ay += to_fixed(p.y, s.fx);
-    const uint32_t idx = d.sorted_idx[j];
-    const uint32_t hb = __float_as_uint(peel_hash(idx, tp.seed_bits));
-    unsigned long long key = ((unsigned long long)hb << 32) | idx;
-    bool dup = false;
+  for (int q = 0; q < kSlots; ++q) {
+    if ((uint32_t)(best[q] >> 32) == hb && best[q] != ~0ull) {
+      dup = true;
+      if (key < best[q]) { best[q] = key; at[q] = pos; }
+    }
+  }
+  if (!dup && key < best[kSlots - 1]) {
 #pragma unroll
     for (int q = 0; q < kSlots; ++q) {
-      if ((uint32_t)(best[q] >> 32) == hb && best[q] != ~0ull) {
-        dup = true;
-        if (key < best[q]) { best[q] = key; at[q] = j; }
-      }
-    }
-    if (!dup && key < best[kSlots - 1]) {
-      uint32_t apos = j;
-#pragma unroll
-      for (int q = 0; q < kSlots; ++q) {
-        if (key < best[q]) {
-          unsigned long long tk = best[q]; best[q] = key; key = tk;
-          uint32_t ta = at[q]; at[q] = apos; apos = ta;
-        }
+      if (key < best[q]) {
+        unsigned long long tk = best[q]; best[q] = key; key = tk;
+        uint32_t ta = at[q]; at[q] = pos; pos = ta;
       }
     }
   }
-  int ns = 0;
-#pragma unroll
-  for (int q = 0; q < kSlots; ++q) ns += best[q] != ~0ull;
-  // move the slots to the head of the segment, in hash order
+}
+
+// Move the ns selected entries to the head of the segment starting at b, in
+// slot (hash) order; the rest of the segment keeps its points in any order.
+__device__ __forceinline__ void move_slots_to_head(const DeviceView& d, uint32_t b, int ns, uint32_t (&at)[kSlots]) {
 #pragma unroll
   for (int q = 0; q < kSlots; ++q) {
     if (q < ns) {
@@ -298,6 +280,223 @@ __global__ void k_cells(DeviceView d, SimScalars s) {
           if (at[r] == tq) at[r] = pq;
       }
     }
+  }
+}
+
+__device__ __forceinline__ unsigned long long peel_key(uint32_t idx, uint32_t seed_bits) {
+  return ((unsigned long long)__float_as_uint(peel_hash(idx, seed_bits)) << 32) | idx;
+}
+
+// Cells holding more than kSmallCell points (lists built by the scan): above
+// kBigCell one CTA per cell, otherwise one warp per cell, so a dense hub cell
+// does not serialise on one thread.  Exact sums by warp/block reduction; slots
+// by per-thread top-8 lists merged in 8 rounds of a minimum over keys whose
+// hash is larger than the previous slot's.  Every global top-8 key is in the
+// top-8 of the thread that holds it, so the merge is exact.
+__device__ void warp_cell(const DeviceView& d, const SimScalars& s, uint32_t seed_bits, uint32_t c) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t b = d.cell_start[c], e = d.cell_start[c + 1];
+  long long ax = 0, ay = 0;
+  unsigned long long best[kSlots];
+  uint32_t at[kSlots];
+#pragma unroll
+  for (int q = 0; q < kSlots; ++q) { best[q] = ~0ull; at[q] = 0; }
+  for (uint32_t j = b + lane; j < e; j += 32) {
+    const float2 p = d.sorted_pos[j];
+    ax += to_fixed(p.x, s.fx);
+    ay += to_fixed(p.y, s.fx);
+    top8_insert(best, at, peel_key(d.sorted_idx[j], seed_bits), j);
+  }
+  ax = warp_sum_ll(ax);
+  ay = warp_sum_ll(ay);
+  uint32_t sel[kSlots];
+  int ns = 0;
+  unsigned long long last = 0;
+#pragma unroll
+  for (int k = 0; k < kSlots; ++k) {
+    unsigned long long m = ~0ull;
+    uint32_t mp = 0;
+#pragma unroll
+    for (int q = 0; q < kSlots; ++q)
+      if (best[q] != ~0ull && (k == 0 || (best[q] >> 32) > (last >> 32)) && best[q] < m) { m = best[q]; mp = at[q]; }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long om = __shfl_xor_sync(0xffffffffu, m, o);
+      const uint32_t op = __shfl_xor_sync(0xffffffffu, mp, o);
+      if (om < m) { m = om; mp = op; }
+    }
+    sel[k] = mp;
+    if (m != ~0ull) { ns = k + 1; last = m; }
+    else last = ~0ull;
+  }
+  // Move the slots to the head [b, b + ns) in slot order, in parallel: lane q
+  // takes slot q's entry; a head entry that is not a slot moves to the place
+  // of the r-th slot that lies outside the head (r = its rank among them).
+  uint32_t take_idx = 0, disp_idx = 0, dest = 0;
+  float2 take_pos = make_float2(0.f, 0.f), disp_pos = make_float2(0.f, 0.f);
+  bool displaced = false;
+  const uint32_t h = b + (uint32_t)lane;
+  bool h_selected = false, sel_outside = false;
+#pragma unroll
+  for (int k = 0; k < kSlots; ++k) {
+    if (k < ns && sel[k] == h) h_selected = true;
+    if (k == lane) sel_outside = k < ns && (sel[k] < b || sel[k] >= b + (uint32_t)ns);
+  }
+  const unsigned out_mask = __ballot_sync(0xffffffffu, sel_outside);
+  const bool in_head = lane < ns;
+  displaced = in_head && !h_selected;
+  const unsigned disp_mask = __ballot_sync(0xffffffffu, displaced);
+  if (in_head) {
+    uint32_t src = 0;
+#pragma unroll
+    for (int k = 0; k < kSlots; ++k) if (k == lane) src = sel[k];
+    take_idx = d.sorted_idx[src];
+    take_pos = d.sorted_pos[src];
+  }
+  if (displaced) {
+    const int r = __popc(disp_mask & ((1u << lane) - 1u));
+    unsigned m = out_mask;
+    for (int t = 0; t < r; ++t) m &= m - 1u;
+    const int k = __ffs(m) - 1;
+#pragma unroll
+    for (int kk = 0; kk < kSlots; ++kk) if (kk == k) dest = sel[kk];
+    disp_idx = d.sorted_idx[h];
+    disp_pos = d.sorted_pos[h];
+  }
+  __syncwarp();
+  if (in_head) {
+    d.sorted_idx[h] = take_idx;
+    d.sorted_pos[h] = take_pos;
+  }
+  if (displaced) {
+    d.sorted_idx[dest] = disp_idx;
+    d.sorted_pos[dest] = disp_pos;
+  }
+  if (lane == 0) {
+    d.big_sx[c] = ax;
+    d.big_sy[c] = ay;
+    d.big_ns[c] = (uint32_t)ns;
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_bigcells(DeviceView d, SimScalars s) {
+  __shared__ unsigned long long skey[kBlock * kSlots];
+  __shared__ uint32_t spos[kBlock * kSlots];
+  __shared__ unsigned long long wmin[kBlock / 32];
+  __shared__ uint32_t wpos[kBlock / 32];
+  __shared__ unsigned long long sel_key;
+  __shared__ uint32_t sel_at[kSlots];
+  __shared__ int sel_n;
+  const TickParams tp = tick_params(d);
+  const uint32_t nbig = d.big_count[0];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (uint32_t wi = blockIdx.x; wi < nbig; wi += gridDim.x) {
+    const uint32_t c = d.big_list[wi];
+    const uint32_t b = d.cell_start[c], e = d.cell_start[c + 1];
+    long long ax = 0, ay = 0;
+    unsigned long long best[kSlots];
+    uint32_t at[kSlots];
+#pragma unroll
+    for (int q = 0; q < kSlots; ++q) { best[q] = ~0ull; at[q] = 0; }
+    for (uint32_t j = b + threadIdx.x; j < e; j += blockDim.x) {
+      const float2 p = d.sorted_pos[j];
+      ax += to_fixed(p.x, s.fx);
+      ay += to_fixed(p.y, s.fx);
+      top8_insert(best, at, peel_key(d.sorted_idx[j], tp.seed_bits), j);
+    }
+#pragma unroll
+    for (int q = 0; q < kSlots; ++q) { skey[threadIdx.x * kSlots + q] = best[q]; spos[threadIdx.x * kSlots + q] = at[q]; }
+    // exact sums: warp then block reduction (integers, order-free)
+    ax = warp_sum_ll(ax); ay = warp_sum_ll(ay);
+    __shared__ long long rx[kBlock / 32], ry[kBlock / 32];
+    if (lane == 0) { rx[w] = ax; ry[w] = ay; }
+    if (threadIdx.x == 0) sel_n = 0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      long long tx = 0, ty = 0;
+      for (int k = 0; k < kBlock / 32; ++k) { tx += rx[k]; ty += ry[k]; }
+      d.big_sx[c] = tx;
+      d.big_sy[c] = ty;
+    }
+    unsigned long long last = 0;
+    for (int k = 0; k < kSlots; ++k) {
+      unsigned long long m = ~0ull;
+      uint32_t mp = 0;
+#pragma unroll
+      for (int q = 0; q < kSlots; ++q) {
+        const unsigned long long key = skey[threadIdx.x * kSlots + q];
+        if (key != ~0ull && (k == 0 || (key >> 32) > (last >> 32)) && key < m) { m = key; mp = spos[threadIdx.x * kSlots + q]; }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long om = __shfl_xor_sync(0xffffffffu, m, o);
+        const uint32_t op = __shfl_xor_sync(0xffffffffu, mp, o);
+        if (om < m) { m = om; mp = op; }
+      }
+      if (lane == 0) { wmin[w] = m; wpos[w] = mp; }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        unsigned long long bm = ~0ull;
+        uint32_t bp = 0;
+        for (int k2 = 0; k2 < kBlock / 32; ++k2)
+          if (wmin[k2] < bm) { bm = wmin[k2]; bp = wpos[k2]; }
+        sel_key = bm;
+        if (bm != ~0ull) { sel_at[sel_n] = bp; sel_n = sel_n + 1; }
+      }
+      __syncthreads();
+      last = sel_key;
+      if (last == ~0ull) break;
+    }
+    if (threadIdx.x == 0) {
+      const int ns = sel_n;
+      uint32_t pat[kSlots];
+#pragma unroll
+      for (int q = 0; q < kSlots; ++q) pat[q] = q < ns ? sel_at[q] : 0;
+      move_slots_to_head(d, b, ns, pat);
+      d.big_ns[c] = (uint32_t)ns;
+    }
+    __syncthreads();
+  }
+  // medium cells: one warp each
+  const uint32_t nmid = d.big_count[1];
+  const uint32_t cells = (uint32_t)(s.gf * s.gf);
+  const uint32_t wid = blockIdx.x * (blockDim.x >> 5) + w, nw = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t wi = wid; wi < nmid; wi += nw) warp_cell(d, s, tp.seed_bits, d.big_list[cells + wi]);
+}
+
+// One thread per finest cell, one CTA per tile x tile block of cells.
+__global__ void k_cells(DeviceView d, SimScalars s) {
+  extern __shared__ long long sm[];   // 3 * tile * tile
+  const TickParams tp = tick_params(d);
+  const int T = s.tile;
+  const int tiles_row = s.gf / T;
+  const int tile_x = blockIdx.x % tiles_row, tile_y = blockIdx.x / tiles_row;
+  const int tx = threadIdx.x % T, ty = threadIdx.x / T;
+  const int cx = tile_x * T + tx, cy = tile_y * T + ty;
+  const uint32_t c = (uint32_t)(cy * s.gf + cx);
+  const uint32_t b = d.cell_start[c], e = d.cell_start[c + 1];
+
+  // exact sums and the 8 smallest distinct peel hashes (build-nearfield-slots.vert)
+  long long ax = 0, ay = 0;
+  int ns = 0;
+  if (e - b > kSmallCell) {   // done cooperatively by k_bigcells
+    ax = d.big_sx[c];
+    ay = d.big_sy[c];
+    ns = (int)d.big_ns[c];
+  } else {
+    unsigned long long best[kSlots];
+    uint32_t at[kSlots];
+#pragma unroll
+    for (int q = 0; q < kSlots; ++q) { best[q] = ~0ull; at[q] = 0; }
+    for (uint32_t j = b; j < e; ++j) {
+      const float2 p = d.sorted_pos[j];
+      ax += to_fixed(p.x, s.fx);
+      ay += to_fixed(p.y, s.fx);
+      top8_insert(best, at, peel_key(d.sorted_idx[j], tp.seed_bits), j);
+    }
+#pragma unroll
+    for (int q = 0; q < kSlots; ++q) ns += best[q] != ~0ull;
+    move_slots_to_head(d, b, ns, at);
   }
   const uint32_t cnt = e - b;
   {
@@ -401,31 +600,44 @@ __global__ void __launch_bounds__(kBlock) k_manybody(DeviceView d, SimScalars s)
   const int fcx = cell_index(px, s.csf, gf), fcy = cell_index(py, s.csf, gf);
   const float k = __fmul_rn(tp.alpha, s.repulsion);
   float vx = 0.f, vy = 0.f;
-  for (int l = 0; l < L; ++l) {
+  {   // level 0 (force-level.frag:70-79): every cell of the 4x4 grid outside the 3x3
+    const int sh = L - 1;
+    const int ex = (fcx >> sh) - 1, ey = (fcy >> sh) - 1;   // first column / row of the 3x3
+    const float4* lv = d.rec;
+    float lx = 0.f, ly = 0.f;
+#pragma unroll 1
+    for (int jj = 0; jj < 4; ++jj) {
+      const bool row_in = (unsigned)(jj - ey) <= 2u;
+#pragma unroll 1
+      for (int ii = 0; ii < 4; ++ii) {
+        if (row_in && (unsigned)(ii - ex) <= 2u) continue;
+        cell_velocity(__ldg(&lv[jj * 4 + ii]), px, py, k, lx, ly);
+      }
+    }
+    vx = __fadd_rn(vx, lx);
+    vy = __fadd_rn(vy, ly);
+  }
+  for (int l = 1; l < L; ++l) {   // force-level.frag:80-95: aligned 6x6 child block minus the 3x3
     const int G = 4 << l;
     const int sh = L - 1 - l;
     const int pcx = fcx >> sh, pcy = fcy >> sh;
+    const int bx = (pcx & ~1) - 2, by = (pcy & ~1) - 2;
+    const int ex = pcx - 1, ey = pcy - 1;
     const float4* lv = d.rec + d.level_off[l];
     float lx = 0.f, ly = 0.f;
-    if (l == 0) {   // force-level.frag:70-79
-#pragma unroll
-      for (int jj = 0; jj < 4; ++jj)
-#pragma unroll
-        for (int ii = 0; ii < 4; ++ii) {
-          if (max(abs(ii - pcx), abs(jj - pcy)) <= 1) continue;
-          cell_velocity(__ldg(&lv[jj * 4 + ii]), px, py, k, lx, ly);
-        }
-    } else {        // force-level.frag:80-95
-      const int bx = (pcx / 2) * 2 - 2, by = (pcy / 2) * 2 - 2;
-#pragma unroll
-      for (int jj = 0; jj < 6; ++jj)
-#pragma unroll
-        for (int ii = 0; ii < 6; ++ii) {
-          const int cx = bx + ii, cy = by + jj;
-          if (cx < 0 || cy < 0 || cx >= G || cy >= G) continue;
-          if (max(abs(cx - pcx), abs(cy - pcy)) <= 1) continue;
-          cell_velocity(__ldg(&lv[cy * G + cx]), px, py, k, lx, ly);
-        }
+#pragma unroll 1
+    for (int jj = 0; jj < 6; ++jj) {
+      const int cy = by + jj;
+      if ((unsigned)cy >= (unsigned)G) continue;
+      const bool row_in = (unsigned)(cy - ey) <= 2u;
+      const float4* row = lv + cy * G;
+#pragma unroll 1
+      for (int ii = 0; ii < 6; ++ii) {
+        const int cx = bx + ii;
+        if ((unsigned)cx >= (unsigned)G) continue;
+        if (row_in && (unsigned)(cx - ex) <= 2u) continue;
+        cell_velocity(__ldg(&row[cx]), px, py, k, lx, ly);
+      }
     }
     vx = __fadd_rn(vx, lx);
     vy = __fadd_rn(vy, ly);
@@ -435,9 +647,9 @@ __global__ void __launch_bounds__(kBlock) k_manybody(DeviceView d, SimScalars s)
   const float self = (float)i;
   const float4* fine = d.rec + d.level_off[L - 1];
   float nx = 0.f, ny = 0.f;
-#pragma unroll
+#pragma unroll 1
   for (int jj = -1; jj <= 1; ++jj)
-#pragma unroll
+#pragma unroll 1
     for (int ii = -1; ii <= 1; ++ii) {
       const int cx = fcx + ii, cy = fcy + jj;
       if (cx < 0 || cy < 0 || cx >= gf || cy >= gf) continue;
@@ -491,12 +703,11 @@ __global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, con
   const float span = __fsub_rn(s.link_r1, s.link_r0);
   float vx = 0.f, vy = 0.f;
   const uint32_t e0 = rowptr[p], e1 = rowptr[p + 1];
-  for (uint32_t at = e0; at < e1; ++at) {
-    const uint4 en = __ldg(&ent[at]);
-    if (en.x == kAbsentTarget) continue;
+  // The loads do not depend on the running velocity: issue them kLinkBatch
+  // links ahead, then apply the springs strictly in list order.
+  auto spring = [&](const uint4 en, const float2 q) {
     float dd = __fadd_rn(__fmul_rn(__uint_as_float(en.y), span), s.link_r0);
     dd = __fmul_rn(dd, s.link_distance);
-    const float2 q = __ldg(&src[en.x]);
     float x = __fsub_rn(q.x, __fadd_rn(pp.x, vx));
     float y = __fsub_rn(q.y, __fadd_rn(pp.y, vy));
     float l = __fsqrt_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)));
@@ -509,6 +720,24 @@ __global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, con
     y = __fmul_rn(y, l);
     vx = __fadd_rn(vx, x);
     vy = __fadd_rn(vy, y);
+  };
+  constexpr int kLinkBatch = 4;
+  uint32_t at = e0;
+  for (; at + kLinkBatch <= e1; at += kLinkBatch) {
+    uint4 en[kLinkBatch];
+    float2 q[kLinkBatch];
+#pragma unroll
+    for (int u = 0; u < kLinkBatch; ++u) en[u] = __ldg(&ent[at + u]);
+#pragma unroll
+    for (int u = 0; u < kLinkBatch; ++u) q[u] = en[u].x != kAbsentTarget ? __ldg(&src[en[u].x]) : make_float2(0.f, 0.f);
+#pragma unroll
+    for (int u = 0; u < kLinkBatch; ++u)
+      if (en[u].x != kAbsentTarget) spring(en[u], q[u]);
+  }
+  for (; at < e1; ++at) {
+    const uint4 en = __ldg(&ent[at]);
+    if (en.x == kAbsentTarget) continue;
+    spring(en, __ldg(&src[en.x]));
   }
   dst[p] = (f & kPinned) ? pp : integrate(pp, vx, vy, s.friction, s.space);
 }
@@ -677,6 +906,7 @@ void launch_scatter(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
 }
 
 void launch_cells(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
+  k_bigcells<<<4 * 152, kBlock, 0, st>>>(d, s);
   const int tiles = (s.gf / s.tile) * (s.gf / s.tile);
   const size_t smem = 3 * sizeof(long long) * s.tile * s.tile;
   k_cells<<<tiles, s.tile * s.tile, smem, st>>>(d, s);

@@ -34,6 +34,11 @@ struct DeviceView {
   long long* acc;             // coarse-level integer sums (x, y, count) per cell, levels < tile level
   uint32_t acc_off[10];       // offset (in cells) of level l in acc
   uint32_t* cells_ticket;     // last-block ticket of the cell kernel
+  uint32_t* big_list;         // [G^2] cells above kBigCell, then [G^2] cells above kSmallCell
+  uint32_t* big_count;        // entries of the two lists this tick (zeroed at tick start)
+  long long* big_sx;          // exact sums of big cells [G^2]
+  long long* big_sy;
+  uint32_t* big_ns;           // slots of big cells [G^2]
   long long* centroid;        // x, y, count sums for ForceCenter
   const TickParams* tick_params;
   uint32_t* tick_ctr;
@@ -68,6 +73,9 @@ struct SimScalars {
   float csf;                  // finest cell size
   FixedScale fx;
 };
+
+constexpr uint32_t kSmallCell = 16;   // cells above this size get a warp of their own
+constexpr uint32_t kBigCell = 2048;   // cells above this size get a CTA of their own
 
 enum PrepassMode : uint32_t { kPreGravity = 1, kPreCentroid = 2, kPreBin = 4 };
 

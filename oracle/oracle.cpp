@@ -20,7 +20,9 @@
 //    this fixes it to correct rounding.
 //  * GLSL builtins: max(x,y) = x<y ? y : x; min(x,y) = y<x ? y : x;
 //    clamp = min(max()); length(v) = sqrt(v.x*v.x + v.y*v.y);
-//    normalize(v) = (v.x/length(v), v.y/length(v)).
+//    normalize(v) = v * (1/length(v)), the reciprocal correctly rounded
+//    (GPUs evaluate normalize as v * inversesqrt(dot(v, v)); GLSL fixes
+//    neither form).
 //  * vec2(cos(atan(y,x)), sin(atan(y,x))) (force-gravity.frag:36-38,
 //    force-center.frag:31-33) is the unit vector (x/r, y/r), r = length,
 //    its exact mathematical value.
@@ -424,11 +426,12 @@ inline void cell_velocity(R cx, R cy, R count, R px, R py, R k, R& vx, R& vy) {
   R dx = px - cx, dy = py - cy;
   R l = dx * dx + dy * dy;
   if (l <= R(0)) { vx = vx + R(0); vy = vy + R(0); return; }
-  R len = rsqrt_op(l);
-  if (l < R(1)) l = rsqrt_op(R(1) * l);
-  R add = k * count / rsqrt_op(l);
-  vx = vx + add * (dx / len);
-  vy = vy + add * (dy / len);
+  R len = rsqrt_op(l);                       // length(distVector)
+  R s = l < R(1) ? rsqrt_op(len) : len;      // sqrt(l) after l = sqrt(1 * l) when l < 1
+  R add = k * count / s;
+  R inv = R(1) / len;                        // normalize(v) = v * (1 / length(v))
+  vx = vx + add * (dx * inv);
+  vy = vy + add * (dy * inv);
 }
 
 template <typename R>
@@ -442,10 +445,11 @@ inline void pair_velocity(R px, R py, R ox, R oy, R rx, R ry, R k, R& sx, R& sy)
     if (l <= R(0)) { sx = sx + R(0); sy = sy + R(0); return; }
   }
   R len = rsqrt_op(l);
-  if (l < R(1)) l = rsqrt_op(R(1) * l);
-  R add = k / rsqrt_op(l);
-  sx = sx + add * (dx / len);
-  sy = sy + add * (dy / len);
+  R s = l < R(1) ? rsqrt_op(len) : len;
+  R add = k / s;
+  R inv = R(1) / len;
+  sx = sx + add * (dx * inv);
+  sy = sy + add * (dy * inv);
 }
 
 // Cell centroids at precision R (double: exact sums divided in FP64).
