@@ -15,7 +15,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OBJ_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcgl_gb300.so")
-SOURCES = ["kernels.cu", "engine.cu"]
+SOURCES = ["kernels.cu", "engine.cu", "noalloc.cu"]
 HEADERS = ["common.cuh", "kernels.cuh"]
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc")

@@ -203,6 +203,24 @@ cgl_status cgl_debug_get_cells(cgl_engine* e, uint32_t level, float* out, uint64
 /* finest level: 8 point indices per cell in slot (hash) order, -1 = empty slot. */
 cgl_status cgl_debug_get_slots(cgl_engine* e, int32_t* out, uint64_t capacity);
 
+/* Many-body grid pyramid without any device allocation.  No counterpart in the
+ * reference: it exists for callers that must not have a library allocate GPU
+ * memory — hosts that own the whole memory budget through their own allocator,
+ * code recording a CUDA graph (cudaMalloc is not allowed during capture), and
+ * frame loops that cannot absorb cudaMalloc's implicit synchronisation.
+ * d_xy: device positions [x0,y0,x1,y1,...] of n_points points (NaN = absent);
+ * d_cells: device output, every level's cells (centroid x, centroid y, count,
+ * 0), level 0 first, row-major — the cells the engine's many-body pass builds
+ * for the same positions (engine levels via cgl_debug_get_cells).  Scratch is
+ * a fixed 8.4 MB static device array (the largest pyramid: finest grid 512, 8
+ * levels); n_points above 2^24 is rejected with CGL_INVALID_ARG.  The first
+ * call on a device looks up that array's device address, so make it before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * race.  err (optional) receives the error text.  Runs on cuda_stream
+ * (NULL = default stream) of the current device; calls no allocator. */
+cgl_status cgl_levels_noalloc(const float* d_xy, uint64_t n_points, double space_size, float* d_cells,
+                              uint64_t cells_capacity_floats, void* cuda_stream, char* err, size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif
