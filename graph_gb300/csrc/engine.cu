@@ -45,6 +45,8 @@ struct cgl_engine {
   int device = 0;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
+  cudaStream_t side_stream = nullptr;       // branch for long link lists
+  cudaEvent_t ev_fork[2] = {nullptr, nullptr}, ev_join[2] = {nullptr, nullptr};
 
   // staged input (copied at set_*, applied at render)
   bool have_pos_input = false, have_link_input = false, have_strength = false, have_sizes = false;
@@ -87,7 +89,8 @@ struct cgl_engine {
   DevBuf b_counts, b_cell_start, b_block_sums, b_tickets, b_rec, b_acc, b_centroid;
   DevBuf b_big_list, b_big_count, b_big_sx, b_big_sy, b_big_ns;
   DevBuf b_params, b_tick_ctr;
-  DevBuf b_rowptr_in, b_rowptr_out, b_ent_in, b_ent_out;
+  DevBuf b_rowptr_in, b_rowptr_out, b_ent_in, b_ent_out, b_heavy_in, b_heavy_out;
+  uint32_t n_heavy_in = 0, n_heavy_out = 0;
   DevBuf b_size, b_cgrid_acc, b_cgrid;
   DeviceView view{};
   uint32_t level_off[10] = {};
@@ -156,7 +159,7 @@ void dev_free_all(cgl_engine* e) {
                    &e->b_tickets, &e->b_rec, &e->b_acc, &e->b_centroid, &e->b_params, &e->b_tick_ctr,
                    &e->b_rowptr_in, &e->b_rowptr_out, &e->b_ent_in, &e->b_ent_out, &e->b_size,
                    &e->b_cgrid_acc, &e->b_cgrid, &e->b_big_list, &e->b_big_count,
-                   &e->b_big_sx, &e->b_big_sy, &e->b_big_ns};
+                   &e->b_big_sx, &e->b_big_sy, &e->b_big_ns, &e->b_heavy_in, &e->b_heavy_out};
   for (DevBuf* b : all) {
     if (b->p) cudaFree(b->p);
     b->p = nullptr;
@@ -239,6 +242,10 @@ void refresh_view(cgl_engine* e) {
   d.ent_in = (const uint4*)e->b_ent_in.p;
   d.rowptr_out = (const uint32_t*)e->b_rowptr_out.p;
   d.ent_out = (const uint4*)e->b_ent_out.p;
+  d.heavy_in = (const uint32_t*)e->b_heavy_in.p;
+  d.heavy_out = (const uint32_t*)e->b_heavy_out.p;
+  d.n_heavy_in = e->n_heavy_in;
+  d.n_heavy_out = e->n_heavy_out;
   d.size = (const float*)e->b_size.p;
   d.cgrid_acc = (long long*)e->b_cgrid_acc.p;
   d.cgrid = (float4*)e->b_cgrid.p;
@@ -315,10 +322,10 @@ cgl_status enqueue_tick(cgl_engine* e, cudaStream_t st, cudaEvent_t* ev) {
   }
   if (p.link_in || p.link_out) {
     mark(6, 0);
-    if (p.link_in) launch_link(d, s, 0, false, st);
+    if (p.link_in) launch_link(d, s, 0, false, st, e->side_stream, e->ev_fork[0], e->ev_join[0]);
     mark(6, 1);
     mark(7, 0);
-    if (p.link_out) launch_link(d, s, 1, p.link_in, st);
+    if (p.link_out) launch_link(d, s, 1, p.link_in, st, e->side_stream, e->ev_fork[1], e->ev_join[1]);
     mark(7, 1);
     if (!(p.link_in && p.link_out))
       CU(cudaMemcpyAsync(d.pos, d.pos_alt, e->N * sizeof(float2), cudaMemcpyDeviceToDevice, st));
@@ -606,6 +613,19 @@ cgl_status do_render(cgl_engine* e, double alpha) {
       rp_out.assign(n + 1, 0);
     }
     e->entries = en_in.size();
+    std::vector<uint32_t> hv_in, hv_out;
+    for (uint64_t p = 0; p < n && !rp_in.empty(); ++p) {
+      if (rp_in[p + 1] - rp_in[p] > kHeavyDegree) hv_in.push_back((uint32_t)p);
+      if (rp_out[p + 1] - rp_out[p] > kHeavyDegree) hv_out.push_back((uint32_t)p);
+    }
+    e->n_heavy_in = (uint32_t)hv_in.size();
+    e->n_heavy_out = (uint32_t)hv_out.size();
+    if ((st = dev_reserve(e, e->b_heavy_in, hv_in.size() * sizeof(uint32_t), false))) return st;
+    if ((st = dev_reserve(e, e->b_heavy_out, hv_out.size() * sizeof(uint32_t), false))) return st;
+    if (!hv_in.empty())
+      CU(cudaMemcpyAsync(e->b_heavy_in.p, hv_in.data(), hv_in.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, e->stream));
+    if (!hv_out.empty())
+      CU(cudaMemcpyAsync(e->b_heavy_out.p, hv_out.data(), hv_out.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, e->stream));
     if ((st = dev_reserve(e, e->b_rowptr_in, (n + 1) * sizeof(uint32_t), false))) return st;
     if ((st = dev_reserve(e, e->b_rowptr_out, (n + 1) * sizeof(uint32_t), false))) return st;
     if ((st = dev_reserve(e, e->b_ent_in, en_in.size() * sizeof(uint4), false))) return st;
@@ -671,6 +691,11 @@ cgl_status cgl_create(const cgl_config* cfg, cgl_engine** out) {
   if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking);
   if (ce == cudaSuccess) ce = cudaMallocHost((void**)&e->h_params, kParamChunk * sizeof(TickParams));
   if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->params_copied, cudaEventDisableTiming);
+  if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->side_stream, cudaStreamNonBlocking);
+  for (int k = 0; k < 2 && ce == cudaSuccess; ++k) {
+    ce = cudaEventCreateWithFlags(&e->ev_fork[k], cudaEventDisableTiming);
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->ev_join[k], cudaEventDisableTiming);
+  }
   if (ce != cudaSuccess) {
     cudaGetLastError();
     static thread_local std::string create_err;
@@ -700,6 +725,11 @@ cgl_status cgl_destroy(cgl_engine* e) {
   dev_free_all(e);
   if (e->params_copied) cudaEventDestroy(e->params_copied);
   if (e->h_params) cudaFreeHost(e->h_params);
+  for (int k = 0; k < 2; ++k) {
+    if (e->ev_fork[k]) cudaEventDestroy(e->ev_fork[k]);
+    if (e->ev_join[k]) cudaEventDestroy(e->ev_join[k]);
+  }
+  if (e->side_stream) cudaStreamDestroy(e->side_stream);
   if (e->own_stream) cudaStreamDestroy(e->own_stream);
   delete e;
   return CGL_OK;
@@ -925,7 +955,7 @@ cgl_status cgl_get_layout(cgl_engine* e, cgl_layout* o) {
   if (p.grav || p.cent || p.mb) k += 1;                // prepass
   if (p.cent) k += 1;
   if (p.mb) k += 6;                                    // scan (2), scatter, big cells, cells, manybody
-  k += (uint32_t)p.link_in + (uint32_t)p.link_out;
+  k += (uint32_t)p.link_in * (1u + (e->n_heavy_in > 0)) + (uint32_t)p.link_out * (1u + (e->n_heavy_out > 0));
   if (p.coll) k += 3;                                  // grid, convert, force
   o->kernels_per_tick = k;
   return CGL_OK;

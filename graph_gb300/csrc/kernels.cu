@@ -689,13 +689,18 @@ __global__ void __launch_bounds__(kBlock) k_manybody(DeviceView d, SimScalars s)
 }
 
 // ------------------------------------------------------------------- link --
+// rows == nullptr: thread t handles point t and skips lists longer than
+// heavy_deg (those run in the heavy pass); otherwise thread t handles rows[t].
 __global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, const uint32_t* __restrict__ rowptr,
                                                  const uint4* __restrict__ ent, const float2* __restrict__ src,
-                                                 float2* __restrict__ dst) {
+                                                 float2* __restrict__ dst, const uint32_t* __restrict__ rows,
+                                                 uint32_t nrows, uint32_t heavy_deg) {
   // ForceLink.run (ForceLink/index.ts:221-263), force-spring.ts:38-96
   const TickParams tp = tick_params(d);
-  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= d.n) return;
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nrows) return;
+  const uint32_t p = rows ? rows[t] : t;
+  if (!rows && rowptr[p + 1] - rowptr[p] > heavy_deg) return;
   const float2 pp = src[p];
   const uint8_t f = d.flags[p];
   if (f & kAbsent) { dst[p] = pp; return; }
@@ -917,13 +922,24 @@ void launch_manybody(const DeviceView& d, const SimScalars& s, cudaStream_t st) 
   if (nb) k_manybody<<<nb, kBlock, 0, st>>>(d, s);
 }
 
-void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool swap_back, cudaStream_t st) {
+void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool swap_back, cudaStream_t st,
+                 cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
   const uint32_t nb = blocks_for(d.n);
   if (!nb) return;
   const uint32_t* rp = direction == 0 ? d.rowptr_in : d.rowptr_out;
   const uint4* en = direction == 0 ? d.ent_in : d.ent_out;
-  if (!swap_back) k_link<<<nb, kBlock, 0, st>>>(d, s, rp, en, d.pos, d.pos_alt);
-  else k_link<<<nb, kBlock, 0, st>>>(d, s, rp, en, d.pos_alt, d.pos);
+  const uint32_t* heavy = direction == 0 ? d.heavy_in : d.heavy_out;
+  const uint32_t nheavy = direction == 0 ? d.n_heavy_in : d.n_heavy_out;
+  const float2* src = swap_back ? d.pos_alt : d.pos;
+  float2* dst = swap_back ? d.pos : d.pos_alt;
+  if (nheavy) {   // long lists first, on a side branch, concurrent with the rest
+    cudaEventRecord(fork, st);
+    cudaStreamWaitEvent(side, fork, 0);
+    k_link<<<blocks_for(nheavy), kBlock, 0, side>>>(d, s, rp, en, src, dst, heavy, nheavy, kHeavyDegree);
+    cudaEventRecord(join, side);
+  }
+  k_link<<<nb, kBlock, 0, st>>>(d, s, rp, en, src, dst, nullptr, d.n, kHeavyDegree);
+  if (nheavy) cudaStreamWaitEvent(st, join, 0);
 }
 
 void launch_collision_grid(const DeviceView& d, const SimScalars& s, cudaStream_t st) {

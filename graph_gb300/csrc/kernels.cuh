@@ -47,6 +47,9 @@ struct DeviceView {
   const uint4* ent_in;        // (col, rnd bits, bias bits, strength bits)
   const uint32_t* rowptr_out;
   const uint4* ent_out;
+  const uint32_t* heavy_in;   // points whose incoming list is longer than kHeavyDegree
+  const uint32_t* heavy_out;
+  uint32_t n_heavy_in, n_heavy_out;
   // collision
   const float* size;          // resolved point sizes [n]
   long long* cgrid_acc;       // 4 grids x G_c^2 x (x, y, size, count)
@@ -74,6 +77,7 @@ struct SimScalars {
   FixedScale fx;
 };
 
+constexpr uint32_t kHeavyDegree = 256;   // longer link lists run on a side branch, started first
 constexpr uint32_t kSmallCell = 16;   // cells above this size get a warp of their own
 constexpr uint32_t kBigCell = 2048;   // cells above this size get a CTA of their own
 
@@ -86,7 +90,8 @@ void launch_scatter(const DeviceView& d, const SimScalars& s, cudaStream_t st);
 void launch_cells(const DeviceView& d, const SimScalars& s, cudaStream_t st);
 void launch_manybody(const DeviceView& d, const SimScalars& s, cudaStream_t st);
 // direction 0 = incoming (reads pos, writes pos_alt), 1 = outgoing (pos_alt -> pos)
-void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool swap_back, cudaStream_t st);
+void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool swap_back, cudaStream_t st,
+                 cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
 void launch_collision_grid(const DeviceView& d, const SimScalars& s, cudaStream_t st);
 void launch_collision_force(const DeviceView& d, const SimScalars& s, cudaStream_t st);
 void launch_tick_end(const DeviceView& d, cudaStream_t st);

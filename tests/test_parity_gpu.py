@@ -140,6 +140,22 @@ def test_tiny_graphs(n):
         _assert_same(eng, orc, (n, t))
 
 
+def test_hub_lists_on_side_branch():
+    # a star and a second hub: lists longer than 256 links run on the side branch
+    n = 3000
+    rng = np.random.default_rng(21)
+    pos = rng.uniform(1000, 3000, size=2 * n).astype(np.float32)
+    star = np.stack([np.zeros(n - 1), np.arange(1, n)], axis=1)
+    hub2 = np.stack([np.arange(2, 900), np.full(898, 1)], axis=1)
+    links = np.concatenate([star, hub2, rng.integers(0, n, size=(4000, 2))]).astype(np.float32).reshape(-1)
+    eng, orc = make_pair(pos, links, dict(random_seed=21, simulation_link_distance=3.0))
+    assert eng.layout().max_degree_in > 256 and eng.layout().max_degree_out > 256
+    for t in range(4):
+        eng.step(1)
+        orc.step(1)
+        _assert_same(eng, orc, ("hub", t))
+
+
 def test_coincident_points_and_outside_space():
     n = 400
     rng = np.random.default_rng(9)
@@ -285,3 +301,29 @@ def test_full_size_properties():
         e.close()
     assert same_bits(outs[0], outs[1])
     assert np.all(outs[0] >= 0) and np.all(outs[0] <= 8192)
+
+
+def test_rmat_scale23_collision_bit_exact():
+    # config 2 shape: R-MAT scale 23 (a,b,c,d = .57,.19,.19,.05), 40M links after
+    # self-loop and duplicate removal, radius U[1,8] (pointSizes = 2r), collision
+    # 0.5, spaceSize 16384.  Hub lists (degree ~1e5) run on the side branch.
+    n = 1 << 23
+    links = generators.rmat(23, 40_000_000, 0.57, 0.19, 0.19, seed=3)
+    pos = generators.uniform_positions(n, 0, 16384, 3)
+    radius = np.random.default_rng(3).uniform(1, 8, size=n).astype(np.float32)
+    fields = dict(space_size=16384, simulation_repulsion=0.1, simulation_gravity=0.25, simulation_friction=0.85,
+                  simulation_link_spring=1.0, simulation_link_distance=2.0, simulation_collision=0.5,
+                  simulation_decay=5000, random_seed=3)
+    eng, orc = make_pair(pos, links, fields, sizes=2 * radius)
+    assert eng.layout().max_degree_in > 1000 and eng.layout().collision_grid == 0
+    for t in range(2):
+        eng.step(1)
+        orc.step(1)
+        _assert_same(eng, orc, ("rmat23", t))
+    lay = eng.layout()
+    assert lay.collision_grid == orc.layout().collision_grid == 512
+    orc.close()
+    eng.step(3)
+    p = eng.get_point_positions()
+    assert np.all(p >= 0) and np.all(p <= 16384)
+    assert eng.cells(lay.levels - 1)[..., 2].sum() == n
