@@ -218,3 +218,17 @@ def declare(lib, prefix: str, engine_t=C.c_void_p):
         fn = getattr(lib, "%s_%s" % (prefix, name))
         fn.argtypes = args
         fn.restype = res
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [
+        ("jobs", C.c_uint64),
+        ("running_jobs", C.c_uint64),
+        ("points", C.c_uint64),
+        ("link_entries", C.c_uint64),
+        ("point_arena", C.c_uint64),
+        ("cell_arena", C.c_uint64),
+        ("device_bytes", C.c_uint64),
+        ("kernels_per_tick", C.c_uint32),
+        ("reserved", C.c_uint32),
+    ]

@@ -1,0 +1,600 @@
+// batch.cu — host side of the batched engine (cgl_batch_* in include/cgl.h).
+//
+// Independent layout jobs share one set of device arenas and advance
+// together: one CUDA-graph launch per tick for every graph in the batch.
+// Jobs join (cgl_batch_add) and leave (cgl_batch_remove) between ticks;
+// each keeps its own alpha, random stream and tick budget, so its trajectory
+// is the one it would have in a plain engine.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "../../include/cgl.h"
+#include "batch.cuh"
+#include "ingest.h"
+
+using namespace cgl;
+
+namespace {
+
+constexpr double kAlphaMin = 0.001;
+constexpr uint32_t kTickChunk = 64;   // ticks per parameter upload
+
+// First-fit range allocator over [0, cap): free ranges below the high-water mark.
+struct Arena {
+  uint64_t cap = 0, hwm = 0;
+  std::map<uint64_t, uint64_t> free_;   // offset -> length
+  bool alloc(uint64_t n, uint64_t* off) {
+    if (n == 0) { *off = 0; return true; }
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second >= n) {
+        *off = it->first;
+        const uint64_t rest = it->second - n, at = it->first + n;
+        free_.erase(it);
+        if (rest) free_[at] = rest;
+        return true;
+      }
+    }
+    if (hwm + n > cap) return false;
+    *off = hwm;
+    hwm += n;
+    return true;
+  }
+  void release(uint64_t off, uint64_t n) {
+    if (n == 0) return;
+    auto it = free_.emplace(off, n).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) { it->second += nx->second; free_.erase(nx); }
+    if (it != free_.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) { pv->second += it->second; free_.erase(it); it = pv; }
+    }
+    if (it->first + it->second == hwm) { hwm = it->first; free_.erase(it); }
+  }
+};
+
+struct Buf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+struct Job {
+  bool used = false;
+  cgl_config cfg{};
+  uint64_t n = 0, live = 0, E = 0, m_in = 0, m_out = 0;
+  uint64_t p_off = 0, cell_off = 0, cells = 0, rec_off = 0, recs = 0, acc_off = 0, accs = 0;
+  uint64_t rp_in = 0, rp_out = 0, e_in = 0, e_out = 0;
+  int gf = 0, levels = 0, tile = 0;
+  uint32_t stages = 0;
+  ingest::Rng rng;
+  double alpha = 1.0, progress = 0.0, decay_factor = 0.0;
+  bool running = true;
+  uint64_t tick = 0;
+  uint32_t max_ticks = 0;
+  bool stop_below_min = false;
+  std::vector<uint32_t> heavy_in, heavy_out;   // local
+  GraphDesc desc{};
+};
+
+}  // namespace
+
+struct cgl_batch {
+  int device = 0;
+  double budget = 0;
+  std::string err;
+  cudaStream_t stream = nullptr, side = nullptr;
+  cudaEvent_t fork[2] = {}, join[2] = {}, params_copied = nullptr;
+  bool params_pending = false;
+  Arena pts, cells, recs, accs, rows, ents;
+  std::vector<Job> jobs;
+  size_t dev_bytes = 0;
+  // point arena
+  Buf gid, pos, pos_alt, flags, jitter, key, rank, sorted_idx, sorted_pos;
+  // cell arena
+  Buf counts, cell_start, cell_gid, big_list, big_sx, big_sy, big_ns, scan1, scan2;
+  Buf big_count, tick_ctr;
+  Buf rec, acc, rowptr, ent, desc, tiles, heavy_in, heavy_out, ticks;
+  uint32_t n_tiles = 0, n_heavy_in = 0, n_heavy_out = 0, slots_cap = 0;
+  BatchTick* h_ticks = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  bool dirty = true;
+  BatchView view{};
+};
+
+namespace {
+
+cgl_status bfail(cgl_batch* b, cgl_status st, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (b) b->err = buf;
+  return st;
+}
+
+#define BCU(call)                                                                                     \
+  do {                                                                                                \
+    cudaError_t _e = (call);                                                                          \
+    if (_e != cudaSuccess)                                                                            \
+      return bfail(b, _e == cudaErrorMemoryAllocation ? CGL_OOM : CGL_CUDA_ERROR, "%s: %s", #call,   \
+                   cudaGetErrorString(_e));                                                           \
+  } while (0)
+
+// Grow a device buffer to `bytes`, keeping its first `keep` bytes; new bytes
+// are filled with `fill` (-1: leave undefined).
+cgl_status grow(cgl_batch* b, Buf& x, size_t bytes, size_t keep, int fill) {
+  if (bytes <= x.bytes) return CGL_OK;
+  if (b->budget > 0 && (double)(b->dev_bytes + bytes - x.bytes) > b->budget)
+    return bfail(b, CGL_OOM, "device memory budget %.0f bytes: cannot grow to %zu more", b->budget, bytes - x.bytes);
+  void* p = nullptr;
+  BCU(cudaMalloc(&p, bytes));
+  if (fill >= 0) BCU(cudaMemsetAsync(p, fill, bytes, b->stream));
+  if (x.p && keep) BCU(cudaMemcpyAsync(p, x.p, std::min(keep, x.bytes), cudaMemcpyDeviceToDevice, b->stream));
+  BCU(cudaStreamSynchronize(b->stream));
+  if (x.p) cudaFree(x.p);
+  b->dev_bytes += bytes - x.bytes;
+  x.p = p;
+  x.bytes = bytes;
+  return CGL_OK;
+}
+
+uint64_t grown(uint64_t cap, uint64_t need) { return std::max<uint64_t>(need, cap + cap / 2 + 1024); }
+
+cgl_status reserve_points(cgl_batch* b, uint64_t cap) {
+  if (cap <= b->pts.cap) return CGL_OK;
+  const uint64_t keep = b->pts.hwm;
+  cgl_status st;
+  if ((st = grow(b, b->gid, cap * 4, keep * 4, 0xFF)) || (st = grow(b, b->pos, cap * 8, keep * 8, -1)) ||
+      (st = grow(b, b->pos_alt, cap * 8, keep * 8, -1)) || (st = grow(b, b->flags, cap, keep, 0)) ||
+      (st = grow(b, b->jitter, cap * 8, keep * 8, -1)) || (st = grow(b, b->key, cap * 4, 0, -1)) ||
+      (st = grow(b, b->rank, cap * 4, 0, -1)) || (st = grow(b, b->sorted_idx, cap * 4, 0, -1)) ||
+      (st = grow(b, b->sorted_pos, cap * 8, 0, -1)))
+    return st;
+  b->pts.cap = cap;
+  return CGL_OK;
+}
+
+cgl_status reserve_cells(cgl_batch* b, uint64_t cap) {
+  if (cap <= b->cells.cap) return CGL_OK;
+  const uint64_t keep = b->cells.hwm;
+  cgl_status st;
+  const uint64_t n1 = cap / 1024 + 2, n2 = n1 / 1024 + 2;
+  if ((st = grow(b, b->counts, cap * 4, keep * 4, 0)) || (st = grow(b, b->cell_start, (cap + 1) * 4, 0, 0)) ||
+      (st = grow(b, b->cell_gid, cap * 4, keep * 4, 0xFF)) || (st = grow(b, b->big_list, 2 * cap * 4, 0, -1)) ||
+      (st = grow(b, b->big_sx, cap * 8, 0, -1)) || (st = grow(b, b->big_sy, cap * 8, 0, -1)) ||
+      (st = grow(b, b->big_ns, cap * 4, 0, -1)) || (st = grow(b, b->scan1, n1 * 4, 0, -1)) ||
+      (st = grow(b, b->scan2, n2 * 4, 0, -1)))
+    return st;
+  b->cells.cap = cap;
+  return CGL_OK;
+}
+
+void refresh_view(cgl_batch* b) {
+  BatchView& v = b->view;
+  v.slots = (uint32_t)b->jobs.size();
+  v.point_hwm = (uint32_t)b->pts.hwm;
+  v.cell_hwm = (uint32_t)b->cells.hwm;
+  v.desc = (const GraphDesc*)b->desc.p;
+  v.gid = (const uint32_t*)b->gid.p;
+  v.cell_gid = (const uint32_t*)b->cell_gid.p;
+  v.pos = (float2*)b->pos.p;
+  v.pos_alt = (float2*)b->pos_alt.p;
+  v.flags = (const uint8_t*)b->flags.p;
+  v.jitter = (const float2*)b->jitter.p;
+  v.key = (uint32_t*)b->key.p;
+  v.rank = (uint32_t*)b->rank.p;
+  v.sorted_idx = (uint32_t*)b->sorted_idx.p;
+  v.sorted_pos = (float2*)b->sorted_pos.p;
+  v.counts = (uint32_t*)b->counts.p;
+  v.cell_start = (uint32_t*)b->cell_start.p;
+  v.scan1 = (uint32_t*)b->scan1.p;
+  v.scan2 = (uint32_t*)b->scan2.p;
+  v.big_list = (uint32_t*)b->big_list.p;
+  v.big_count = (uint32_t*)b->big_count.p;
+  v.big_sx = (long long*)b->big_sx.p;
+  v.big_sy = (long long*)b->big_sy.p;
+  v.big_ns = (uint32_t*)b->big_ns.p;
+  v.rec = (float4*)b->rec.p;
+  v.acc = (long long*)b->acc.p;
+  v.tiles = (const uint2*)b->tiles.p;
+  v.n_tiles = b->n_tiles;
+  v.rowptr = (const uint32_t*)b->rowptr.p;
+  v.ent = (const uint4*)b->ent.p;
+  v.heavy_in = (const uint32_t*)b->heavy_in.p;
+  v.n_heavy_in = b->n_heavy_in;
+  v.heavy_out = (const uint32_t*)b->heavy_out.p;
+  v.n_heavy_out = b->n_heavy_out;
+  v.ticks = (const BatchTick*)b->ticks.p;
+  v.tick_ctr = (uint32_t*)b->tick_ctr.p;
+}
+
+// Descriptors, the cell-kernel work list and the long-list rows of all jobs.
+cgl_status rebuild_tables(cgl_batch* b) {
+  BCU(cudaStreamSynchronize(b->stream));   // no parameter upload may still read h_ticks
+  b->params_pending = false;
+  const size_t slots = b->jobs.size();
+  std::vector<GraphDesc> descs(slots);
+  std::vector<uint2> tiles;
+  std::vector<uint32_t> hin, hout;
+  for (size_t g = 0; g < slots; ++g) {
+    const Job& j = b->jobs[g];
+    if (!j.used) { std::memset(&descs[g], 0, sizeof(GraphDesc)); continue; }
+    descs[g] = j.desc;
+    if (j.stages & kGManybody) {
+      const int per_row = j.gf / j.tile;
+      for (int t = 0; t < per_row * per_row; ++t) tiles.push_back(make_uint2((uint32_t)g, (uint32_t)t));
+    }
+    for (uint32_t p : j.heavy_in) hin.push_back((uint32_t)j.p_off + p);
+    for (uint32_t p : j.heavy_out) hout.push_back((uint32_t)j.p_off + p);
+  }
+  cgl_status st;
+  if ((st = grow(b, b->desc, std::max<size_t>(slots, 1) * sizeof(GraphDesc), 0, 0))) return st;
+  if ((st = grow(b, b->tiles, std::max<size_t>(tiles.size(), 1) * sizeof(uint2), 0, -1))) return st;
+  if ((st = grow(b, b->heavy_in, std::max<size_t>(hin.size(), 1) * 4, 0, -1))) return st;
+  if ((st = grow(b, b->heavy_out, std::max<size_t>(hout.size(), 1) * 4, 0, -1))) return st;
+  if (slots) BCU(cudaMemcpyAsync(b->desc.p, descs.data(), slots * sizeof(GraphDesc), cudaMemcpyHostToDevice, b->stream));
+  if (!tiles.empty())
+    BCU(cudaMemcpyAsync(b->tiles.p, tiles.data(), tiles.size() * sizeof(uint2), cudaMemcpyHostToDevice, b->stream));
+  if (!hin.empty()) BCU(cudaMemcpyAsync(b->heavy_in.p, hin.data(), hin.size() * 4, cudaMemcpyHostToDevice, b->stream));
+  if (!hout.empty()) BCU(cudaMemcpyAsync(b->heavy_out.p, hout.data(), hout.size() * 4, cudaMemcpyHostToDevice, b->stream));
+  if (slots > b->slots_cap) {
+    if ((st = grow(b, b->ticks, (size_t)kTickChunk * slots * sizeof(BatchTick), 0, 0))) return st;
+    if (b->h_ticks) cudaFreeHost(b->h_ticks);
+    b->h_ticks = nullptr;
+    BCU(cudaMallocHost((void**)&b->h_ticks, (size_t)kTickChunk * slots * sizeof(BatchTick)));
+    b->slots_cap = (uint32_t)slots;
+  }
+  BCU(cudaStreamSynchronize(b->stream));
+  b->n_tiles = (uint32_t)tiles.size();
+  b->n_heavy_in = (uint32_t)hin.size();
+  b->n_heavy_out = (uint32_t)hout.size();
+  refresh_view(b);
+  return CGL_OK;
+}
+
+cgl_status prepare(cgl_batch* b) {
+  if (!b->dirty && b->graph) return CGL_OK;
+  cgl_status st = rebuild_tables(b);
+  if (st) return st;
+  if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+  cudaGraph_t g = nullptr;
+  BCU(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  batch_launch_tick(b->view, b->stream, b->side, b->fork, b->join);
+  cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+  if (ce != cudaSuccess) return bfail(b, CGL_CUDA_ERROR, "batch graph capture: %s", cudaGetErrorString(ce));
+  ce = cudaGraphInstantiate(&b->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (ce != cudaSuccess) { b->graph = nullptr; return bfail(b, CGL_CUDA_ERROR, "batch graph: %s", cudaGetErrorString(ce)); }
+  b->dirty = false;
+  return CGL_OK;
+}
+
+// One tick of one job on the host: whether it runs, its f32 alpha and peel
+// seed, then Store.addAlpha (Store/index.ts:328-332).
+BatchTick host_tick(Job& j) {
+  BatchTick t{0.f, 0u, 0u, 0u};
+  if (!j.used) return t;
+  if (j.max_ticks && j.tick >= j.max_ticks) j.running = false;
+  if (j.running && j.stop_below_min && j.alpha < kAlphaMin) { j.running = false; j.progress = 1; }
+  if (!j.running) return t;
+  t.active = 1;
+  t.alpha = (float)j.alpha;
+  if (j.stages & kGManybody) {
+    const float seed = (float)j.rng.uniform(0, 1);
+    std::memcpy(&t.seed_bits, &seed, 4);
+  }
+  j.alpha += (0 - j.alpha) * j.decay_factor;
+  j.progress = std::sqrt(std::min(1.0, kAlphaMin / j.alpha));
+  j.tick++;
+  return t;
+}
+
+void release(cgl_batch* b, Job& j) {
+  b->pts.release(j.p_off, j.n);
+  b->cells.release(j.cell_off, j.cells);
+  b->recs.release(j.rec_off, j.recs);
+  b->accs.release(j.acc_off, j.accs);
+  b->rows.release(j.rp_in, j.n + 1);
+  b->rows.release(j.rp_out, j.n + 1);
+  b->ents.release(j.e_in, j.m_in);
+  b->ents.release(j.e_out, j.m_out);
+}
+
+}  // namespace
+
+extern "C" {
+
+cgl_status cgl_batch_create(int32_t device, double hbm_budget_bytes, cgl_batch** out) {
+  if (!out) return CGL_INVALID_ARG;
+  *out = nullptr;
+  cgl_batch* b = new cgl_batch();
+  b->device = device;
+  b->budget = hbm_budget_bytes;
+  cudaError_t ce = cudaSetDevice(device);
+  if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+  for (int k = 0; k < 2 && ce == cudaSuccess; ++k) {
+    ce = cudaEventCreateWithFlags(&b->fork[k], cudaEventDisableTiming);
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming);
+  }
+  if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&b->params_copied, cudaEventDisableTiming);
+  if (ce != cudaSuccess) {
+    cudaGetLastError();
+    cgl_batch_destroy(b);
+    return CGL_CUDA_ERROR;
+  }
+  cgl_status st;
+  if ((st = grow(b, b->big_count, 8, 0, 0)) || (st = grow(b, b->tick_ctr, 4, 0, 0)) ||
+      (st = reserve_cells(b, 1024)) || (st = reserve_points(b, 1024))) {
+    cgl_batch_destroy(b);
+    return st;
+  }
+  refresh_view(b);
+  *out = b;
+  return CGL_OK;
+}
+
+cgl_status cgl_batch_destroy(cgl_batch* b) {
+  if (!b) return CGL_INVALID_ARG;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  Buf* all[] = {&b->gid, &b->pos, &b->pos_alt, &b->flags, &b->jitter, &b->key, &b->rank, &b->sorted_idx,
+                &b->sorted_pos, &b->counts, &b->cell_start, &b->cell_gid, &b->big_list, &b->big_sx, &b->big_sy,
+                &b->big_ns, &b->scan1, &b->scan2, &b->big_count, &b->tick_ctr, &b->rec, &b->acc, &b->rowptr,
+                &b->ent, &b->desc, &b->tiles, &b->heavy_in, &b->heavy_out, &b->ticks};
+  for (Buf* x : all)
+    if (x->p) cudaFree(x->p);
+  if (b->h_ticks) cudaFreeHost(b->h_ticks);
+  for (int k = 0; k < 2; ++k) {
+    if (b->fork[k]) cudaEventDestroy(b->fork[k]);
+    if (b->join[k]) cudaEventDestroy(b->join[k]);
+  }
+  if (b->params_copied) cudaEventDestroy(b->params_copied);
+  if (b->side) cudaStreamDestroy(b->side);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return CGL_OK;
+}
+
+const char* cgl_batch_last_error(cgl_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+cgl_status cgl_batch_add(cgl_batch* b, const cgl_config* cfg, const float* xy, uint64_t n_floats, const float* links,
+                         uint64_t n_link_floats, uint32_t max_ticks, int32_t stop_below_alpha_min, uint32_t* id) {
+  if (!b || !cfg || !id || (!xy && n_floats) || (!links && n_link_floats)) return CGL_INVALID_ARG;
+  b->err.clear();
+  if (cudaSetDevice(b->device) != cudaSuccess) return bfail(b, CGL_CUDA_ERROR, "cudaSetDevice");
+  const uint32_t mask = cfg->stage_mask;
+  if ((cfg->simulation_center != 0 && (mask & CGL_STAGE_CENTER)) ||
+      (cfg->simulation_collision != 0 && (mask & CGL_STAGE_COLLISION)))
+    return bfail(b, CGL_INVALID_ARG, "batched jobs run gravity, many-body and link forces; center and collision need a plain engine");
+  if (!cfg->enable_simulation) return bfail(b, CGL_INVALID_ARG, "enableSimulation is off");
+  Job j;
+  j.used = true;
+  j.cfg = *cfg;
+  j.n = n_floats / 2;
+  j.E = n_link_floats / 2;
+  if (j.n == 0) return bfail(b, CGL_INVALID_ARG, "a job needs points");
+  if (j.n > (1ull << 24)) return bfail(b, CGL_INVALID_ARG, "%llu points exceed 2^24", (unsigned long long)j.n);
+  if (cfg->has_random_seed) j.rng.seed = cfg->random_seed;
+  else { std::random_device rd; j.rng.seed = ((uint64_t)rd() << 32) ^ rd(); }
+  const double space = ingest::adjusted_space(*cfg);
+  // ingest exactly as cgl_render does for a fresh plain engine
+  std::vector<float2> pos;
+  std::vector<uint8_t> absent;
+  j.live = ingest::canonical_positions(xy, j.n, pos, absent);
+  int fbits = 0;
+  const FixedScale fx = ingest::fixed_for(j.n, space, &fbits);
+  const ingest::Grid grid = ingest::grid_for(j.n);
+  j.gf = grid.gf;
+  j.levels = grid.levels;
+  j.tile = std::min(16, j.gf);
+  std::vector<float2> jit;
+  ingest::jitter(j.rng, j.n, jit);
+  ingest::Csr cin, cout_;
+  const bool has_links = j.E > 0;
+  if (has_links) ingest::build_links(links, j.E, j.n, nullptr, absent, j.rng, cin, cout_);
+  else { cin.rowptr.assign(j.n + 1, 0); cout_.rowptr.assign(j.n + 1, 0); }
+  j.m_in = cin.ent.size();
+  j.m_out = cout_.ent.size();
+  j.heavy_in = cin.heavy;
+  j.heavy_out = cout_.heavy;
+  j.stages = 0;
+  if (cfg->simulation_gravity != 0 && (mask & CGL_STAGE_GRAVITY)) j.stages |= kGGravity;
+  if (mask & CGL_STAGE_MANYBODY) j.stages |= kGManybody;
+  if (has_links && (mask & CGL_STAGE_LINK_IN)) j.stages |= kGLinkIn;
+  if (has_links && (mask & CGL_STAGE_LINK_OUT)) j.stages |= kGLinkOut;
+  j.decay_factor = 1 - std::pow(kAlphaMin, 1 / cfg->simulation_decay);
+  j.max_ticks = max_ticks;
+  j.stop_below_min = stop_below_alpha_min != 0;
+  j.cells = (uint64_t)j.gf * j.gf;
+  j.recs = ingest::level_base(j.levels);
+  int lv_tile = j.levels - 1;
+  for (int g = j.tile; g > 1 && lv_tile > 0; g >>= 1) --lv_tile;
+  j.accs = ingest::level_base(lv_tile);
+  // arena ranges (grow the arenas when full)
+  cgl_status st;
+  auto take = [&](Arena& a, uint64_t n, uint64_t* off, int kind) -> cgl_status {
+    if (a.alloc(n, off)) return CGL_OK;
+    const uint64_t cap = grown(a.cap, a.hwm + n);
+    cgl_status s2 = CGL_OK;
+    if (kind == 0) s2 = reserve_points(b, cap);
+    else if (kind == 1) s2 = reserve_cells(b, cap);
+    else if (kind == 2) s2 = grow(b, b->rec, cap * sizeof(float4), a.hwm * sizeof(float4), 0);
+    else if (kind == 3) s2 = grow(b, b->acc, cap * 3 * sizeof(long long), a.hwm * 3 * sizeof(long long), 0);
+    else if (kind == 4) s2 = grow(b, b->rowptr, cap * 4, a.hwm * 4, -1);
+    else s2 = grow(b, b->ent, cap * sizeof(uint4), a.hwm * sizeof(uint4), -1);
+    if (s2) return s2;
+    if (kind >= 2) a.cap = cap;
+    b->dirty = true;
+    return a.alloc(n, off) ? CGL_OK : bfail(b, CGL_OOM, "arena allocation failed");
+  };
+  if ((st = take(b->pts, j.n, &j.p_off, 0)) || (st = take(b->cells, j.cells, &j.cell_off, 1)) ||
+      (st = take(b->recs, j.recs, &j.rec_off, 2)) || (st = take(b->accs, j.accs, &j.acc_off, 3)) ||
+      (st = take(b->rows, j.n + 1, &j.rp_in, 4)) || (st = take(b->rows, j.n + 1, &j.rp_out, 4)) ||
+      (st = take(b->ents, j.m_in, &j.e_in, 5)) || (st = take(b->ents, j.m_out, &j.e_out, 5))) {
+    release(b, j);
+    return st;
+  }
+  if (b->pts.hwm > 0xFFFFFF00ull || b->cells.hwm > 0xFFFFFF00ull || b->ents.hwm > 0xFFFFFF00ull) {
+    release(b, j);
+    return bfail(b, CGL_OOM, "arena index space (32 bits) exhausted");
+  }
+  // upload: absolute indices for rows and neighbours
+  std::vector<uint32_t> rp_in(j.n + 1), rp_out(j.n + 1);
+  for (uint64_t i = 0; i <= j.n; ++i) {
+    rp_in[i] = (uint32_t)(j.e_in + cin.rowptr[i]);
+    rp_out[i] = (uint32_t)(j.e_out + cout_.rowptr[i]);
+  }
+  for (auto& e : cin.ent) if (e.x != kAbsentTarget) e.x += (uint32_t)j.p_off;
+  for (auto& e : cout_.ent) if (e.x != kAbsentTarget) e.x += (uint32_t)j.p_off;
+  std::vector<uint8_t> flags(j.n);
+  for (uint64_t i = 0; i < j.n; ++i) flags[i] = absent[i] ? kAbsent : 0;
+  const uint32_t g = [&]() {
+    for (uint32_t s = 0; s < b->jobs.size(); ++s)
+      if (!b->jobs[s].used) return s;
+    b->jobs.emplace_back();
+    return (uint32_t)(b->jobs.size() - 1);
+  }();
+  std::vector<uint32_t> gids(j.n, g), cgids(j.cells, g);
+  cudaStream_t s = b->stream;
+  BCU(cudaMemcpyAsync((float2*)b->pos.p + j.p_off, pos.data(), j.n * 8, cudaMemcpyHostToDevice, s));
+  BCU(cudaMemcpyAsync((float2*)b->jitter.p + j.p_off, jit.data(), j.n * 8, cudaMemcpyHostToDevice, s));
+  BCU(cudaMemcpyAsync((uint8_t*)b->flags.p + j.p_off, flags.data(), j.n, cudaMemcpyHostToDevice, s));
+  BCU(cudaMemcpyAsync((uint32_t*)b->gid.p + j.p_off, gids.data(), j.n * 4, cudaMemcpyHostToDevice, s));
+  BCU(cudaMemcpyAsync((uint32_t*)b->cell_gid.p + j.cell_off, cgids.data(), j.cells * 4, cudaMemcpyHostToDevice, s));
+  BCU(cudaMemsetAsync((uint32_t*)b->counts.p + j.cell_off, 0, j.cells * 4, s));
+  BCU(cudaMemsetAsync((long long*)b->acc.p + 3 * j.acc_off, 0, j.accs * 3 * sizeof(long long), s));
+  BCU(cudaMemcpyAsync((uint32_t*)b->rowptr.p + j.rp_in, rp_in.data(), (j.n + 1) * 4, cudaMemcpyHostToDevice, s));
+  BCU(cudaMemcpyAsync((uint32_t*)b->rowptr.p + j.rp_out, rp_out.data(), (j.n + 1) * 4, cudaMemcpyHostToDevice, s));
+  if (j.m_in) BCU(cudaMemcpyAsync((uint4*)b->ent.p + j.e_in, cin.ent.data(), j.m_in * 16, cudaMemcpyHostToDevice, s));
+  if (j.m_out)
+    BCU(cudaMemcpyAsync((uint4*)b->ent.p + j.e_out, cout_.ent.data(), j.m_out * 16, cudaMemcpyHostToDevice, s));
+  BCU(cudaStreamSynchronize(s));
+  GraphDesc& D = j.desc;
+  D.p_off = (uint32_t)j.p_off;
+  D.n = (uint32_t)j.n;
+  D.cell_off = (uint32_t)j.cell_off;
+  D.rec_off = (uint32_t)j.rec_off;
+  D.acc_off = (uint32_t)j.acc_off;
+  D.acc_cells = (uint32_t)j.accs;
+  D.rp_in = (uint32_t)j.rp_in;
+  D.rp_out = (uint32_t)j.rp_out;
+  D.gf = j.gf;
+  D.levels = j.levels;
+  D.tile = j.tile;
+  D.stages = j.stages;
+  D.space = (float)space;
+  D.csf = (float)(space / j.gf);
+  D.friction = (float)cfg->simulation_friction;
+  D.gravity = (float)cfg->simulation_gravity;
+  D.repulsion = (float)cfg->simulation_repulsion;
+  D.link_spring = (float)cfg->simulation_link_spring;
+  D.link_distance = (float)cfg->simulation_link_distance;
+  D.link_r0 = (float)cfg->simulation_link_dist_random_variation_range[0];
+  D.link_r1 = (float)cfg->simulation_link_dist_random_variation_range[1];
+  D.fx = fx;
+  b->jobs[g] = std::move(j);
+  b->dirty = true;
+  *id = g;
+  return CGL_OK;
+}
+
+cgl_status cgl_batch_remove(cgl_batch* b, uint32_t id) {
+  if (!b || id >= b->jobs.size() || !b->jobs[id].used) return CGL_INVALID_ARG;
+  if (cudaSetDevice(b->device) != cudaSuccess) return bfail(b, CGL_CUDA_ERROR, "cudaSetDevice");
+  Job& j = b->jobs[id];
+  BCU(cudaStreamSynchronize(b->stream));
+  BCU(cudaMemsetAsync((uint32_t*)b->gid.p + j.p_off, 0xFF, j.n * 4, b->stream));
+  release(b, j);
+  j = Job();
+  b->dirty = true;
+  return CGL_OK;
+}
+
+cgl_status cgl_batch_step(cgl_batch* b, uint32_t ticks) {
+  if (!b) return CGL_INVALID_ARG;
+  b->err.clear();
+  if (cudaSetDevice(b->device) != cudaSuccess) return bfail(b, CGL_CUDA_ERROR, "cudaSetDevice");
+  if (b->jobs.empty() || ticks == 0) return CGL_OK;
+  cgl_status st = prepare(b);
+  if (st) return st;
+  const size_t slots = b->jobs.size();
+  uint32_t done = 0;
+  while (done < ticks) {
+    const uint32_t n = std::min(kTickChunk, ticks - done);
+    if (b->params_pending) { BCU(cudaEventSynchronize(b->params_copied)); b->params_pending = false; }
+    for (uint32_t t = 0; t < n; ++t)
+      for (size_t g = 0; g < slots; ++g) b->h_ticks[(size_t)t * slots + g] = host_tick(b->jobs[g]);
+    BCU(cudaMemcpyAsync(b->ticks.p, b->h_ticks, (size_t)n * slots * sizeof(BatchTick), cudaMemcpyHostToDevice,
+                        b->stream));
+    BCU(cudaEventRecord(b->params_copied, b->stream));
+    b->params_pending = true;
+    BCU(cudaMemsetAsync(b->tick_ctr.p, 0, 4, b->stream));
+    for (uint32_t t = 0; t < n; ++t) BCU(cudaGraphLaunch(b->graph, b->stream));
+    done += n;
+  }
+  return CGL_OK;
+}
+
+cgl_status cgl_batch_synchronize(cgl_batch* b) {
+  if (!b) return CGL_INVALID_ARG;
+  BCU(cudaStreamSynchronize(b->stream));
+  return CGL_OK;
+}
+
+cgl_status cgl_batch_get_point_positions(cgl_batch* b, uint32_t id, float* out, uint64_t cap) {
+  if (!b || id >= b->jobs.size() || !b->jobs[id].used) return CGL_INVALID_ARG;
+  const Job& j = b->jobs[id];
+  if (cap < 2 * j.n || !out) return bfail(b, CGL_INVALID_ARG, "output holds %llu floats, need %llu",
+                                          (unsigned long long)cap, (unsigned long long)(2 * j.n));
+  if (cudaSetDevice(b->device) != cudaSuccess) return bfail(b, CGL_CUDA_ERROR, "cudaSetDevice");
+  BCU(cudaMemcpyAsync(out, (float2*)b->pos.p + j.p_off, j.n * 8, cudaMemcpyDeviceToHost, b->stream));
+  BCU(cudaStreamSynchronize(b->stream));
+  return CGL_OK;
+}
+
+cgl_status cgl_batch_get_state(cgl_batch* b, uint32_t id, cgl_state* s) {
+  if (!b || !s || id >= b->jobs.size() || !b->jobs[id].used) return CGL_INVALID_ARG;
+  const Job& j = b->jobs[id];
+  std::memset(s, 0, sizeof(*s));
+  s->alpha = j.alpha;
+  s->progress = j.progress;
+  s->is_simulation_running = j.running && !(j.max_ticks && j.tick >= j.max_ticks) &&
+                             !(j.stop_below_min && j.alpha < kAlphaMin);
+  s->tick = j.tick;
+  s->points_number = j.n;
+  s->links_number = j.E;
+  s->rng_draws = j.rng.ctr;
+  return CGL_OK;
+}
+
+cgl_status cgl_batch_get_info(cgl_batch* b, cgl_batch_info* out) {
+  if (!b || !out) return CGL_INVALID_ARG;
+  std::memset(out, 0, sizeof(*out));
+  for (const Job& j : b->jobs) {
+    if (!j.used) continue;
+    out->jobs++;
+    out->points += j.n;
+    out->link_entries += j.m_in;
+    if (j.running && !(j.max_ticks && j.tick >= j.max_ticks) && !(j.stop_below_min && j.alpha < kAlphaMin))
+      out->running_jobs++;
+  }
+  out->point_arena = b->pts.cap;
+  out->cell_arena = b->cells.cap;
+  out->device_bytes = b->dev_bytes;
+  refresh_view(b);
+  out->kernels_per_tick = batch_kernels_per_tick(b->view);
+  return CGL_OK;
+}
+
+}  // extern "C"

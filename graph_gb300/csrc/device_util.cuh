@@ -1,0 +1,74 @@
+// device_util.cuh — warp/block primitives and the near-field slot selection
+// shared by the plain and the batched tick kernels.
+#pragma once
+#include <cstdint>
+
+#include "common.cuh"
+
+namespace cgl {
+
+constexpr int kBlock = 256;
+
+__device__ __forceinline__ long long warp_sum_ll(long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+static __device__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total) {
+  __shared__ uint32_t warp_tot[kBlock / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    uint32_t t = lane < (kBlock / 32) ? warp_tot[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    if (lane < (kBlock / 32)) warp_tot[lane] = t;
+  }
+  __syncthreads();
+  const uint32_t before = w > 0 ? warp_tot[w - 1] : 0;
+  *total = warp_tot[kBlock / 32 - 1];
+  __syncthreads();
+  return before + x - v;
+}
+
+// Insert (hash bits, index) into a sorted list of the 8 smallest DISTINCT
+// hashes, each kept with its lowest index (the peel's tie rule,
+// build-nearfield-slots.vert:146-162); `at` tracks segment positions.
+__device__ __forceinline__ void top8_insert(unsigned long long (&best)[kSlots], uint32_t (&at)[kSlots],
+                                            unsigned long long key, uint32_t pos) {
+  const uint32_t hb = (uint32_t)(key >> 32);
+  bool dup = false;
+#pragma unroll
+  for (int q = 0; q < kSlots; ++q) {
+    if ((uint32_t)(best[q] >> 32) == hb && best[q] != ~0ull) {
+      dup = true;
+      if (key < best[q]) { best[q] = key; at[q] = pos; }
+    }
+  }
+  if (!dup && key < best[kSlots - 1]) {
+#pragma unroll
+    for (int q = 0; q < kSlots; ++q) {
+      if (key < best[q]) {
+        unsigned long long tk = best[q]; best[q] = key; key = tk;
+        uint32_t ta = at[q]; at[q] = pos; pos = ta;
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ unsigned long long peel_key(uint32_t idx, uint32_t seed_bits) {
+  return ((unsigned long long)__float_as_uint(peel_hash(idx, seed_bits)) << 32) | idx;
+}
+
+}  // namespace cgl

@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/cgl.h"
+#include "ingest.h"
 #include "kernels.cuh"
 
 using namespace cgl;
@@ -22,14 +23,6 @@ namespace {
 
 constexpr double kAlphaMin = 0.001;   // ALPHA_MIN (Store/index.ts:8)
 constexpr uint32_t kParamChunk = 4096; // ticks per parameter upload
-
-// SplitMix64 draw k (0-based) of seed s; u = top 53 bits / 2^53.
-inline uint64_t splitmix_draw(uint64_t seed, uint64_t k) {
-  uint64_t z = seed + (k + 1) * 0x9E3779B97F4A7C15ull;
-  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-  return z ^ (z >> 31);
-}
 
 struct DevBuf {
   void* p = nullptr;
@@ -105,8 +98,10 @@ struct cgl_engine {
   bool use_graph = true;
 
   double rnd(double mn, double mx) {
-    double u = (double)(splitmix_draw(rng_seed, rng_ctr++) >> 11) * 0x1.0p-53;
-    return mn + (mx - mn) * u;
+    ingest::Rng r{rng_seed, rng_ctr};
+    const double v = r.uniform(mn, mx);
+    rng_ctr = r.ctr;
+    return v;
   }
 };
 
@@ -168,37 +163,9 @@ void dev_free_all(cgl_engine* e) {
   e->dev_bytes = 0;
 }
 
-void adjust_space_size(cgl_engine* e) {
-  // Store.adjustSpaceSize (Store/index.ts:209-233)
-  double s = e->cfg.space_size;
-  if (!(s > 0) || !std::isfinite(s)) s = 4096;
-  if (s < 2) s = 2;
-  const double m = e->cfg.max_texture_dimension;
-  if (m > 0 && std::isfinite(m) && m >= 2 && s >= m) s = std::max(m / 2, 2.0);
-  e->adjusted_space = s;
-}
+void adjust_space_size(cgl_engine* e) { e->adjusted_space = ingest::adjusted_space(e->cfg); }
 
-bool is_point_index(double v, uint64_t n) {
-  // GraphData.isPointIndex (GraphData/index.ts:286-289)
-  return std::isfinite(v) && v == std::floor(v) && v >= 0 && v < (double)n;
-}
-
-int ceil_log2_u64(uint64_t v) { int k = 0; while ((1ull << k) < v) ++k; return k; }
-
-void setup_fixed(cgl_engine* e) {
-  // Exact cell sums: coordinates saturate at B = smallest power of two >= 2*S,
-  // scaled by 2^F with F = 62 - ceil(log2 N) - log2 B (N * B * 2^F <= 2^62).
-  const float S = (float)e->adjusted_space;
-  int lb = 0;
-  while (std::ldexp(1.0, lb) < 2.0 * (double)S) ++lb;
-  const int ln = ceil_log2_u64(e->N < 1 ? 1 : e->N);
-  int F = 62 - ln - lb;
-  if (F > 60) F = 60;
-  e->fixed_bits = F;
-  e->fx.bound = (float)std::ldexp(1.0, lb);
-  e->fx.scale = std::ldexp(1.0f, F);
-  e->fx.inv = std::ldexp(1.0f, -F);
-}
+void setup_fixed(cgl_engine* e) { e->fx = ingest::fixed_for(e->N, e->adjusted_space, &e->fixed_bits); }
 
 float resolved_size(const cgl_engine* e, uint64_t i) {
   // GraphData.getResolvedPointSize (GraphData/index.ts:189-194); EXIT_DEFAULT_SIZE = 0
@@ -455,59 +422,6 @@ cgl_status apply_pinned(cgl_engine* e) {
   return CGL_OK;
 }
 
-// ForceLink.create for one direction (ForceLink/index.ts:40-83): CSR stable in
-// link-index order, bias / strength in FP64 rounded to f32, one random draw
-// per entry in CSR order.
-void build_csr(cgl_engine* e, const std::vector<float>& links, bool incoming, const std::vector<uint32_t>& deg,
-               std::vector<uint32_t>& rowptr, std::vector<uint4>& ent, uint32_t& max_deg) {
-  const uint64_t N = e->N, E = e->E;
-  rowptr.assign(N + 1, 0);
-  std::vector<uint8_t> valid(E, 0);
-  for (uint64_t i = 0; i < E; ++i) {
-    const double s = links[2 * i], t = links[2 * i + 1];
-    if (!is_point_index(s, N) || !is_point_index(t, N)) continue;
-    valid[i] = 1;
-    const uint32_t p = (uint32_t)(incoming ? s : t);
-    rowptr[p + 1]++;
-  }
-  max_deg = 0;
-  for (uint64_t p = 0; p < N; ++p) {
-    max_deg = std::max(max_deg, rowptr[p + 1]);
-    rowptr[p + 1] += rowptr[p];
-  }
-  const uint32_t M = rowptr[N];
-  ent.assign(M, make_uint4(0, 0, 0, 0));
-  std::vector<uint32_t> lidx(M);
-  std::vector<uint32_t> cur(rowptr.begin(), rowptr.end() - 1);
-  for (uint64_t i = 0; i < E; ++i) {
-    if (!valid[i]) continue;
-    const uint32_t s = (uint32_t)links[2 * i], t = (uint32_t)links[2 * i + 1];
-    const uint32_t p = incoming ? s : t, q = incoming ? t : s;
-    const uint32_t at = cur[p]++;
-    ent[at].x = q;
-    lidx[at] = (uint32_t)i;
-  }
-  for (uint64_t p = 0; p < N; ++p) {
-    for (uint32_t at = rowptr[p]; at < rowptr[p + 1]; ++at) {
-      const uint32_t q = ent[at].x;
-      const double degree = deg[q], connected = deg[p];
-      const double sum = degree + connected;
-      const double bias = sum != 0 ? degree / sum : 0.5;
-      const double mind = std::min(degree, connected);
-      double strength;
-      const double si = e->has_strength ? (double)e->in_strength[lidx[at]] : 0.0;
-      if (!e->has_strength || !std::isfinite(si) || si < 0) strength = 1.0 / std::max(mind, 1.0);
-      else strength = si;
-      strength = std::sqrt(strength);
-      const float fb = (float)bias, fs = (float)strength, fr = (float)e->rnd(0, 1);
-      std::memcpy(&ent[at].y, &fr, 4);
-      std::memcpy(&ent[at].z, &fb, 4);
-      std::memcpy(&ent[at].w, &fs, 4);
-      if (e->absent[q]) ent[at].x = kAbsentTarget;   // skipped at run time (force-spring.ts:71-74)
-    }
-  }
-}
-
 cgl_status do_render(cgl_engine* e, double alpha) {
   // GraphData.update (GraphData/index.ts:443-462)
   const uint64_t N = e->have_pos_input ? e->in_pos.size() / 2 : 0;
@@ -530,17 +444,8 @@ cgl_status do_render(cgl_engine* e, double alpha) {
   if (pos_changed) {
     e->graph_dirty = true;
     // Points.updatePositions (Points/index.ts:390-592)
-    std::vector<float> pos(2 * n);
-    e->absent.assign(n, 0);
-    e->live = 0;
-    for (size_t i = 0; i < n; ++i) {
-      const float x = e->in_pos[2 * i], y = e->in_pos[2 * i + 1];
-      const bool ab = std::isnan(x) || std::isnan(y);
-      e->absent[i] = ab;
-      e->live += !ab;
-      pos[2 * i] = ab ? NAN : x;
-      pos[2 * i + 1] = ab ? NAN : y;
-    }
+    std::vector<float2> pos;
+    e->live = ingest::canonical_positions(e->in_pos.data(), n, pos, e->absent);
     if ((st = dev_reserve(e, e->b_pos, n * sizeof(float2), false))) return st;
     if ((st = dev_reserve(e, e->b_pos_alt, n * sizeof(float2), false))) return st;
     if ((st = dev_reserve(e, e->b_flags, n, false))) return st;
@@ -558,10 +463,9 @@ cgl_status do_render(cgl_engine* e, double alpha) {
     // the jitter texture (2 draws per texel of pointsTextureSize^2, :133-138)
     e->mb_ready = false;
     if (e->T) {
-      const double target = 2 * std::sqrt((double)e->N);
-      const double g = std::min((double)kMaxGrid, std::max(8.0, std::pow(2.0, std::ceil(std::log2(target)))));
-      e->Gf = (int)g;
-      e->L = (int)std::log2(g) - 1;
+      const ingest::Grid grid = ingest::grid_for(e->N);
+      e->Gf = grid.gf;
+      e->L = grid.levels;
       e->tile = std::min(16, e->Gf);
       uint32_t off = 0;
       for (int l = 0; l < e->L; ++l) { e->level_off[l] = off; off += (uint32_t)((4 << l) * (4 << l)); }
@@ -580,13 +484,10 @@ cgl_status do_render(cgl_engine* e, double alpha) {
       if ((st = dev_reserve(e, e->b_big_sx, cells * sizeof(long long), false))) return st;
       if ((st = dev_reserve(e, e->b_big_sy, cells * sizeof(long long), false))) return st;
       if ((st = dev_reserve(e, e->b_big_ns, cells * sizeof(uint32_t), false))) return st;
-      std::vector<float2> jit(n);
-      const uint64_t texels = (uint64_t)e->T * e->T;
-      for (uint64_t t = 0; t < texels; ++t) {
-        const float jx = (float)(e->rnd(-1, 1) * 0.00001);
-        const float jy = (float)(e->rnd(-1, 1) * 0.00001);
-        if (t < n) jit[t] = make_float2(jx, jy);
-      }
+      std::vector<float2> jit;
+      ingest::Rng rng{e->rng_seed, e->rng_ctr};
+      ingest::jitter(rng, n, jit);
+      e->rng_ctr = rng.ctr;
       if (n) CU(cudaMemcpyAsync(e->b_jitter.p, jit.data(), n * sizeof(float2), cudaMemcpyHostToDevice, e->stream));
       CU(cudaStreamSynchronize(e->stream));
       e->mb_ready = true;
@@ -597,27 +498,25 @@ cgl_status do_render(cgl_engine* e, double alpha) {
   if (links_changed) {
     e->graph_dirty = true;
     // ForceLink.create(INCOMING) then (OUTGOING) (src/index.ts:1663-1666)
-    std::vector<uint32_t> rp_in, rp_out;
-    std::vector<uint4> en_in, en_out;
-    e->max_deg_in = e->max_deg_out = 0;
+    ingest::Csr cin, cout_;
     if (e->T && e->W) {
-      std::vector<uint32_t> deg(n, 0);
-      for (uint64_t i = 0; i < E; ++i) {
-        const double s = e->in_links[2 * i], t = e->in_links[2 * i + 1];
-        if (is_point_index(s, n) && is_point_index(t, n)) { deg[(size_t)s]++; deg[(size_t)t]++; }
-      }
-      build_csr(e, e->in_links, true, deg, rp_in, en_in, e->max_deg_in);
-      build_csr(e, e->in_links, false, deg, rp_out, en_out, e->max_deg_out);
+      ingest::Rng rng{e->rng_seed, e->rng_ctr};
+      ingest::build_links(e->in_links.data(), E, n, e->has_strength ? e->in_strength.data() : nullptr, e->absent, rng,
+                          cin, cout_);
+      e->rng_ctr = rng.ctr;
     } else {
-      rp_in.assign(n + 1, 0);
-      rp_out.assign(n + 1, 0);
+      cin.rowptr.assign(n + 1, 0);
+      cout_.rowptr.assign(n + 1, 0);
     }
+    std::vector<uint32_t>& rp_in = cin.rowptr;
+    std::vector<uint32_t>& rp_out = cout_.rowptr;
+    std::vector<uint4>& en_in = cin.ent;
+    std::vector<uint4>& en_out = cout_.ent;
+    std::vector<uint32_t>& hv_in = cin.heavy;
+    std::vector<uint32_t>& hv_out = cout_.heavy;
+    e->max_deg_in = cin.max_degree;
+    e->max_deg_out = cout_.max_degree;
     e->entries = en_in.size();
-    std::vector<uint32_t> hv_in, hv_out;
-    for (uint64_t p = 0; p < n && !rp_in.empty(); ++p) {
-      if (rp_in[p + 1] - rp_in[p] > kHeavyDegree) hv_in.push_back((uint32_t)p);
-      if (rp_out[p + 1] - rp_out[p] > kHeavyDegree) hv_out.push_back((uint32_t)p);
-    }
     e->n_heavy_in = (uint32_t)hv_in.size();
     e->n_heavy_out = (uint32_t)hv_out.size();
     if ((st = dev_reserve(e, e->b_heavy_in, hv_in.size() * sizeof(uint32_t), false))) return st;

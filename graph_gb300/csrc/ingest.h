@@ -1,0 +1,191 @@
+// ingest.h — host-side ingest shared by the plain and the batched engine:
+// what Graph.render does before the first tick (GraphData.update,
+// Points.updatePositions, ForceManyBody.create, ForceLink.create).
+// Both engines call these functions, so a graph ingested into a batch gets the
+// same device data, random draws included, as the same graph on its own.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "../../include/cgl.h"
+#include "common.cuh"
+
+namespace cgl {
+namespace ingest {
+
+// SplitMix64 draw k (0-based) of seed s; u = top 53 bits / 2^53, and
+// Random.float(min, max) = min + (max - min) * u (Store/index.ts:200-202).
+inline uint64_t splitmix_draw(uint64_t seed, uint64_t k) {
+  uint64_t z = seed + (k + 1) * 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+struct Rng {
+  uint64_t seed = 0, ctr = 0;
+  double uniform(double mn, double mx) {
+    const double u = (double)(splitmix_draw(seed, ctr++) >> 11) * 0x1.0p-53;
+    return mn + (mx - mn) * u;
+  }
+};
+
+// Store.adjustSpaceSize (Store/index.ts:209-233)
+inline double adjusted_space(const cgl_config& c) {
+  double s = c.space_size;
+  if (!(s > 0) || !std::isfinite(s)) s = 4096;
+  if (s < 2) s = 2;
+  const double m = c.max_texture_dimension;
+  if (m > 0 && std::isfinite(m) && m >= 2 && s >= m) s = std::max(m / 2, 2.0);
+  return s;
+}
+
+// GraphData.isPointIndex (GraphData/index.ts:286-289)
+inline bool is_point_index(double v, uint64_t n) {
+  return std::isfinite(v) && v == std::floor(v) && v >= 0 && v < (double)n;
+}
+
+// Exact cell sums: coordinates saturate at B = smallest power of two >= 2*S,
+// scaled by 2^F with F = 62 - ceil(log2 N) - log2 B (N * B * 2^F <= 2^62).
+inline FixedScale fixed_for(uint64_t n, double space, int* bits) {
+  const float S = (float)space;
+  int lb = 0;
+  while (std::ldexp(1.0, lb) < 2.0 * (double)S) ++lb;
+  int ln = 0;
+  while ((1ull << ln) < (n < 1 ? 1 : n)) ++ln;
+  int F = 62 - ln - lb;
+  if (F > 60) F = 60;
+  if (bits) *bits = F;
+  FixedScale fx;
+  fx.bound = (float)std::ldexp(1.0, lb);
+  fx.scale = std::ldexp(1.0f, F);
+  fx.inv = std::ldexp(1.0f, -F);
+  return fx;
+}
+
+// ForceManyBody.createLevels (ForceManyBody/index.ts:646-667)
+struct Grid {
+  int gf = 0, levels = 0;
+};
+inline Grid grid_for(uint64_t n) {
+  Grid g;
+  const double target = 2 * std::sqrt((double)n);
+  const double f = std::min((double)kMaxGrid, std::max(8.0, std::pow(2.0, std::ceil(std::log2(target)))));
+  g.gf = (int)f;
+  g.levels = (int)std::log2(f) - 1;
+  return g;
+}
+// cells of all levels of a pyramid with `levels` levels, and the offset of level l
+inline uint32_t level_base(int l) { uint32_t o = 0; for (int m = 0; m < l; ++m) o += (uint32_t)((4 << m) * (4 << m)); return o; }
+
+// Points.updatePositions (Points/index.ts:390-592, position-utils.ts:9-27):
+// a NaN in either coordinate makes the point absent (both coordinates NaN).
+inline uint64_t canonical_positions(const float* xy, uint64_t n, std::vector<float2>& pos, std::vector<uint8_t>& absent) {
+  pos.resize(n);
+  absent.assign(n, 0);
+  uint64_t live = 0;
+  for (uint64_t i = 0; i < n; ++i) {
+    const float x = xy[2 * i], y = xy[2 * i + 1];
+    const bool ab = std::isnan(x) || std::isnan(y);
+    absent[i] = ab;
+    live += !ab;
+    pos[i] = ab ? make_float2(NAN, NAN) : make_float2(x, y);
+  }
+  return live;
+}
+
+// ForceManyBody.create jitter (ForceManyBody/index.ts:133-138): two draws per
+// texel of the pointsTextureSize^2 texture, texel order, only the first n kept.
+inline void jitter(Rng& rng, uint64_t n, std::vector<float2>& out) {
+  out.resize(n);
+  const uint64_t T = (uint64_t)std::ceil(std::sqrt((double)n));
+  const uint64_t texels = T * T;
+  for (uint64_t t = 0; t < texels; ++t) {
+    const float jx = (float)(rng.uniform(-1, 1) * 0.00001);
+    const float jy = (float)(rng.uniform(-1, 1) * 0.00001);
+    if (t < n) out[t] = make_float2(jx, jy);
+  }
+}
+
+struct Csr {
+  std::vector<uint32_t> rowptr;   // n + 1
+  std::vector<uint4> ent;         // (neighbour, random distance draw bits, bias bits, strength bits)
+  std::vector<uint32_t> heavy;    // points whose list is longer than kHeavyDegree
+  uint32_t max_degree = 0;
+};
+
+// ForceLink.create for one direction (ForceLink/index.ts:40-83): lists in
+// link-index order (GraphData/index.ts:534-547); bias and strength in FP64
+// rounded to f32; one random draw per entry in list order.  Links to absent
+// points keep their draw and carry the kAbsentTarget sentinel.
+inline void build_direction(const float* links, uint64_t E, uint64_t N, bool incoming, const std::vector<uint32_t>& deg,
+                            const float* strength, const std::vector<uint8_t>& absent, Rng& rng, Csr& c) {
+  c.rowptr.assign(N + 1, 0);
+  std::vector<uint8_t> valid(E, 0);
+  for (uint64_t i = 0; i < E; ++i) {
+    const double s = links[2 * i], t = links[2 * i + 1];
+    if (!is_point_index(s, N) || !is_point_index(t, N)) continue;
+    valid[i] = 1;
+    c.rowptr[(uint32_t)(incoming ? s : t) + 1]++;
+  }
+  c.max_degree = 0;
+  c.heavy.clear();
+  for (uint64_t p = 0; p < N; ++p) {
+    c.max_degree = std::max(c.max_degree, c.rowptr[p + 1]);
+    if (c.rowptr[p + 1] > kHeavyDegree) c.heavy.push_back((uint32_t)p);
+    c.rowptr[p + 1] += c.rowptr[p];
+  }
+  const uint32_t M = c.rowptr[N];
+  c.ent.assign(M, make_uint4(0, 0, 0, 0));
+  std::vector<uint32_t> lidx(M);
+  std::vector<uint32_t> cur(c.rowptr.begin(), c.rowptr.end() - 1);
+  for (uint64_t i = 0; i < E; ++i) {
+    if (!valid[i]) continue;
+    const uint32_t s = (uint32_t)links[2 * i], t = (uint32_t)links[2 * i + 1];
+    const uint32_t p = incoming ? s : t, q = incoming ? t : s;
+    const uint32_t at = cur[p]++;
+    c.ent[at].x = q;
+    lidx[at] = (uint32_t)i;
+  }
+  for (uint64_t p = 0; p < N; ++p) {
+    for (uint32_t at = c.rowptr[p]; at < c.rowptr[p + 1]; ++at) {
+      const uint32_t q = c.ent[at].x;
+      const double degree = deg[q], connected = deg[p];
+      const double sum = degree + connected;
+      const double bias = sum != 0 ? degree / sum : 0.5;
+      const double mind = std::min(degree, connected);
+      double st;
+      const double si = strength ? (double)strength[lidx[at]] : 0.0;
+      if (!strength || !std::isfinite(si) || si < 0) st = 1.0 / std::max(mind, 1.0);
+      else st = si;
+      st = std::sqrt(st);
+      const float fb = (float)bias, fs = (float)st, fr = (float)rng.uniform(0, 1);
+      std::memcpy(&c.ent[at].y, &fr, 4);
+      std::memcpy(&c.ent[at].z, &fb, 4);
+      std::memcpy(&c.ent[at].w, &fs, 4);
+      if (absent[q]) c.ent[at].x = kAbsentTarget;
+    }
+  }
+}
+
+// ForceLink.create(INCOMING) then (OUTGOING) (src/index.ts:1663-1666).
+// `strength` is used only when its length matched linksNumber
+// (GraphData/index.ts:408-418); pass nullptr otherwise.
+inline void build_links(const float* links, uint64_t E, uint64_t N, const float* strength,
+                        const std::vector<uint8_t>& absent, Rng& rng, Csr& in, Csr& out) {
+  std::vector<uint32_t> deg(N, 0);
+  for (uint64_t i = 0; i < E; ++i) {
+    const double s = links[2 * i], t = links[2 * i + 1];
+    if (is_point_index(s, N) && is_point_index(t, N)) { deg[(size_t)s]++; deg[(size_t)t]++; }
+  }
+  build_direction(links, E, N, true, deg, strength, absent, rng, in);
+  build_direction(links, E, N, false, deg, strength, absent, rng, out);
+}
+
+}  // namespace ingest
+}  // namespace cgl

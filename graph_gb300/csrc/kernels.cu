@@ -18,22 +18,15 @@
 //                (build-grid.vert, force-collision-spatial.frag)
 // Kernels read the tick's alpha and peel seed from device memory so that one
 // captured CUDA graph serves every tick.
+#include "device_util.cuh"
 #include "kernels.cuh"
 
 namespace cgl {
 
 namespace {
 
-constexpr int kBlock = 256;
-
 __device__ __forceinline__ TickParams tick_params(const DeviceView& d) {
   return d.tick_params[*d.tick_ctr];
-}
-
-__device__ __forceinline__ long long warp_sum_ll(long long v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  return v;
 }
 
 // Block-reduce three integer sums and add them to dst[0..2] (one atomic each).
@@ -131,33 +124,6 @@ __global__ void __launch_bounds__(kBlock) k_center(DeviceView d, SimScalars s) {
 constexpr int kScanItems = 4;
 constexpr int kScanChunk = kBlock * kScanItems;   // cells per scan block
 
-__device__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total) {
-  __shared__ uint32_t warp_tot[kBlock / 32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  uint32_t x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) warp_tot[w] = x;
-  __syncthreads();
-  if (w == 0) {
-    uint32_t t = lane < (kBlock / 32) ? warp_tot[lane] : 0;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
-      if (lane >= o) t += y;
-    }
-    if (lane < (kBlock / 32)) warp_tot[lane] = t;
-  }
-  __syncthreads();
-  const uint32_t before = w > 0 ? warp_tot[w - 1] : 0;
-  *total = warp_tot[kBlock / 32 - 1];
-  __syncthreads();
-  return before + x - v;
-}
-
 __global__ void __launch_bounds__(kBlock) k_scan_reduce(DeviceView d, uint32_t cells) {
   const uint32_t base = blockIdx.x * kScanChunk;
   uint32_t sum = 0;
@@ -238,31 +204,6 @@ __global__ void __launch_bounds__(kBlock) k_scatter(DeviceView d) {
 }
 
 // ------------------------------------------------------------------ cells --
-// Insert (hash bits, index) into a sorted list of the 8 smallest DISTINCT
-// hashes, each kept with its lowest index (the peel's tie rule,
-// build-nearfield-slots.vert:146-162); `at` tracks segment positions.
-__device__ __forceinline__ void top8_insert(unsigned long long (&best)[kSlots], uint32_t (&at)[kSlots],
-                                            unsigned long long key, uint32_t pos) {
-  const uint32_t hb = (uint32_t)(key >> 32);
-  bool dup = false;
-#pragma unroll
-  for (int q = 0; q < kSlots; ++q) {
-    if ((uint32_t)(best[q] >> 32) == hb && best[q] != ~0ull) {
-      dup = true;
-      if (key < best[q]) { best[q] = key; at[q] = pos; }
-    }
-  }
-  if (!dup && key < best[kSlots - 1]) {
-#pragma unroll
-    for (int q = 0; q < kSlots; ++q) {
-      if (key < best[q]) {
-        unsigned long long tk = best[q]; best[q] = key; key = tk;
-        uint32_t ta = at[q]; at[q] = pos; pos = ta;
-      }
-    }
-  }
-}
-
 // Move the ns selected entries to the head of the segment starting at b, in
 // slot (hash) order; the rest of the segment keeps its points in any order.
 __device__ __forceinline__ void move_slots_to_head(const DeviceView& d, uint32_t b, int ns, uint32_t (&at)[kSlots]) {
@@ -281,10 +222,6 @@ __device__ __forceinline__ void move_slots_to_head(const DeviceView& d, uint32_t
       }
     }
   }
-}
-
-__device__ __forceinline__ unsigned long long peel_key(uint32_t idx, uint32_t seed_bits) {
-  return ((unsigned long long)__float_as_uint(peel_hash(idx, seed_bits)) << 32) | idx;
 }
 
 // Cells holding more than kSmallCell points (lists built by the scan): above

@@ -77,9 +77,6 @@ struct SimScalars {
   FixedScale fx;
 };
 
-constexpr uint32_t kHeavyDegree = 256;   // longer link lists run on a side branch, started first
-constexpr uint32_t kSmallCell = 16;   // cells above this size get a warp of their own
-constexpr uint32_t kBigCell = 2048;   // cells above this size get a CTA of their own
 
 enum PrepassMode : uint32_t { kPreGravity = 1, kPreCentroid = 2, kPreBin = 4 };
 

@@ -203,6 +203,46 @@ cgl_status cgl_debug_get_cells(cgl_engine* e, uint32_t level, float* out, uint64
 /* finest level: 8 point indices per cell in slot (hash) order, -1 = empty slot. */
 cgl_status cgl_debug_get_slots(cgl_engine* e, int32_t* out, uint64_t capacity);
 
+/* --- Batched engine (no counterpart in the reference) -----------------------
+ * Many independent layout jobs advance together: one CUDA-graph launch per
+ * tick runs every job in the batch.  Each job behaves exactly as a plain
+ * engine created with the same config, given the same positions and links,
+ * rendered and started at alpha 1 (cgl_create + cgl_set_point_positions +
+ * cgl_set_links + cgl_render + cgl_start), stepping the same ticks.  Jobs join
+ * and leave between ticks (continuous batching).  Jobs run gravity, many-body
+ * and link forces; center and collision need a plain engine. */
+typedef struct cgl_batch cgl_batch;
+
+typedef struct cgl_batch_info {
+  uint64_t jobs;              /* jobs in the batch */
+  uint64_t running_jobs;      /* jobs that still advance */
+  uint64_t points;            /* points of all jobs */
+  uint64_t link_entries;      /* link entries per direction, all jobs */
+  uint64_t point_arena;       /* device capacities */
+  uint64_t cell_arena;
+  uint64_t device_bytes;
+  uint32_t kernels_per_tick;
+  uint32_t reserved;
+} cgl_batch_info;
+
+/* hbm_budget_bytes: device memory the batch may hold (0 = unlimited); an add
+ * that would exceed it fails with CGL_OOM (admission control). */
+cgl_status cgl_batch_create(int32_t device, double hbm_budget_bytes, cgl_batch** out);
+cgl_status cgl_batch_destroy(cgl_batch* b);
+/* Add a job; it advances on every later cgl_batch_step until it has run
+ * max_ticks ticks (0 = no limit) or, when stop_below_alpha_min is set, until
+ * alpha < ALPHA_MIN before a tick (the animation-frame loop's end condition,
+ * src/index.ts:2164-2169). */
+cgl_status cgl_batch_add(cgl_batch* b, const cgl_config* cfg, const float* xy, uint64_t n_floats, const float* links,
+                         uint64_t n_link_floats, uint32_t max_ticks, int32_t stop_below_alpha_min, uint32_t* id);
+cgl_status cgl_batch_remove(cgl_batch* b, uint32_t id);
+cgl_status cgl_batch_step(cgl_batch* b, uint32_t ticks);
+cgl_status cgl_batch_synchronize(cgl_batch* b);
+cgl_status cgl_batch_get_point_positions(cgl_batch* b, uint32_t id, float* out_xy, uint64_t capacity_floats);
+cgl_status cgl_batch_get_state(cgl_batch* b, uint32_t id, cgl_state* out);
+cgl_status cgl_batch_get_info(cgl_batch* b, cgl_batch_info* out);
+const char* cgl_batch_last_error(cgl_batch* b);
+
 /* Many-body grid pyramid without any device allocation.  No counterpart in the
  * reference: it exists for callers that must not have a library allocate GPU
  * memory — hosts that own the whole memory budget through their own allocator,

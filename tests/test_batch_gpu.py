@@ -1,0 +1,129 @@
+"""Batched engine: every job in a batch advances exactly as it would alone.
+
+The reference runs one graph per `Graph`; the batch is an engine extension
+whose contract is equivalence: a job's positions after T ticks in a batch are
+bit-identical to a plain engine (cgl_create, set positions and links, render,
+start(1), step T) with the same config — and so, transitively, to the oracle.
+"""
+import numpy as np
+import pytest
+
+from graph_gb300 import _abi, generators
+
+from helpers import first_mismatch, same_bits
+
+pytestmark = pytest.mark.gpu
+
+
+def _alone(pos, links, fields, ticks):
+    from graph_gb300.engine import Engine
+    e = Engine(**fields)
+    e.set_point_positions(pos)
+    if links is not None:
+        e.set_links(links)
+    e.render()
+    e.start(1.0)
+    e.step(ticks)
+    out = e.get_point_positions()
+    e.close()
+    return out
+
+
+def _jobs(seed=0):
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for k, n in enumerate([1, 2, 3, 40, 150, 600, 2500, 9000, 30000]):
+        space = float(2 ** int(np.ceil(np.log2(max(64.0, 40 * np.sqrt(n))))))
+        pos = rng.uniform(0, space, size=2 * n).astype(np.float32)
+        if k % 2:
+            links = generators.barabasi_albert(n, 3, seed + k) if n > 3 else None
+        else:
+            links = generators.erdos_renyi(n, 6, seed + k) if n > 3 else None
+        fields = dict(space_size=space, simulation_repulsion=float(rng.uniform(0.05, 0.5)),
+                      simulation_link_distance=2.0, random_seed=1000 + k)
+        jobs.append((pos, links, fields))
+    # special cases: absent points, a hub list on the side branch, masked stages, no gravity
+    pos, links, fields = jobs[6]
+    pos = pos.copy()
+    pos[10:30] = np.nan
+    jobs.append((pos, links, dict(fields, random_seed=77)))
+    n = 1200
+    star = np.stack([np.zeros(n - 1), np.arange(1, n)], axis=1).astype(np.float32).reshape(-1)
+    jobs.append((rng.uniform(500, 1500, size=2 * n).astype(np.float32), star, dict(space_size=2048.0, random_seed=78)))
+    jobs.append((jobs[5][0], jobs[5][1], dict(jobs[5][2], stage_mask=_abi.STAGE_MANYBODY | _abi.STAGE_LINK_IN,
+                                              random_seed=79)))
+    jobs.append((jobs[7][0], jobs[7][1], dict(jobs[7][2], simulation_gravity=0.0, random_seed=80)))
+    return jobs
+
+
+def test_batch_equals_each_job_alone():
+    from graph_gb300.batch import Batch
+    jobs = _jobs()
+    ticks = 12
+    with Batch() as b:
+        ids = [b.add(pos, links, **fields) for pos, links, fields in jobs]
+        info = b.info()
+        assert info.jobs == len(jobs)
+        b.step(5)
+        b.step(ticks - 5)
+        for (pos, links, fields), jid in zip(jobs, ids):
+            got = b.get_point_positions(jid)
+            want = _alone(pos, links, fields, ticks)
+            assert same_bits(got, want), (fields, first_mismatch(got, want))
+            assert b.state(jid).tick == ticks
+
+
+def test_tick_budgets_and_alpha_stop():
+    from graph_gb300.batch import Batch
+    jobs = _jobs(1)[:6]
+    with Batch() as b:
+        budgets = [3, 7, 0, 11, 5, 9]
+        ids = [b.add(pos, links, max_ticks=t, **fields) for (pos, links, fields), t in zip(jobs, budgets)]
+        stopper = b.add(jobs[5][0], jobs[5][1], stop_below_alpha_min=True,
+                        **dict(jobs[5][2], simulation_decay=3.5, random_seed=5))
+        b.step(15)
+        for (pos, links, fields), jid, t in zip(jobs, ids, budgets):
+            run = t if t else 15
+            assert b.state(jid).tick == run
+            assert same_bits(b.get_point_positions(jid), _alone(pos, links, fields, run))
+        # decay 3.5: alpha is 0.0027 after 3 ticks and 0.00037 after 4, so the loop stops before tick 5
+        s = b.state(stopper)
+        assert s.tick == 4 and not s.is_simulation_running
+
+
+def test_jobs_join_and_leave_between_ticks():
+    from graph_gb300.batch import Batch
+    jobs = _jobs(2)
+    with Batch() as b:
+        first = [b.add(pos, links, **fields) for pos, links, fields in jobs[:5]]
+        b.step(4)
+        b.remove(first[1])
+        b.remove(first[3])
+        later = [b.add(pos, links, **fields) for pos, links, fields in jobs[5:9]]   # reuse freed ranges
+        b.step(6)
+        for k in (0, 2, 4):
+            pos, links, fields = jobs[k]
+            assert same_bits(b.get_point_positions(first[k]), _alone(pos, links, fields, 10))
+        for (pos, links, fields), jid in zip(jobs[5:9], later):
+            assert same_bits(b.get_point_positions(jid), _alone(pos, links, fields, 6))
+
+
+def test_batch_rejects_center_and_collision():
+    from graph_gb300.batch import Batch
+    from graph_gb300._calls import StatusError
+    pos = generators.uniform_positions(100, 0, 4096, 1)
+    with Batch() as b:
+        with pytest.raises(StatusError):
+            b.add(pos, None, simulation_center=0.5)
+        with pytest.raises(StatusError):
+            b.add(pos, None, simulation_collision=0.5)
+
+
+def test_batch_budget_refuses_admission():
+    from graph_gb300.batch import Batch
+    from graph_gb300._calls import StatusError
+    pos = generators.uniform_positions(200_000, 0, 8192, 1)
+    with Batch(hbm_budget_bytes=8e6) as b:
+        with pytest.raises(StatusError) as ex:
+            b.add(pos, None, space_size=8192)
+        assert ex.value.status == _abi.CGL_OOM
