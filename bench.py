@@ -208,7 +208,11 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="sbm1m", choices=["sbm1m", "ba10k"])
+    ap.add_argument("--workload", default="sbm1m", choices=["sbm1m", "ba10k", "batch"])
+    ap.add_argument("--graphs", type=int, default=4096, help="jobs of the batched workload")
+    ap.add_argument("--ticks", type=int, default=300, help="ticks per job of the batched workload")
+    ap.add_argument("--plain-sample", type=int, default=0,
+                    help="time the plain engine on this many jobs only (0 = all) and scale to the whole set")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of oracle ticks for cpu_baseline")
     ap.add_argument("--save-positions", default=None, help="write the final positions (.npy) for profiling runs")
@@ -226,6 +230,9 @@ def main():
         if rank != 0:
             return
         run_reference(args)
+        return
+    if args.workload == "batch":
+        run_batch(args)
         return
 
     import torch
@@ -351,6 +358,86 @@ def main():
     eng.close()
     if dist:
         dist.destroy_process_group()
+
+
+def run_batch(args):
+    """Config 3: independent jobs advanced together by the batched engine,
+    against the plain engine run job by job on the same GPU.  Both sides do
+    the same work per job: ingest (positions, links, render), `ticks` ticks,
+    read-back of the final positions."""
+    import torch
+    from graph_gb300.batch import Batch
+    from graph_gb300.engine import Engine
+    torch.cuda.set_device(0)
+    t0 = time.perf_counter()
+    jobs = list(generators.batch_workload(args.graphs, seed=7))
+    gen_s = time.perf_counter() - t0
+    n_points = sum(p.size // 2 for p, _, _ in jobs)
+    n_links = sum(l.size // 2 for _, l, _ in jobs)
+    # batched
+    t0 = time.perf_counter()
+    b = Batch()
+    ids = [b.add(p, l, max_ticks=args.ticks, **f) for p, l, f in jobs]
+    b.synchronize()
+    t1 = time.perf_counter()
+    b.step(args.ticks)
+    b.synchronize()
+    t2 = time.perf_counter()
+    out_batch = [b.get_point_positions(i) for i in ids]
+    t3 = time.perf_counter()
+    info = b.info()
+    batch = {"ingest_s": t1 - t0, "simulate_s": t2 - t1, "readback_s": t3 - t2}
+    b.close()
+    # plain engine, job by job
+    idx = list(range(len(jobs)))
+    if args.plain_sample and args.plain_sample < len(jobs):
+        rng = np.random.default_rng(11)
+        idx = sorted(rng.choice(len(jobs), size=args.plain_sample, replace=False).tolist())
+    plain = {"ingest_s": 0.0, "simulate_s": 0.0, "readback_s": 0.0}
+    mismatches = 0
+    for k in idx:
+        p, l, f = jobs[k]
+        ta = time.perf_counter()
+        e = Engine(**f)
+        e.set_point_positions(p)
+        e.set_links(l)
+        e.render()
+        e.start(1.0)
+        e.synchronize()
+        tb = time.perf_counter()
+        e.step(args.ticks)
+        e.synchronize()
+        tc = time.perf_counter()
+        out = e.get_point_positions()
+        td = time.perf_counter()
+        e.close()
+        plain["ingest_s"] += tb - ta
+        plain["simulate_s"] += tc - tb
+        plain["readback_s"] += td - tc
+        a, o = out, out_batch[k]
+        same = np.array_equal(np.isnan(a), np.isnan(o)) and np.array_equal(a[~np.isnan(a)].view(np.uint32),
+                                                                           o[~np.isnan(o)].view(np.uint32))
+        mismatches += 0 if same else 1
+    scale = len(jobs) / len(idx)
+    plain = {k: v * scale for k, v in plain.items()}
+    tot_b = sum(batch.values())
+    tot_p = sum(plain.values())
+    out = {
+        "metric": "batched layouts/s", "value": len(jobs) / tot_b, "unit": "layouts/s",
+        "higher_is_better": True, "n_gpus": 1, "data": "synthetic",
+        "config": {"workload": "%d jobs, sizes log-uniform [100, 100000], half preferential attachment "
+                               "(m 2-6), half Erdos-Renyi (mean degree 4-12), %d ticks each" % (len(jobs), args.ticks),
+                   "points": int(n_points), "links": int(n_links), "generate_s": round(gen_s, 1)},
+        "batched": dict(batch, layouts_per_s=len(jobs) / tot_b, simulate_layouts_per_s=len(jobs) / batch["simulate_s"],
+                        point_iter_per_s=n_points * args.ticks / batch["simulate_s"],
+                        kernels_per_tick=int(info.kernels_per_tick), device_gb=info.device_bytes / 1e9),
+        "plain": dict(plain, layouts_per_s=len(jobs) / tot_p, simulate_layouts_per_s=len(jobs) / plain["simulate_s"],
+                      jobs_timed=len(idx), scaled_to_all=scale != 1.0),
+        "speedup_end_to_end": tot_p / tot_b,
+        "speedup_simulate": plain["simulate_s"] / batch["simulate_s"],
+        "bit_exact_vs_plain": "%d of %d jobs checked identical" % (len(idx) - mismatches, len(idx)),
+    }
+    print(json.dumps(out))
 
 
 def run_reference(args):

@@ -146,3 +146,74 @@ def uniform_positions(n, lo, hi, seed):
 def centred_square(n, space, seed):
     """Uniform in the centred square of side space/4."""
     return uniform_positions(n, space * 3 / 8, space * 5 / 8, seed)
+
+
+def preferential_attachment(n, m, seed):
+    """Barabasi-Albert-style graph by edge copying (Batagelj & Brandes 2005), vectorised.
+
+    Node v >= m adds m edges; each target is an endpoint drawn uniformly from
+    all endpoints of earlier edges (degree-proportional), resolved by pointer
+    jumping.  Self-loops and duplicate pairs are dropped, so a node keeps at
+    most m edges.
+    """
+    rng = np.random.default_rng(seed)
+    m = int(m)
+    if n <= m:
+        return np.zeros(0, dtype=np.float32)
+    k = np.arange(m * (n - m), dtype=np.int64)          # edge index
+    src = m + k // m
+    # endpoints: 2k = source of edge k, 2k+1 = target of edge k; the first m
+    # edges (node m) attach to nodes 0..m-1 directly
+    ptr = (rng.random(k.size) * (2 * k)).astype(np.int64)
+    tgt = np.full(k.size, -1, dtype=np.int64)
+    first = k < m
+    tgt[first] = k[first]
+    ptr[first] = -1
+    even = (~first) & (ptr % 2 == 0)
+    tgt[even] = src[ptr[even] // 2]
+    todo = np.nonzero(tgt < 0)[0]
+    ref = ptr[todo] // 2                                 # points at the target of an earlier edge
+    while todo.size:
+        t = tgt[ref]
+        done = t >= 0
+        tgt[todo[done]] = t[done]
+        todo, ref = todo[~done], ptr[ref[~done]]
+        odd = ref % 2 == 1
+        # ref now holds raw endpoint positions; even ones are sources
+        res = np.where(odd, -1, src[np.maximum(ref, 0) // 2])
+        hit = ~odd
+        tgt[todo[hit]] = res[hit]
+        todo, ref = todo[~hit], ref[~hit] // 2
+    keep = tgt != src
+    s, t = src[keep], tgt[keep]
+    key = np.minimum(s, t) * n + np.maximum(s, t)
+    _, first_idx = np.unique(key, return_index=True)
+    first_idx = np.sort(first_idx)
+    links = np.empty(2 * first_idx.size, dtype=np.float32)
+    links[0::2] = s[first_idx]
+    links[1::2] = t[first_idx]
+    return links
+
+
+def batch_workload(count, seed, n_min=100, n_max=100_000):
+    """Independent layout jobs: sizes log-uniform over [n_min, n_max], half
+    preferential-attachment (m in 2..6) and half Erdos-Renyi (mean degree in
+    4..12), each with its own seed, a power-of-two spaceSize fitted to its size
+    (2^round(log2(41 sqrt(n))), within [512, 16384]) and repulsion drawn from
+    [0.05, 0.5]; positions uniform in the centred square of side spaceSize/4.
+    Yields (positions, links, config fields)."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(n_min), np.log(n_max), size=count)).astype(np.int64)
+    for g in range(count):
+        n = int(sizes[g])
+        gseed = int(rng.integers(0, 2**31))
+        if g % 2 == 0:
+            links = preferential_attachment(n, int(rng.integers(2, 7)), gseed)
+        else:
+            links = erdos_renyi(n, float(rng.uniform(4, 12)), gseed)
+        space = float(2 ** int(np.clip(np.round(np.log2(41 * np.sqrt(n))), 9, 14)))
+        pos = centred_square(n, space, gseed + 1)
+        fields = dict(space_size=space, simulation_repulsion=float(rng.uniform(0.05, 0.5)),
+                      simulation_gravity=0.25, simulation_friction=0.85, simulation_link_spring=1.0,
+                      simulation_link_distance=2.0, simulation_decay=5000, random_seed=gseed)
+        yield pos, links, fields
