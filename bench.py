@@ -208,7 +208,9 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="sbm1m", choices=["sbm1m", "ba10k", "batch"])
+    ap.add_argument("--workload", default="sbm1m", choices=["sbm1m", "ba10k", "batch", "serve"])
+    ap.add_argument("--rates", default="50,100,200,500,1000,2000", help="request rates (req/s) of the serving sweep")
+    ap.add_argument("--requests", type=int, default=200, help="requests per rate of the serving sweep")
     ap.add_argument("--graphs", type=int, default=4096, help="jobs of the batched workload")
     ap.add_argument("--ticks", type=int, default=300, help="ticks per job of the batched workload")
     ap.add_argument("--plain-sample", type=int, default=0,
@@ -233,6 +235,9 @@ def main():
         return
     if args.workload == "batch":
         run_batch(args)
+        return
+    if args.workload == "serve":
+        run_serve(args)
         return
 
     import torch
@@ -437,6 +442,103 @@ def run_batch(args):
         "speedup_simulate": plain["simulate_s"] / batch["simulate_s"],
         "bit_exact_vs_plain": "%d of %d jobs checked identical" % (len(idx) - mismatches, len(idx)),
     }
+    print(json.dumps(out))
+
+
+def serve_requests(count, seed):
+    """Config 4 jobs: sizes log-normal (median 5,000 points, sigma 1.5, capped at
+    2,000,000), graph type as the batched workload, each until alpha < 0.001 or
+    1,000 ticks."""
+    rng = np.random.default_rng(seed)
+    sizes = np.minimum(2_000_000, np.maximum(2, np.round(np.exp(rng.normal(np.log(5000), 1.5, size=count)))))
+    out = []
+    for k, n in enumerate(sizes.astype(np.int64)):
+        n = int(n)
+        gseed = int(rng.integers(0, 2**31))
+        if k % 2 == 0:
+            links = generators.preferential_attachment(n, int(rng.integers(2, 7)), gseed)
+        else:
+            links = generators.erdos_renyi(n, float(rng.uniform(4, 12)), gseed)
+        space = float(2 ** int(np.clip(np.round(np.log2(41 * np.sqrt(n))), 9, 14)))
+        fields = dict(space_size=space, simulation_repulsion=float(rng.uniform(0.05, 0.5)),
+                      simulation_link_distance=2.0, simulation_decay=5000, random_seed=gseed)
+        out.append((generators.centred_square(n, space, gseed + 1), links, fields))
+    return out
+
+
+def run_serve(args):
+    """Config 4: Poisson arrivals at each rate; continuous batching (jobs join
+    and leave the device batch between rounds of 10 ticks, snapshots every 50
+    ticks, 150 GB admission budget) against a first-come-first-served queue
+    that runs one job at a time on a plain engine."""
+    import torch
+    from graph_gb300.engine import Engine
+    from graph_gb300.serve import LayoutService
+    torch.cuda.set_device(0)
+    jobs = serve_requests(args.requests, seed=9)
+    points = sum(p.size // 2 for p, _, _ in jobs)
+    max_ticks = 1000
+    # plain FIFO: measured service time of each job, then the queue recurrence
+    service = []
+    for p, l, f in jobs:
+        t0 = time.perf_counter()
+        e = Engine(**f)
+        e.set_point_positions(p)
+        e.set_links(l)
+        e.render()
+        e.start(1.0)
+        done = 0
+        while done < max_ticks:
+            n = e.run(50)
+            done += n
+            e.get_point_positions()          # the 50-tick snapshot
+            if n < 50:
+                break
+        e.close()
+        service.append(time.perf_counter() - t0)
+    rows = []
+    for rate in [float(r) for r in args.rates.split(",")]:
+        rng = np.random.default_rng(int(rate))
+        offsets = np.cumsum(rng.exponential(1.0 / rate, size=len(jobs)))
+        # FIFO plain engine
+        fin, lat = 0.0, []
+        for off, st in zip(offsets, service):
+            start = max(off, fin)
+            fin = start + st
+            lat.append(fin - off)
+        fifo = {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                "layouts_per_s": len(jobs) / (fin - offsets[0])}
+        # continuous batching, in real time
+        svc = LayoutService(hbm_budget_bytes=150e9, ticks_per_round=10, snapshot_every=50)
+        t0 = time.perf_counter()
+        nxt = 0
+        while True:
+            now = time.perf_counter() - t0
+            while nxt < len(jobs) and offsets[nxt] <= now:
+                p, l, f = jobs[nxt]
+                svc.submit(nxt, p, l, f, max_ticks=max_ticks, arrival=t0 + offsets[nxt])
+                nxt += 1
+            if svc.idle():
+                if nxt >= len(jobs):
+                    break
+                time.sleep(max(0.0, offsets[nxt] - (time.perf_counter() - t0)))
+                continue
+            svc.step_round()
+        lat_b = [r.finished - r.arrival for r in svc.done]
+        last = max(r.finished for r in svc.done) - t0
+        batched = {"p50_s": float(np.percentile(lat_b, 50)), "p99_s": float(np.percentile(lat_b, 99)),
+                   "layouts_per_s": len(jobs) / (last - offsets[0]),
+                   "snapshots": int(sum(r.snapshots for r in svc.done))}
+        svc.close()
+        rows.append({"rate_req_s": rate, "batched": batched, "fifo_plain": fifo})
+    out = {"metric": "serving p50/p99 time-to-converged-layout and layouts/s", "unit": "s, layouts/s",
+           "n_gpus": 1, "data": "synthetic",
+           "config": {"requests_per_rate": len(jobs), "points_total": int(points), "max_ticks": max_ticks,
+                      "sizes": "log-normal median 5000 sigma 1.5 cap 2,000,000", "round_ticks": 10,
+                      "snapshot_every": 50, "budget_gb": 150},
+           "plain_service_s": {"mean": float(np.mean(service)), "p50": float(np.percentile(service, 50)),
+                               "p99": float(np.percentile(service, 99))},
+           "sweep": rows}
     print(json.dumps(out))
 
 

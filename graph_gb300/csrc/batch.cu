@@ -438,16 +438,23 @@ cgl_status cgl_batch_add(cgl_batch* b, const cgl_config* cfg, const float* xy, u
     b->dirty = true;
     return a.alloc(n, off) ? CGL_OK : bfail(b, CGL_OOM, "arena allocation failed");
   };
-  if ((st = take(b->pts, j.n, &j.p_off, 0)) || (st = take(b->cells, j.cells, &j.cell_off, 1)) ||
-      (st = take(b->recs, j.recs, &j.rec_off, 2)) || (st = take(b->accs, j.accs, &j.acc_off, 3)) ||
-      (st = take(b->rows, j.n + 1, &j.rp_in, 4)) || (st = take(b->rows, j.n + 1, &j.rp_out, 4)) ||
-      (st = take(b->ents, j.m_in, &j.e_in, 5)) || (st = take(b->ents, j.m_out, &j.e_out, 5))) {
-    release(b, j);
-    return st;
+  // Take every range; on a refusal give back exactly the ranges already taken.
+  struct Want { Arena* a; uint64_t n; uint64_t* off; int kind; };
+  const Want wants[] = {{&b->pts, j.n, &j.p_off, 0},        {&b->cells, j.cells, &j.cell_off, 1},
+                        {&b->recs, j.recs, &j.rec_off, 2},   {&b->accs, j.accs, &j.acc_off, 3},
+                        {&b->rows, j.n + 1, &j.rp_in, 4},    {&b->rows, j.n + 1, &j.rp_out, 4},
+                        {&b->ents, j.m_in, &j.e_in, 5},      {&b->ents, j.m_out, &j.e_out, 5}};
+  int taken = 0;
+  st = CGL_OK;
+  for (const Want& w : wants) {
+    if ((st = take(*w.a, w.n, w.off, w.kind))) break;
+    ++taken;
   }
-  if (b->pts.hwm > 0xFFFFFF00ull || b->cells.hwm > 0xFFFFFF00ull || b->ents.hwm > 0xFFFFFF00ull) {
-    release(b, j);
-    return bfail(b, CGL_OOM, "arena index space (32 bits) exhausted");
+  if (!st && (b->pts.hwm > 0xFFFFFF00ull || b->cells.hwm > 0xFFFFFF00ull || b->ents.hwm > 0xFFFFFF00ull))
+    st = bfail(b, CGL_OOM, "arena index space (32 bits) exhausted");
+  if (st) {
+    for (int k = 0; k < taken; ++k) wants[k].a->release(*wants[k].off, wants[k].n);
+    return st;
   }
   // upload: absolute indices for rows and neighbours
   std::vector<uint32_t> rp_in(j.n + 1), rp_out(j.n + 1);
