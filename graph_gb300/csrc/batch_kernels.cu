@@ -170,7 +170,20 @@ __device__ void kb_warp_cell(const BatchView& v, uint32_t c) {
   uint32_t at[kSlots];
 #pragma unroll
   for (int q = 0; q < kSlots; ++q) { best[q] = ~0ull; at[q] = 0; }
-  for (uint32_t j = b + lane; j < e; j += 32) {
+  uint32_t j = b + lane;
+  for (; j + 96 < e; j += 128) {   // loads four points ahead of the selection
+    float2 p[4];
+    uint32_t ix[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) { p[u] = v.sorted_pos[j + 32 * u]; ix[u] = v.sorted_idx[j + 32 * u]; }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      ax += to_fixed(p[u].x, D.fx);
+      ay += to_fixed(p[u].y, D.fx);
+      top8_insert(best, at, local_key(ix[u], D.p_off, seed), j + 32 * u);
+    }
+  }
+  for (; j < e; j += 32) {
     const float2 p = v.sorted_pos[j];
     ax += to_fixed(p.x, D.fx);
     ay += to_fixed(p.y, D.fx);
@@ -513,9 +526,9 @@ __global__ void __launch_bounds__(kBlock) kb_manybody(BatchView v) {
       float sx = 0.f, sy = 0.f, sampled = 0.f;
 #pragma unroll 1
       for (int q = 0; q < kSlots; ++q) {
-        if (q >= ns) { sx = __fadd_rn(sx, 0.f); sy = __fadd_rn(sy, 0.f); continue; }
+        if (q >= ns) break;
         const uint32_t oi = __ldg(&v.sorted_idx[b + q]);
-        if ((float)(oi - D.p_off) == self) { sx = __fadd_rn(sx, 0.f); sy = __fadd_rn(sy, 0.f); continue; }
+        if ((float)(oi - D.p_off) == self) continue;
         const float2 o = __ldg(&v.sorted_pos[b + q]);
         sampled = __fadd_rn(sampled, 1.0f);
         pair_velocity(px, py, o.x, o.y, rj.x, rj.y, k, sx, sy);

@@ -512,13 +512,15 @@ cgl_status do_render(cgl_engine* e, double alpha) {
     std::vector<uint32_t>& rp_out = cout_.rowptr;
     std::vector<uint4>& en_in = cin.ent;
     std::vector<uint4>& en_out = cout_.ent;
-    std::vector<uint32_t>& hv_in = cin.heavy;
-    std::vector<uint32_t>& hv_out = cout_.heavy;
+    if (cin.order.empty()) { cin.order.resize(n); for (size_t p = 0; p < n; ++p) cin.order[p] = (uint32_t)p; }
+    if (cout_.order.empty()) { cout_.order.resize(n); for (size_t p = 0; p < n; ++p) cout_.order[p] = (uint32_t)p; }
+    std::vector<uint32_t>& hv_in = cin.order;
+    std::vector<uint32_t>& hv_out = cout_.order;
     e->max_deg_in = cin.max_degree;
     e->max_deg_out = cout_.max_degree;
     e->entries = en_in.size();
-    e->n_heavy_in = (uint32_t)hv_in.size();
-    e->n_heavy_out = (uint32_t)hv_out.size();
+    e->n_heavy_in = (uint32_t)cin.heavy.size();
+    e->n_heavy_out = (uint32_t)cout_.heavy.size();
     if ((st = dev_reserve(e, e->b_heavy_in, hv_in.size() * sizeof(uint32_t), false))) return st;
     if ((st = dev_reserve(e, e->b_heavy_out, hv_out.size() * sizeof(uint32_t), false))) return st;
     if (!hv_in.empty())

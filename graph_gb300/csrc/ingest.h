@@ -116,6 +116,7 @@ struct Csr {
   std::vector<uint32_t> rowptr;   // n + 1
   std::vector<uint4> ent;         // (neighbour, random distance draw bits, bias bits, strength bits)
   std::vector<uint32_t> heavy;    // points whose list is longer than kHeavyDegree
+  std::vector<uint32_t> order;    // all points by list length, longest first (ties by index)
   uint32_t max_degree = 0;
 };
 
@@ -138,8 +139,15 @@ inline void build_direction(const float* links, uint64_t E, uint64_t N, bool inc
   for (uint64_t p = 0; p < N; ++p) {
     c.max_degree = std::max(c.max_degree, c.rowptr[p + 1]);
     if (c.rowptr[p + 1] > kHeavyDegree) c.heavy.push_back((uint32_t)p);
-    c.rowptr[p + 1] += c.rowptr[p];
   }
+  {   // counting sort of the points by list length, descending
+    std::vector<uint32_t> bucket((size_t)c.max_degree + 2, 0);
+    for (uint64_t p = 0; p < N; ++p) bucket[c.max_degree - c.rowptr[p + 1] + 1]++;
+    for (size_t k = 1; k < bucket.size(); ++k) bucket[k] += bucket[k - 1];
+    c.order.assign(N, 0);
+    for (uint64_t p = 0; p < N; ++p) c.order[bucket[c.max_degree - c.rowptr[p + 1]]++] = (uint32_t)p;
+  }
+  for (uint64_t p = 0; p < N; ++p) c.rowptr[p + 1] += c.rowptr[p];
   const uint32_t M = c.rowptr[N];
   c.ent.assign(M, make_uint4(0, 0, 0, 0));
   std::vector<uint32_t> lidx(M);

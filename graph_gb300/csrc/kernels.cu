@@ -238,7 +238,20 @@ __device__ void warp_cell(const DeviceView& d, const SimScalars& s, uint32_t see
   uint32_t at[kSlots];
 #pragma unroll
   for (int q = 0; q < kSlots; ++q) { best[q] = ~0ull; at[q] = 0; }
-  for (uint32_t j = b + lane; j < e; j += 32) {
+  uint32_t j = b + lane;
+  for (; j + 96 < e; j += 128) {   // loads four points ahead of the selection
+    float2 p[4];
+    uint32_t ix[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) { p[u] = d.sorted_pos[j + 32 * u]; ix[u] = d.sorted_idx[j + 32 * u]; }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      ax += to_fixed(p[u].x, s.fx);
+      ay += to_fixed(p[u].y, s.fx);
+      top8_insert(best, at, peel_key(ix[u], seed_bits), j + 32 * u);
+    }
+  }
+  for (; j < e; j += 32) {
     const float2 p = d.sorted_pos[j];
     ax += to_fixed(p.x, s.fx);
     ay += to_fixed(p.y, s.fx);
@@ -598,9 +611,9 @@ __global__ void __launch_bounds__(kBlock) k_manybody(DeviceView d, SimScalars s)
       const uint32_t b = __ldg(&d.cell_start[c]);
       float sx = 0.f, sy = 0.f, sampled = 0.f;
       for (int q = 0; q < kSlots; ++q) {
-        if (q >= ns) { sx = __fadd_rn(sx, 0.f); sy = __fadd_rn(sy, 0.f); continue; }
+        if (q >= ns) break;
         const uint32_t oi = __ldg(&d.sorted_idx[b + q]);
-        if ((float)oi == self) { sx = __fadd_rn(sx, 0.f); sy = __fadd_rn(sy, 0.f); continue; }
+        if ((float)oi == self) continue;
         const float2 o = __ldg(&d.sorted_pos[b + q]);
         sampled = __fadd_rn(sampled, 1.0f);
         pair_velocity(px, py, o.x, o.y, rj.x, rj.y, k, sx, sy);
@@ -626,18 +639,17 @@ __global__ void __launch_bounds__(kBlock) k_manybody(DeviceView d, SimScalars s)
 }
 
 // ------------------------------------------------------------------- link --
-// rows == nullptr: thread t handles point t and skips lists longer than
-// heavy_deg (those run in the heavy pass); otherwise thread t handles rows[t].
+// Thread t handles point rows[t]: the points in order of list length, so the
+// lanes of a warp walk lists of (nearly) the same length.
 __global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, const uint32_t* __restrict__ rowptr,
                                                  const uint4* __restrict__ ent, const float2* __restrict__ src,
                                                  float2* __restrict__ dst, const uint32_t* __restrict__ rows,
-                                                 uint32_t nrows, uint32_t heavy_deg) {
+                                                 uint32_t nrows) {
   // ForceLink.run (ForceLink/index.ts:221-263), force-spring.ts:38-96
   const TickParams tp = tick_params(d);
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nrows) return;
-  const uint32_t p = rows ? rows[t] : t;
-  if (!rows && rowptr[p + 1] - rowptr[p] > heavy_deg) return;
+  const uint32_t p = rows[t];
   const float2 pp = src[p];
   const uint8_t f = d.flags[p];
   if (f & kAbsent) { dst[p] = pp; return; }
@@ -865,17 +877,17 @@ void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool s
   if (!nb) return;
   const uint32_t* rp = direction == 0 ? d.rowptr_in : d.rowptr_out;
   const uint4* en = direction == 0 ? d.ent_in : d.ent_out;
-  const uint32_t* heavy = direction == 0 ? d.heavy_in : d.heavy_out;
+  const uint32_t* order = direction == 0 ? d.heavy_in : d.heavy_out;   // all points, longest lists first
   const uint32_t nheavy = direction == 0 ? d.n_heavy_in : d.n_heavy_out;
   const float2* src = swap_back ? d.pos_alt : d.pos;
   float2* dst = swap_back ? d.pos : d.pos_alt;
   if (nheavy) {   // long lists first, on a side branch, concurrent with the rest
     cudaEventRecord(fork, st);
     cudaStreamWaitEvent(side, fork, 0);
-    k_link<<<blocks_for(nheavy), kBlock, 0, side>>>(d, s, rp, en, src, dst, heavy, nheavy, kHeavyDegree);
+    k_link<<<blocks_for(nheavy), kBlock, 0, side>>>(d, s, rp, en, src, dst, order, nheavy);
     cudaEventRecord(join, side);
   }
-  k_link<<<nb, kBlock, 0, st>>>(d, s, rp, en, src, dst, nullptr, d.n, kHeavyDegree);
+  if (d.n > nheavy) k_link<<<blocks_for(d.n - nheavy), kBlock, 0, st>>>(d, s, rp, en, src, dst, order + nheavy, d.n - nheavy);
   if (nheavy) cudaStreamWaitEvent(st, join, 0);
 }
 

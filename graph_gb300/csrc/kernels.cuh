@@ -47,8 +47,8 @@ struct DeviceView {
   const uint4* ent_in;        // (col, rnd bits, bias bits, strength bits)
   const uint32_t* rowptr_out;
   const uint4* ent_out;
-  const uint32_t* heavy_in;   // points whose incoming list is longer than kHeavyDegree
-  const uint32_t* heavy_out;
+  const uint32_t* heavy_in;   // all points by incoming list length, longest first;
+  const uint32_t* heavy_out;  // the first n_heavy_* have lists longer than kHeavyDegree
   uint32_t n_heavy_in, n_heavy_out;
   // collision
   const float* size;          // resolved point sizes [n]
