@@ -182,6 +182,7 @@ void refresh_view(cgl_batch* b) {
   BatchView& v = b->view;
   v.slots = (uint32_t)b->jobs.size();
   v.point_hwm = (uint32_t)b->pts.hwm;
+  v.units = PairUnits{1.0f, -0.0f};
   v.cell_hwm = (uint32_t)b->cells.hwm;
   v.desc = (const GraphDesc*)b->desc.p;
   v.gid = (const uint32_t*)b->gid.p;

@@ -78,6 +78,7 @@ struct BatchView {
   uint32_t n_heavy_out;
   const BatchTick* ticks;      // [tick][slot]
   uint32_t* tick_ctr;
+  PairUnits units;             // {1, -0}: operands of the paired sums and products
 };
 
 void batch_launch_tick(const BatchView& v, cudaStream_t st, cudaStream_t side, cudaEvent_t* fork, cudaEvent_t* join);

@@ -462,23 +462,23 @@ __global__ void __launch_bounds__(kBlock) kb_manybody(BatchView v) {
   const int gf = D.gf, L = D.levels;
   const int fcx = cell_index(px, D.csf, gf), fcy = cell_index(py, D.csf, gf);
   const float k = __fmul_rn(tp.alpha, D.repulsion);
+  const PairUnits pu = v.units;
   const float4* rec = v.rec + D.rec_off;
-  float vx = 0.f, vy = 0.f;
+  float2 vel = make_float2(0.f, 0.f);
   {   // level 0 (force-level.frag:70-79)
     const int sh = L - 1;
     const int ex = (fcx >> sh) - 1, ey = (fcy >> sh) - 1;
-    float lx = 0.f, ly = 0.f;
+    float2 lv2 = make_float2(0.f, 0.f);
 #pragma unroll 1
     for (int jj = 0; jj < 4; ++jj) {
       const bool row_in = (unsigned)(jj - ey) <= 2u;
 #pragma unroll 1
       for (int ii = 0; ii < 4; ++ii) {
         if (row_in && (unsigned)(ii - ex) <= 2u) continue;
-        cell_velocity(__ldg(&rec[jj * 4 + ii]), px, py, k, lx, ly);
+        cell_velocity(__ldg(&rec[jj * 4 + ii]), p, k, lv2, pu);
       }
     }
-    vx = __fadd_rn(vx, lx);
-    vy = __fadd_rn(vy, ly);
+    vel = add2(vel, lv2, pu);
   }
 #pragma unroll 1
   for (int l = 1; l < L; ++l) {   // force-level.frag:80-95
@@ -488,7 +488,7 @@ __global__ void __launch_bounds__(kBlock) kb_manybody(BatchView v) {
     const int bx = (pcx & ~1) - 2, by = (pcy & ~1) - 2;
     const int ex = pcx - 1, ey = pcy - 1;
     const float4* lv = rec + level_base(l);
-    float lx = 0.f, ly = 0.f;
+    float2 lv2 = make_float2(0.f, 0.f);
 #pragma unroll 1
     for (int jj = 0; jj < 6; ++jj) {
       const int cy = by + jj;
@@ -500,17 +500,16 @@ __global__ void __launch_bounds__(kBlock) kb_manybody(BatchView v) {
         const int cx = bx + ii;
         if ((unsigned)cx >= (unsigned)G) continue;
         if (row_in && (unsigned)(cx - ex) <= 2u) continue;
-        cell_velocity(__ldg(&row[cx]), px, py, k, lx, ly);
+        cell_velocity(__ldg(&row[cx]), p, k, lv2, pu);
       }
     }
-    vx = __fadd_rn(vx, lx);
-    vy = __fadd_rn(vy, ly);
+    vel = add2(vel, lv2, pu);
   }
   // near field (force-nearfield.frag:199-263)
   const float2 rj = v.jitter[P];
   const float self = (float)(P - D.p_off);
   const float4* fine = rec + level_base(L - 1);
-  float nx = 0.f, ny = 0.f;
+  float2 nf = make_float2(0.f, 0.f);
 #pragma unroll 1
   for (int jj = -1; jj <= 1; ++jj)
 #pragma unroll 1
@@ -523,7 +522,8 @@ __global__ void __launch_bounds__(kBlock) kb_manybody(BatchView v) {
       if (others <= 0.f) continue;
       const int ns = (int)r.w;
       const uint32_t b = __ldg(&v.cell_start[D.cell_off + lc]);
-      float sx = 0.f, sy = 0.f, sampled = 0.f;
+      float2 sum = make_float2(0.f, 0.f);
+      float sampled = 0.f;
 #pragma unroll 1
       for (int q = 0; q < kSlots; ++q) {
         if (q >= ns) break;
@@ -531,26 +531,20 @@ __global__ void __launch_bounds__(kBlock) kb_manybody(BatchView v) {
         if ((float)(oi - D.p_off) == self) continue;
         const float2 o = __ldg(&v.sorted_pos[b + q]);
         sampled = __fadd_rn(sampled, 1.0f);
-        pair_velocity(px, py, o.x, o.y, rj.x, rj.y, k, sx, sy);
+        pair_velocity(p, o, rj, k, sum, pu);
       }
       if (sampled > 0.f) {
         const float w = __fdiv_rn(others, sampled);
-        nx = __fadd_rn(nx, __fmul_rn(w, sx));
-        ny = __fadd_rn(ny, __fmul_rn(w, sy));
+        nf = add2(nf, mul2(splat(w), sum, pu), pu);
       }
     }
-  nx = __fadd_rn(nx, __fmul_rn(nx, rj.x));
-  ny = __fadd_rn(ny, __fmul_rn(ny, rj.y));
+  nf = add2(nf, mul2(nf, rj, pu), pu);
   const float max_step = __fmul_rn(2.0f, D.csf);
-  const float speed = __fsqrt_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)));
-  if (speed > max_step) {
-    const float sc = __fdiv_rn(max_step, speed);
-    nx = __fmul_rn(nx, sc);
-    ny = __fmul_rn(ny, sc);
-  }
-  vx = __fadd_rn(vx, nx);
-  vy = __fadd_rn(vy, ny);
-  if (!(v.flags[P] & kPinned)) v.pos[P] = integrate(p, vx, vy, D.friction, D.space);
+  const float2 nsq = mul2(nf, nf, pu);
+  const float speed = __fsqrt_rn(__fadd_rn(nsq.x, nsq.y));
+  if (speed > max_step) nf = mul2(nf, splat(__fdiv_rn(max_step, speed)), pu);
+  vel = add2(vel, nf, pu);
+  if (!(v.flags[P] & kPinned)) v.pos[P] = integrate(p, vel.x, vel.y, D.friction, D.space);
 }
 
 // ------------------------------------------------------------------- link --
@@ -575,24 +569,24 @@ __global__ void __launch_bounds__(kBlock) kb_link(BatchView v, int direction, co
   const uint8_t f = v.flags[P];
   if (!tp.active || !(D.stages & stage) || (f & kAbsent)) { dst[P] = pp; return; }
   const float sa = __fmul_rn(D.link_spring, tp.alpha);
+  const PairUnits pu = v.units;
   const float span = __fsub_rn(D.link_r1, D.link_r0);
-  float vx = 0.f, vy = 0.f;
+  float2 vel = make_float2(0.f, 0.f);
   auto spring = [&](const uint4 en, const float2 q) {
     float dd = __fadd_rn(__fmul_rn(__uint_as_float(en.y), span), D.link_r0);
     dd = __fmul_rn(dd, D.link_distance);
-    float x = __fsub_rn(q.x, __fadd_rn(pp.x, vx));
-    float y = __fsub_rn(q.y, __fadd_rn(pp.y, vy));
-    float l = __fsqrt_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)));
+    const float2 t = add2(pp, vel, pu);                     // p + v, then q - (p + v)
+    const float2 d = add2(q, make_float2(-t.x, -t.y), pu);
+    const float2 sq = mul2(d, d, pu);
+    float l = __fsqrt_rn(__fadd_rn(sq.x, sq.y));
     l = gmax(l, __fmul_rn(dd, 0.99f));
     l = __fdiv_rn(__fsub_rn(l, dd), l);
     l = __fmul_rn(l, sa);
     l = __fmul_rn(l, __uint_as_float(en.w));
     l = __fmul_rn(l, __uint_as_float(en.z));
-    x = __fmul_rn(x, l);
-    y = __fmul_rn(y, l);
-    vx = __fadd_rn(vx, x);
-    vy = __fadd_rn(vy, y);
+    vel = add2(vel, mul2(d, splat(l), pu), pu);
   };
+
   constexpr int kLinkBatch = 4;
   uint32_t at = e0;
   for (; at + kLinkBatch <= e1; at += kLinkBatch) {
@@ -611,7 +605,7 @@ __global__ void __launch_bounds__(kBlock) kb_link(BatchView v, int direction, co
     if (en.x == kAbsentTarget) continue;
     spring(en, __ldg(&src[en.x]));
   }
-  dst[P] = (f & kPinned) ? pp : integrate(pp, vx, vy, D.friction, D.space);
+  dst[P] = (f & kPinned) ? pp : integrate(pp, vel.x, vel.y, D.friction, D.space);
 }
 
 __global__ void kb_tick_end(BatchView v) { *v.tick_ctr += 1; }

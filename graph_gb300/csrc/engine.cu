@@ -240,6 +240,7 @@ SimScalars make_scalars(const cgl_engine* e) {
   s.tile = e->tile;
   s.csf = e->Gf ? (float)(e->adjusted_space / e->Gf) : 1.f;
   s.fx = e->fx;
+  s.units = PairUnits{1.0f, -0.0f};
   return s;
 }
 

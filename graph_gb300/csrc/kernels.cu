@@ -549,23 +549,23 @@ __global__ void __launch_bounds__(kBlock) k_manybody(DeviceView d, SimScalars s)
   const int gf = s.gf, L = s.levels;
   const int fcx = cell_index(px, s.csf, gf), fcy = cell_index(py, s.csf, gf);
   const float k = __fmul_rn(tp.alpha, s.repulsion);
-  float vx = 0.f, vy = 0.f;
+  const PairUnits pu = s.units;
+  float2 vel = make_float2(0.f, 0.f);
   {   // level 0 (force-level.frag:70-79): every cell of the 4x4 grid outside the 3x3
     const int sh = L - 1;
     const int ex = (fcx >> sh) - 1, ey = (fcy >> sh) - 1;   // first column / row of the 3x3
     const float4* lv = d.rec;
-    float lx = 0.f, ly = 0.f;
+    float2 lv2 = make_float2(0.f, 0.f);
 #pragma unroll 1
     for (int jj = 0; jj < 4; ++jj) {
       const bool row_in = (unsigned)(jj - ey) <= 2u;
 #pragma unroll 1
       for (int ii = 0; ii < 4; ++ii) {
         if (row_in && (unsigned)(ii - ex) <= 2u) continue;
-        cell_velocity(__ldg(&lv[jj * 4 + ii]), px, py, k, lx, ly);
+        cell_velocity(__ldg(&lv[jj * 4 + ii]), p, k, lv2, pu);
       }
     }
-    vx = __fadd_rn(vx, lx);
-    vy = __fadd_rn(vy, ly);
+    vel = add2(vel, lv2, pu);
   }
   for (int l = 1; l < L; ++l) {   // force-level.frag:80-95: aligned 6x6 child block minus the 3x3
     const int G = 4 << l;
@@ -574,7 +574,7 @@ __global__ void __launch_bounds__(kBlock) k_manybody(DeviceView d, SimScalars s)
     const int bx = (pcx & ~1) - 2, by = (pcy & ~1) - 2;
     const int ex = pcx - 1, ey = pcy - 1;
     const float4* lv = d.rec + d.level_off[l];
-    float lx = 0.f, ly = 0.f;
+    float2 lv2 = make_float2(0.f, 0.f);
 #pragma unroll 1
     for (int jj = 0; jj < 6; ++jj) {
       const int cy = by + jj;
@@ -586,17 +586,16 @@ __global__ void __launch_bounds__(kBlock) k_manybody(DeviceView d, SimScalars s)
         const int cx = bx + ii;
         if ((unsigned)cx >= (unsigned)G) continue;
         if (row_in && (unsigned)(cx - ex) <= 2u) continue;
-        cell_velocity(__ldg(&row[cx]), px, py, k, lx, ly);
+        cell_velocity(__ldg(&row[cx]), p, k, lv2, pu);
       }
     }
-    vx = __fadd_rn(vx, lx);
-    vy = __fadd_rn(vy, ly);
+    vel = add2(vel, lv2, pu);
   }
   // near field (force-nearfield.frag:199-263)
   const float2 rj = d.jitter[i];
   const float self = (float)i;
   const float4* fine = d.rec + d.level_off[L - 1];
-  float nx = 0.f, ny = 0.f;
+  float2 nf = make_float2(0.f, 0.f);
 #pragma unroll 1
   for (int jj = -1; jj <= 1; ++jj)
 #pragma unroll 1
@@ -609,33 +608,28 @@ __global__ void __launch_bounds__(kBlock) k_manybody(DeviceView d, SimScalars s)
       if (others <= 0.f) continue;
       const int ns = (int)r.w;
       const uint32_t b = __ldg(&d.cell_start[c]);
-      float sx = 0.f, sy = 0.f, sampled = 0.f;
+      float2 sum = make_float2(0.f, 0.f);
+      float sampled = 0.f;
       for (int q = 0; q < kSlots; ++q) {
         if (q >= ns) break;
         const uint32_t oi = __ldg(&d.sorted_idx[b + q]);
         if ((float)oi == self) continue;
         const float2 o = __ldg(&d.sorted_pos[b + q]);
         sampled = __fadd_rn(sampled, 1.0f);
-        pair_velocity(px, py, o.x, o.y, rj.x, rj.y, k, sx, sy);
+        pair_velocity(p, o, rj, k, sum, pu);
       }
       if (sampled > 0.f) {
         const float w = __fdiv_rn(others, sampled);
-        nx = __fadd_rn(nx, __fmul_rn(w, sx));
-        ny = __fadd_rn(ny, __fmul_rn(w, sy));
+        nf = add2(nf, mul2(splat(w), sum, pu), pu);
       }
     }
-  nx = __fadd_rn(nx, __fmul_rn(nx, rj.x));
-  ny = __fadd_rn(ny, __fmul_rn(ny, rj.y));
+  nf = add2(nf, mul2(nf, rj, pu), pu);
   const float max_step = __fmul_rn(2.0f, s.csf);
-  const float speed = __fsqrt_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)));
-  if (speed > max_step) {
-    const float sc = __fdiv_rn(max_step, speed);
-    nx = __fmul_rn(nx, sc);
-    ny = __fmul_rn(ny, sc);
-  }
-  vx = __fadd_rn(vx, nx);
-  vy = __fadd_rn(vy, ny);
-  if (!(d.flags[i] & kPinned)) d.pos[i] = integrate(p, vx, vy, s.friction, s.space);
+  const float2 nsq = mul2(nf, nf, pu);
+  const float speed = __fsqrt_rn(__fadd_rn(nsq.x, nsq.y));
+  if (speed > max_step) nf = mul2(nf, splat(__fdiv_rn(max_step, speed)), pu);
+  vel = add2(vel, nf, pu);
+  if (!(d.flags[i] & kPinned)) d.pos[i] = integrate(p, vel.x, vel.y, s.friction, s.space);
 }
 
 // ------------------------------------------------------------------- link --
@@ -654,27 +648,27 @@ __global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, con
   const uint8_t f = d.flags[p];
   if (f & kAbsent) { dst[p] = pp; return; }
   const float sa = __fmul_rn(s.link_spring, tp.alpha);
+  const PairUnits pu = s.units;
   const float span = __fsub_rn(s.link_r1, s.link_r0);
-  float vx = 0.f, vy = 0.f;
   const uint32_t e0 = rowptr[p], e1 = rowptr[p + 1];
   // The loads do not depend on the running velocity: issue them kLinkBatch
   // links ahead, then apply the springs strictly in list order.
+  float2 vel = make_float2(0.f, 0.f);
   auto spring = [&](const uint4 en, const float2 q) {
     float dd = __fadd_rn(__fmul_rn(__uint_as_float(en.y), span), s.link_r0);
     dd = __fmul_rn(dd, s.link_distance);
-    float x = __fsub_rn(q.x, __fadd_rn(pp.x, vx));
-    float y = __fsub_rn(q.y, __fadd_rn(pp.y, vy));
-    float l = __fsqrt_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)));
+    const float2 t = add2(pp, vel, pu);                     // p + v, then q - (p + v)
+    const float2 d = add2(q, make_float2(-t.x, -t.y), pu);
+    const float2 sq = mul2(d, d, pu);
+    float l = __fsqrt_rn(__fadd_rn(sq.x, sq.y));
     l = gmax(l, __fmul_rn(dd, 0.99f));
     l = __fdiv_rn(__fsub_rn(l, dd), l);
     l = __fmul_rn(l, sa);
     l = __fmul_rn(l, __uint_as_float(en.w));
     l = __fmul_rn(l, __uint_as_float(en.z));
-    x = __fmul_rn(x, l);
-    y = __fmul_rn(y, l);
-    vx = __fadd_rn(vx, x);
-    vy = __fadd_rn(vy, y);
+    vel = add2(vel, mul2(d, splat(l), pu), pu);
   };
+
   constexpr int kLinkBatch = 4;
   uint32_t at = e0;
   for (; at + kLinkBatch <= e1; at += kLinkBatch) {
@@ -693,7 +687,7 @@ __global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, con
     if (en.x == kAbsentTarget) continue;
     spring(en, __ldg(&src[en.x]));
   }
-  dst[p] = (f & kPinned) ? pp : integrate(pp, vx, vy, s.friction, s.space);
+  dst[p] = (f & kPinned) ? pp : integrate(pp, vel.x, vel.y, s.friction, s.space);
 }
 
 // -------------------------------------------------------------- collision --

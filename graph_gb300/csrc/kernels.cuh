@@ -75,6 +75,7 @@ struct SimScalars {
   int tile;                   // cell-kernel tile edge
   float csf;                  // finest cell size
   FixedScale fx;
+  PairUnits units;            // {1, -0}: operands of the paired sums and products
 };
 
 
