@@ -60,9 +60,21 @@ def make_workload(name, seed=1):
                       simulation_link_spring=1.0, simulation_link_distance=2.0, simulation_decay=5000,
                       random_seed=seed)
         desc = "Barabasi-Albert 10,000 points m=5 / spaceSize 4096"
+    elif name == "rmat8m":
+        n = 1 << 23
+        links = generators.rmat(23, 40_000_000, 0.57, 0.19, 0.19, seed=seed)
+        pos = generators.uniform_positions(n, 0, 16384, seed)
+        radius = np.random.default_rng(seed).uniform(1, 8, size=n).astype(np.float32)
+        sizes = 2 * radius
+        fields = dict(space_size=16384, simulation_repulsion=0.1, simulation_gravity=0.25, simulation_friction=0.85,
+                      simulation_link_spring=1.0, simulation_link_distance=2.0, simulation_collision=0.5,
+                      simulation_decay=5000, random_seed=seed)
+        desc = ("R-MAT scale 23 (8,388,608 points, a,b,c,d = .57,.19,.19,.05) / 40,000,000 links / "
+                "collision 0.5, radius U[1,8] / spaceSize 16384")
+        return pos, links, fields, desc, sizes
     else:
         raise SystemExit("unknown workload %r" % name)
-    return pos, links, fields, desc
+    return pos, links, fields, desc, None
 
 
 # Algorithmic bytes per launch of each stage (bytes each stage must move at
@@ -163,12 +175,14 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- CPU side --
-def time_oracle(pos, links, fields, budget_s, max_ticks, warmup=1):
+def time_oracle(pos, links, fields, budget_s, max_ticks, warmup=1, sizes=None):
     """Oracle ticks on all host cores; returns (point-iter/s, ticks timed, seconds, cores)."""
     from oracle import OracleEngine
     o = OracleEngine(**fields)
     o.set_point_positions(pos)
     o.set_links(links)
+    if sizes is not None:
+        o.set_point_sizes(sizes)
     o.render()
     o.start(1.0)
     for _ in range(warmup):
@@ -208,7 +222,7 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="sbm1m", choices=["sbm1m", "ba10k", "batch", "serve"])
+    ap.add_argument("--workload", default="sbm1m", choices=["sbm1m", "ba10k", "rmat8m", "batch", "serve"])
     ap.add_argument("--rates", default="50,100,200,500,1000,2000", help="request rates (req/s) of the serving sweep")
     ap.add_argument("--requests", type=int, default=200, help="requests per rate of the serving sweep")
     ap.add_argument("--graphs", type=int, default=4096, help="jobs of the batched workload")
@@ -247,7 +261,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    pos, links, fields, desc = make_workload(args.workload, seed=1 + rank)
+    pos, links, fields, desc, sizes = make_workload(args.workload, seed=1 + rank)
     if args.positions_from:
         pos = np.load(args.positions_from).astype(np.float32)
         desc += " (evolved positions from %s)" % os.path.basename(args.positions_from)
@@ -255,6 +269,8 @@ def main():
     eng = Engine(**dict(fields, device=local_rank))
     eng.set_point_positions(pos)
     eng.set_links(links)
+    if sizes is not None:
+        eng.set_point_sizes(sizes)
     eng.render()
     eng.start(1.0)
     lay = eng.layout()
@@ -330,7 +346,7 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, ticks, secs, cores = time_oracle(pos, links, fields, args.cpu_budget, 50)
+        v, ticks, secs, cores = time_oracle(pos, links, fields, args.cpu_budget, 50, sizes=sizes)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": "%d ticks of the same %s workload on the oracle (C++ restatement, OpenMP, %s), %.1f s"
                          % (ticks, args.workload, cpu_model(), secs)}
@@ -543,12 +559,14 @@ def run_serve(args):
 
 
 def run_reference(args):
-    pos, links, fields, desc = make_workload(args.workload, seed=1)
+    pos, links, fields, desc, sizes = make_workload(args.workload, seed=1)
     budget = 150.0
     from oracle import OracleEngine
     o = OracleEngine(**fields)
     o.set_point_positions(pos)
     o.set_links(links)
+    if sizes is not None:
+        o.set_point_sizes(sizes)
     o.render()
     o.start(1.0)
     live = o.layout().live_points

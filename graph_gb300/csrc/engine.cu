@@ -38,8 +38,6 @@ struct cgl_engine {
   int device = 0;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
-  cudaStream_t side_stream = nullptr;       // branch for long link lists
-  cudaEvent_t ev_fork[2] = {nullptr, nullptr}, ev_join[2] = {nullptr, nullptr};
 
   // staged input (copied at set_*, applied at render)
   bool have_pos_input = false, have_link_input = false, have_strength = false, have_sizes = false;
@@ -290,17 +288,19 @@ cgl_status enqueue_tick(cgl_engine* e, cudaStream_t st, cudaEvent_t* ev) {
   }
   if (p.link_in || p.link_out) {
     mark(6, 0);
-    if (p.link_in) launch_link(d, s, 0, false, st, e->side_stream, e->ev_fork[0], e->ev_join[0]);
+    if (p.link_in) launch_link(d, s, 0, false, st);
     mark(6, 1);
     mark(7, 0);
-    if (p.link_out) launch_link(d, s, 1, p.link_in, st, e->side_stream, e->ev_fork[1], e->ev_join[1]);
+    if (p.link_out) launch_link(d, s, 1, p.link_in, st);
     mark(7, 1);
     if (!(p.link_in && p.link_out))
       CU(cudaMemcpyAsync(d.pos, d.pos_alt, e->N * sizeof(float2), cudaMemcpyDeviceToDevice, st));
   }
   if (p.coll) {
-    mark(8, 0); launch_collision_grid(d, s, st); mark(8, 1);
-    mark(9, 0); launch_collision_force(d, s, st); mark(9, 1);
+    // the many-body pass left every live point in sorted_idx, grouped by cell
+    const uint32_t* order = p.mb ? d.sorted_idx : nullptr;
+    mark(8, 0); launch_collision_grid(d, s, order, (uint32_t)e->live, st); mark(8, 1);
+    mark(9, 0); launch_collision_force(d, s, order, (uint32_t)e->live, st); mark(9, 1);
   }
   launch_tick_end(d, st);
   CU(cudaGetLastError());
@@ -593,11 +593,6 @@ cgl_status cgl_create(const cgl_config* cfg, cgl_engine** out) {
   if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking);
   if (ce == cudaSuccess) ce = cudaMallocHost((void**)&e->h_params, kParamChunk * sizeof(TickParams));
   if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->params_copied, cudaEventDisableTiming);
-  if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->side_stream, cudaStreamNonBlocking);
-  for (int k = 0; k < 2 && ce == cudaSuccess; ++k) {
-    ce = cudaEventCreateWithFlags(&e->ev_fork[k], cudaEventDisableTiming);
-    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->ev_join[k], cudaEventDisableTiming);
-  }
   if (ce != cudaSuccess) {
     cudaGetLastError();
     static thread_local std::string create_err;
@@ -627,11 +622,6 @@ cgl_status cgl_destroy(cgl_engine* e) {
   dev_free_all(e);
   if (e->params_copied) cudaEventDestroy(e->params_copied);
   if (e->h_params) cudaFreeHost(e->h_params);
-  for (int k = 0; k < 2; ++k) {
-    if (e->ev_fork[k]) cudaEventDestroy(e->ev_fork[k]);
-    if (e->ev_join[k]) cudaEventDestroy(e->ev_join[k]);
-  }
-  if (e->side_stream) cudaStreamDestroy(e->side_stream);
   if (e->own_stream) cudaStreamDestroy(e->own_stream);
   delete e;
   return CGL_OK;
@@ -857,7 +847,7 @@ cgl_status cgl_get_layout(cgl_engine* e, cgl_layout* o) {
   if (p.grav || p.cent || p.mb) k += 1;                // prepass
   if (p.cent) k += 1;
   if (p.mb) k += 6;                                    // scan (2), scatter, big cells, cells, manybody
-  k += (uint32_t)p.link_in * (1u + (e->n_heavy_in > 0)) + (uint32_t)p.link_out * (1u + (e->n_heavy_out > 0));
+  k += (uint32_t)p.link_in + (uint32_t)p.link_out;
   if (p.coll) k += 3;                                  // grid, convert, force
   o->kernels_per_tick = k;
   return CGL_OK;

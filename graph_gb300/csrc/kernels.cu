@@ -633,23 +633,112 @@ __global__ void __launch_bounds__(kBlock) k_manybody(DeviceView d, SimScalars s)
 }
 
 // ------------------------------------------------------------------- link --
-// Thread t handles point rows[t]: the points in order of list length, so the
-// lanes of a warp walk lists of (nearly) the same length.
+// One spring (force-spring.ts:61-91) against the running velocity `vel`:
+// dx = q - (p + v); l = max(|dx|, 0.99 d); v += dx * ((l - d) / l * spring *
+// alpha * strength * bias).  `dd99` = d * 0.99, rounded, as the shader has it.
+__device__ __forceinline__ void spring_step(float2 pp, float2& vel, float2 q, float dd, float dd99, float sa,
+                                            float strength, float bias, PairUnits pu) {
+  const float2 t = add2(pp, vel, pu);                     // p + v, then q - (p + v)
+  const float2 d = add2(q, make_float2(-t.x, -t.y), pu);
+  const float2 sq = mul2(d, d, pu);
+  float l = __fsqrt_rn(__fadd_rn(sq.x, sq.y));
+  l = gmax(l, dd99);
+  l = __fdiv_rn(__fsub_rn(l, dd), l);
+  l = __fmul_rn(l, sa);
+  l = __fmul_rn(l, strength);
+  l = __fmul_rn(l, bias);
+  vel = add2(vel, mul2(d, splat(l), pu), pu);
+}
+
+// Hub rows: a list of thousands of links is one strictly sequential chain
+// (each spring reads the velocity the previous one left).  One CTA per hub:
+// warps 1..7 gather the next kHubChunk links (entry, neighbour position,
+// rest length) into one shared buffer while lane 0 of warp 0 runs the chain
+// over the other, so the chain never waits on a global load.
+constexpr int kHubChunk = kBlock - 32;
+struct HubStage {
+  float4 a[2][kHubChunk];   // neighbour x, y, rest length d, 0.99 d
+  float4 b[2][kHubChunk];   // strength, bias, absent flag, -
+};
+
+// Stages link at + (thread - 32); returns whether its target is absent.
+__device__ __forceinline__ int hub_fill(HubStage& st, int buf, uint32_t at, uint32_t e1, const uint4* __restrict__ ent,
+                                        const float2* __restrict__ src, float span, float r0, float dist) {
+  const int k = threadIdx.x - 32;
+  if (at + k >= e1) return 0;
+  const uint4 en = __ldg(&ent[at + k]);
+  const bool absent = en.x == kAbsentTarget;
+  const float2 q = absent ? make_float2(0.f, 0.f) : __ldg(&src[en.x]);
+  const float dd = __fmul_rn(__fadd_rn(__fmul_rn(__uint_as_float(en.y), span), r0), dist);
+  st.a[buf][k] = make_float4(q.x, q.y, dd, __fmul_rn(dd, 0.99f));
+  st.b[buf][k] = make_float4(__uint_as_float(en.w), __uint_as_float(en.z), absent ? 1.f : 0.f, 0.f);
+  return absent;
+}
+
+// Blocks [0, nhub) take the hub rows rows[0..nhub) (longest first, so the
+// longest chain starts first); the other blocks take one row per thread from
+// rows[nhub..nrows): the rest of the points by list length, so the lanes of a
+// warp walk lists of (nearly) the same length.
 __global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, const uint32_t* __restrict__ rowptr,
                                                  const uint4* __restrict__ ent, const float2* __restrict__ src,
                                                  float2* __restrict__ dst, const uint32_t* __restrict__ rows,
-                                                 uint32_t nrows) {
+                                                 uint32_t nrows, uint32_t nhub) {
   // ForceLink.run (ForceLink/index.ts:221-263), force-spring.ts:38-96
+  extern __shared__ float4 hub_smem[];   // a HubStage when nhub > 0, else nothing
+  HubStage& hub = *reinterpret_cast<HubStage*>(hub_smem);
   const TickParams tp = tick_params(d);
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const float sa = __fmul_rn(s.link_spring, tp.alpha);
+  const PairUnits pu = s.units;
+  const float span = __fsub_rn(s.link_r1, s.link_r0);
+  if (blockIdx.x < nhub) {
+    const uint32_t p = rows[blockIdx.x];
+    const float2 pp = src[p];
+    const uint8_t f = d.flags[p];
+    if (f & kAbsent) {
+      if (threadIdx.x == 0) dst[p] = pp;
+      return;
+    }
+    const uint32_t e0 = rowptr[p], e1 = rowptr[p + 1];
+    const uint32_t chunks = (e1 - e0 + kHubChunk - 1) / kHubChunk;
+    int absent = 0;   // some link of the staged chunk has an absent target
+    if (threadIdx.x >= 32) absent = hub_fill(hub, 0, e0, e1, ent, src, span, s.link_r0, s.link_distance);
+    absent = __syncthreads_or(absent);
+    float2 vel = make_float2(0.f, 0.f);
+    for (uint32_t c = 0; c < chunks; ++c) {
+      const int buf = c & 1;
+      int next = 0;
+      if (threadIdx.x >= 32) {
+        if (c + 1 < chunks)
+          next = hub_fill(hub, buf ^ 1, e0 + (c + 1) * kHubChunk, e1, ent, src, span, s.link_r0, s.link_distance);
+      } else if (threadIdx.x == 0) {
+        const uint32_t len = min((uint32_t)kHubChunk, e1 - e0 - c * kHubChunk);
+        if (!absent) {   // no per-link branch: the chain runs back to back
+#pragma unroll 4
+          for (uint32_t k = 0; k < len; ++k) {
+            const float4 a = hub.a[buf][k];
+            const float4 b = hub.b[buf][k];
+            spring_step(pp, vel, make_float2(a.x, a.y), a.z, a.w, sa, b.x, b.y, pu);
+          }
+        } else {
+          for (uint32_t k = 0; k < len; ++k) {
+            const float4 a = hub.a[buf][k];
+            const float4 b = hub.b[buf][k];
+            if (b.z != 0.f) continue;
+            spring_step(pp, vel, make_float2(a.x, a.y), a.z, a.w, sa, b.x, b.y, pu);
+          }
+        }
+      }
+      absent = __syncthreads_or(next);
+    }
+    if (threadIdx.x == 0) dst[p] = (f & kPinned) ? pp : integrate(pp, vel.x, vel.y, s.friction, s.space);
+    return;
+  }
+  const uint32_t t = nhub + (blockIdx.x - nhub) * kBlock + threadIdx.x;
   if (t >= nrows) return;
   const uint32_t p = rows[t];
   const float2 pp = src[p];
   const uint8_t f = d.flags[p];
   if (f & kAbsent) { dst[p] = pp; return; }
-  const float sa = __fmul_rn(s.link_spring, tp.alpha);
-  const PairUnits pu = s.units;
-  const float span = __fsub_rn(s.link_r1, s.link_r0);
   const uint32_t e0 = rowptr[p], e1 = rowptr[p + 1];
   // The loads do not depend on the running velocity: issue them kLinkBatch
   // links ahead, then apply the springs strictly in list order.
@@ -657,16 +746,7 @@ __global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, con
   auto spring = [&](const uint4 en, const float2 q) {
     float dd = __fadd_rn(__fmul_rn(__uint_as_float(en.y), span), s.link_r0);
     dd = __fmul_rn(dd, s.link_distance);
-    const float2 t = add2(pp, vel, pu);                     // p + v, then q - (p + v)
-    const float2 d = add2(q, make_float2(-t.x, -t.y), pu);
-    const float2 sq = mul2(d, d, pu);
-    float l = __fsqrt_rn(__fadd_rn(sq.x, sq.y));
-    l = gmax(l, __fmul_rn(dd, 0.99f));
-    l = __fdiv_rn(__fsub_rn(l, dd), l);
-    l = __fmul_rn(l, sa);
-    l = __fmul_rn(l, __uint_as_float(en.w));
-    l = __fmul_rn(l, __uint_as_float(en.z));
-    vel = add2(vel, mul2(d, splat(l), pu), pu);
+    spring_step(pp, vel, q, dd, __fmul_rn(dd, 0.99f), sa, __uint_as_float(en.w), __uint_as_float(en.z), pu);
   };
 
   constexpr int kLinkBatch = 4;
@@ -701,25 +781,69 @@ __device__ __forceinline__ float coll_bin(float p, float o, float cs, float gm1)
 __constant__ float kOffX[4] = {0.f, 0.5f, 0.f, 0.5f};
 __constant__ float kOffY[4] = {0.f, 0.f, 0.5f, 0.5f};
 
-__global__ void __launch_bounds__(kBlock) k_coll_grid(DeviceView d, SimScalars s) {
-  // build-grid.vert:28-62 for the 4 offsets (ForceCollision/index.ts:19-24)
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.n) return;
-  if (d.flags[i] & kAbsent) return;
-  const float2 p = d.pos[i];
-  const float sz = d.size[i];
-  const float gm1 = (float)s.coll_grid - 1.0f;
-  const long long fx = to_fixed(p.x, s.fx), fy = to_fixed(p.y, s.fx), fs = to_fixed(sz, s.fx);
-  const uint32_t G2 = (uint32_t)(s.coll_grid * s.coll_grid);
+// Warp-wide sum of a 64-bit value (all 32 lanes take part).
+__device__ __forceinline__ long long warp_sum64(long long v) {
 #pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Points are taken in `order` (the many-body pass's cell order) when given,
+// so the lanes of a warp fall into a few grid cells; the lanes of each cell
+// sum their integer terms first and one lane adds the cell's total (at most
+// kCollRounds cells per warp and grid, the rest add their own terms).
+// Integer sums are order-free, so the grid is the same in any order.
+constexpr int kCollRounds = 6;
+__global__ void __launch_bounds__(kBlock) k_coll_grid(DeviceView d, SimScalars s, const uint32_t* __restrict__ order,
+                                                      uint32_t count) {
+  // build-grid.vert:28-62 for the 4 offsets (ForceCollision/index.ts:19-24)
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  uint32_t i = 0;
+  bool live = t < count;
+  if (live) {
+    i = order ? order[t] : t;
+    live = !(d.flags[i] & kAbsent);
+  }
+  if (!__any_sync(0xffffffffu, live)) return;   // warp-uniform
+  float2 p = make_float2(0.f, 0.f);
+  float sz = 0.f;
+  if (live) { p = d.pos[i]; sz = d.size[i]; }
+  const float gm1 = (float)s.coll_grid - 1.0f;
+  const long long fx = live ? to_fixed(p.x, s.fx) : 0, fy = live ? to_fixed(p.y, s.fx) : 0;
+  const long long fs = live ? to_fixed(sz, s.fx) : 0;
+  const uint32_t G2 = (uint32_t)(s.coll_grid * s.coll_grid);
+  const unsigned active = __ballot_sync(0xffffffffu, live);
+#pragma unroll 1
   for (int g = 0; g < 4; ++g) {
     const int cx = (int)coll_bin(p.x, kOffX[g], s.coll_cell, gm1);
     const int cy = (int)coll_bin(p.y, kOffY[g], s.coll_cell, gm1);
-    long long* a = d.cgrid_acc + 4 * ((size_t)g * G2 + (uint32_t)(cy * s.coll_grid + cx));
-    atomicAdd((unsigned long long*)&a[0], (unsigned long long)fx);
-    atomicAdd((unsigned long long*)&a[1], (unsigned long long)fy);
-    atomicAdd((unsigned long long*)&a[2], (unsigned long long)fs);
-    atomicAdd((unsigned long long*)&a[3], 1ull);
+    const uint32_t key = (uint32_t)(cy * s.coll_grid + cx);
+    long long* a = d.cgrid_acc + 4 * ((size_t)g * G2 + key);
+    unsigned todo = active;
+#pragma unroll 1
+    for (int r = 0; r < kCollRounds && todo; ++r) {
+      const int l = __ffs(todo) - 1;
+      const uint32_t kl = __shfl_sync(0xffffffffu, key, l);
+      const bool mine = ((todo >> lane) & 1u) && key == kl;
+      const unsigned grp = __ballot_sync(0xffffffffu, mine);
+      const long long sx = warp_sum64(mine ? fx : 0);
+      const long long sy = warp_sum64(mine ? fy : 0);
+      const long long ss = warp_sum64(mine ? fs : 0);
+      if (lane == l) {
+        atomicAdd((unsigned long long*)&a[0], (unsigned long long)sx);
+        atomicAdd((unsigned long long*)&a[1], (unsigned long long)sy);
+        atomicAdd((unsigned long long*)&a[2], (unsigned long long)ss);
+        atomicAdd((unsigned long long*)&a[3], (unsigned long long)__popc(grp));
+      }
+      todo &= ~grp;
+    }
+    if ((todo >> lane) & 1u) {
+      atomicAdd((unsigned long long*)&a[0], (unsigned long long)fx);
+      atomicAdd((unsigned long long*)&a[1], (unsigned long long)fy);
+      atomicAdd((unsigned long long*)&a[2], (unsigned long long)fs);
+      atomicAdd((unsigned long long*)&a[3], 1ull);
+    }
   }
 }
 
@@ -732,11 +856,13 @@ __global__ void __launch_bounds__(kBlock) k_coll_convert(DeviceView d, SimScalar
   a[0] = 0; a[1] = 0; a[2] = 0; a[3] = 0;
 }
 
-__global__ void __launch_bounds__(kBlock) k_coll_force(DeviceView d, SimScalars s) {
+__global__ void __launch_bounds__(kBlock) k_coll_force(DeviceView d, SimScalars s, const uint32_t* __restrict__ order,
+                                                       uint32_t count) {
   // force-collision-spatial.frag:103-168, 4 passes blended, then update
   const TickParams tp = tick_params(d);
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.n) return;
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const uint32_t i = order ? order[t] : t;   // cell order: neighbouring lanes read the same grid cells
   const uint8_t f = d.flags[i];
   if (f & kAbsent) return;
   const float2 p = d.pos[i];
@@ -865,36 +991,32 @@ void launch_manybody(const DeviceView& d, const SimScalars& s, cudaStream_t st) 
   if (nb) k_manybody<<<nb, kBlock, 0, st>>>(d, s);
 }
 
-void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool swap_back, cudaStream_t st,
-                 cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
-  const uint32_t nb = blocks_for(d.n);
-  if (!nb) return;
+void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool swap_back, cudaStream_t st) {
+  if (!d.n) return;
   const uint32_t* rp = direction == 0 ? d.rowptr_in : d.rowptr_out;
   const uint4* en = direction == 0 ? d.ent_in : d.ent_out;
   const uint32_t* order = direction == 0 ? d.heavy_in : d.heavy_out;   // all points, longest lists first
-  const uint32_t nheavy = direction == 0 ? d.n_heavy_in : d.n_heavy_out;
+  const uint32_t nhub = direction == 0 ? d.n_heavy_in : d.n_heavy_out;
   const float2* src = swap_back ? d.pos_alt : d.pos;
   float2* dst = swap_back ? d.pos : d.pos_alt;
-  if (nheavy) {   // long lists first, on a side branch, concurrent with the rest
-    cudaEventRecord(fork, st);
-    cudaStreamWaitEvent(side, fork, 0);
-    k_link<<<blocks_for(nheavy), kBlock, 0, side>>>(d, s, rp, en, src, dst, order, nheavy);
-    cudaEventRecord(join, side);
-  }
-  if (d.n > nheavy) k_link<<<blocks_for(d.n - nheavy), kBlock, 0, st>>>(d, s, rp, en, src, dst, order + nheavy, d.n - nheavy);
-  if (nheavy) cudaStreamWaitEvent(st, join, 0);
+  const uint32_t nb = nhub + blocks_for(d.n - nhub);
+  k_link<<<nb, kBlock, nhub ? sizeof(HubStage) : 0, st>>>(d, s, rp, en, src, dst, order, d.n, nhub);
 }
 
-void launch_collision_grid(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
-  const uint32_t nb = blocks_for(d.n);
-  if (nb) k_coll_grid<<<nb, kBlock, 0, st>>>(d, s);
+void launch_collision_grid(const DeviceView& d, const SimScalars& s, const uint32_t* order, uint32_t count,
+                           cudaStream_t st) {
+  if (!order) count = d.n;
+  const uint32_t nb = blocks_for(count);
+  if (nb) k_coll_grid<<<nb, kBlock, 0, st>>>(d, s, order, count);
   const uint32_t cells = 4u * (uint32_t)(s.coll_grid * s.coll_grid);
   k_coll_convert<<<blocks_for(cells), kBlock, 0, st>>>(d, s);
 }
 
-void launch_collision_force(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
-  const uint32_t nb = blocks_for(d.n);
-  if (nb) k_coll_force<<<nb, kBlock, 0, st>>>(d, s);
+void launch_collision_force(const DeviceView& d, const SimScalars& s, const uint32_t* order, uint32_t count,
+                            cudaStream_t st) {
+  if (!order) count = d.n;
+  const uint32_t nb = blocks_for(count);
+  if (nb) k_coll_force<<<nb, kBlock, 0, st>>>(d, s, order, count);
 }
 
 void launch_tick_end(const DeviceView& d, cudaStream_t st) { k_tick_end<<<1, 1, 0, st>>>(d); }

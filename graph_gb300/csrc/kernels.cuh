@@ -88,10 +88,14 @@ void launch_scatter(const DeviceView& d, const SimScalars& s, cudaStream_t st);
 void launch_cells(const DeviceView& d, const SimScalars& s, cudaStream_t st);
 void launch_manybody(const DeviceView& d, const SimScalars& s, cudaStream_t st);
 // direction 0 = incoming (reads pos, writes pos_alt), 1 = outgoing (pos_alt -> pos)
-void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool swap_back, cudaStream_t st,
-                 cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
-void launch_collision_grid(const DeviceView& d, const SimScalars& s, cudaStream_t st);
-void launch_collision_force(const DeviceView& d, const SimScalars& s, cudaStream_t st);
+// The first n_heavy_* rows of the order each get a CTA of their own.
+void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool swap_back, cudaStream_t st);
+// `order`: the live points in cell order (sorted_idx of this tick's many-body
+// pass, `count` of them), or nullptr to take all points in index order.
+void launch_collision_grid(const DeviceView& d, const SimScalars& s, const uint32_t* order, uint32_t count,
+                           cudaStream_t st);
+void launch_collision_force(const DeviceView& d, const SimScalars& s, const uint32_t* order, uint32_t count,
+                            cudaStream_t st);
 void launch_tick_end(const DeviceView& d, cudaStream_t st);
 
 uint32_t scan_blocks(uint32_t cells);
