@@ -21,12 +21,13 @@ STAGE_MANYBODY = 1 << 2
 STAGE_LINK_IN = 1 << 3
 STAGE_LINK_OUT = 1 << 4
 STAGE_COLLISION = 1 << 5
-STAGE_ALL = 0x3F
+STAGE_CLUSTERS = 1 << 6
+STAGE_ALL = 0x7F
 
-NUM_STAGE_TIMES = 10
+NUM_STAGE_TIMES = 11
 STAGE_TIME_NAMES = [
     "prepass", "center", "scan", "scatter", "cells", "manybody", "link_in", "link_out",
-    "collision_grid", "collision_force",
+    "collision_grid", "collision_force", "clusters",
 ]
 
 
@@ -53,6 +54,7 @@ class Config(C.Structure):
         ("stage_mask", C.c_uint32),
         ("device", C.c_int32),
         ("hbm_budget_bytes", C.c_double),
+        ("simulation_cluster", C.c_double),
     ]
 
 
@@ -113,6 +115,7 @@ DEFAULTS = dict(
     stage_mask=STAGE_ALL,
     device=0,
     hbm_budget_bytes=0.0,
+    simulation_cluster=0.1,
 )
 
 # Reference config keys (camelCase, src/config.ts) -> C field names.
@@ -133,6 +136,7 @@ CAMEL_TO_FIELD = {
     "pointDefaultSize": "point_default_size",
     "enableSimulation": "enable_simulation",
     "randomSeed": "random_seed",
+    "simulationCluster": "simulation_cluster",
 }
 
 
@@ -200,6 +204,10 @@ def declare(lib, prefix: str, engine_t=C.c_void_p):
         "set_link_strength": ([E, f, C.c_uint64], C.c_int),
         "set_point_sizes": ([E, f, C.c_uint64], C.c_int),
         "set_pinned_points": ([E, C.POINTER(C.c_double), C.c_uint64], C.c_int),
+        "set_point_clusters": ([E, f, C.c_uint64], C.c_int),
+        "set_cluster_positions": ([E, f, C.c_uint64], C.c_int),
+        "set_point_cluster_strength": ([E, f, C.c_uint64], C.c_int),
+        "get_cluster_positions": ([E, C.POINTER(C.c_double), C.c_uint64, C.POINTER(C.c_uint64)], C.c_int),
         "render": ([E, C.c_double], C.c_int),
         "start": ([E, C.c_double], C.c_int),
         "stop": ([E], C.c_int),

@@ -75,6 +75,38 @@ class EngineCalls:
         a = np.ascontiguousarray(np.asarray(idx, dtype=np.float64))
         return self._call("set_pinned_points", a.ctypes.data_as(C.POINTER(C.c_double)), a.size)
 
+    def set_point_clusters(self, clusters):
+        """One value per point; None or NaN = no cluster (the reference's `undefined`)."""
+        if clusters is None:
+            return self._call("set_point_clusters", None, 0)
+        a = _f32([math.nan if v is None else v for v in clusters]
+                 if isinstance(clusters, (list, tuple)) else clusters)
+        return self._call("set_point_clusters", _fptr(a), a.size)
+
+    def set_cluster_positions(self, xy):
+        """x, y per cluster; None or NaN = centre of mass.  None clears them."""
+        if xy is None:
+            return self._call("set_cluster_positions", None, 0)
+        a = _f32([math.nan if v is None else v for v in xy] if isinstance(xy, (list, tuple)) else xy)
+        if a.size == 0:
+            a = np.zeros(1, dtype=np.float32)   # a non-null pointer: `[]` counts as set
+            return self._call("set_cluster_positions", _fptr(a), 0)
+        return self._call("set_cluster_positions", _fptr(a), a.size)
+
+    def set_point_cluster_strength(self, s):
+        if s is None:
+            return self._call("set_point_cluster_strength", None, 0)
+        a = _f32(s)
+        return self._call("set_point_cluster_strength", _fptr(a), a.size)
+
+    def get_cluster_positions(self):
+        n = C.c_uint64(0)
+        self._call("get_cluster_positions", None, 0, C.byref(n))
+        out = np.empty(n.value, dtype=np.float64)
+        if n.value:
+            self._call("get_cluster_positions", out.ctypes.data_as(C.POINTER(C.c_double)), out.size, C.byref(n))
+        return out
+
     def render(self, alpha=None):
         return self._call("render", math.nan if alpha is None else float(alpha))
 

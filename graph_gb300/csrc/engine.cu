@@ -45,6 +45,9 @@ struct cgl_engine {
   bool pinned_set = false;
   std::vector<double> pinned_input;
   bool pos_dirty = false, links_dirty = false, sizes_dirty = false;
+  bool have_clusters = false, have_cluster_pos = false, have_cluster_strength = false;
+  std::vector<float> in_clusters, in_cluster_pos, in_cluster_strength;
+  bool clusters_dirty = false;
 
   // applied data
   uint64_t N = 0, E = 0;
@@ -66,6 +69,10 @@ struct cgl_engine {
   int cgrid = 0;
   float ccell = 0.f;
 
+  // clusters (Clusters/index.ts)
+  bool point_clusters = false, cluster_positions = false;
+  uint32_t n_clusters = 0;
+
   // simulation state (Store)
   double adjusted_space = 4096;
   double alpha = 1.0;
@@ -83,6 +90,7 @@ struct cgl_engine {
   DevBuf b_rowptr_in, b_rowptr_out, b_ent_in, b_ent_out, b_heavy_in, b_heavy_out;
   uint32_t n_heavy_in = 0, n_heavy_out = 0;
   DevBuf b_size, b_cgrid_acc, b_cgrid;
+  DevBuf b_cl_of, b_cl_coeff, b_cl_custom, b_cl_acc;
   DeviceView view{};
   uint32_t level_off[10] = {};
   uint32_t acc_off[10] = {};
@@ -152,7 +160,8 @@ void dev_free_all(cgl_engine* e) {
                    &e->b_tickets, &e->b_rec, &e->b_acc, &e->b_centroid, &e->b_params, &e->b_tick_ctr,
                    &e->b_rowptr_in, &e->b_rowptr_out, &e->b_ent_in, &e->b_ent_out, &e->b_size,
                    &e->b_cgrid_acc, &e->b_cgrid, &e->b_big_list, &e->b_big_count,
-                   &e->b_big_sx, &e->b_big_sy, &e->b_big_ns, &e->b_heavy_in, &e->b_heavy_out};
+                   &e->b_big_sx, &e->b_big_sy, &e->b_big_ns, &e->b_heavy_in, &e->b_heavy_out,
+                   &e->b_cl_of, &e->b_cl_coeff, &e->b_cl_custom, &e->b_cl_acc};
   for (DevBuf* b : all) {
     if (b->p) cudaFree(b->p);
     b->p = nullptr;
@@ -214,6 +223,11 @@ void refresh_view(cgl_engine* e) {
   d.size = (const float*)e->b_size.p;
   d.cgrid_acc = (long long*)e->b_cgrid_acc.p;
   d.cgrid = (float4*)e->b_cgrid.p;
+  d.cluster_of = (const uint32_t*)e->b_cl_of.p;
+  d.cluster_coeff = (const float*)e->b_cl_coeff.p;
+  d.cluster_custom = (const float2*)e->b_cl_custom.p;
+  d.cluster_acc = (long long*)e->b_cl_acc.p;
+  d.n_clusters = e->n_clusters;
 }
 
 SimScalars make_scalars(const cgl_engine* e) {
@@ -239,12 +253,14 @@ SimScalars make_scalars(const cgl_engine* e) {
   s.csf = e->Gf ? (float)(e->adjusted_space / e->Gf) : 1.f;
   s.fx = e->fx;
   s.units = PairUnits{1.0f, -0.0f};
+  s.cluster = (float)e->cfg.simulation_cluster;
   return s;
 }
 
 // ------------------------------------------------------------------ tick --
 struct TickPlan {
   bool grav, cent, mb, link_in, link_out, coll;
+  bool clus, clus_sum;   // the cluster pass runs / needs the centres of mass
 };
 
 TickPlan plan_tick(const cgl_engine* e) {
@@ -257,6 +273,9 @@ TickPlan plan_tick(const cgl_engine* e) {
   p.link_in = links && (m & CGL_STAGE_LINK_IN);
   p.link_out = links && (m & CGL_STAGE_LINK_OUT);
   p.coll = e->cfg.simulation_collision != 0 && (m & CGL_STAGE_COLLISION) && e->N > 0;
+  // src/index.ts:2057-2061: runs whenever per-point clusters or cluster positions are set
+  p.clus = (e->point_clusters || e->cluster_positions) && (m & CGL_STAGE_CLUSTERS) && e->N > 0;
+  p.clus_sum = p.clus && e->point_clusters;
   return p;
 }
 
@@ -295,6 +314,15 @@ cgl_status enqueue_tick(cgl_engine* e, cudaStream_t st, cudaEvent_t* ev) {
     mark(7, 1);
     if (!(p.link_in && p.link_out))
       CU(cudaMemcpyAsync(d.pos, d.pos_alt, e->N * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+  }
+  if (p.clus) {
+    mark(10, 0);
+    if (p.clus_sum) {
+      CU(cudaMemsetAsync(d.cluster_acc, 0, 3 * (size_t)e->n_clusters * sizeof(long long), st));
+      launch_cluster_sum(d, s, st);
+    }
+    launch_cluster_force(d, s, st);
+    mark(10, 1);
   }
   if (p.coll) {
     // the many-body pass left every live point in sorted_idx, grouped by cell
@@ -540,8 +568,29 @@ cgl_status do_render(cgl_engine* e, double alpha) {
       CU(cudaMemcpyAsync(e->b_ent_out.p, en_out.data(), en_out.size() * sizeof(uint4), cudaMemcpyHostToDevice, e->stream));
     CU(cudaStreamSynchronize(e->stream));
   }
+  if (e->clusters_dirty || pos_changed) {
+    // Clusters.create (Clusters/index.ts:54-100), src/index.ts:1668
+    e->graph_dirty = true;
+    ingest::Clusters c;
+    ingest::build_clusters(n, e->have_clusters, e->in_clusters, e->have_cluster_pos, e->in_cluster_pos,
+                           e->have_cluster_strength, e->in_cluster_strength, c);
+    e->point_clusters = c.point_clusters;
+    e->cluster_positions = c.positions;
+    e->n_clusters = (c.point_clusters || c.positions) ? c.count : 0;
+    if (e->n_clusters) {
+      if ((st = dev_reserve(e, e->b_cl_of, n * sizeof(uint32_t), false))) return st;
+      if ((st = dev_reserve(e, e->b_cl_coeff, n * sizeof(float), false))) return st;
+      if ((st = dev_reserve(e, e->b_cl_custom, e->n_clusters * sizeof(float2), false))) return st;
+      if ((st = dev_reserve(e, e->b_cl_acc, 3 * (size_t)e->n_clusters * sizeof(long long), true))) return st;
+      CU(cudaMemcpyAsync(e->b_cl_of.p, c.of.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, e->stream));
+      CU(cudaMemcpyAsync(e->b_cl_coeff.p, c.coeff.data(), n * sizeof(float), cudaMemcpyHostToDevice, e->stream));
+      CU(cudaMemcpyAsync(e->b_cl_custom.p, c.custom.data(), e->n_clusters * sizeof(float2), cudaMemcpyHostToDevice,
+                         e->stream));
+      CU(cudaStreamSynchronize(e->stream));
+    }
+  }
   refresh_view(e);
-  e->pos_dirty = e->links_dirty = e->sizes_dirty = false;
+  e->pos_dirty = e->links_dirty = e->sizes_dirty = e->clusters_dirty = false;
   if (!std::isnan(alpha)) e->alpha = alpha;
   return CGL_OK;
 }
@@ -576,6 +625,7 @@ void cgl_config_defaults(cgl_config* c) {
   c->stage_mask = CGL_STAGE_ALL;
   c->device = 0;
   c->hbm_budget_bytes = 0;
+  c->simulation_cluster = 0.1;
 }
 
 cgl_status cgl_create(const cgl_config* cfg, cgl_engine** out) {
@@ -673,6 +723,7 @@ cgl_status cgl_set_point_positions(cgl_engine* e, const float* xy, uint64_t n) {
   e->in_pos.assign(xy, xy + n);
   e->have_pos_input = true;
   e->pos_dirty = e->links_dirty = e->sizes_dirty = true;
+  e->clusters_dirty = true;   // src/index.ts:570
   return st;
 }
 
@@ -703,6 +754,56 @@ cgl_status cgl_set_point_sizes(cgl_engine* e, const float* v, uint64_t n) {
   if (!v) { e->in_sizes.clear(); e->have_sizes = false; }
   else { e->in_sizes.assign(v, v + n); e->have_sizes = true; }
   e->sizes_dirty = true;
+  return CGL_OK;
+}
+
+cgl_status cgl_set_point_clusters(cgl_engine* e, const float* v, uint64_t n) {
+  CHECK_E(e);
+  if (!v || n == 0) { e->in_clusters.clear(); e->have_clusters = false; }
+  else { e->in_clusters.assign(v, v + n); e->have_clusters = true; }
+  e->clusters_dirty = true;
+  return CGL_OK;
+}
+
+cgl_status cgl_set_cluster_positions(cgl_engine* e, const float* v, uint64_t n) {
+  CHECK_E(e);
+  if (!v) { e->in_cluster_pos.clear(); e->have_cluster_pos = false; }
+  else { e->in_cluster_pos.assign(v, v + n); e->have_cluster_pos = true; }
+  e->clusters_dirty = true;
+  return CGL_OK;
+}
+
+cgl_status cgl_set_point_cluster_strength(cgl_engine* e, const float* v, uint64_t n) {
+  CHECK_E(e);
+  if (!v || n == 0) { e->in_cluster_strength.clear(); e->have_cluster_strength = false; }
+  else { e->in_cluster_strength.assign(v, v + n); e->have_cluster_strength = true; }
+  e->clusters_dirty = true;
+  return CGL_OK;
+}
+
+cgl_status cgl_get_cluster_positions(cgl_engine* e, double* out, uint64_t cap, uint64_t* n_out) {
+  CHECK_E(e);
+  // Clusters.getCentroidPositions (Clusters/index.ts:389-423): sum / count in
+  // FP64 of the f32 sums, from the current positions
+  const uint64_t n = e->point_clusters ? 2 * (uint64_t)e->n_clusters : 0;
+  if (n_out) *n_out = n;
+  if (!out || n == 0) return CGL_OK;
+  if (cap < n) return fail(e, CGL_INVALID_ARG, "output holds %llu doubles, need %llu", (unsigned long long)cap,
+                           (unsigned long long)n);
+  const DeviceView& d = e->view;
+  const SimScalars s = make_scalars(e);
+  CU(cudaMemsetAsync(d.cluster_acc, 0, 3 * (size_t)e->n_clusters * sizeof(long long), e->stream));
+  launch_cluster_sum(d, s, e->stream);
+  CU(cudaGetLastError());
+  std::vector<long long> acc(3 * (size_t)e->n_clusters);
+  CU(cudaMemcpyAsync(acc.data(), d.cluster_acc, acc.size() * sizeof(long long), cudaMemcpyDeviceToHost, e->stream));
+  CU(cudaStreamSynchronize(e->stream));
+  for (uint32_t c = 0; c < e->n_clusters; ++c) {
+    const float sx = (float)acc[3 * (size_t)c] * e->fx.inv, sy = (float)acc[3 * (size_t)c + 1] * e->fx.inv;
+    const float cnt = (float)acc[3 * (size_t)c + 2];
+    out[2 * (size_t)c] = (double)sx / (double)cnt;
+    out[2 * (size_t)c + 1] = (double)sy / (double)cnt;
+  }
   return CGL_OK;
 }
 
@@ -849,6 +950,7 @@ cgl_status cgl_get_layout(cgl_engine* e, cgl_layout* o) {
   if (p.mb) k += 6;                                    // scan (2), scatter, big cells, cells, manybody
   k += (uint32_t)p.link_in + (uint32_t)p.link_out;
   if (p.coll) k += 3;                                  // grid, convert, force
+  if (p.clus) k += 1 + (uint32_t)p.clus_sum;           // sums, pull + update
   o->kernels_per_tick = k;
   return CGL_OK;
 }

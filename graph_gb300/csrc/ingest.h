@@ -195,5 +195,44 @@ inline void build_links(const float* links, uint64_t E, uint64_t N, const float*
   build_direction(links, E, N, false, deg, strength, absent, rng, out);
 }
 
+// Clusters.create (Clusters/index.ts:54-100) on GraphData.updateClusters
+// (GraphData/index.ts:420-441): per-point clusters apply only when there is
+// one value per point, cluster positions whenever set, per-point strength only
+// when there is one value per point.  A cluster index is a non-negative
+// integer below 2^24; NaN (undefined), negative, non-integer and infinite
+// values leave the point unclustered.  clusterCount = max index + 1 (at least
+// 1); a cluster position is (x, y), -1 where undefined (NaN) or not given.
+struct Clusters {
+  bool point_clusters = false;     // GraphData.pointClusters defined
+  bool positions = false;          // GraphData.clusterPositions defined
+  uint32_t count = 0;              // clusterCount
+  std::vector<uint32_t> of;        // [N] cluster of each point, kNoClusterId if none
+  std::vector<float> coeff;        // [N] clusterForceCoefficient
+  std::vector<float2> custom;      // [count] cluster position, negative = centre of mass
+};
+inline void build_clusters(uint64_t N, bool have_idx, const std::vector<float>& idx, bool have_pos,
+                           const std::vector<float>& cpos, bool have_str, const std::vector<float>& str, Clusters& c) {
+  c.point_clusters = have_idx && N > 0 && idx.size() == N;
+  c.positions = have_pos && N > 0;
+  c.of.assign(N, kNoClusterId);
+  c.coeff.assign(N, 1.0f);
+  uint32_t maxc = 0;
+  if (c.point_clusters)
+    for (uint64_t i = 0; i < N; ++i) {
+      const float v = idx[i];
+      if (!(v >= 0.f) || !(v < 16777216.f) || v != std::floor(v)) continue;
+      c.of[i] = (uint32_t)v;
+      maxc = std::max(maxc, (uint32_t)v);
+    }
+  c.count = maxc + 1;
+  if (have_str && str.size() == N) std::copy(str.begin(), str.end(), c.coeff.begin());
+  c.custom.assign(c.count, make_float2(-1.f, -1.f));
+  if (c.positions)
+    for (uint32_t k = 0; k < c.count; ++k) {
+      if (2 * (size_t)k < cpos.size() && !std::isnan(cpos[2 * (size_t)k])) c.custom[k].x = cpos[2 * (size_t)k];
+      if (2 * (size_t)k + 1 < cpos.size() && !std::isnan(cpos[2 * (size_t)k + 1])) c.custom[k].y = cpos[2 * (size_t)k + 1];
+    }
+}
+
 }  // namespace ingest
 }  // namespace cgl

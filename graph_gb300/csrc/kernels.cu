@@ -938,6 +938,98 @@ __global__ void __launch_bounds__(kBlock) k_coll_force(DeviceView d, SimScalars 
   if (!(f & kPinned)) d.pos[i] = integrate(p, vx, vy, s.friction, s.space);
 }
 
+// --------------------------------------------------------------- clusters --
+// Clusters.run (Clusters/index.ts:426-469).  Centre of mass per cluster
+// (calculate-centermass.vert:22-52: live, clustered points only) as exact
+// integer sums.  The lanes of a warp sum their terms per cluster first
+// (kCollRounds distinct clusters per warp, the rest add their own); with at
+// most kClusterSmem clusters a block also sums in shared memory and adds each
+// cluster's total once, so a few clusters do not serialise on a few atomics.
+constexpr uint32_t kClusterSmem = 256;
+
+template <bool SMEM>
+__global__ void __launch_bounds__(kBlock) k_cluster_sum(DeviceView d, SimScalars s) {
+  __shared__ unsigned long long tab[SMEM ? 3 * kClusterSmem : 1];
+  const uint32_t K = d.n_clusters;
+  if (SMEM) {
+    for (uint32_t k = threadIdx.x; k < 3 * K; k += blockDim.x) tab[k] = 0;
+    __syncthreads();
+  }
+  const int lane = threadIdx.x & 31;
+  auto add = [&](uint32_t c, long long x, long long y, long long n) {
+    unsigned long long* a = SMEM ? &tab[3 * c] : (unsigned long long*)&d.cluster_acc[3 * (size_t)c];
+    atomicAdd(&a[0], (unsigned long long)x);
+    atomicAdd(&a[1], (unsigned long long)y);
+    atomicAdd(&a[2], (unsigned long long)n);
+  };
+  const uint32_t stride = SMEM ? gridDim.x * blockDim.x : d.n;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < d.n; base += stride) {   // uniform per block
+    const uint32_t i = base + threadIdx.x;
+    uint32_t c = kNoClusterId;
+    bool on = i < d.n;
+    if (on) {
+      c = d.cluster_of[i];
+      on = c != kNoClusterId && !(d.flags[i] & kAbsent);
+    }
+    unsigned todo = __ballot_sync(0xffffffffu, on);
+    if (!todo) continue;   // warp-uniform
+    const float2 p = on ? d.pos[i] : make_float2(0.f, 0.f);
+    const long long fx = on ? to_fixed(p.x, s.fx) : 0, fy = on ? to_fixed(p.y, s.fx) : 0;
+#pragma unroll 1
+    for (int r = 0; r < kCollRounds && todo; ++r) {
+      const int l = __ffs(todo) - 1;
+      const uint32_t cl = __shfl_sync(0xffffffffu, c, l);
+      const bool mine = ((todo >> lane) & 1u) && c == cl;
+      const unsigned grp = __ballot_sync(0xffffffffu, mine);
+      const long long sx = warp_sum64(mine ? fx : 0);
+      const long long sy = warp_sum64(mine ? fy : 0);
+      if (lane == l) add(cl, sx, sy, __popc(grp));
+      todo &= ~grp;
+    }
+    if ((todo >> lane) & 1u) add(c, fx, fy, 1);
+  }
+  if (SMEM) {
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < K; k += blockDim.x) {
+      if (!tab[3 * k + 2]) continue;
+      unsigned long long* a = (unsigned long long*)&d.cluster_acc[3 * (size_t)k];
+      atomicAdd(&a[0], tab[3 * k]);
+      atomicAdd(&a[1], tab[3 * k + 1]);
+      atomicAdd(&a[2], tab[3 * k + 2]);
+    }
+  }
+}
+
+// force-cluster.frag:28-53, then the update (update-position.frag:26-59).
+__global__ void __launch_bounds__(kBlock) k_cluster_force(DeviceView d, SimScalars s) {
+  const TickParams tp = tick_params(d);
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n) return;
+  const uint8_t f = d.flags[i];
+  if (f & kAbsent) return;   // absent points keep their (NaN) position
+  const float2 p = d.pos[i];
+  float vx = 0.f, vy = 0.f;
+  const uint32_t c = d.cluster_of[i];
+  if (c != kNoClusterId) {
+    float2 t = d.cluster_custom[c];
+    if (t.x < 0.f || t.y < 0.f) {   // no custom position: centre of mass
+      const long long* a = d.cluster_acc + 3 * (size_t)c;
+      const float cnt = (float)a[2];
+      t = make_float2(__fdiv_rn(from_fixed(a[0], s.fx), cnt), __fdiv_rn(from_fixed(a[1], s.fx), cnt));
+    }
+    const float dx = __fsub_rn(t.x, p.x), dy = __fsub_rn(t.y, p.y);
+    const float dist = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
+    if (dist > 0.f) {
+      const float add = __fmul_rn(__fmul_rn(__fmul_rn(tp.alpha, dist), s.cluster), d.cluster_coeff[i]);
+      const float inv = __frcp_rn(dist);   // normalize(v) = v * (1 / length(v))
+      // velocity starts at vec4(0) and `+=` adds to it: 0 + w turns a -0 into +0
+      vx = __fadd_rn(0.f, __fmul_rn(add, __fmul_rn(dx, inv)));
+      vy = __fadd_rn(0.f, __fmul_rn(add, __fmul_rn(dy, inv)));
+    }
+  }
+  if (!(f & kPinned)) d.pos[i] = integrate(p, vx, vy, s.friction, s.space);
+}
+
 __global__ void k_tick_end(DeviceView d) { *d.tick_ctr += 1; }
 
 inline uint32_t blocks_for(uint32_t n) { return (n + kBlock - 1) / kBlock; }
@@ -1001,6 +1093,19 @@ void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool s
   float2* dst = swap_back ? d.pos : d.pos_alt;
   const uint32_t nb = nhub + blocks_for(d.n - nhub);
   k_link<<<nb, kBlock, nhub ? sizeof(HubStage) : 0, st>>>(d, s, rp, en, src, dst, order, d.n, nhub);
+}
+
+void launch_cluster_sum(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
+  if (!d.n) return;
+  if (d.n_clusters <= kClusterSmem)
+    k_cluster_sum<true><<<std::min(blocks_for(d.n), 4u * 152u), kBlock, 0, st>>>(d, s);
+  else
+    k_cluster_sum<false><<<blocks_for(d.n), kBlock, 0, st>>>(d, s);
+}
+
+void launch_cluster_force(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
+  const uint32_t nb = blocks_for(d.n);
+  if (nb) k_cluster_force<<<nb, kBlock, 0, st>>>(d, s);
 }
 
 void launch_collision_grid(const DeviceView& d, const SimScalars& s, const uint32_t* order, uint32_t count,

@@ -54,6 +54,12 @@ struct DeviceView {
   const float* size;          // resolved point sizes [n]
   long long* cgrid_acc;       // 4 grids x G_c^2 x (x, y, size, count)
   float4* cgrid;              // 4 grids x G_c^2 (sx, sy, ssize, count)
+  // clusters
+  const uint32_t* cluster_of;     // cluster of each point, 0xFFFFFFFF if none [n]
+  const float* cluster_coeff;     // pull coefficient of each point [n]
+  const float2* cluster_custom;   // cluster position, negative = centre of mass [K]
+  long long* cluster_acc;         // x, y, count sums per cluster [3K]
+  uint32_t n_clusters;            // K
 };
 
 struct SimScalars {
@@ -76,6 +82,7 @@ struct SimScalars {
   float csf;                  // finest cell size
   FixedScale fx;
   PairUnits units;            // {1, -0}: operands of the paired sums and products
+  float cluster;              // simulationCluster
 };
 
 
@@ -96,6 +103,10 @@ void launch_collision_grid(const DeviceView& d, const SimScalars& s, const uint3
                            cudaStream_t st);
 void launch_collision_force(const DeviceView& d, const SimScalars& s, const uint32_t* order, uint32_t count,
                             cudaStream_t st);
+// Sums of each cluster's live points (cluster_acc must be zero on entry).
+void launch_cluster_sum(const DeviceView& d, const SimScalars& s, cudaStream_t st);
+// The cluster pull and the update of every point.
+void launch_cluster_force(const DeviceView& d, const SimScalars& s, cudaStream_t st);
 void launch_tick_end(const DeviceView& d, cudaStream_t st);
 
 uint32_t scan_blocks(uint32_t cells);

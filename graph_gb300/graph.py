@@ -2,8 +2,9 @@
 
 Mirrors cosmos.gl's `Graph` (src/index.ts) for the parts that drive the force
 simulation: setPointPositions / setLinks / setLinkStrength / setPointSizes /
-setPinnedPoints / render / start / stop / pause / unpause / step /
-getPointPositions / progress / isSimulationRunning / setConfig /
+setPinnedPoints / setPointClusters / setClusterPositions /
+setPointClusterStrength / render / start / stop / pause / unpause / step /
+getPointPositions / getClusterPositions / progress / isSimulationRunning / setConfig /
 setConfigPartial / destroy, and the onSimulation* callbacks.  Rendering,
 zoom, hover and picking stay in the browser and are not part of this class.
 
@@ -110,6 +111,24 @@ class Graph:
             return
         self._staged["sizes"] = pointSizes
 
+    def setPointClusters(self, pointClusters):
+        """Cluster index per point; None (the reference's `undefined`) = no cluster (src/index.ts:854-859)."""
+        if self._destroyed:
+            return
+        self._staged["clusters"] = pointClusters
+
+    def setClusterPositions(self, clusterPositions):
+        """x, y per cluster; None = centre of mass (src/index.ts:871-876)."""
+        if self._destroyed:
+            return
+        self._staged["cluster_positions"] = clusterPositions
+
+    def setPointClusterStrength(self, clusterStrength):
+        """Per-point coefficient of the cluster pull (src/index.ts:888-893)."""
+        if self._destroyed:
+            return
+        self._staged["cluster_strength"] = clusterStrength
+
     def setPinnedPoints(self, pinnedIndices):
         if self._destroyed:
             return
@@ -128,6 +147,12 @@ class Graph:
             self._engine.set_link_strength(s.pop("strength"))
         if "sizes" in s:
             self._engine.set_point_sizes(s.pop("sizes"))
+        if "clusters" in s:
+            self._engine.set_point_clusters(s.pop("clusters"))
+        if "cluster_positions" in s:
+            self._engine.set_cluster_positions(s.pop("cluster_positions"))
+        if "cluster_strength" in s:
+            self._engine.set_point_cluster_strength(s.pop("cluster_strength"))
         self._engine.render(simulationAlpha)
 
     # --- control (src/index.ts:1457-1540) ------------------------------------
@@ -207,6 +232,12 @@ class Graph:
         if self._destroyed:
             return np.zeros(0, dtype=np.float32)
         return self._engine.get_point_positions()
+
+    def getClusterPositions(self):
+        """Centre of mass of each cluster as float64 [x0, y0, x1, y1, ...] (src/index.ts:1135-1139)."""
+        if self._destroyed:
+            return np.zeros(0, dtype=np.float64)
+        return self._engine.get_cluster_positions()
 
     @property
     def progress(self):

@@ -50,7 +50,8 @@ enum {
   CGL_STAGE_LINK_IN = 1u << 3,
   CGL_STAGE_LINK_OUT = 1u << 4,
   CGL_STAGE_COLLISION = 1u << 5,
-  CGL_STAGE_ALL = 0x3Fu
+  CGL_STAGE_CLUSTERS = 1u << 6,
+  CGL_STAGE_ALL = 0x7Fu
 };
 
 /* Simulation configuration.  Field meanings and defaults follow the reference:
@@ -80,6 +81,7 @@ typedef struct cgl_config {
   uint32_t stage_mask;                       /* CGL_STAGE_* bits, default CGL_STAGE_ALL */
   int32_t device;                            /* CUDA device ordinal, default 0 */
   double hbm_budget_bytes;                   /* device-memory admission budget for this handle; 0 = unlimited */
+  double simulation_cluster;                 /* simulationCluster, default 0.1 (config.ts:435, variables.ts:79) */
 } cgl_config;
 
 typedef struct cgl_state {
@@ -132,6 +134,27 @@ cgl_status cgl_set_point_sizes(cgl_engine* e, const float* sizes, uint64_t n);
  * (Points/index.ts:1264-1304).  Non-integer or out-of-range indices are ignored. */
 cgl_status cgl_set_pinned_points(cgl_engine* e, const double* indices, uint64_t n);
 
+/* Graph.setPointClusters((number | undefined)[]) — src/index.ts:854-859.  One
+ * value per point: a non-negative integer is the point's cluster; NaN stands
+ * for `undefined` (no cluster).  Negative values leave the point unclustered,
+ * as in the reference (its cluster texel gets a negative row); non-integer and
+ * infinite values are treated as unclustered too (the reference documents
+ * integers only).  Applied at render only when n == points_number
+ * (GraphData/index.ts:426-430); n = 0 or a null pointer clears the clusters. */
+cgl_status cgl_set_point_clusters(cgl_engine* e, const float* clusters, uint64_t n);
+
+/* Graph.setClusterPositions((number | undefined)[]) — src/index.ts:871-876.
+ * x, y per cluster; NaN stands for `undefined` (the cluster is pulled to its
+ * centre of mass, Clusters/index.ts:77-82, force-cluster.frag:41-44).  Entries
+ * beyond the cluster count are ignored.  A null pointer clears them; an empty
+ * non-null array counts as set (the reference runs the pass for `[]`). */
+cgl_status cgl_set_cluster_positions(cgl_engine* e, const float* xy, uint64_t n_floats);
+
+/* Graph.setPointClusterStrength(Float32Array) — src/index.ts:888-893; per-point
+ * coefficient of the cluster pull (default 1), used only when n ==
+ * points_number (GraphData/index.ts:436-440).  Null or n = 0 clears it. */
+cgl_status cgl_set_point_cluster_strength(cgl_engine* e, const float* strength, uint64_t n);
+
 /* Graph.render(simulationAlpha?) — src/index.ts:936-1003: ingests staged data
  * (GraphData.update :443-462, Graph.update :1987-1994, Graph.create :1635-1688).
  * alpha = NaN keeps the current alpha. */
@@ -159,6 +182,15 @@ cgl_status cgl_run(cgl_engine* e, uint32_t max_ticks, uint32_t* ticks_done);
  * out_xy holds 2 * points_number floats.  Synchronises the engine stream. */
 cgl_status cgl_get_point_positions(cgl_engine* e, float* out_xy, uint64_t capacity_floats);
 
+/* Graph.getClusterPositions() — src/index.ts:1135-1139, Clusters.getCentroidPositions
+ * (Clusters/index.ts:389-423): the centre of mass of each cluster's live points,
+ * x then y per cluster, sum / count in FP64 of the f32 sums (NaN for a cluster
+ * with no live point).  Computed from the current positions (the reference reads
+ * the texture of the pass before the last one while the simulation runs).
+ * *n_out = 2 * cluster count, 0 when no per-point clusters are applied.  out may
+ * be null to query the size.  Synchronises the engine stream. */
+cgl_status cgl_get_cluster_positions(cgl_engine* e, double* out, uint64_t capacity_doubles, uint64_t* n_out);
+
 /* Graph.progress / Graph.isSimulationRunning — src/index.ts:469, :477. */
 cgl_status cgl_get_state(cgl_engine* e, cgl_state* out);
 
@@ -172,8 +204,10 @@ cgl_status cgl_set_stream(cgl_engine* e, void* cuda_stream);
 /* Block until all queued work on the engine stream finished. */
 cgl_status cgl_synchronize(cgl_engine* e);
 /* Average device time per tick stage over `ticks` profiled ticks, in ms, via CUDA
- * events between stages (no CUDA graph).  Stage order: see CGL_NUM_STAGE_TIMES. */
-#define CGL_NUM_STAGE_TIMES 10
+ * events between stages (no CUDA graph).  Stage order: prepass, center, scan,
+ * scatter, cells, manybody, link_in, link_out, collision_grid, collision_force,
+ * clusters. */
+#define CGL_NUM_STAGE_TIMES 11
 cgl_status cgl_profile_stages(cgl_engine* e, uint32_t ticks, double* ms_out /*[CGL_NUM_STAGE_TIMES]*/);
 
 /* Static layout facts of the applied data (for tests, benches and byte models). */

@@ -225,6 +225,17 @@ struct orc_engine {
   int cgrid = 0;
   float ccell = 0.f;
 
+  // clusters (Clusters/index.ts): staged input, applied data
+  bool have_clusters = false, have_cluster_pos = false, have_cluster_strength = false;
+  std::vector<float> in_clusters, in_cluster_pos, in_cluster_strength;
+  bool clusters_dirty = false;
+  bool point_clusters = false;     // GraphData.pointClusters defined (length == N)
+  bool cluster_positions = false;  // GraphData.clusterPositions defined
+  uint32_t K = 0;                  // clusterCount
+  std::vector<uint32_t> cluster_of;   // N, kNoCluster when unclustered
+  std::vector<float> cluster_coeff;   // N, clusterForceCoefficient (default 1)
+  std::vector<float> cluster_custom;  // 2K, -1 where undefined
+
   // simulation state (Store)
   double adjusted_space = 4096;
   double alpha = 1.0;
@@ -798,6 +809,91 @@ void run_collision(orc_engine* e, float a) {
   }
 }
 
+constexpr uint32_t kNoCluster = 0xFFFFFFFFu;
+
+// Clusters.create (Clusters/index.ts:54-100) on the applied data
+// (GraphData.updateClusters, GraphData/index.ts:420-441).
+void clusters_create(orc_engine* e) {
+  const uint64_t N = e->N;
+  e->point_clusters = e->have_clusters && e->in_clusters.size() == N && N > 0;
+  e->cluster_positions = e->have_cluster_pos && N > 0;
+  const bool strength = e->have_cluster_strength && e->in_cluster_strength.size() == N;
+  e->cluster_of.assign(N, kNoCluster);
+  e->cluster_coeff.assign(N, 1.0f);
+  // clusterCount = max index + 1 over defined non-negative indices (:66-69)
+  uint32_t maxc = 0;
+  if (e->point_clusters) {
+    for (uint64_t i = 0; i < N; ++i) {
+      const float v = e->in_clusters[i];
+      // a non-negative integer; NaN (undefined), negatives, non-integers and
+      // infinities leave the point unclustered
+      if (!(v >= 0.f) || !std::isfinite(v) || v != std::floor(v) || v >= 4294967295.f) continue;
+      e->cluster_of[i] = (uint32_t)v;
+      maxc = std::max(maxc, (uint32_t)v);
+    }
+  }
+  e->K = maxc + 1;
+  if (strength)
+    for (uint64_t i = 0; i < N; ++i) e->cluster_coeff[i] = e->in_cluster_strength[i];
+  // clusterPositions texel c = (cp[2c] ?? -1, cp[2c+1] ?? -1) (:77-82)
+  e->cluster_custom.assign(2 * (size_t)e->K, -1.0f);
+  if (e->cluster_positions)
+    for (size_t j = 0; j < 2 * (size_t)e->K && j < e->in_cluster_pos.size(); ++j)
+      if (!std::isnan(e->in_cluster_pos[j])) e->cluster_custom[j] = e->in_cluster_pos[j];
+}
+
+// calculate-centermass.vert:22-52: per cluster, the sums of the live clustered
+// points' positions and their count (additive blending: exact integer sums
+// rounded once to f32, or f32 in index order in sum mode 1).
+void cluster_sums(const orc_engine* e, const std::vector<float>& p, std::vector<float>& sx, std::vector<float>& sy,
+                  std::vector<float>& sn) {
+  const size_t K = e->K;
+  sx.assign(K, 0.f); sy.assign(K, 0.f); sn.assign(K, 0.f);
+  if (!e->point_clusters) return;
+  if (e->sum_mode == 0) {
+    std::vector<int64_t> ax(K, 0), ay(K, 0), an(K, 0);
+    for (uint64_t i = 0; i < e->N; ++i) {
+      const uint32_t c = e->cluster_of[i];
+      if (e->absent[i] || c == kNoCluster) continue;
+      ax[c] += e->fx.to(p[2 * i]); ay[c] += e->fx.to(p[2 * i + 1]); an[c] += 1;
+    }
+    for (size_t c = 0; c < K; ++c) { sx[c] = e->fx.from(ax[c]); sy[c] = e->fx.from(ay[c]); sn[c] = (float)an[c]; }
+  } else {
+    for (uint64_t i = 0; i < e->N; ++i) {
+      const uint32_t c = e->cluster_of[i];
+      if (e->absent[i] || c == kNoCluster) continue;
+      sx[c] = sx[c] + p[2 * i]; sy[c] = sy[c] + p[2 * i + 1]; sn[c] = sn[c] + 1.0f;
+    }
+  }
+}
+
+void run_clusters(orc_engine* e, float a) {
+  // Clusters.run (Clusters/index.ts:426-469): centre of mass, force-cluster.frag:28-53, update
+  std::vector<float> prev = e->pos;
+  const int64_t N = (int64_t)e->N;
+  std::vector<float> sx, sy, sn;
+  cluster_sums(e, prev, sx, sy, sn);
+  const float cc = (float)e->cfg.simulation_cluster;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < N; ++i) {
+    float vx = 0.f, vy = 0.f;
+    const uint32_t c = e->cluster_of[i];
+    if (c != kNoCluster) {
+      float tx = e->cluster_custom[2 * (size_t)c], ty = e->cluster_custom[2 * (size_t)c + 1];
+      if (tx < 0.f || ty < 0.f) { tx = sx[c] / sn[c]; ty = sy[c] / sn[c]; }
+      const float dx = tx - prev[2 * i], dy = ty - prev[2 * i + 1];
+      const float dist = sqrtf(dx * dx + dy * dy);
+      if (dist > 0.f) {
+        const float add = a * dist * cc * e->cluster_coeff[i];
+        const float inv = 1.0f / dist;   // normalize(v) = v * (1 / length(v))
+        vx = 0.f + add * (dx * inv);
+        vy = 0.f + add * (dy * inv);
+      }
+    }
+    update_point(e, (size_t)i, prev.data(), vx, vy, e->pos.data());
+  }
+}
+
 void run_tick(orc_engine* e) {
   // Graph.runSimulationStep (src/index.ts:2006-2099)
   const uint32_t m = e->cfg.stage_mask;
@@ -809,6 +905,7 @@ void run_tick(orc_engine* e) {
     if (m & CGL_STAGE_LINK_IN) run_links(e, e->csr_in, a);
     if (m & CGL_STAGE_LINK_OUT) run_links(e, e->csr_out, a);
   }
+  if ((e->point_clusters || e->cluster_positions) && (m & CGL_STAGE_CLUSTERS)) run_clusters(e, a);
   if (e->cfg.simulation_collision != 0 && (m & CGL_STAGE_COLLISION)) run_collision(e, a);
   // Store.addAlpha (Store/index.ts:328-332), progress (src/index.ts:2088)
   e->alpha += (0 - e->alpha) * (1 - std::pow(kAlphaMin, 1 / e->cfg.simulation_decay));
@@ -854,7 +951,44 @@ int orc_set_point_positions(orc_engine* e, const float* xy, uint64_t n) {
   e->in_pos.assign(xy, xy + n);
   e->have_pos_input = true;
   e->pos_dirty = true; e->links_dirty = true; e->sizes_dirty = true;
+  e->clusters_dirty = true;   // src/index.ts:570
   return st;
+}
+
+int orc_set_point_clusters(orc_engine* e, const float* v, uint64_t n) {
+  if (!v || n == 0) { e->in_clusters.clear(); e->have_clusters = false; }
+  else { e->in_clusters.assign(v, v + n); e->have_clusters = true; }
+  e->clusters_dirty = true;
+  return 0;
+}
+
+int orc_set_cluster_positions(orc_engine* e, const float* v, uint64_t n) {
+  if (!v) { e->in_cluster_pos.clear(); e->have_cluster_pos = false; }
+  else { e->in_cluster_pos.assign(v, v + n); e->have_cluster_pos = true; }
+  e->clusters_dirty = true;
+  return 0;
+}
+
+int orc_set_point_cluster_strength(orc_engine* e, const float* v, uint64_t n) {
+  if (!v || n == 0) { e->in_cluster_strength.clear(); e->have_cluster_strength = false; }
+  else { e->in_cluster_strength.assign(v, v + n); e->have_cluster_strength = true; }
+  e->clusters_dirty = true;
+  return 0;
+}
+
+int orc_get_cluster_positions(orc_engine* e, double* out, uint64_t cap, uint64_t* n_out) {
+  // Clusters.getCentroidPositions (Clusters/index.ts:389-423), from the current positions
+  const uint64_t n = e->point_clusters ? 2 * (uint64_t)e->K : 0;
+  if (n_out) *n_out = n;
+  if (!out || n == 0) return 0;
+  if (cap < n) return CGL_INVALID_ARG;
+  std::vector<float> sx, sy, sn;
+  cluster_sums(e, e->pos, sx, sy, sn);
+  for (uint32_t c = 0; c < e->K; ++c) {
+    out[2 * c] = (double)sx[c] / (double)sn[c];
+    out[2 * c + 1] = (double)sy[c] / (double)sn[c];
+  }
+  return 0;
 }
 
 int orc_set_links(orc_engine* e, const float* st, uint64_t n) {
@@ -954,7 +1088,8 @@ int orc_render(orc_engine* e, double alpha) {
       e->csr_out.rowptr.assign(e->N + 1, 0);
     }
   }
-  e->pos_dirty = e->links_dirty = e->sizes_dirty = false;
+  if (e->clusters_dirty) clusters_create(e);   // Graph.create (src/index.ts:1668)
+  e->pos_dirty = e->links_dirty = e->sizes_dirty = e->clusters_dirty = false;
   if (!std::isnan(alpha)) e->alpha = alpha;
   return 0;
 }

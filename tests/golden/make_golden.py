@@ -4,8 +4,10 @@ Each case is worked out here from the reference's formulas in plain FP64
 Python, independently of the C++ oracle (which computes in FP32): gravity
 (force-gravity.frag:24-40), center (force-center.frag:22-36), a linked pair
 (force-spring.ts:38-96, ForceLink/index.ts:40-83), a repelling pair resolved
-by the near field alone (force-nearfield.frag:64-263), and an overlapping
-collision pair (force-collision-spatial.frag:103-168).  The update is
+by the near field alone (force-nearfield.frag:64-263), an overlapping
+collision pair (force-collision-spatial.frag:103-168), and the cluster pull
+towards a centre of mass or a given cluster position (force-cluster.frag:28-53,
+calculate-centermass.vert:22-52).  The update is
 update-position.frag:52-57 and alpha follows Store/index.ts:328-332.  Random
 draws follow the project's SplitMix64 stream in the reference's order.
 Run:  python tests/golden/make_golden.py
@@ -15,7 +17,7 @@ import math
 import os
 
 M64 = (1 << 64) - 1
-STAGE = dict(gravity=1, center=2, manybody=4, link_in=8, link_out=16, collision=32)
+STAGE = dict(gravity=1, center=2, manybody=4, link_in=8, link_out=16, collision=32, clusters=64)
 
 
 def splitmix(seed, k):
@@ -136,8 +138,52 @@ def case_collision_pair():
                 positions=[1000.3, 1000.3, 1000.9, 1001.1], links=[], ticks=1, expected=out, atol=2e-4)
 
 
+def cluster_ticks(pts, of, custom, coeff, cc, ticks, fr=0.85, S=4096.0):
+    """alpha*dist*cc*coeff * (d/dist) = alpha*cc*coeff*d towards the cluster's
+    given position, else its live members' centre of mass; unclustered points
+    only get the update."""
+    a = 1.0
+    for _ in range(ticks):
+        cm = {}
+        for k in set(c for c in of if c is not None):
+            mem = [q for q, c in zip(pts, of) if c == k]
+            cm[k] = (sum(q[0] for q in mem) / len(mem), sum(q[1] for q in mem) / len(mem))
+        new = []
+        for q, c, w in zip(pts, of, coeff):
+            if c is None:
+                new.append(q)
+                continue
+            t = custom.get(c, cm[c])
+            new.append([clamp(q[0] + fr * a * cc * w * (t[0] - q[0]), 0, S),
+                        clamp(q[1] + fr * a * cc * w * (t[1] - q[1]), 0, S)])
+        pts = new
+        a = alpha_next(a)
+    return [v for q in pts for v in q]
+
+
+def case_cluster_centroid():
+    pos = [[1000.0, 1200.0], [1400.0, 1000.0], [3000.0, 3100.0], [2000.0, 2000.0], [900.0, 1500.0]]
+    of = [0, 0, 1, None, 0]
+    exp = cluster_ticks(pos, of, {}, [1.0] * 5, 0.5, 3)
+    return dict(name="cluster_centroid", config=dict(random_seed=16, simulation_cluster=0.5,
+                                                      stage_mask=STAGE["clusters"]),
+                positions=[v for q in pos for v in q], links=[], clusters=[0, 0, 1, None, 0], ticks=3,
+                expected=exp, atol=2e-3)
+
+
+def case_cluster_custom():
+    pos = [[1000.0, 1200.0], [1400.0, 1000.0], [3000.0, 3100.0], [2000.0, 2000.0]]
+    of = [0, 1, 1, 0]
+    coeff = [1.0, 0.5, 2.0, 0.25]
+    exp = cluster_ticks(pos, of, {0: (500.0, 600.0)}, coeff, 0.1, 2)
+    return dict(name="cluster_custom_position", config=dict(random_seed=17, stage_mask=STAGE["clusters"]),
+                positions=[v for q in pos for v in q], links=[], clusters=of, cluster_positions=[500.0, 600.0, None, None],
+                cluster_strength=coeff, ticks=2, expected=exp, atol=2e-3)
+
+
 def main():
-    cases = [case_gravity(), case_center(), case_link_pair(), case_repulsion_pair(), case_collision_pair()]
+    cases = [case_gravity(), case_center(), case_link_pair(), case_repulsion_pair(), case_collision_pair(),
+             case_cluster_centroid(), case_cluster_custom()]
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.json")
     with open(path, "w") as f:
         json.dump(dict(generator="tests/golden/make_golden.py", cases=cases), f, indent=1)

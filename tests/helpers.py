@@ -41,7 +41,8 @@ def scenario(kind, seed=1):
     raise KeyError(kind)
 
 
-def make_pair(pos, links, fields, extra=None, sizes=None, strength=None, pinned=None):
+def make_pair(pos, links, fields, extra=None, sizes=None, strength=None, pinned=None, clusters=None,
+              cluster_positions=None, cluster_strength=None):
     """Engine and oracle with identical staged data, rendered and started."""
     from graph_gb300.engine import Engine
     from oracle import OracleEngine
@@ -58,6 +59,12 @@ def make_pair(pos, links, fields, extra=None, sizes=None, strength=None, pinned=
             e.set_point_sizes(sizes)
         if pinned is not None:
             e.set_pinned_points(pinned)
+        if clusters is not None:
+            e.set_point_clusters(clusters)
+        if cluster_positions is not None:
+            e.set_cluster_positions(cluster_positions)
+        if cluster_strength is not None:
+            e.set_point_cluster_strength(cluster_strength)
         e.render()
         e.start(1.0)
         pair.append(e)

@@ -318,6 +318,12 @@ def test_golden_fixtures():
         o.set_point_positions(np.array(case["positions"], dtype=np.float32))
         if case.get("links"):
             o.set_links(np.array(case["links"], dtype=np.float32))
+        if "clusters" in case:
+            o.set_point_clusters(case["clusters"])
+        if "cluster_positions" in case:
+            o.set_cluster_positions(case["cluster_positions"])
+        if "cluster_strength" in case:
+            o.set_point_cluster_strength(case["cluster_strength"])
         o.render()
         o.start(1.0)
         o.step(case["ticks"])
