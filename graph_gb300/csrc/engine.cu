@@ -91,6 +91,7 @@ struct cgl_engine {
   uint32_t n_heavy_in = 0, n_heavy_out = 0;
   DevBuf b_size, b_cgrid_acc, b_cgrid;
   DevBuf b_cl_of, b_cl_coeff, b_cl_custom, b_cl_acc;
+  DevBuf b_texture;                        // staging for pageable texture read-back
   DeviceView view{};
   uint32_t level_off[10] = {};
   uint32_t acc_off[10] = {};
@@ -161,7 +162,7 @@ void dev_free_all(cgl_engine* e) {
                    &e->b_rowptr_in, &e->b_rowptr_out, &e->b_ent_in, &e->b_ent_out, &e->b_size,
                    &e->b_cgrid_acc, &e->b_cgrid, &e->b_big_list, &e->b_big_count,
                    &e->b_big_sx, &e->b_big_sy, &e->b_big_ns, &e->b_heavy_in, &e->b_heavy_out,
-                   &e->b_cl_of, &e->b_cl_coeff, &e->b_cl_custom, &e->b_cl_acc};
+                   &e->b_cl_of, &e->b_cl_coeff, &e->b_cl_custom, &e->b_cl_acc, &e->b_texture};
   for (DevBuf* b : all) {
     if (b->p) cudaFree(b->p);
     b->p = nullptr;
@@ -804,6 +805,67 @@ cgl_status cgl_get_cluster_positions(cgl_engine* e, double* out, uint64_t cap, u
     out[2 * (size_t)c] = (double)sx / (double)cnt;
     out[2 * (size_t)c + 1] = (double)sy / (double)cnt;
   }
+  return CGL_OK;
+}
+
+namespace {
+// Device address of `out` when the engine's device can write it directly:
+// device memory of that device, managed memory, or pinned host memory (mapped
+// into the device's address space).  nullptr for pageable host memory.
+cgl_status texture_target(cgl_engine* e, float* out, float4** dev) {
+  *dev = nullptr;
+  cudaPointerAttributes a{};
+  cudaError_t ce = cudaPointerGetAttributes(&a, out);
+  if (ce != cudaSuccess) { cudaGetLastError(); return CGL_OK; }   // unknown to CUDA: pageable
+  if (a.type == cudaMemoryTypeDevice) {
+    if (a.device != e->device) return fail(e, CGL_INVALID_ARG, "texture buffer is on device %d, engine on %d", a.device, e->device);
+    *dev = (float4*)a.devicePointer;
+  } else if (a.type == cudaMemoryTypeManaged || a.type == cudaMemoryTypeHost) {
+    *dev = (float4*)a.devicePointer;
+  }
+  return CGL_OK;
+}
+
+cgl_status texture_common(cgl_engine* e, float* out, uint64_t cap, uint64_t* texels) {
+  *texels = (uint64_t)e->T * e->T;
+  if (!out && *texels) return fail(e, CGL_INVALID_ARG, "null texture buffer");
+  if (cap < 4 * *texels)
+    return fail(e, CGL_INVALID_ARG, "texture buffer holds %llu floats, need %llu", (unsigned long long)cap,
+                (unsigned long long)(4 * *texels));
+  return CGL_OK;
+}
+}  // namespace
+
+cgl_status cgl_get_position_texture(cgl_engine* e, float* out, uint64_t cap) {
+  CHECK_E(e);
+  uint64_t texels;
+  cgl_status st = texture_common(e, out, cap, &texels);
+  if (st || !texels) return st;
+  float4* dev;
+  if ((st = texture_target(e, out, &dev))) return st;
+  if (dev) {
+    launch_position_texture(e->view, dev, (uint32_t)texels, e->stream);
+    CU(cudaGetLastError());
+  } else {
+    if ((st = dev_reserve(e, e->b_texture, texels * sizeof(float4), false))) return st;
+    launch_position_texture(e->view, (float4*)e->b_texture.p, (uint32_t)texels, e->stream);
+    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(out, e->b_texture.p, texels * sizeof(float4), cudaMemcpyDeviceToHost, e->stream));
+  }
+  CU(cudaStreamSynchronize(e->stream));
+  return CGL_OK;
+}
+
+cgl_status cgl_enqueue_position_texture(cgl_engine* e, float* out, uint64_t cap) {
+  CHECK_E(e);
+  uint64_t texels;
+  cgl_status st = texture_common(e, out, cap, &texels);
+  if (st || !texels) return st;
+  float4* dev;
+  if ((st = texture_target(e, out, &dev))) return st;
+  if (!dev) return fail(e, CGL_INVALID_ARG, "queued texture read-back needs device or pinned host memory");
+  launch_position_texture(e->view, dev, (uint32_t)texels, e->stream);
+  CU(cudaGetLastError());
   return CGL_OK;
 }
 

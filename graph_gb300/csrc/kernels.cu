@@ -1032,6 +1032,19 @@ __global__ void __launch_bounds__(kBlock) k_cluster_force(DeviceView d, SimScala
 
 __global__ void k_tick_end(DeviceView d) { *d.tick_ctr += 1; }
 
+// buildPositionTextureData (Points/position-utils.ts:9-27): texel i = (x, y, i, 0)
+// for the points, zeros for the rest of the T x T texture.
+__global__ void __launch_bounds__(kBlock) k_position_texture(DeviceView d, float4* __restrict__ out, uint32_t texels) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= texels) return;
+  float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (t < d.n) {
+    const float2 p = d.pos[t];
+    v = make_float4(p.x, p.y, (float)t, 0.f);
+  }
+  out[t] = v;
+}
+
 inline uint32_t blocks_for(uint32_t n) { return (n + kBlock - 1) / kBlock; }
 
 }  // namespace
@@ -1125,5 +1138,10 @@ void launch_collision_force(const DeviceView& d, const SimScalars& s, const uint
 }
 
 void launch_tick_end(const DeviceView& d, cudaStream_t st) { k_tick_end<<<1, 1, 0, st>>>(d); }
+
+void launch_position_texture(const DeviceView& d, float4* out, uint32_t texels, cudaStream_t st) {
+  const uint32_t nb = blocks_for(texels);
+  if (nb) k_position_texture<<<nb, kBlock, 0, st>>>(d, out, texels);
+}
 
 }  // namespace cgl

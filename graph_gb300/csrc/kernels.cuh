@@ -108,6 +108,8 @@ void launch_cluster_sum(const DeviceView& d, const SimScalars& s, cudaStream_t s
 // The cluster pull and the update of every point.
 void launch_cluster_force(const DeviceView& d, const SimScalars& s, cudaStream_t st);
 void launch_tick_end(const DeviceView& d, cudaStream_t st);
+// The renderer's points texture: texels [0, texels), (x, y, index, 0) below n.
+void launch_position_texture(const DeviceView& d, float4* out, uint32_t texels, cudaStream_t st);
 
 uint32_t scan_blocks(uint32_t cells);
 

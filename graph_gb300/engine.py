@@ -44,6 +44,9 @@ def load_library(build_if_missing: bool = True):
     lib.cgl_synchronize.restype = C.c_int
     lib.cgl_profile_stages.argtypes = [E, C.c_uint32, C.POINTER(C.c_double)]
     lib.cgl_profile_stages.restype = C.c_int
+    for name in ("cgl_get_position_texture", "cgl_enqueue_position_texture"):
+        getattr(lib, name).argtypes = [E, C.c_void_p, C.c_uint64]
+        getattr(lib, name).restype = C.c_int
     lib.cgl_levels_noalloc.argtypes = [C.c_void_p, C.c_uint64, C.c_double, C.c_void_p, C.c_uint64, C.c_void_p,
                                        C.c_char_p, C.c_size_t]
     lib.cgl_levels_noalloc.restype = C.c_int
@@ -111,6 +114,21 @@ class Engine(EngineCalls):
         out = (C.c_double * _abi.NUM_STAGE_TIMES)()
         self._call("profile_stages", int(ticks), out)
         return dict(zip(_abi.STAGE_TIME_NAMES, list(out)))
+
+    def get_position_texture(self):
+        """The renderer's points texture: float32 [T*T, 4] of (x, y, index, 0)."""
+        t = self.layout().points_texture_size
+        out = np.empty((t * t, 4), dtype=np.float32)
+        self._call("get_position_texture", C.c_void_p(out.ctypes.data), out.size)
+        return out
+
+    def get_position_texture_into(self, ptr, capacity_floats):
+        """Write the texture to `ptr` (host, pinned host or device memory) and wait."""
+        return self._call("get_position_texture", C.c_void_p(ptr), int(capacity_floats))
+
+    def enqueue_position_texture(self, ptr, capacity_floats):
+        """Queue the texture write to device or pinned host memory at `ptr` (done by the next synchronize)."""
+        return self._call("enqueue_position_texture", C.c_void_p(ptr), int(capacity_floats))
 
     def get_point_positions_into(self, out):
         """Read positions into a caller-owned float32 buffer (e.g. pinned host memory)."""

@@ -191,6 +191,22 @@ cgl_status cgl_get_point_positions(cgl_engine* e, float* out_xy, uint64_t capaci
  * be null to query the size.  Synchronises the engine stream. */
 cgl_status cgl_get_cluster_positions(cgl_engine* e, double* out, uint64_t capacity_doubles, uint64_t* n_out);
 
+/* Position hand-off to the renderer: the points texture the reference's draw
+ * passes read (Points.currentPositionTexture, written by
+ * buildPositionTextureData, Points/position-utils.ts:9-27): T x T RGBA32F texels,
+ * T = points_texture_size, texel i = (x, y, i, 0) for i < points_number (x, y
+ * NaN for absent points) and (0, 0, 0, 0) beyond.  `out` holds 4*T*T floats and
+ * may be host memory (pageable or pinned) or device memory of the engine's
+ * device; device and pinned host memory are written directly by one kernel (no
+ * staging copy), pageable memory through a staging buffer.  Returns when the
+ * texture is written. */
+cgl_status cgl_get_position_texture(cgl_engine* e, float* out, uint64_t capacity_floats);
+/* The same, queued on the engine stream after the work already queued and not
+ * waited for: `out` must be device memory or pinned host memory; it is complete
+ * after the next cgl_synchronize (or any call that synchronises).  For
+ * streaming snapshots between cgl_step calls without a stall. */
+cgl_status cgl_enqueue_position_texture(cgl_engine* e, float* out, uint64_t capacity_floats);
+
 /* Graph.progress / Graph.isSimulationRunning — src/index.ts:469, :477. */
 cgl_status cgl_get_state(cgl_engine* e, cgl_state* out);
 

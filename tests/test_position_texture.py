@@ -1,0 +1,72 @@
+"""Position hand-off in the renderer's texture layout (Points/position-utils.ts:9-27)."""
+import numpy as np
+import pytest
+
+from helpers import make_pair, scenario
+
+pytestmark = pytest.mark.gpu
+
+
+def _expected(xy, t):
+    n = xy.size // 2
+    tex = np.zeros((t * t, 4), dtype=np.float32)
+    tex[:n, 0] = xy[0::2]
+    tex[:n, 1] = xy[1::2]
+    tex[:n, 2] = np.arange(n, dtype=np.float32)
+    return tex
+
+
+def _same(a, b):
+    return np.array_equal(a.view(np.uint32), b.view(np.uint32)) or \
+        (np.array_equal(np.isnan(a), np.isnan(b)) and np.array_equal(a[~np.isnan(a)], b[~np.isnan(b)]))
+
+
+def test_texture_layout_host_pinned_device():
+    torch = pytest.importorskip("torch")
+    pos, links, fields = scenario("ba_small")
+    pos = pos.copy()
+    pos[2 * 5: 2 * 8] = np.nan                 # absent points read NaN, keep their index
+    n = pos.size // 2
+    eng, orc = make_pair(pos, links, fields)
+    eng.step(3)
+    orc.step(3)
+    t = eng.layout().points_texture_size
+    assert t * t >= n and (t - 1) * (t - 1) < n
+    want = _expected(orc.get_point_positions(), t)
+    got = eng.get_position_texture()                                 # pageable host memory
+    assert _same(got, want)
+    pinned = torch.empty(4 * t * t, dtype=torch.float32, pin_memory=True)
+    eng.get_position_texture_into(pinned.data_ptr(), pinned.numel())  # written by the kernel itself
+    assert _same(pinned.numpy().reshape(-1, 4), want)
+    dev = torch.full((4 * t * t,), 7.0, dtype=torch.float32, device="cuda")
+    eng.enqueue_position_texture(dev.data_ptr(), dev.numel())
+    eng.synchronize()
+    assert _same(dev.cpu().numpy().reshape(-1, 4), want)
+
+
+def test_queued_snapshots_between_ticks():
+    torch = pytest.importorskip("torch")
+    pos, links, fields = scenario("collision")
+    eng, orc = make_pair(pos, links, fields)
+    t = eng.layout().points_texture_size
+    snaps = [torch.empty(4 * t * t, dtype=torch.float32, pin_memory=True) for _ in range(3)]
+    for s in snaps:           # no stall between the ticks: each snapshot is queued after its tick
+        eng.step(1)
+        eng.enqueue_position_texture(s.data_ptr(), s.numel())
+    eng.synchronize()
+    for s in snaps:
+        orc.step(1)
+        assert _same(s.numpy().reshape(-1, 4), _expected(orc.get_point_positions(), t))
+
+
+def test_texture_rejects_small_buffers():
+    from graph_gb300._calls import StatusError
+    pos, links, fields = scenario("center")
+    eng, orc = make_pair(pos, links, fields)
+    out = np.empty(8, dtype=np.float32)
+    with pytest.raises(StatusError):
+        eng.get_position_texture_into(out.ctypes.data, out.size)
+    with pytest.raises(StatusError):          # pageable memory cannot be written asynchronously
+        t = eng.layout().points_texture_size
+        big = np.empty(4 * t * t, dtype=np.float32)
+        eng.enqueue_position_texture(big.ctypes.data, big.size)
