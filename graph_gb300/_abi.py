@@ -55,6 +55,9 @@ class Config(C.Structure):
         ("device", C.c_int32),
         ("hbm_budget_bytes", C.c_double),
         ("simulation_cluster", C.c_double),
+        ("simulation_repulsion_from_mouse", C.c_double),
+        ("enable_right_click_repulsion", C.c_int32),
+        ("enable_drag", C.c_int32),
     ]
 
 
@@ -116,6 +119,9 @@ DEFAULTS = dict(
     device=0,
     hbm_budget_bytes=0.0,
     simulation_cluster=0.1,
+    simulation_repulsion_from_mouse=2.0,
+    enable_right_click_repulsion=0,
+    enable_drag=0,
 )
 
 # Reference config keys (camelCase, src/config.ts) -> C field names.
@@ -137,6 +143,9 @@ CAMEL_TO_FIELD = {
     "enableSimulation": "enable_simulation",
     "randomSeed": "random_seed",
     "simulationCluster": "simulation_cluster",
+    "simulationRepulsionFromMouse": "simulation_repulsion_from_mouse",
+    "enableRightClickRepulsion": "enable_right_click_repulsion",
+    "enableDrag": "enable_drag",
 }
 
 
@@ -208,6 +217,9 @@ def declare(lib, prefix: str, engine_t=C.c_void_p):
         "set_cluster_positions": ([E, f, C.c_uint64], C.c_int),
         "set_point_cluster_strength": ([E, f, C.c_uint64], C.c_int),
         "get_cluster_positions": ([E, C.POINTER(C.c_double), C.c_uint64, C.POINTER(C.c_uint64)], C.c_int),
+        "set_pointer": ([E, C.c_double, C.c_double, C.c_int32], C.c_int),
+        "set_drag": ([E, C.c_int64], C.c_int),
+        "frame": ([E, C.c_uint32, C.POINTER(C.c_uint32)], C.c_int),
         "render": ([E, C.c_double], C.c_int),
         "start": ([E, C.c_double], C.c_int),
         "stop": ([E], C.c_int),

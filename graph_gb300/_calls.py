@@ -125,6 +125,17 @@ class EngineCalls:
     def step(self, ticks=1):
         return self._call("step", int(ticks))
 
+    def set_pointer(self, x, y, right_button=False):
+        return self._call("set_pointer", float(x), float(y), 1 if right_button else 0)
+
+    def set_drag(self, index):
+        return self._call("set_drag", -1 if index is None else int(index))
+
+    def frame(self, frames=1):
+        done = C.c_uint32(0)
+        self._call("frame", int(frames), C.byref(done))
+        return done.value
+
     def run(self, max_ticks):
         done = C.c_uint32(0)
         self._call("run", int(max_ticks), C.byref(done))

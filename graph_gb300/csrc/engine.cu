@@ -73,6 +73,11 @@ struct cgl_engine {
   bool point_clusters = false, cluster_positions = false;
   uint32_t n_clusters = 0;
 
+  // interaction: Store.mousePosition, Graph.isRightClickMouse, the dragged point
+  double mouse_x = 0, mouse_y = 0;
+  bool right_button = false;
+  int64_t drag_index = -1;
+
   // simulation state (Store)
   double adjusted_space = 4096;
   double alpha = 1.0;
@@ -388,6 +393,15 @@ cgl_status prepare_tick(cgl_engine* e) {
 
 // Host side of one tick: the f32 alpha uniform and the peel seed draw
 // (ForceManyBody/index.ts:521), then Store.addAlpha (Store/index.ts:328-332).
+// Right-click repulsion is on (src/index.ts:2011, 2083)
+bool mouse_active(const cgl_engine* e) { return e->right_button && e->cfg.enable_right_click_repulsion; }
+bool interactive(const cgl_engine* e) { return mouse_active(e) || (e->drag_index >= 0 && e->cfg.enable_drag); }
+
+void launch_pointer_force(cgl_engine* e) {
+  launch_mouse(e->view, make_scalars(e), make_float2((float)e->mouse_x, (float)e->mouse_y),
+               (float)e->cfg.simulation_repulsion_from_mouse, e->stream);
+}
+
 TickParams host_tick(cgl_engine* e, bool draws_seed) {
   TickParams tp;
   tp.alpha = (float)e->alpha;
@@ -397,6 +411,7 @@ TickParams host_tick(cgl_engine* e, bool draws_seed) {
     std::memcpy(&tp.seed_bits, &seed, 4);
   }
   e->alpha += (0 - e->alpha) * (1 - std::pow(kAlphaMin, 1 / e->cfg.simulation_decay));
+  if (mouse_active(e)) e->alpha = std::max(e->alpha, 0.1);   // src/index.ts:2083-2085
   e->progress = std::sqrt(std::min(1.0, kAlphaMin / e->alpha));
   e->tick++;
   return tp;
@@ -407,6 +422,7 @@ cgl_status run_ticks(cgl_engine* e, uint32_t ticks, cudaEvent_t* ev, double* sta
   cgl_status st = prepare_tick(e);
   if (st) return st;
   const bool seed = plan_tick(e).mb;
+  const bool mouse = mouse_active(e);   // ForceMouse pass before each tick's forces
   uint32_t done = 0;
   while (done < ticks) {
     const uint32_t n = std::min(kParamChunk, ticks - done);
@@ -417,6 +433,7 @@ cgl_status run_ticks(cgl_engine* e, uint32_t ticks, cudaEvent_t* ev, double* sta
     e->params_pending = true;
     CU(cudaMemsetAsync(e->b_tick_ctr.p, 0, sizeof(uint32_t), e->stream));
     for (uint32_t t = 0; t < n; ++t) {
+      if (mouse) launch_pointer_force(e);
       if (ev) {
         st = enqueue_tick(e, e->stream, ev);
         if (st) return st;
@@ -627,6 +644,9 @@ void cgl_config_defaults(cgl_config* c) {
   c->device = 0;
   c->hbm_budget_bytes = 0;
   c->simulation_cluster = 0.1;
+  c->simulation_repulsion_from_mouse = 2;
+  c->enable_right_click_repulsion = 0;
+  c->enable_drag = 0;
 }
 
 cgl_status cgl_create(const cgl_config* cfg, cgl_engine** out) {
@@ -918,9 +938,80 @@ cgl_status cgl_step(cgl_engine* e, uint32_t ticks) {
   return run_ticks(e, ticks, nullptr, nullptr);
 }
 
+namespace {
+// One animation frame (src/index.ts:2161-2175, renderFrame :2237-2317).
+cgl_status one_frame(cgl_engine* e, uint32_t* ticks) {
+  if (e->alpha < kAlphaMin && e->running) { e->running = false; e->progress = 1; }   // end()
+  if (e->cfg.enable_simulation && e->T) {   // runSimulationStep(false)
+    if (e->running) {
+      cgl_status st = run_ticks(e, 1, nullptr, nullptr);   // includes the pointer pass
+      if (st) return st;
+      ++*ticks;
+    } else if (mouse_active(e)) {
+      launch_pointer_force(e);
+      CU(cudaGetLastError());
+    }
+  }
+  if (e->drag_index >= 0 && e->cfg.enable_drag) {
+    launch_drag(e->view, (uint32_t)e->drag_index, make_float2((float)e->mouse_x, (float)e->mouse_y), e->stream);
+    CU(cudaGetLastError());
+  }
+  return CGL_OK;
+}
+}  // namespace
+
+cgl_status cgl_set_pointer(cgl_engine* e, double x, double y, int32_t right_button_down) {
+  CHECK_E(e);
+  e->mouse_x = x;
+  e->mouse_y = y;
+  e->right_button = right_button_down != 0;
+  return CGL_OK;
+}
+
+cgl_status cgl_set_drag(cgl_engine* e, int64_t index) {
+  CHECK_E(e);
+  if (!e->cfg.enable_drag) return CGL_OK;
+  if (index >= (int64_t)e->N) return fail(e, CGL_INVALID_ARG, "drag index %lld outside %llu points", (long long)index,
+                                          (unsigned long long)e->N);
+  e->drag_index = index < 0 ? -1 : index;
+  return CGL_OK;
+}
+
+cgl_status cgl_frame(cgl_engine* e, uint32_t frames, uint32_t* ticks_done) {
+  CHECK_E(e);
+  uint32_t n = 0;
+  if (!e->T) { if (ticks_done) *ticks_done = 0; return CGL_OK; }   // frame() needs points (:2159)
+  if (!interactive(e)) {
+    // alpha evolves on the host only: the frames that tick are known up front
+    if (e->cfg.enable_simulation && e->running) {
+      double a = e->alpha;
+      const double f = 1 - std::pow(kAlphaMin, 1 / e->cfg.simulation_decay);
+      while (n < frames && !(a < kAlphaMin)) { a += (0 - a) * f; ++n; }
+      cgl_status st = run_ticks(e, n, nullptr, nullptr);
+      if (st) return st;
+      if (n < frames && e->alpha < kAlphaMin) { e->running = false; e->progress = 1; }
+    }
+  } else {
+    for (uint32_t k = 0; k < frames; ++k) {
+      cgl_status st = one_frame(e, &n);
+      if (st) return st;
+    }
+  }
+  if (ticks_done) *ticks_done = n;
+  return CGL_OK;
+}
+
 cgl_status cgl_run(cgl_engine* e, uint32_t max_ticks, uint32_t* ticks_done) {
   CHECK_E(e);
   uint32_t n = 0;
+  if (e->cfg.enable_simulation && e->T && e->running && interactive(e)) {
+    while (n < max_ticks && e->running) {
+      cgl_status st = one_frame(e, &n);
+      if (st) return st;
+    }
+    if (ticks_done) *ticks_done = n;
+    return CGL_OK;
+  }
   if (e->cfg.enable_simulation && e->T && e->running) {
     // alpha evolves on the host only, so the tick count is known up front
     double a = e->alpha;

@@ -1032,6 +1032,30 @@ __global__ void __launch_bounds__(kBlock) k_cluster_force(DeviceView d, SimScala
 
 __global__ void k_tick_end(DeviceView d) { *d.tick_ctr += 1; }
 
+// ---------------------------------------------------------------- pointer --
+// force-mouse.frag:23-38 then the update: push away from the pointer with
+// 100 * repulsion / max(|d|, 10)^2 along (cos, sin)(atan(d.y, d.x)) = d / |d|
+// (the direction of atan2(0, 0) = 0, (1, 0), when the pointer is on the point).
+__global__ void __launch_bounds__(kBlock) k_mouse(DeviceView d, SimScalars s, float2 mouse, float repulsion) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n) return;
+  const uint8_t f = d.flags[i];
+  if (f & (kAbsent | kPinned)) return;
+  const float2 p = d.pos[i];
+  const float dx = __fsub_rn(mouse.x, p.x), dy = __fsub_rn(mouse.y, p.y);
+  const float r = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
+  const float dist = gmax(r, 10.0f);
+  const float add = __fdiv_rn(__fmul_rn(100.0f, repulsion), __fmul_rn(dist, dist));
+  float cx = 1.f, cy = 0.f;
+  if (r > 0.f) { cx = __fdiv_rn(dx, r); cy = __fdiv_rn(dy, r); }
+  const float vx = __fsub_rn(0.f, __fmul_rn(add, cx)), vy = __fsub_rn(0.f, __fmul_rn(add, cy));
+  d.pos[i] = integrate(p, vx, vy, s.friction, s.space);
+}
+
+// drag-point.frag:22-31: the texel whose index channel equals the dragged
+// index takes the pointer position (pinned and absence flags are not consulted).
+__global__ void k_drag(DeviceView d, uint32_t index, float2 mouse) { d.pos[index] = mouse; }
+
 // buildPositionTextureData (Points/position-utils.ts:9-27): texel i = (x, y, i, 0)
 // for the points, zeros for the rest of the T x T texture.
 __global__ void __launch_bounds__(kBlock) k_position_texture(DeviceView d, float4* __restrict__ out, uint32_t texels) {
@@ -1138,6 +1162,15 @@ void launch_collision_force(const DeviceView& d, const SimScalars& s, const uint
 }
 
 void launch_tick_end(const DeviceView& d, cudaStream_t st) { k_tick_end<<<1, 1, 0, st>>>(d); }
+
+void launch_mouse(const DeviceView& d, const SimScalars& s, float2 mouse, float repulsion, cudaStream_t st) {
+  const uint32_t nb = blocks_for(d.n);
+  if (nb) k_mouse<<<nb, kBlock, 0, st>>>(d, s, mouse, repulsion);
+}
+
+void launch_drag(const DeviceView& d, uint32_t index, float2 mouse, cudaStream_t st) {
+  if (index < d.n) k_drag<<<1, 1, 0, st>>>(d, index, mouse);
+}
 
 void launch_position_texture(const DeviceView& d, float4* out, uint32_t texels, cudaStream_t st) {
   const uint32_t nb = blocks_for(texels);

@@ -108,6 +108,10 @@ void launch_cluster_sum(const DeviceView& d, const SimScalars& s, cudaStream_t s
 // The cluster pull and the update of every point.
 void launch_cluster_force(const DeviceView& d, const SimScalars& s, cudaStream_t st);
 void launch_tick_end(const DeviceView& d, cudaStream_t st);
+// Right-click repulsion from the pointer (force-mouse.frag) and the update.
+void launch_mouse(const DeviceView& d, const SimScalars& s, float2 mouse, float repulsion, cudaStream_t st);
+// The dragged point follows the pointer (drag-point.frag).
+void launch_drag(const DeviceView& d, uint32_t index, float2 mouse, cudaStream_t st);
 // The renderer's points texture: texels [0, texels), (x, y, index, 0) below n.
 void launch_position_texture(const DeviceView& d, float4* out, uint32_t texels, cudaStream_t st);
 

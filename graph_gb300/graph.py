@@ -22,7 +22,7 @@ from .engine import Engine
 ALPHA_MIN = 0.001
 
 _CALLBACKS = ("onSimulationStart", "onSimulationTick", "onSimulationEnd", "onSimulationPause",
-              "onSimulationUnpause")
+              "onSimulationUnpause", "onDragStart", "onDragEnd")
 
 
 def _to_fields(config):
@@ -35,7 +35,7 @@ def _to_fields(config):
             continue   # visual keys of the reference are accepted and ignored here
         if f == "simulation_collision_radius" and v is None:
             v = math.nan
-        if f == "enable_simulation":
+        if f in ("enable_simulation", "enable_right_click_repulsion", "enable_drag"):
             v = 1 if v else 0
         fields[f] = v
     return fields
@@ -232,6 +232,36 @@ class Graph:
         if self._destroyed:
             return np.zeros(0, dtype=np.float32)
         return self._engine.get_point_positions()
+
+    # --- interaction (the reference takes these from DOM pointer events) ----
+    def setPointer(self, x, y, rightButton=False):
+        """Pointer in simulation space and the right button (Store.mousePosition, isRightClickMouse)."""
+        if self._destroyed:
+            return
+        self._engine.set_pointer(x, y, rightButton)
+
+    def startDrag(self, index):
+        """Drag.start on the hovered point `index` (Drag/index.ts:22-28); needs enableDrag."""
+        if self._destroyed:
+            return
+        self._engine.set_drag(index)
+        self._cb("onDragStart")
+
+    def endDrag(self):
+        if self._destroyed:
+            return
+        self._engine.set_drag(None)
+        self._cb("onDragEnd")
+
+    def frame(self, frames=1):
+        """Run `frames` animation frames' simulation work; returns the ticks run."""
+        if self._destroyed:
+            return 0
+        running = self._engine.state().is_simulation_running
+        done = self._engine.frame(frames)
+        if running and not self._engine.state().is_simulation_running:
+            self._cb("onSimulationEnd")
+        return done
 
     def getClusterPositions(self):
         """Centre of mass of each cluster as float64 [x0, y0, x1, y1, ...] (src/index.ts:1135-1139)."""

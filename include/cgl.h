@@ -82,6 +82,9 @@ typedef struct cgl_config {
   int32_t device;                            /* CUDA device ordinal, default 0 */
   double hbm_budget_bytes;                   /* device-memory admission budget for this handle; 0 = unlimited */
   double simulation_cluster;                 /* simulationCluster, default 0.1 (config.ts:435, variables.ts:79) */
+  double simulation_repulsion_from_mouse;    /* simulationRepulsionFromMouse, default 2 (variables.ts:77) */
+  int32_t enable_right_click_repulsion;      /* enableRightClickRepulsion, default 0 (variables.ts:83) */
+  int32_t enable_drag;                       /* enableDrag, default 0 (variables.ts:132) */
 } cgl_config;
 
 typedef struct cgl_state {
@@ -177,6 +180,30 @@ cgl_status cgl_step(cgl_engine* e, uint32_t ticks);
  * while running, end the simulation when alpha < ALPHA_MIN before a tick
  * (:2164-2169, end() :2335-2339), else run a tick; at most max_ticks ticks. */
 cgl_status cgl_run(cgl_engine* e, uint32_t max_ticks, uint32_t* ticks_done);
+
+/* Interaction.  The pointer in simulation space (Store.mousePosition, which the
+ * reference derives from pointer events through the zoom transform,
+ * src/index.ts:updateMousePosition) and whether the right button is held
+ * (Graph.isRightClickMouse).  With enable_right_click_repulsion, every frame and
+ * every step first pushes the points away from the pointer (ForceMouse.run,
+ * force-mouse.frag:23-38) and keeps alpha at 0.1 or more after its decay
+ * (src/index.ts:2011-2016, 2082-2085). */
+cgl_status cgl_set_pointer(cgl_engine* e, double x, double y, int32_t right_button_down);
+
+/* Drag start / end (Drag/index.ts:22-36): `index` is the hovered point being
+ * dragged, -1 ends the drag.  While a drag is active every frame ends by moving
+ * that point to the pointer (Points.drag, drag-point.frag:22-31, called from
+ * src/index.ts:2303-2310).  Ignored unless enable_drag (the reference attaches
+ * no drag behaviour then); an index outside the points is INVALID_ARG. */
+cgl_status cgl_set_drag(cgl_engine* e, int64_t index);
+
+/* `frames` animation frames' simulation work (the rAF callback,
+ * src/index.ts:2152-2177, and renderFrame :2237-2317), one per frame: end the
+ * simulation if alpha < ALPHA_MIN while running; the right-click repulsion pass
+ * if held; one tick if running; the drag pass if dragging.  *ticks_done (may be
+ * null) = ticks run.  With no pointer interaction this is cgl_run plus idle
+ * frames. */
+cgl_status cgl_frame(cgl_engine* e, uint32_t frames, uint32_t* ticks_done);
 
 /* Graph.getPointPositions() — src/index.ts:1106-1129; absent points read NaN.
  * out_xy holds 2 * points_number floats.  Synchronises the engine stream. */

@@ -236,6 +236,11 @@ struct orc_engine {
   std::vector<float> cluster_coeff;   // N, clusterForceCoefficient (default 1)
   std::vector<float> cluster_custom;  // 2K, -1 where undefined
 
+  // interaction: Store.mousePosition, Graph.isRightClickMouse, the dragged point
+  double mouse_x = 0, mouse_y = 0;
+  bool right_button = false;
+  int64_t drag_index = -1;
+
   // simulation state (Store)
   double adjusted_space = 4096;
   double alpha = 1.0;
@@ -894,8 +899,38 @@ void run_clusters(orc_engine* e, float a) {
   }
 }
 
+bool mouse_active(const orc_engine* e) { return e->right_button && e->cfg.enable_right_click_repulsion; }
+
+void run_mouse(orc_engine* e) {
+  // ForceMouse.run, force-mouse.frag:23-38, then the update.  cos/sin of
+  // atan(d.y, d.x) = d / |d|; atan(0, 0) = 0 gives (1, 0).
+  std::vector<float> prev = e->pos;
+  const float mx = (float)e->mouse_x, my = (float)e->mouse_y;
+  const float rep = (float)e->cfg.simulation_repulsion_from_mouse;
+  const int64_t N = (int64_t)e->N;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < N; ++i) {
+    const float dx = mx - prev[2 * i], dy = my - prev[2 * i + 1];
+    const float r = sqrtf(dx * dx + dy * dy);
+    const float dist = gmax(r, 10.0f);
+    const float add = 100.0f * rep / (dist * dist);
+    float cx = 1.f, cy = 0.f;
+    if (r > 0.f) { cx = dx / r; cy = dy / r; }
+    update_point(e, (size_t)i, prev.data(), 0.f - add * cx, 0.f - add * cy, e->pos.data());
+  }
+}
+
+void run_drag(orc_engine* e) {
+  // Points.drag, drag-point.frag:22-31
+  if (e->drag_index >= 0 && (uint64_t)e->drag_index < e->N) {
+    e->pos[2 * (size_t)e->drag_index] = (float)e->mouse_x;
+    e->pos[2 * (size_t)e->drag_index + 1] = (float)e->mouse_y;
+  }
+}
+
 void run_tick(orc_engine* e) {
   // Graph.runSimulationStep (src/index.ts:2006-2099)
+  if (mouse_active(e)) run_mouse(e);   // :2011-2016
   const uint32_t m = e->cfg.stage_mask;
   const float a = (float)e->alpha;
   if (e->cfg.simulation_gravity != 0 && (m & CGL_STAGE_GRAVITY)) run_gravity(e, a);
@@ -909,8 +944,19 @@ void run_tick(orc_engine* e) {
   if (e->cfg.simulation_collision != 0 && (m & CGL_STAGE_COLLISION)) run_collision(e, a);
   // Store.addAlpha (Store/index.ts:328-332), progress (src/index.ts:2088)
   e->alpha += (0 - e->alpha) * (1 - std::pow(kAlphaMin, 1 / e->cfg.simulation_decay));
+  if (mouse_active(e)) e->alpha = std::max(e->alpha, 0.1);   // :2083-2085
   e->progress = std::sqrt(std::min(1.0, kAlphaMin / e->alpha));
   e->tick++;
+}
+
+// One animation frame (src/index.ts:2161-2175, renderFrame :2237-2317).
+void run_frame(orc_engine* e, uint32_t* ticks) {
+  if (e->alpha < kAlphaMin && e->running) { e->running = false; e->progress = 1; }
+  if (e->cfg.enable_simulation && e->T) {
+    if (e->running) { run_tick(e); ++*ticks; }
+    else if (mouse_active(e)) run_mouse(e);
+  }
+  if (e->cfg.enable_drag) run_drag(e);
 }
 
 }  // namespace
@@ -1109,15 +1155,31 @@ int orc_step(orc_engine* e, uint32_t ticks) {
   return 0;
 }
 
-int orc_run(orc_engine* e, uint32_t max_ticks, uint32_t* done) {
+int orc_set_pointer(orc_engine* e, double x, double y, int32_t right) {
+  e->mouse_x = x; e->mouse_y = y; e->right_button = right != 0;
+  return 0;
+}
+
+int orc_set_drag(orc_engine* e, int64_t index) {
+  if (!e->cfg.enable_drag) return 0;
+  if (index >= (int64_t)e->N) return CGL_INVALID_ARG;
+  e->drag_index = index < 0 ? -1 : index;
+  return 0;
+}
+
+int orc_frame(orc_engine* e, uint32_t frames, uint32_t* done) {
   uint32_t n = 0;
-  if (e->cfg.enable_simulation && e->T) {
-    while (n < max_ticks && e->running) {
-      if (e->alpha < kAlphaMin) { e->running = false; e->progress = 1; break; }
-      run_tick(e);
-      ++n;
-    }
-  }
+  if (e->T)
+    for (uint32_t k = 0; k < frames; ++k) run_frame(e, &n);
+  if (done) *done = n;
+  return 0;
+}
+
+int orc_run(orc_engine* e, uint32_t max_ticks, uint32_t* done) {
+  // frames until the simulation ends (src/index.ts:2161-2175)
+  uint32_t n = 0;
+  if (e->cfg.enable_simulation && e->T)
+    while (n < max_ticks && e->running) run_frame(e, &n);
   if (done) *done = n;
   return 0;
 }
