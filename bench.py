@@ -43,7 +43,7 @@ UNIT = "point-iter/s"
 
 
 # ------------------------------------------------------------------ workload --
-def make_workload(name, seed=1):
+def make_workload(name, seed=1, rmat_scale=23):
     if name == "sbm1m":
         n = 1_000_000
         links = generators.sbm_zipf(n, 200, 1.2, 10, 0.9, seed=seed)
@@ -60,17 +60,18 @@ def make_workload(name, seed=1):
                       simulation_link_spring=1.0, simulation_link_distance=2.0, simulation_decay=5000,
                       random_seed=seed)
         desc = "Barabasi-Albert 10,000 points m=5 / spaceSize 4096"
-    elif name == "rmat8m":
-        n = 1 << 23
-        links = generators.rmat(23, 40_000_000, 0.57, 0.19, 0.19, seed=seed)
+    elif name == "rmat":
+        n = 1 << rmat_scale
+        m = 40_000_000 >> (23 - rmat_scale) if rmat_scale <= 23 else 40_000_000 << (rmat_scale - 23)
+        links = generators.rmat(rmat_scale, m, 0.57, 0.19, 0.19, seed=seed)
         pos = generators.uniform_positions(n, 0, 16384, seed)
         radius = np.random.default_rng(seed).uniform(1, 8, size=n).astype(np.float32)
         sizes = 2 * radius
         fields = dict(space_size=16384, simulation_repulsion=0.1, simulation_gravity=0.25, simulation_friction=0.85,
                       simulation_link_spring=1.0, simulation_link_distance=2.0, simulation_collision=0.5,
                       simulation_decay=5000, random_seed=seed)
-        desc = ("R-MAT scale 23 (8,388,608 points, a,b,c,d = .57,.19,.19,.05) / 40,000,000 links / "
-                "collision 0.5, radius U[1,8] / spaceSize 16384")
+        desc = ("R-MAT scale %d (%s points, a,b,c,d = .57,.19,.19,.05) / %s links / "
+                "collision 0.5, radius U[1,8] / spaceSize 16384" % (rmat_scale, format(n, ","), format(m, ",")))
         return pos, links, fields, desc, sizes
     else:
         raise SystemExit("unknown workload %r" % name)
@@ -93,6 +94,7 @@ def stage_bytes(stage, n, m, c, cl):
         "link_out": 21 * n + 24 * m,
         "collision_grid": 13 * n,
         "collision_force": 21 * n,
+        "clusters": 54 * n,         # sums: pos 8, cluster 4, flags 1 R (+ K records); pull: pos 8, cluster 4, coeff 4, flags 1 R, pos 8 W
     }[stage]
 
 
@@ -222,7 +224,8 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="sbm1m", choices=["sbm1m", "ba10k", "rmat8m", "batch", "serve"])
+    ap.add_argument("--workload", default="sbm1m", choices=["sbm1m", "ba10k", "rmat", "batch", "serve"])
+    ap.add_argument("--rmat-scale", type=int, default=23, help="R-MAT workload: 2^scale points, 40M * 2^(scale-23) links")
     ap.add_argument("--rates", default="50,100,200,500,1000,2000", help="request rates (req/s) of the serving sweep")
     ap.add_argument("--requests", type=int, default=200, help="requests per rate of the serving sweep")
     ap.add_argument("--graphs", type=int, default=4096, help="jobs of the batched workload")
@@ -261,7 +264,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    pos, links, fields, desc, sizes = make_workload(args.workload, seed=1 + rank)
+    pos, links, fields, desc, sizes = make_workload(args.workload, seed=1 + rank, rmat_scale=args.rmat_scale)
     if args.positions_from:
         pos = np.load(args.positions_from).astype(np.float32)
         desc += " (evolved positions from %s)" % os.path.basename(args.positions_from)
@@ -559,7 +562,7 @@ def run_serve(args):
 
 
 def run_reference(args):
-    pos, links, fields, desc, sizes = make_workload(args.workload, seed=1)
+    pos, links, fields, desc, sizes = make_workload(args.workload, seed=1, rmat_scale=args.rmat_scale)
     budget = 150.0
     from oracle import OracleEngine
     o = OracleEngine(**fields)
