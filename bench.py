@@ -224,7 +224,7 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="sbm1m", choices=["sbm1m", "ba10k", "rmat", "batch", "serve"])
+    ap.add_argument("--workload", default="sbm1m", choices=["sbm1m", "ba10k", "rmat", "batch", "serve", "ingest"])
     ap.add_argument("--rmat-scale", type=int, default=23, help="R-MAT workload: 2^scale points, 40M * 2^(scale-23) links")
     ap.add_argument("--rates", default="50,100,200,500,1000,2000", help="request rates (req/s) of the serving sweep")
     ap.add_argument("--requests", type=int, default=200, help="requests per rate of the serving sweep")
@@ -255,6 +255,9 @@ def main():
         return
     if args.workload == "serve":
         run_serve(args)
+        return
+    if args.workload == "ingest":
+        run_ingest(args)
         return
 
     import torch
@@ -382,6 +385,36 @@ def main():
     eng.close()
     if dist:
         dist.destroy_process_group()
+
+
+def run_ingest(args):
+    """Graph.render time (setPointPositions + setLinks applied: positions, jitter,
+    both link lists) of the R-MAT graph with the link lists built on the host and
+    on the device; the lists are identical (tests/test_device_ingest.py)."""
+    import math
+    from graph_gb300.engine import Engine
+    from graph_gb300 import _abi
+    pos, links, fields, desc, sizes = make_workload("rmat", seed=1, rmat_scale=args.rmat_scale)
+    out = {}
+    for name, dmin in (("host", math.inf), ("device", 0.0)):
+        times = []
+        for rep in range(max(1, args.steps)):
+            eng = Engine(_abi.make_config(**dict(fields, device_ingest_min_links=dmin)))
+            eng.set_point_positions(pos)
+            eng.set_links(links)
+            eng.synchronize()
+            t0 = time.perf_counter()
+            eng.render()
+            eng.synchronize()
+            times.append(time.perf_counter() - t0)
+            eng.close()
+        out[name] = min(times)
+    m = links.size // 2
+    print(json.dumps({"metric": "links ingested/s", "value": m / out["device"], "unit": "links/s", "n_gpus": 1,
+                      "steps": max(1, args.steps), "higher_is_better": True, "data": "synthetic",
+                      "config": {"workload": desc, "step": "Graph.render: positions, jitter, both link lists"},
+                      "render_s": {"host_build": out["host"], "device_build": out["device"]},
+                      "speedup": out["host"] / out["device"]}))
 
 
 def run_batch(args):

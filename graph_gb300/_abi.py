@@ -58,6 +58,7 @@ class Config(C.Structure):
         ("simulation_repulsion_from_mouse", C.c_double),
         ("enable_right_click_repulsion", C.c_int32),
         ("enable_drag", C.c_int32),
+        ("device_ingest_min_links", C.c_double),
     ]
 
 
@@ -122,6 +123,7 @@ DEFAULTS = dict(
     simulation_repulsion_from_mouse=2.0,
     enable_right_click_repulsion=0,
     enable_drag=0,
+    device_ingest_min_links=65536.0,
 )
 
 # Reference config keys (camelCase, src/config.ts) -> C field names.

@@ -15,6 +15,7 @@
 
 #include "../../include/cgl.h"
 #include "ingest.h"
+#include "ingest_device.cuh"
 #include "kernels.cuh"
 
 using namespace cgl;
@@ -158,6 +159,15 @@ cgl_status dev_reserve(cgl_engine* e, DevBuf& b, size_t bytes, bool zero) {
   e->dev_bytes += bytes;
   if (zero) CU(cudaMemsetAsync(b.p, 0, bytes, e->stream));
   return CGL_OK;
+}
+
+void dev_release(cgl_engine* e, DevBuf& b) {
+  if (!b.p) return;
+  cudaStreamSynchronize(e->stream);
+  cudaFree(b.p);
+  e->dev_bytes -= b.bytes;
+  b.p = nullptr;
+  b.bytes = 0;
 }
 
 void dev_free_all(cgl_engine* e) {
@@ -455,6 +465,96 @@ cgl_status run_ticks(cgl_engine* e, uint32_t ticks, cudaEvent_t* ev, double* sta
   return CGL_OK;
 }
 
+// ForceLink.create(INCOMING) then (OUTGOING) built on the device
+// (ingest_device.cu); the same lists, draws and order as ingest::build_links.
+cgl_status build_links_device(cgl_engine* e, uint64_t E64, size_t n) {
+  using namespace dingest;
+  cudaStream_t st = e->stream;
+  const uint32_t E = (uint32_t)E64, N = (uint32_t)n;
+  DevBuf t_links, t_str, t_valid, t_len_in, t_len_out, t_kin, t_kout, t_vin, t_vout, t_tmp, t_stats;
+  DevBuf* temps[] = {&t_links, &t_str, &t_valid, &t_len_in, &t_len_out, &t_kin, &t_kout, &t_vin, &t_vout, &t_tmp,
+                     &t_stats};
+  auto done = [&](cgl_status rc) {
+    for (DevBuf* b : temps) dev_release(e, *b);
+    return rc;
+  };
+  cgl_status rc;
+  const uint64_t big = std::max<uint64_t>(E64 + 1, n + 1);
+  const size_t tmp_words = std::max(sort_temp_words(big), scan_temp_words(big));
+  if ((rc = dev_reserve(e, t_links, E64 * sizeof(float2), false)) ||
+      (rc = dev_reserve(e, t_valid, (E64 + 1) * sizeof(uint32_t), true)) ||
+      (rc = dev_reserve(e, t_len_in, (n + 1) * sizeof(uint32_t), true)) ||
+      (rc = dev_reserve(e, t_len_out, (n + 1) * sizeof(uint32_t), true)) ||
+      (rc = dev_reserve(e, t_tmp, tmp_words * sizeof(uint32_t), false)) ||
+      (rc = dev_reserve(e, t_stats, 4 * sizeof(uint32_t), true)))
+    return done(rc);
+  if (cudaMemcpyAsync(t_links.p, e->in_links.data(), E64 * sizeof(float2), cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return done(fail(e, CGL_CUDA_ERROR, "link upload failed"));
+  const float* strength = nullptr;
+  if (e->has_strength) {
+    if ((rc = dev_reserve(e, t_str, E64 * sizeof(float), false))) return done(rc);
+    if (cudaMemcpyAsync(t_str.p, e->in_strength.data(), E64 * sizeof(float), cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return done(fail(e, CGL_CUDA_ERROR, "link strength upload failed"));
+    strength = (const float*)t_str.p;
+  }
+  const float2* links = (const float2*)t_links.p;
+  uint32_t* valid = (uint32_t*)t_valid.p;
+  uint32_t* len_in = (uint32_t*)t_len_in.p;
+  uint32_t* len_out = (uint32_t*)t_len_out.p;
+  uint32_t* tmp = (uint32_t*)t_tmp.p;
+  uint32_t* stats = (uint32_t*)t_stats.p;
+  count_links(links, E, N, valid, len_in, len_out, st);
+  scan_exclusive(valid, E + 1, tmp, st);
+  len_stats(len_in, N, stats, st);
+  len_stats(len_out, N, stats + 2, st);
+  uint32_t h[5];
+  CU(cudaMemcpyAsync(h, valid + E, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  CU(cudaMemcpyAsync(h + 1, stats, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  CU(cudaStreamSynchronize(st));
+  const uint32_t M = h[0];
+  const size_t pairs = std::max<size_t>(M, n);   // the pair buffers also hold the length sort
+  if ((rc = dev_reserve(e, t_kin, pairs * sizeof(uint32_t), false)) ||
+      (rc = dev_reserve(e, t_kout, pairs * sizeof(uint32_t), false)) ||
+      (rc = dev_reserve(e, t_vin, pairs * sizeof(uint32_t), false)) ||
+      (rc = dev_reserve(e, t_vout, pairs * sizeof(uint32_t), false)) ||
+      (rc = dev_reserve(e, e->b_ent_in, (size_t)M * sizeof(uint4), false)) ||
+      (rc = dev_reserve(e, e->b_ent_out, (size_t)M * sizeof(uint4), false)) ||
+      (rc = dev_reserve(e, e->b_rowptr_in, (n + 1) * sizeof(uint32_t), false)) ||
+      (rc = dev_reserve(e, e->b_rowptr_out, (n + 1) * sizeof(uint32_t), false)) ||
+      (rc = dev_reserve(e, e->b_heavy_in, n * sizeof(uint32_t), false)) ||
+      (rc = dev_reserve(e, e->b_heavy_out, n * sizeof(uint32_t), false)))
+    return done(rc);
+  uint32_t *kin = (uint32_t*)t_kin.p, *kout = (uint32_t*)t_kout.p, *vin = (uint32_t*)t_vin.p, *vout = (uint32_t*)t_vout.p;
+  compact_links(links, E, valid, kin, kout, vin, vout, st);
+  const int row_bits = key_bits(n ? n - 1 : 0);
+  sort_pairs(kin, vin, M, row_bits, tmp, st);
+  sort_pairs(kout, vout, M, row_bits, tmp, st);
+  const uint64_t base = e->rng_ctr;
+  fill_csr(kin, vin, M, links, true, len_in, len_out, strength, (const uint8_t*)e->b_flags.p, e->rng_seed, base,
+           (uint4*)e->b_ent_in.p, st);
+  fill_csr(kout, vout, M, links, false, len_in, len_out, strength, (const uint8_t*)e->b_flags.p, e->rng_seed,
+           base + M, (uint4*)e->b_ent_out.p, st);
+  e->rng_ctr += 2 * (uint64_t)M;
+  // rowptr = exclusive scan of the list lengths (len[n] = 0 makes rowptr[n] = M)
+  copy_u32(len_in, (uint32_t*)e->b_rowptr_in.p, N + 1, st);
+  scan_exclusive((uint32_t*)e->b_rowptr_in.p, N + 1, tmp, st);
+  copy_u32(len_out, (uint32_t*)e->b_rowptr_out.p, N + 1, st);
+  scan_exclusive((uint32_t*)e->b_rowptr_out.p, N + 1, tmp, st);
+  // points by list length, longest first, ties by index
+  len_keys(len_in, N, stats, kin, (uint32_t*)e->b_heavy_in.p, st);
+  sort_pairs(kin, (uint32_t*)e->b_heavy_in.p, N, key_bits(h[1]), tmp, st);
+  len_keys(len_out, N, stats + 2, kout, (uint32_t*)e->b_heavy_out.p, st);
+  sort_pairs(kout, (uint32_t*)e->b_heavy_out.p, N, key_bits(h[3]), tmp, st);
+  CU(cudaGetLastError());
+  CU(cudaStreamSynchronize(st));
+  e->entries = M;
+  e->max_deg_in = h[1];
+  e->n_heavy_in = h[2];
+  e->max_deg_out = h[3];
+  e->n_heavy_out = h[4];
+  return done(CGL_OK);
+}
+
 cgl_status apply_pinned(cgl_engine* e) {
   // Points.updatePinnedStatus (Points/index.ts:1264-1277) -> device flags
   e->pinned.assign(e->N, 0);
@@ -531,11 +631,18 @@ cgl_status do_render(cgl_engine* e, double alpha) {
       if ((st = dev_reserve(e, e->b_big_sx, cells * sizeof(long long), false))) return st;
       if ((st = dev_reserve(e, e->b_big_sy, cells * sizeof(long long), false))) return st;
       if ((st = dev_reserve(e, e->b_big_ns, cells * sizeof(uint32_t), false))) return st;
-      std::vector<float2> jit;
-      ingest::Rng rng{e->rng_seed, e->rng_ctr};
-      ingest::jitter(rng, n, jit);
-      e->rng_ctr = rng.ctr;
-      if (n) CU(cudaMemcpyAsync(e->b_jitter.p, jit.data(), n * sizeof(float2), cudaMemcpyHostToDevice, e->stream));
+      const uint64_t texels = (uint64_t)e->T * e->T;
+      if (!(e->cfg.device_ingest_min_links > (double)n)) {   // drawn on the device, same draws
+        dingest::jitter(e->rng_seed, e->rng_ctr, (uint32_t)n, (float2*)e->b_jitter.p, e->stream);
+        CU(cudaGetLastError());
+        e->rng_ctr += 2 * texels;
+      } else {
+        std::vector<float2> jit;
+        ingest::Rng rng{e->rng_seed, e->rng_ctr};
+        ingest::jitter(rng, n, jit);
+        e->rng_ctr = rng.ctr;
+        if (n) CU(cudaMemcpyAsync(e->b_jitter.p, jit.data(), n * sizeof(float2), cudaMemcpyHostToDevice, e->stream));
+      }
       CU(cudaStreamSynchronize(e->stream));
       e->mb_ready = true;
     }
@@ -545,6 +652,10 @@ cgl_status do_render(cgl_engine* e, double alpha) {
   if (links_changed) {
     e->graph_dirty = true;
     // ForceLink.create(INCOMING) then (OUTGOING) (src/index.ts:1663-1666)
+    const double dmin = e->cfg.device_ingest_min_links;
+    if (e->T && e->W && E > 0 && !(dmin > (double)E)) {
+      if ((st = build_links_device(e, E, n))) return st;
+    } else {
     ingest::Csr cin, cout_;
     if (e->T && e->W) {
       ingest::Rng rng{e->rng_seed, e->rng_ctr};
@@ -585,6 +696,7 @@ cgl_status do_render(cgl_engine* e, double alpha) {
     if (!en_out.empty())
       CU(cudaMemcpyAsync(e->b_ent_out.p, en_out.data(), en_out.size() * sizeof(uint4), cudaMemcpyHostToDevice, e->stream));
     CU(cudaStreamSynchronize(e->stream));
+    }
   }
   if (e->clusters_dirty || pos_changed) {
     // Clusters.create (Clusters/index.ts:54-100), src/index.ts:1668
@@ -647,6 +759,7 @@ void cgl_config_defaults(cgl_config* c) {
   c->simulation_repulsion_from_mouse = 2;
   c->enable_right_click_repulsion = 0;
   c->enable_drag = 0;
+  c->device_ingest_min_links = 65536;
 }
 
 cgl_status cgl_create(const cgl_config* cfg, cgl_engine** out) {

@@ -85,6 +85,9 @@ typedef struct cgl_config {
   double simulation_repulsion_from_mouse;    /* simulationRepulsionFromMouse, default 2 (variables.ts:77) */
   int32_t enable_right_click_repulsion;      /* enableRightClickRepulsion, default 0 (variables.ts:83) */
   int32_t enable_drag;                       /* enableDrag, default 0 (variables.ts:132) */
+  double device_ingest_min_links;            /* the link lists (from this many links up) and the many-body jitter
+                                                (from this many points up) are built on the GPU; default 65536,
+                                                0 = always, +inf = never; both builds give the same data */
 } cgl_config;
 
 typedef struct cgl_state {
