@@ -226,6 +226,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="sbm1m", choices=["sbm1m", "ba10k", "rmat", "batch", "serve", "ingest"])
     ap.add_argument("--rmat-scale", type=int, default=23, help="R-MAT workload: 2^scale points, 40M * 2^(scale-23) links")
+    ap.add_argument("--device-ingest-min", type=float, default=None,
+                    help="batched workload: build link lists and jitter on the GPU from this many links/points up")
     ap.add_argument("--rates", default="50,100,200,500,1000,2000", help="request rates (req/s) of the serving sweep")
     ap.add_argument("--requests", type=int, default=200, help="requests per rate of the serving sweep")
     ap.add_argument("--graphs", type=int, default=4096, help="jobs of the batched workload")
@@ -428,6 +430,8 @@ def run_batch(args):
     torch.cuda.set_device(0)
     t0 = time.perf_counter()
     jobs = list(generators.batch_workload(args.graphs, seed=7))
+    if args.device_ingest_min is not None:
+        jobs = [(p, l, dict(f, device_ingest_min_links=args.device_ingest_min)) for p, l, f in jobs]
     gen_s = time.perf_counter() - t0
     n_points = sum(p.size // 2 for p, _, _ in jobs)
     n_links = sum(l.size // 2 for _, l, _ in jobs)

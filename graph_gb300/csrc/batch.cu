@@ -20,6 +20,7 @@
 #include "../../include/cgl.h"
 #include "batch.cuh"
 #include "ingest.h"
+#include "ingest_device.cuh"
 
 using namespace cgl;
 
@@ -111,6 +112,23 @@ struct cgl_batch {
 
 namespace {
 
+// Transient device buffers of one cgl_batch_add, freed when it returns.
+struct Temp {
+  cgl_batch* b;
+  std::vector<void*> ptrs;
+  ~Temp();
+  template <class T>
+  T* get(size_t n) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(n * sizeof(T), 16)) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    ptrs.push_back(p);
+    return (T*)p;
+  }
+};
+
 cgl_status bfail(cgl_batch* b, cgl_status st, const char* fmt, ...) {
   char buf[512];
   va_list ap;
@@ -119,6 +137,12 @@ cgl_status bfail(cgl_batch* b, cgl_status st, const char* fmt, ...) {
   va_end(ap);
   if (b) b->err = buf;
   return st;
+}
+
+Temp::~Temp() {
+  if (ptrs.empty()) return;
+  cudaStreamSynchronize(b->stream);
+  for (void* p : ptrs) cudaFree(p);
 }
 
 #define BCU(call)                                                                                     \
@@ -399,16 +423,67 @@ cgl_status cgl_batch_add(cgl_batch* b, const cgl_config* cfg, const float* xy, u
   j.gf = grid.gf;
   j.levels = grid.levels;
   j.tile = std::min(16, j.gf);
+  // the jitter draws come first (ForceManyBody.create), then the link draws
+  const uint64_t T = (uint64_t)std::ceil(std::sqrt((double)j.n));
+  const bool dev_jitter = !(cfg->device_ingest_min_links > (double)j.n);
+  const uint64_t jitter_base = j.rng.ctr;
   std::vector<float2> jit;
-  ingest::jitter(j.rng, j.n, jit);
+  if (dev_jitter) j.rng.ctr += 2 * T * T;
+  else ingest::jitter(j.rng, j.n, jit);
   ingest::Csr cin, cout_;
   const bool has_links = j.E > 0;
-  if (has_links) ingest::build_links(links, j.E, j.n, nullptr, absent, j.rng, cin, cout_);
-  else { cin.rowptr.assign(j.n + 1, 0); cout_.rowptr.assign(j.n + 1, 0); }
-  j.m_in = cin.ent.size();
-  j.m_out = cout_.ent.size();
-  j.heavy_in = cin.heavy;
-  j.heavy_out = cout_.heavy;
+  // link lists on the device when asked for and when its transient buffers fit
+  // the budget (ingest_device.cu; the same lists as ingest::build_links)
+  Temp tmp{b};
+  bool dev_links = has_links && j.E < 0xFFFFFFF0ull && !(cfg->device_ingest_min_links > (double)j.E);
+  const uint64_t big = std::max<uint64_t>(j.E + 1, j.n + 1);
+  const size_t tmp_words = std::max(dingest::sort_temp_words(big), dingest::scan_temp_words(big));
+  if (dev_links && b->budget > 0 &&
+      (double)b->dev_bytes + 8.0 * j.E + 4.0 * (j.E + 1) + 8.0 * (j.n + 1) + 16.0 * big + 4.0 * tmp_words > b->budget)
+    dev_links = false;
+  float2* d_links = nullptr;
+  uint32_t *d_valid = nullptr, *d_len_in = nullptr, *d_len_out = nullptr, *d_tmp = nullptr, *d_stats = nullptr;
+  uint32_t *d_kin = nullptr, *d_kout = nullptr, *d_vin = nullptr, *d_vout = nullptr;
+  uint32_t dev_m = 0, dev_stats[4] = {0, 0, 0, 0};
+  const uint64_t links_base = j.rng.ctr;
+  if (dev_links) {
+    d_links = tmp.get<float2>(j.E);
+    d_valid = tmp.get<uint32_t>(j.E + 1);
+    d_len_in = tmp.get<uint32_t>(j.n + 1);
+    d_len_out = tmp.get<uint32_t>(j.n + 1);
+    d_tmp = tmp.get<uint32_t>(tmp_words);
+    d_stats = tmp.get<uint32_t>(4);
+    d_kin = tmp.get<uint32_t>(big);
+    d_kout = tmp.get<uint32_t>(big);
+    d_vin = tmp.get<uint32_t>(big);
+    d_vout = tmp.get<uint32_t>(big);
+    dev_links = d_links && d_valid && d_len_in && d_len_out && d_tmp && d_stats && d_kin && d_kout && d_vin && d_vout;
+  }
+  if (dev_links) {
+    cudaStream_t s = b->stream;
+    const uint32_t E32 = (uint32_t)j.E, N32 = (uint32_t)j.n;
+    BCU(cudaMemcpyAsync(d_links, links, j.E * sizeof(float2), cudaMemcpyHostToDevice, s));
+    BCU(cudaMemsetAsync(d_valid, 0, (j.E + 1) * 4, s));
+    BCU(cudaMemsetAsync(d_len_in, 0, (j.n + 1) * 4, s));
+    BCU(cudaMemsetAsync(d_len_out, 0, (j.n + 1) * 4, s));
+    BCU(cudaMemsetAsync(d_stats, 0, 16, s));
+    dingest::count_links(d_links, E32, N32, d_valid, d_len_in, d_len_out, s);
+    dingest::scan_exclusive(d_valid, E32 + 1, d_tmp, s);
+    dingest::len_stats(d_len_in, N32, d_stats, s);
+    dingest::len_stats(d_len_out, N32, d_stats + 2, s);
+    BCU(cudaMemcpyAsync(&dev_m, d_valid + j.E, 4, cudaMemcpyDeviceToHost, s));
+    BCU(cudaMemcpyAsync(dev_stats, d_stats, 16, cudaMemcpyDeviceToHost, s));
+    BCU(cudaStreamSynchronize(s));
+    j.m_in = j.m_out = dev_m;
+    j.rng.ctr += 2 * (uint64_t)dev_m;
+  } else {
+    if (has_links) ingest::build_links(links, j.E, j.n, nullptr, absent, j.rng, cin, cout_);
+    else { cin.rowptr.assign(j.n + 1, 0); cout_.rowptr.assign(j.n + 1, 0); }
+    j.m_in = cin.ent.size();
+    j.m_out = cout_.ent.size();
+    j.heavy_in = cin.heavy;
+    j.heavy_out = cout_.heavy;
+  }
   j.stages = 0;
   if (cfg->simulation_gravity != 0 && (mask & CGL_STAGE_GRAVITY)) j.stages |= kGGravity;
   if (mask & CGL_STAGE_MANYBODY) j.stages |= kGManybody;
@@ -458,13 +533,17 @@ cgl_status cgl_batch_add(cgl_batch* b, const cgl_config* cfg, const float* xy, u
     return st;
   }
   // upload: absolute indices for rows and neighbours
-  std::vector<uint32_t> rp_in(j.n + 1), rp_out(j.n + 1);
-  for (uint64_t i = 0; i <= j.n; ++i) {
-    rp_in[i] = (uint32_t)(j.e_in + cin.rowptr[i]);
-    rp_out[i] = (uint32_t)(j.e_out + cout_.rowptr[i]);
+  std::vector<uint32_t> rp_in, rp_out;
+  if (!dev_links) {
+    rp_in.resize(j.n + 1);
+    rp_out.resize(j.n + 1);
+    for (uint64_t i = 0; i <= j.n; ++i) {
+      rp_in[i] = (uint32_t)(j.e_in + cin.rowptr[i]);
+      rp_out[i] = (uint32_t)(j.e_out + cout_.rowptr[i]);
+    }
+    for (auto& e : cin.ent) if (e.x != kAbsentTarget) e.x += (uint32_t)j.p_off;
+    for (auto& e : cout_.ent) if (e.x != kAbsentTarget) e.x += (uint32_t)j.p_off;
   }
-  for (auto& e : cin.ent) if (e.x != kAbsentTarget) e.x += (uint32_t)j.p_off;
-  for (auto& e : cout_.ent) if (e.x != kAbsentTarget) e.x += (uint32_t)j.p_off;
   std::vector<uint8_t> flags(j.n);
   for (uint64_t i = 0; i < j.n; ++i) flags[i] = absent[i] ? kAbsent : 0;
   const uint32_t g = [&]() {
@@ -476,17 +555,49 @@ cgl_status cgl_batch_add(cgl_batch* b, const cgl_config* cfg, const float* xy, u
   std::vector<uint32_t> gids(j.n, g), cgids(j.cells, g);
   cudaStream_t s = b->stream;
   BCU(cudaMemcpyAsync((float2*)b->pos.p + j.p_off, pos.data(), j.n * 8, cudaMemcpyHostToDevice, s));
-  BCU(cudaMemcpyAsync((float2*)b->jitter.p + j.p_off, jit.data(), j.n * 8, cudaMemcpyHostToDevice, s));
+  if (dev_jitter) dingest::jitter(j.rng.seed, jitter_base, (uint32_t)j.n, (float2*)b->jitter.p + j.p_off, s);
+  else BCU(cudaMemcpyAsync((float2*)b->jitter.p + j.p_off, jit.data(), j.n * 8, cudaMemcpyHostToDevice, s));
   BCU(cudaMemcpyAsync((uint8_t*)b->flags.p + j.p_off, flags.data(), j.n, cudaMemcpyHostToDevice, s));
   BCU(cudaMemcpyAsync((uint32_t*)b->gid.p + j.p_off, gids.data(), j.n * 4, cudaMemcpyHostToDevice, s));
   BCU(cudaMemcpyAsync((uint32_t*)b->cell_gid.p + j.cell_off, cgids.data(), j.cells * 4, cudaMemcpyHostToDevice, s));
   BCU(cudaMemsetAsync((uint32_t*)b->counts.p + j.cell_off, 0, j.cells * 4, s));
   BCU(cudaMemsetAsync((long long*)b->acc.p + 3 * j.acc_off, 0, j.accs * 3 * sizeof(long long), s));
-  BCU(cudaMemcpyAsync((uint32_t*)b->rowptr.p + j.rp_in, rp_in.data(), (j.n + 1) * 4, cudaMemcpyHostToDevice, s));
-  BCU(cudaMemcpyAsync((uint32_t*)b->rowptr.p + j.rp_out, rp_out.data(), (j.n + 1) * 4, cudaMemcpyHostToDevice, s));
-  if (j.m_in) BCU(cudaMemcpyAsync((uint4*)b->ent.p + j.e_in, cin.ent.data(), j.m_in * 16, cudaMemcpyHostToDevice, s));
-  if (j.m_out)
-    BCU(cudaMemcpyAsync((uint4*)b->ent.p + j.e_out, cout_.ent.data(), j.m_out * 16, cudaMemcpyHostToDevice, s));
+  if (dev_links) {
+    // (row, link) pairs sorted by row, entries filled in place with arena
+    // indices; the flags of this job are already queued above
+    const uint32_t E32 = (uint32_t)j.E, N32 = (uint32_t)j.n, M = dev_m;
+    const uint8_t* flags_j = (const uint8_t*)b->flags.p + j.p_off;
+    dingest::compact_links(d_links, E32, d_valid, d_kin, d_kout, d_vin, d_vout, s);
+    const int row_bits = dingest::key_bits(j.n - 1);
+    dingest::sort_pairs(d_kin, d_vin, M, row_bits, d_tmp, s);
+    dingest::sort_pairs(d_kout, d_vout, M, row_bits, d_tmp, s);
+    dingest::fill_csr(d_kin, d_vin, M, d_links, true, d_len_in, d_len_out, nullptr, flags_j, j.rng.seed, links_base,
+                      (uint32_t)j.p_off, (uint4*)b->ent.p + j.e_in, s);
+    dingest::fill_csr(d_kout, d_vout, M, d_links, false, d_len_in, d_len_out, nullptr, flags_j, j.rng.seed,
+                      links_base + M, (uint32_t)j.p_off, (uint4*)b->ent.p + j.e_out, s);
+    // the long lists (rows by length, longest first; the first stats[1] / stats[3])
+    j.heavy_in.resize(dev_stats[1]);
+    j.heavy_out.resize(dev_stats[3]);
+    for (int dir = 0; dir < 2; ++dir) {
+      std::vector<uint32_t>& hv = dir == 0 ? j.heavy_in : j.heavy_out;
+      if (hv.empty()) continue;
+      dingest::len_keys(dir == 0 ? d_len_in : d_len_out, N32, d_stats + 2 * dir, d_kin, d_vin, s);
+      dingest::sort_pairs(d_kin, d_vin, N32, dingest::key_bits(dev_stats[2 * dir]), d_tmp, s);
+      BCU(cudaMemcpyAsync(hv.data(), d_vin, hv.size() * 4, cudaMemcpyDeviceToHost, s));
+    }
+    // row pointers: exclusive scan of the lengths, offset by the entry range
+    dingest::scan_exclusive(d_len_in, N32 + 1, d_tmp, s);
+    dingest::copy_u32(d_len_in, (uint32_t*)b->rowptr.p + j.rp_in, N32 + 1, s, (uint32_t)j.e_in);
+    dingest::scan_exclusive(d_len_out, N32 + 1, d_tmp, s);
+    dingest::copy_u32(d_len_out, (uint32_t*)b->rowptr.p + j.rp_out, N32 + 1, s, (uint32_t)j.e_out);
+    BCU(cudaGetLastError());
+  } else {
+    BCU(cudaMemcpyAsync((uint32_t*)b->rowptr.p + j.rp_in, rp_in.data(), (j.n + 1) * 4, cudaMemcpyHostToDevice, s));
+    BCU(cudaMemcpyAsync((uint32_t*)b->rowptr.p + j.rp_out, rp_out.data(), (j.n + 1) * 4, cudaMemcpyHostToDevice, s));
+    if (j.m_in) BCU(cudaMemcpyAsync((uint4*)b->ent.p + j.e_in, cin.ent.data(), j.m_in * 16, cudaMemcpyHostToDevice, s));
+    if (j.m_out)
+      BCU(cudaMemcpyAsync((uint4*)b->ent.p + j.e_out, cout_.ent.data(), j.m_out * 16, cudaMemcpyHostToDevice, s));
+  }
   BCU(cudaStreamSynchronize(s));
   GraphDesc& D = j.desc;
   D.p_off = (uint32_t)j.p_off;

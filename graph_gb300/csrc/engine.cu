@@ -531,9 +531,9 @@ cgl_status build_links_device(cgl_engine* e, uint64_t E64, size_t n) {
   sort_pairs(kout, vout, M, row_bits, tmp, st);
   const uint64_t base = e->rng_ctr;
   fill_csr(kin, vin, M, links, true, len_in, len_out, strength, (const uint8_t*)e->b_flags.p, e->rng_seed, base,
-           (uint4*)e->b_ent_in.p, st);
+           0, (uint4*)e->b_ent_in.p, st);
   fill_csr(kout, vout, M, links, false, len_in, len_out, strength, (const uint8_t*)e->b_flags.p, e->rng_seed,
-           base + M, (uint4*)e->b_ent_out.p, st);
+           base + M, 0, (uint4*)e->b_ent_out.p, st);
   e->rng_ctr += 2 * (uint64_t)M;
   // rowptr = exclusive scan of the list lengths (len[n] = 0 makes rowptr[n] = M)
   copy_u32(len_in, (uint32_t*)e->b_rowptr_in.p, N + 1, st);

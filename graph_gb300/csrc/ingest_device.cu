@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(kBlock) k_csr_fill(const uint32_t* __restrict_
                                                      const uint32_t* __restrict__ len_out,
                                                      const float* __restrict__ strength,
                                                      const uint8_t* __restrict__ flags, uint64_t seed,
-                                                     uint64_t draw_base, uint4* __restrict__ ent) {
+                                                     uint64_t draw_base, uint32_t point_off, uint4* __restrict__ ent) {
   const uint32_t at = blockIdx.x * blockDim.x + threadIdx.x;
   if (at >= M) return;
   const uint32_t i = lidx[at], p = rows[at];
@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(kBlock) k_csr_fill(const uint32_t* __restrict_
   st = __dsqrt_rn(st);
   // Random.float(0, 1) = 0 + (1 - 0) * u, u = top 53 bits / 2^53 (exact), rounded to f32
   const double u = (double)(splitmix_draw(seed, draw_base + at) >> 11) * 0x1.0p-53;
-  ent[at] = make_uint4((flags[q] & kAbsent) ? kAbsentTarget : q, __float_as_uint(__double2float_rn(u)),
+  ent[at] = make_uint4((flags[q] & kAbsent) ? kAbsentTarget : q + point_off, __float_as_uint(__double2float_rn(u)),
                        __float_as_uint(__double2float_rn(bias)), __float_as_uint(__double2float_rn(st)));
 }
 
@@ -263,9 +263,9 @@ __global__ void __launch_bounds__(kBlock) k_jitter(uint64_t seed, uint64_t base,
   out[t] = make_float2(r[0], r[1]);
 }
 
-__global__ void k_copy_u32(const uint32_t* __restrict__ a, uint32_t* __restrict__ b, uint32_t n) {
+__global__ void k_copy_u32(const uint32_t* __restrict__ a, uint32_t* __restrict__ b, uint32_t n, uint32_t add) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) b[i] = a[i];
+  if (i < n) b[i] = a[i] + add;
 }
 
 }  // namespace
@@ -322,8 +322,8 @@ void sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t n, int bits, uint32_t* 
     t = va; va = vb; vb = t;
   }
   if (ka != keys) {
-    k_copy_u32<<<ceil_div(n, kBlock), kBlock, 0, st>>>(ka, keys, n);
-    k_copy_u32<<<ceil_div(n, kBlock), kBlock, 0, st>>>(va, vals, n);
+    k_copy_u32<<<ceil_div(n, kBlock), kBlock, 0, st>>>(ka, keys, n, 0u);
+    k_copy_u32<<<ceil_div(n, kBlock), kBlock, 0, st>>>(va, vals, n, 0u);
   }
 }
 
@@ -339,10 +339,10 @@ void compact_links(const float2* links, uint32_t E, const uint32_t* pos, uint32_
 
 void fill_csr(const uint32_t* rows, const uint32_t* lidx, uint32_t M, const float2* links, bool incoming,
               const uint32_t* len_in, const uint32_t* len_out, const float* strength, const uint8_t* flags,
-              uint64_t seed, uint64_t draw_base, uint4* ent, cudaStream_t st) {
+              uint64_t seed, uint64_t draw_base, uint32_t point_off, uint4* ent, cudaStream_t st) {
   if (M)
     k_csr_fill<<<ceil_div(M, kBlock), kBlock, 0, st>>>(rows, lidx, M, links, incoming ? 1 : 0, len_in, len_out,
-                                                        strength, flags, seed, draw_base, ent);
+                                                        strength, flags, seed, draw_base, point_off, ent);
 }
 
 void len_stats(const uint32_t* len, uint32_t N, uint32_t* stats, cudaStream_t st) {
@@ -357,8 +357,8 @@ void jitter(uint64_t seed, uint64_t base, uint32_t n, float2* out, cudaStream_t 
   if (n) k_jitter<<<ceil_div(n, kBlock), kBlock, 0, st>>>(seed, base, n, out);
 }
 
-void copy_u32(const uint32_t* a, uint32_t* b, uint32_t n, cudaStream_t st) {
-  if (n) k_copy_u32<<<ceil_div(n, kBlock), kBlock, 0, st>>>(a, b, n);
+void copy_u32(const uint32_t* a, uint32_t* b, uint32_t n, cudaStream_t st, uint32_t add) {
+  if (n) k_copy_u32<<<ceil_div(n, kBlock), kBlock, 0, st>>>(a, b, n, add);
 }
 
 }  // namespace dingest

@@ -127,3 +127,33 @@ def test_batch_budget_refuses_admission():
         with pytest.raises(StatusError) as ex:
             b.add(pos, None, space_size=8192)
         assert ex.value.status == _abi.CGL_OOM
+
+
+@pytest.mark.parametrize("dmin", [0.0, float("inf")])
+def test_batch_device_and_host_ingest_match_oracle(dmin):
+    # the same awkward link set through the batch's device build (0) and host build (inf)
+    import math
+    from graph_gb300.batch import Batch
+    from helpers import make_pair
+    rng = np.random.default_rng(9)
+    n = 3000
+    pos = rng.uniform(0, 4096, size=2 * n).astype(np.float32)
+    pos[2 * 5: 2 * 9] = np.nan
+    links = generators.erdos_renyi(n, 5, 9).reshape(-1, 2)
+    hub = np.stack([np.full(600, 17.0), rng.integers(0, n, 600)], axis=1)
+    bad = np.array([[math.nan, 1], [2, -1], [3, n], [4.5, 6], [7, 7], [8, 9], [8, 9]])
+    all_links = np.concatenate([links, hub, bad]).astype(np.float32)
+    rng.shuffle(all_links)
+    all_links = all_links.reshape(-1)
+    fields = dict(space_size=4096.0, simulation_repulsion=0.3, simulation_link_distance=2.0, random_seed=91,
+                  device_ingest_min_links=dmin)
+    with Batch() as b:
+        other = b.add(generators.uniform_positions(500, 0, 1024, 3), generators.erdos_renyi(500, 4, 3),
+                      space_size=1024.0, random_seed=92, device_ingest_min_links=dmin)
+        jid = b.add(pos, all_links, **fields)
+        b.step(4)
+        got = b.get_point_positions(jid)
+    eng, orc = make_pair(pos, all_links, fields)
+    orc.step(4)
+    want = orc.get_point_positions()
+    assert same_bits(got, want), first_mismatch(got, want)
