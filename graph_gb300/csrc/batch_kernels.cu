@@ -462,6 +462,7 @@ __global__ void __launch_bounds__(kBlock) kb_manybody(BatchView v) {
   const int gf = D.gf, L = D.levels;
   const int fcx = cell_index(px, D.csf, gf), fcy = cell_index(py, D.csf, gf);
   const float k = __fmul_rn(tp.alpha, D.repulsion);
+  const bool fast = quotient_by_recip(k);   // the repulsion quotients from the reciprocals
   const PairUnits pu = v.units;
   const float4* rec = v.rec + D.rec_off;
   float2 vel = make_float2(0.f, 0.f);
@@ -475,7 +476,7 @@ __global__ void __launch_bounds__(kBlock) kb_manybody(BatchView v) {
 #pragma unroll 1
       for (int ii = 0; ii < 4; ++ii) {
         if (row_in && (unsigned)(ii - ex) <= 2u) continue;
-        cell_velocity(__ldg(&rec[jj * 4 + ii]), p, k, lv2, pu);
+        cell_velocity(__ldg(&rec[jj * 4 + ii]), p, k, fast, lv2, pu);
       }
     }
     vel = add2(vel, lv2, pu);
@@ -500,7 +501,7 @@ __global__ void __launch_bounds__(kBlock) kb_manybody(BatchView v) {
         const int cx = bx + ii;
         if ((unsigned)cx >= (unsigned)G) continue;
         if (row_in && (unsigned)(cx - ex) <= 2u) continue;
-        cell_velocity(__ldg(&row[cx]), p, k, lv2, pu);
+        cell_velocity(__ldg(&row[cx]), p, k, fast, lv2, pu);
       }
     }
     vel = add2(vel, lv2, pu);
@@ -531,7 +532,7 @@ __global__ void __launch_bounds__(kBlock) kb_manybody(BatchView v) {
         if ((float)(oi - D.p_off) == self) continue;
         const float2 o = __ldg(&v.sorted_pos[b + q]);
         sampled = __fadd_rn(sampled, 1.0f);
-        pair_velocity(p, o, rj, k, sum, pu);
+        pair_velocity(p, o, rj, k, fast, sum, pu);
       }
       if (sampled > 0.f) {
         const float w = __fdiv_rn(others, sampled);

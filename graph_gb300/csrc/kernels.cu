@@ -549,6 +549,7 @@ __global__ void __launch_bounds__(kBlock) k_manybody(DeviceView d, SimScalars s)
   const int gf = s.gf, L = s.levels;
   const int fcx = cell_index(px, s.csf, gf), fcy = cell_index(py, s.csf, gf);
   const float k = __fmul_rn(tp.alpha, s.repulsion);
+  const bool fast = quotient_by_recip(k);   // the repulsion quotients from the reciprocals
   const PairUnits pu = s.units;
   float2 vel = make_float2(0.f, 0.f);
   {   // level 0 (force-level.frag:70-79): every cell of the 4x4 grid outside the 3x3
@@ -562,7 +563,7 @@ __global__ void __launch_bounds__(kBlock) k_manybody(DeviceView d, SimScalars s)
 #pragma unroll 1
       for (int ii = 0; ii < 4; ++ii) {
         if (row_in && (unsigned)(ii - ex) <= 2u) continue;
-        cell_velocity(__ldg(&lv[jj * 4 + ii]), p, k, lv2, pu);
+        cell_velocity(__ldg(&lv[jj * 4 + ii]), p, k, fast, lv2, pu);
       }
     }
     vel = add2(vel, lv2, pu);
@@ -586,7 +587,7 @@ __global__ void __launch_bounds__(kBlock) k_manybody(DeviceView d, SimScalars s)
         const int cx = bx + ii;
         if ((unsigned)cx >= (unsigned)G) continue;
         if (row_in && (unsigned)(cx - ex) <= 2u) continue;
-        cell_velocity(__ldg(&row[cx]), p, k, lv2, pu);
+        cell_velocity(__ldg(&row[cx]), p, k, fast, lv2, pu);
       }
     }
     vel = add2(vel, lv2, pu);
@@ -616,7 +617,7 @@ __global__ void __launch_bounds__(kBlock) k_manybody(DeviceView d, SimScalars s)
         if ((float)oi == self) continue;
         const float2 o = __ldg(&d.sorted_pos[b + q]);
         sampled = __fadd_rn(sampled, 1.0f);
-        pair_velocity(p, o, rj, k, sum, pu);
+        pair_velocity(p, o, rj, k, fast, sum, pu);
       }
       if (sampled > 0.f) {
         const float w = __fdiv_rn(others, sampled);
