@@ -108,15 +108,16 @@ def load_peaks():
         return 6800.0, "fallback"
 
 
-def load_traffic(stage):
-    """DRAM bytes per launch of `stage` from the committed ncu summary, if present."""
-    path = os.path.join(ROOT, "profiles", "traffic_sbm1m.json")
+def load_ncu(workload, stage):
+    """From the committed ncu summary of `workload` (profiles/ncu_<workload>.json):
+    DRAM bytes per launch of `stage` and its issue-slot utilisation, or Nones."""
+    path = os.path.join(ROOT, "profiles", "ncu_%s.json" % workload)
     try:
         with open(path) as f:
             t = json.load(f)
-        return t.get(stage)
+        return t.get("dram_bytes", {}).get(stage), t.get("issue_active", {}).get(stage)
     except Exception:
-        return None
+        return None, None
 
 
 # ------------------------------------------------------------------- clocks --
@@ -328,6 +329,7 @@ def main():
     alg = stage_bytes(dom, live, m, c, cl)
     peak, peak_kind = load_peaks()
     achieved = alg / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
+    traffic, issue = load_ncu(args.workload if not args.positions_from else "none", dom)
     per_stage = {k: round(v * 1e3, 2) for k, v in stages.items() if v > 0}
     stage_gbs = {k: round(stage_bytes(k, live, m, c, cl) / (stages[k] / 1e3) / 1e9, 1)
                  for k in stages if stages[k] > 0}
@@ -366,8 +368,13 @@ def main():
                              % int((29 * live + 24 * 2 * m + 60 * live) / 1e6),
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": load_traffic(dom),
-                         "algorithmic_bytes": alg, "launch_ms": dom_ms, "peak_source": peak_kind},
+                         "frac": achieved / peak, "traffic": traffic,
+                         "algorithmic_bytes": alg, "launch_ms": dom_ms, "peak_source": peak_kind,
+                         "issue_active_ncu": issue,
+                         "note": ("k_manybody is bound by instruction issue (correctly rounded sqrt, division and "
+                                  "reciprocal per term for bit-exact parity), not by HBM; issue_active_ncu is its "
+                                  "share of busy issue slots from the committed ncu summary")
+                         if dom == "manybody" else None},
             "stage_us": per_stage,
             "stage_alg_gbs": stage_gbs,
             "cpu_baseline": cpu,
