@@ -140,8 +140,8 @@ def test_tiny_graphs(n):
         _assert_same(eng, orc, (n, t))
 
 
-def test_hub_lists_on_side_branch():
-    # a star and a second hub: lists longer than 256 links run on the side branch
+def test_hub_lists():
+    # a star and a second hub: lists longer than 256 links get a CTA each
     n = 3000
     rng = np.random.default_rng(21)
     pos = rng.uniform(1000, 3000, size=2 * n).astype(np.float32)
@@ -306,7 +306,7 @@ def test_full_size_properties():
 def test_rmat_scale23_collision_bit_exact():
     # config 2 shape: R-MAT scale 23 (a,b,c,d = .57,.19,.19,.05), 40M links after
     # self-loop and duplicate removal, radius U[1,8] (pointSizes = 2r), collision
-    # 0.5, spaceSize 16384.  Hub lists (degree ~1e5) run on the side branch.
+    # 0.5, spaceSize 16384.  Hub lists (up to ~57,000 links) get a CTA each.
     n = 1 << 23
     links = generators.rmat(23, 40_000_000, 0.57, 0.19, 0.19, seed=3)
     pos = generators.uniform_positions(n, 0, 16384, 3)
