@@ -17,8 +17,15 @@ seeded.  One step = one simulation tick (Graph.step()) over the whole graph.
          per-tick algorithm; the reference itself is TypeScript/WebGL and
          cannot run here) on all host cores, same workload and metric.
 
+Other workloads (--workload): ba10k (Barabasi-Albert 10,000 points), rmat
+(R-MAT scale 23 with collision, --rmat-scale to resize), batch (4,096
+independent jobs in one batched engine vs the plain engine job by job), serve
+(continuous batching vs a one-job-at-a-time queue under Poisson arrivals),
+ingest (Graph.render with the link lists built on the host and on the GPU).
+
 Multi-GPU (torchrun): replicas only — each rank lays out its own copy of the
-graph, no collective on the data path; value sums the ranks.
+graph, no collective on the data path; value = all ranks' points x ticks over
+the slowest rank's time (graph_gb300/replicas.py).
 """
 import argparse
 import json
