@@ -263,6 +263,13 @@ class Graph:
             self._cb("onSimulationEnd")
         return done
 
+    def getPositionTexture(self):
+        """The renderer's points texture (Points/position-utils.ts:9-27): float32 (T*T, 4) of
+        (x, y, index, 0); the engine writes it in the layout the draw passes read."""
+        if self._destroyed:
+            return np.zeros((0, 4), dtype=np.float32)
+        return self._engine.get_position_texture()
+
     def getClusterPositions(self):
         """Centre of mass of each cluster as float64 [x0, y0, x1, y1, ...] (src/index.ts:1135-1139)."""
         if self._destroyed:

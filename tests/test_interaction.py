@@ -140,3 +140,38 @@ def test_frame_loop_end_matches():
     n1, n2 = eng.frame(400), orc.frame(400)
     assert n1 == n2 < 400 and not eng.state().is_simulation_running
     _same(eng, orc, "ended")
+
+
+@pytest.mark.gpu
+def test_graph_surface_clusters_pointer_texture():
+    # the flow INTEGRATION.md shows, through the camelCase Graph
+    from graph_gb300 import Graph, generators
+    n = 2000
+    pos = generators.uniform_positions(n, 1000, 3000, 4)
+    links = generators.erdos_renyi(n, 4, 4)
+    clusters = [k % 3 if k % 7 else None for k in range(n)]
+    events = []
+    g = Graph({"spaceSize": 4096, "simulationCluster": 0.3, "enableDrag": True, "enableRightClickRepulsion": True,
+               "simulationRepulsionFromMouse": 2, "randomSeed": 3,
+               "onDragStart": lambda: events.append("drag"), "onDragEnd": lambda: events.append("drop")})
+    g.setPointPositions(pos)
+    g.setLinks(links)
+    g.setPointClusters(clusters)
+    g.setClusterPositions([500, 600, None, None])
+    g.render()
+    g.start()
+    g.setPointer(1200.0, 900.0, rightButton=True)
+    g.startDrag(3)
+    assert g.frame(5) == 5
+    p = g.getPointPositions()
+    assert p[6] == np.float32(1200.0) and p[7] == np.float32(900.0)   # the dragged point sits on the pointer
+    g.endDrag()
+    assert events == ["drag", "drop"]
+    tex = g.getPositionTexture()
+    t = int(np.ceil(np.sqrt(n)))
+    assert tex.shape == (t * t, 4)
+    assert np.array_equal(tex[:n, 0], p[0::2]) and np.array_equal(tex[:n, 2], np.arange(n, dtype=np.float32))
+    assert not tex[n:].any()
+    c = g.getClusterPositions()
+    assert c.size == 6 and np.isfinite(c).all()
+    g.destroy()
