@@ -449,20 +449,12 @@ __global__ void __launch_bounds__(kBlock) kb_coarse(BatchView v) {
 }
 
 // --------------------------------------------------------------- manybody --
-__global__ void __launch_bounds__(kBlock) kb_manybody(BatchView v) {
-  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t total = v.cell_start[v.cell_hwm];
-  if (j >= total) return;
-  const uint32_t P = v.sorted_idx[j];
-  const uint32_t g = v.gid[P];
-  const GraphDesc& D = v.desc[g];
-  const BatchTick tp = tick_of(v, g);
-  const float2 p = v.sorted_pos[j];
+// FAST: the repulsion quotients come from the reciprocals (quotient_by_recip(k)).
+template <bool FAST>
+__device__ __forceinline__ void kb_manybody_point(const BatchView& v, const GraphDesc& D, uint32_t P, float2 p, float k) {
   const float px = p.x, py = p.y;
   const int gf = D.gf, L = D.levels;
   const int fcx = cell_index(px, D.csf, gf), fcy = cell_index(py, D.csf, gf);
-  const float k = __fmul_rn(tp.alpha, D.repulsion);
-  const bool fast = quotient_by_recip(k);   // the repulsion quotients from the reciprocals
   const PairUnits pu = v.units;
   const float4* rec = v.rec + D.rec_off;
   float2 vel = make_float2(0.f, 0.f);
@@ -476,7 +468,7 @@ __global__ void __launch_bounds__(kBlock) kb_manybody(BatchView v) {
 #pragma unroll 1
       for (int ii = 0; ii < 4; ++ii) {
         if (row_in && (unsigned)(ii - ex) <= 2u) continue;
-        cell_velocity(__ldg(&rec[jj * 4 + ii]), p, k, fast, lv2, pu);
+        cell_velocity<FAST>(__ldg(&rec[jj * 4 + ii]), p, k, lv2, pu);
       }
     }
     vel = add2(vel, lv2, pu);
@@ -501,7 +493,7 @@ __global__ void __launch_bounds__(kBlock) kb_manybody(BatchView v) {
         const int cx = bx + ii;
         if ((unsigned)cx >= (unsigned)G) continue;
         if (row_in && (unsigned)(cx - ex) <= 2u) continue;
-        cell_velocity(__ldg(&row[cx]), p, k, fast, lv2, pu);
+        cell_velocity<FAST>(__ldg(&row[cx]), p, k, lv2, pu);
       }
     }
     vel = add2(vel, lv2, pu);
@@ -532,7 +524,7 @@ __global__ void __launch_bounds__(kBlock) kb_manybody(BatchView v) {
         if ((float)(oi - D.p_off) == self) continue;
         const float2 o = __ldg(&v.sorted_pos[b + q]);
         sampled = __fadd_rn(sampled, 1.0f);
-        pair_velocity(p, o, rj, k, fast, sum, pu);
+        pair_velocity<FAST>(p, o, rj, k, sum, pu);
       }
       if (sampled > 0.f) {
         const float w = __fdiv_rn(others, sampled);
@@ -546,6 +538,20 @@ __global__ void __launch_bounds__(kBlock) kb_manybody(BatchView v) {
   if (speed > max_step) nf = mul2(nf, splat(__fdiv_rn(max_step, speed)), pu);
   vel = add2(vel, nf, pu);
   if (!(v.flags[P] & kPinned)) v.pos[P] = integrate(p, vel.x, vel.y, D.friction, D.space);
+}
+
+__global__ void __launch_bounds__(kBlock) kb_manybody(BatchView v) {
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t total = v.cell_start[v.cell_hwm];
+  if (j >= total) return;
+  const uint32_t P = v.sorted_idx[j];
+  const uint32_t g = v.gid[P];
+  const GraphDesc& D = v.desc[g];
+  const BatchTick tp = tick_of(v, g);
+  const float2 p = v.sorted_pos[j];
+  const float k = __fmul_rn(tp.alpha, D.repulsion);
+  if (quotient_by_recip(k)) kb_manybody_point<true>(v, D, P, p, k);
+  else kb_manybody_point<false>(v, D, P, p, k);
 }
 
 // ------------------------------------------------------------------- link --

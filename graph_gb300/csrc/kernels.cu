@@ -538,18 +538,15 @@ __global__ void k_cells(DeviceView d, SimScalars s) {
 }
 
 // --------------------------------------------------------------- manybody --
-__global__ void __launch_bounds__(kBlock) k_manybody(DeviceView d, SimScalars s) {
-  const TickParams tp = tick_params(d);
-  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t total = d.cell_start[s.gf * s.gf];
-  if (j >= total) return;
+// FAST: the repulsion quotients come from the reciprocals (quotient_by_recip(k),
+// the same for every point of a pass, so each launch runs one of the two).
+template <bool FAST>
+__device__ __forceinline__ void manybody_point(const DeviceView& d, const SimScalars& s, uint32_t j, float k) {
   const uint32_t i = d.sorted_idx[j];
   const float2 p = d.sorted_pos[j];
   const float px = p.x, py = p.y;
   const int gf = s.gf, L = s.levels;
   const int fcx = cell_index(px, s.csf, gf), fcy = cell_index(py, s.csf, gf);
-  const float k = __fmul_rn(tp.alpha, s.repulsion);
-  const bool fast = quotient_by_recip(k);   // the repulsion quotients from the reciprocals
   const PairUnits pu = s.units;
   float2 vel = make_float2(0.f, 0.f);
   {   // level 0 (force-level.frag:70-79): every cell of the 4x4 grid outside the 3x3
@@ -563,7 +560,7 @@ __global__ void __launch_bounds__(kBlock) k_manybody(DeviceView d, SimScalars s)
 #pragma unroll 1
       for (int ii = 0; ii < 4; ++ii) {
         if (row_in && (unsigned)(ii - ex) <= 2u) continue;
-        cell_velocity(__ldg(&lv[jj * 4 + ii]), p, k, fast, lv2, pu);
+        cell_velocity<FAST>(__ldg(&lv[jj * 4 + ii]), p, k, lv2, pu);
       }
     }
     vel = add2(vel, lv2, pu);
@@ -587,7 +584,7 @@ __global__ void __launch_bounds__(kBlock) k_manybody(DeviceView d, SimScalars s)
         const int cx = bx + ii;
         if ((unsigned)cx >= (unsigned)G) continue;
         if (row_in && (unsigned)(cx - ex) <= 2u) continue;
-        cell_velocity(__ldg(&row[cx]), p, k, fast, lv2, pu);
+        cell_velocity<FAST>(__ldg(&row[cx]), p, k, lv2, pu);
       }
     }
     vel = add2(vel, lv2, pu);
@@ -617,7 +614,7 @@ __global__ void __launch_bounds__(kBlock) k_manybody(DeviceView d, SimScalars s)
         if ((float)oi == self) continue;
         const float2 o = __ldg(&d.sorted_pos[b + q]);
         sampled = __fadd_rn(sampled, 1.0f);
-        pair_velocity(p, o, rj, k, fast, sum, pu);
+        pair_velocity<FAST>(p, o, rj, k, sum, pu);
       }
       if (sampled > 0.f) {
         const float w = __fdiv_rn(others, sampled);
@@ -631,6 +628,16 @@ __global__ void __launch_bounds__(kBlock) k_manybody(DeviceView d, SimScalars s)
   if (speed > max_step) nf = mul2(nf, splat(__fdiv_rn(max_step, speed)), pu);
   vel = add2(vel, nf, pu);
   if (!(d.flags[i] & kPinned)) d.pos[i] = integrate(p, vel.x, vel.y, s.friction, s.space);
+}
+
+__global__ void __launch_bounds__(kBlock) k_manybody(DeviceView d, SimScalars s) {
+  const TickParams tp = tick_params(d);
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t total = d.cell_start[s.gf * s.gf];
+  if (j >= total) return;
+  const float k = __fmul_rn(tp.alpha, s.repulsion);
+  if (quotient_by_recip(k)) manybody_point<true>(d, s, j, k);
+  else manybody_point<false>(d, s, j, k);
 }
 
 // ------------------------------------------------------------------- link --
