@@ -500,7 +500,6 @@ __device__ __forceinline__ void kb_manybody_point(const BatchView& v, const Grap
   }
   // near field (force-nearfield.frag:199-263)
   const float2 rj = v.jitter[P];
-  const float self = (float)(P - D.p_off);
   const float4* fine = rec + level_base(L - 1);
   float2 nf = make_float2(0.f, 0.f);
 #pragma unroll 1
@@ -521,7 +520,7 @@ __device__ __forceinline__ void kb_manybody_point(const BatchView& v, const Grap
       for (int q = 0; q < kSlots; ++q) {
         if (q >= ns) break;
         const uint32_t oi = __ldg(&v.sorted_idx[b + q]);
-        if ((float)(oi - D.p_off) == self) continue;
+        if (oi == P) continue;   // the shader compares f32 indices; below 2^24 they are exact
         const float2 o = __ldg(&v.sorted_pos[b + q]);
         sampled = __fadd_rn(sampled, 1.0f);
         pair_velocity<FAST>(p, o, rj, k, sum, pu);
