@@ -166,50 +166,88 @@ __device__ void kb_warp_cell(const BatchView& v, uint32_t c) {
   const uint32_t seed = tick_of(v, g).seed_bits;
   const uint32_t b = v.cell_start[c], e = v.cell_start[c + 1];
   long long ax = 0, ay = 0;
-  unsigned long long best[kSlots];
-  uint32_t at[kSlots];
-#pragma unroll
-  for (int q = 0; q < kSlots; ++q) { best[q] = ~0ull; at[q] = 0; }
-  uint32_t j = b + lane;
-  for (; j + 96 < e; j += 128) {   // loads four points ahead of the selection
-    float2 p[4];
-    uint32_t ix[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) { p[u] = v.sorted_pos[j + 32 * u]; ix[u] = v.sorted_idx[j + 32 * u]; }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      ax += to_fixed(p[u].x, D.fx);
-      ay += to_fixed(p[u].y, D.fx);
-      top8_insert(best, at, local_key(ix[u], D.p_off, seed), j + 32 * u);
-    }
-  }
-  for (; j < e; j += 32) {
-    const float2 p = v.sorted_pos[j];
-    ax += to_fixed(p.x, D.fx);
-    ay += to_fixed(p.y, D.fx);
-    top8_insert(best, at, local_key(v.sorted_idx[j], D.p_off, seed), j);
-  }
-  ax = warp_sum_ll(ax);
-  ay = warp_sum_ll(ay);
   uint32_t sel[kSlots];
   int ns = 0;
-  unsigned long long last = 0;
+  if (e - b <= 128) {   // at most 4 points per lane: select from the keys in registers (kernels.cu warp_cell_small)
+    unsigned long long key[4];
 #pragma unroll
-  for (int k = 0; k < kSlots; ++k) {
-    unsigned long long m = ~0ull;
-    uint32_t mp = 0;
-#pragma unroll
-    for (int q = 0; q < kSlots; ++q)
-      if (best[q] != ~0ull && (k == 0 || (best[q] >> 32) > (last >> 32)) && best[q] < m) { m = best[q]; mp = at[q]; }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const unsigned long long om = __shfl_xor_sync(0xffffffffu, m, o);
-      const uint32_t op = __shfl_xor_sync(0xffffffffu, mp, o);
-      if (om < m) { m = om; mp = op; }
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t j = b + lane + 32u * u;
+      key[u] = ~0ull;
+      if (j < e) {
+        const float2 p = v.sorted_pos[j];
+        ax += to_fixed(p.x, D.fx);
+        ay += to_fixed(p.y, D.fx);
+        key[u] = local_key(v.sorted_idx[j], D.p_off, seed);
+      }
     }
-    sel[k] = mp;
-    if (m != ~0ull) { ns = k + 1; last = m; }
-    else last = ~0ull;
+    ax = warp_sum_ll(ax);
+    ay = warp_sum_ll(ay);
+    unsigned long long last = 0;
+#pragma unroll
+    for (int k = 0; k < kSlots; ++k) {
+      unsigned long long m = ~0ull;
+      uint32_t mp = 0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (key[u] != ~0ull && (k == 0 || (key[u] >> 32) > (last >> 32)) && key[u] < m) {
+          m = key[u];
+          mp = b + lane + 32u * u;
+        }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long om = __shfl_xor_sync(0xffffffffu, m, o);
+        const uint32_t op = __shfl_xor_sync(0xffffffffu, mp, o);
+        if (om < m) { m = om; mp = op; }
+      }
+      sel[k] = mp;
+      if (m != ~0ull) { ns = k + 1; last = m; }
+      else last = ~0ull;
+    }
+  } else {
+    unsigned long long best[kSlots];
+    uint32_t at[kSlots];
+#pragma unroll
+    for (int q = 0; q < kSlots; ++q) { best[q] = ~0ull; at[q] = 0; }
+    uint32_t j = b + lane;
+    for (; j + 96 < e; j += 128) {   // loads four points ahead of the selection
+      float2 p[4];
+      uint32_t ix[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) { p[u] = v.sorted_pos[j + 32 * u]; ix[u] = v.sorted_idx[j + 32 * u]; }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        ax += to_fixed(p[u].x, D.fx);
+        ay += to_fixed(p[u].y, D.fx);
+        top8_insert(best, at, local_key(ix[u], D.p_off, seed), j + 32 * u);
+      }
+    }
+    for (; j < e; j += 32) {
+      const float2 p = v.sorted_pos[j];
+      ax += to_fixed(p.x, D.fx);
+      ay += to_fixed(p.y, D.fx);
+      top8_insert(best, at, local_key(v.sorted_idx[j], D.p_off, seed), j);
+    }
+    ax = warp_sum_ll(ax);
+    ay = warp_sum_ll(ay);
+    unsigned long long last = 0;
+#pragma unroll
+    for (int k = 0; k < kSlots; ++k) {
+      unsigned long long m = ~0ull;
+      uint32_t mp = 0;
+#pragma unroll
+      for (int q = 0; q < kSlots; ++q)
+        if (best[q] != ~0ull && (k == 0 || (best[q] >> 32) > (last >> 32)) && best[q] < m) { m = best[q]; mp = at[q]; }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long om = __shfl_xor_sync(0xffffffffu, m, o);
+        const uint32_t op = __shfl_xor_sync(0xffffffffu, mp, o);
+        if (om < m) { m = om; mp = op; }
+      }
+      sel[k] = mp;
+      if (m != ~0ull) { ns = k + 1; last = m; }
+      else last = ~0ull;
+    }
   }
   // parallel move of the slots to the head (see kernels.cu warp_cell)
   const uint32_t h = b + (uint32_t)lane;
