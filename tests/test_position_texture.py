@@ -70,3 +70,22 @@ def test_texture_rejects_small_buffers():
         t = eng.layout().points_texture_size
         big = np.empty(4 * t * t, dtype=np.float32)
         eng.enqueue_position_texture(big.ctypes.data, big.size)
+
+
+def test_positions_into_pinned_memory():
+    # read-back into pinned host memory (the e2e path), at 16- and 8-byte alignment
+    torch = pytest.importorskip("torch")
+    pos, links, fields = scenario("center")
+    pos = np.concatenate([pos, np.float32([1.5, 2.5])])       # an odd number of points
+    eng, orc = make_pair(pos, links, fields)
+    eng.step(2)
+    want = eng.get_point_positions()
+    n = want.size
+    pinned = torch.empty(n, dtype=torch.float32, pin_memory=True)
+    eng.get_point_positions_into(pinned.numpy())
+    assert _same(pinned.numpy(), want)
+    off = torch.empty(n + 2, dtype=torch.float32, pin_memory=True)   # 8- but not 16-byte aligned view
+    eng.get_point_positions_into(off.numpy()[2:])
+    assert _same(off.numpy()[2:], want)
+    orc.step(2)
+    assert _same(want, orc.get_point_positions())
