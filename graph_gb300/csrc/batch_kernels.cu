@@ -671,7 +671,7 @@ void batch_launch_tick(const BatchView& v, cudaStream_t st, cudaStream_t side, c
     kb_scan_cells<<<n1, kBlock, 0, st>>>(v, v.scan1);
   }
   if (v.point_hwm) kb_scatter<<<blocks(v.point_hwm), kBlock, 0, st>>>(v);
-  kb_bigcells<<<4 * 152, kBlock, 0, st>>>(v);
+  kb_bigcells<<<8 * sm_count(), kBlock, 0, st>>>(v);   // as k_bigcells: 8 blocks per SM
   if (v.n_tiles) kb_cells<<<v.n_tiles, kBlock, 0, st>>>(v);
   if (v.slots) kb_coarse<<<v.slots, kBlock, 0, st>>>(v);
   if (v.point_hwm) kb_manybody<<<blocks(v.point_hwm), kBlock, 0, st>>>(v);

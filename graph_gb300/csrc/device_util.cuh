@@ -1,6 +1,8 @@
 // device_util.cuh — warp/block primitives and the near-field slot selection
 // shared by the plain and the batched tick kernels.
 #pragma once
+#include <cuda_runtime.h>
+
 #include <cstdint>
 
 #include "common.cuh"
@@ -8,6 +10,14 @@
 namespace cgl {
 
 constexpr int kBlock = 256;
+
+// Streaming multiprocessors of the current device.
+inline uint32_t sm_count() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms > 0 ? (uint32_t)sms : 1u;
+}
 
 __device__ __forceinline__ long long warp_sum_ll(long long v) {
 #pragma unroll

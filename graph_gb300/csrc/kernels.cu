@@ -1177,7 +1177,10 @@ void launch_scatter(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
 }
 
 void launch_cells(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
-  k_bigcells<<<4 * 152, kBlock, 0, st>>>(d, s);
+  // grid-stride over the dense cells; blocks beyond one resident wave (3 per SM)
+  // start as others finish and even out the cells' unequal sizes (measured
+  // best at 8 per SM)
+  k_bigcells<<<8 * sm_count(), kBlock, 0, st>>>(d, s);
   const int tiles = (s.gf / s.tile) * (s.gf / s.tile);
   const size_t smem = 3 * sizeof(long long) * s.tile * s.tile;
   k_cells<<<tiles, s.tile * s.tile, smem, st>>>(d, s);
@@ -1203,7 +1206,7 @@ void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool s
 void launch_cluster_sum(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
   if (!d.n) return;
   if (d.n_clusters <= kClusterSmem)
-    k_cluster_sum<true><<<std::min(blocks_for(d.n), 4u * 152u), kBlock, 0, st>>>(d, s);
+    k_cluster_sum<true><<<std::min(blocks_for(d.n), 4u * sm_count()), kBlock, 0, st>>>(d, s);
   else
     k_cluster_sum<false><<<blocks_for(d.n), kBlock, 0, st>>>(d, s);
 }
