@@ -13,11 +13,15 @@
 //   manybody     level passes + near field + update (force-level.frag,
 //                force-nearfield.frag, update-position.frag)
 //   link in/out  spring force over each direction's link lists + update
-//                (force-spring.ts)
+//                (force-spring.ts); hub lists get a CTA each
+//   clusters     centre of mass per cluster + cluster pull + update
+//                (calculate-centermass.vert, force-cluster.frag)   [if set]
 //   collision    4 offset grids + spatial collision force + update
 //                (build-grid.vert, force-collision-spatial.frag)
 // Kernels read the tick's alpha and peel seed from device memory so that one
-// captured CUDA graph serves every tick.
+// captured CUDA graph serves every tick.  Outside the tick: the pointer's
+// repulsion and drag passes (force-mouse.frag, drag-point.frag) and the
+// renderer's position texture.
 #include "device_util.cuh"
 #include "kernels.cuh"
 
