@@ -784,7 +784,16 @@ __global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, con
           next = hub_fill(hub, buf ^ 1, e0 + (c + 1) * kHubChunk, e1, ent, src, span, s.link_r0, s.link_distance);
       } else if (threadIdx.x == 0) {
         const uint32_t len = min((uint32_t)kHubChunk, e1 - e0 - c * kHubChunk);
-        if (!absent) {   // no per-link branch: the chain runs back to back
+        if (!absent && len == (uint32_t)kHubChunk) {   // a full chunk: constant trip count
+          const float4* A = hub.a[buf];
+          const float4* B = hub.b[buf];
+#pragma unroll 4
+          for (int k = 0; k < kHubChunk; ++k) {
+            const float4 a = A[k];
+            const float4 b = B[k];
+            spring_step(pp, vel, make_float2(a.x, a.y), a.z, a.w, sa, b.x, b.y, pu);
+          }
+        } else if (!absent) {   // no per-link branch: the chain runs back to back
 #pragma unroll 4
           for (uint32_t k = 0; k < len; ++k) {
             const float4 a = hub.a[buf][k];
