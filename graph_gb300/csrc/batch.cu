@@ -532,6 +532,19 @@ cgl_status cgl_batch_add(cgl_batch* b, const cgl_config* cfg, const float* xy, u
     for (int k = 0; k < taken; ++k) wants[k].a->release(*wants[k].off, wants[k].n);
     return st;
   }
+  // From here on a CUDA error gives the job's arena ranges back before returning.
+  auto give_back = [&]() {
+    for (const Want& w : wants) w.a->release(*w.off, w.n);
+  };
+#define JCU(call)                                                                                    \
+  do {                                                                                               \
+    cudaError_t _e = (call);                                                                         \
+    if (_e != cudaSuccess) {                                                                         \
+      give_back();                                                                                   \
+      return bfail(b, _e == cudaErrorMemoryAllocation ? CGL_OOM : CGL_CUDA_ERROR, "%s: %s", #call,  \
+                   cudaGetErrorString(_e));                                                          \
+    }                                                                                                \
+  } while (0)
   // upload: absolute indices for rows and neighbours
   std::vector<uint32_t> rp_in, rp_out;
   if (!dev_links) {
@@ -554,14 +567,14 @@ cgl_status cgl_batch_add(cgl_batch* b, const cgl_config* cfg, const float* xy, u
   }();
   std::vector<uint32_t> gids(j.n, g), cgids(j.cells, g);
   cudaStream_t s = b->stream;
-  BCU(cudaMemcpyAsync((float2*)b->pos.p + j.p_off, pos.data(), j.n * 8, cudaMemcpyHostToDevice, s));
+  JCU(cudaMemcpyAsync((float2*)b->pos.p + j.p_off, pos.data(), j.n * 8, cudaMemcpyHostToDevice, s));
   if (dev_jitter) dingest::jitter(j.rng.seed, jitter_base, (uint32_t)j.n, (float2*)b->jitter.p + j.p_off, s);
-  else BCU(cudaMemcpyAsync((float2*)b->jitter.p + j.p_off, jit.data(), j.n * 8, cudaMemcpyHostToDevice, s));
-  BCU(cudaMemcpyAsync((uint8_t*)b->flags.p + j.p_off, flags.data(), j.n, cudaMemcpyHostToDevice, s));
-  BCU(cudaMemcpyAsync((uint32_t*)b->gid.p + j.p_off, gids.data(), j.n * 4, cudaMemcpyHostToDevice, s));
-  BCU(cudaMemcpyAsync((uint32_t*)b->cell_gid.p + j.cell_off, cgids.data(), j.cells * 4, cudaMemcpyHostToDevice, s));
-  BCU(cudaMemsetAsync((uint32_t*)b->counts.p + j.cell_off, 0, j.cells * 4, s));
-  BCU(cudaMemsetAsync((long long*)b->acc.p + 3 * j.acc_off, 0, j.accs * 3 * sizeof(long long), s));
+  else JCU(cudaMemcpyAsync((float2*)b->jitter.p + j.p_off, jit.data(), j.n * 8, cudaMemcpyHostToDevice, s));
+  JCU(cudaMemcpyAsync((uint8_t*)b->flags.p + j.p_off, flags.data(), j.n, cudaMemcpyHostToDevice, s));
+  JCU(cudaMemcpyAsync((uint32_t*)b->gid.p + j.p_off, gids.data(), j.n * 4, cudaMemcpyHostToDevice, s));
+  JCU(cudaMemcpyAsync((uint32_t*)b->cell_gid.p + j.cell_off, cgids.data(), j.cells * 4, cudaMemcpyHostToDevice, s));
+  JCU(cudaMemsetAsync((uint32_t*)b->counts.p + j.cell_off, 0, j.cells * 4, s));
+  JCU(cudaMemsetAsync((long long*)b->acc.p + 3 * j.acc_off, 0, j.accs * 3 * sizeof(long long), s));
   if (dev_links) {
     // (row, link) pairs sorted by row, entries filled in place with arena
     // indices; the flags of this job are already queued above
@@ -583,22 +596,23 @@ cgl_status cgl_batch_add(cgl_batch* b, const cgl_config* cfg, const float* xy, u
       if (hv.empty()) continue;
       dingest::len_keys(dir == 0 ? d_len_in : d_len_out, N32, d_stats + 2 * dir, d_kin, d_vin, s);
       dingest::sort_pairs(d_kin, d_vin, N32, dingest::key_bits(dev_stats[2 * dir]), d_tmp, s);
-      BCU(cudaMemcpyAsync(hv.data(), d_vin, hv.size() * 4, cudaMemcpyDeviceToHost, s));
+      JCU(cudaMemcpyAsync(hv.data(), d_vin, hv.size() * 4, cudaMemcpyDeviceToHost, s));
     }
     // row pointers: exclusive scan of the lengths, offset by the entry range
     dingest::scan_exclusive(d_len_in, N32 + 1, d_tmp, s);
     dingest::copy_u32(d_len_in, (uint32_t*)b->rowptr.p + j.rp_in, N32 + 1, s, (uint32_t)j.e_in);
     dingest::scan_exclusive(d_len_out, N32 + 1, d_tmp, s);
     dingest::copy_u32(d_len_out, (uint32_t*)b->rowptr.p + j.rp_out, N32 + 1, s, (uint32_t)j.e_out);
-    BCU(cudaGetLastError());
+    JCU(cudaGetLastError());
   } else {
-    BCU(cudaMemcpyAsync((uint32_t*)b->rowptr.p + j.rp_in, rp_in.data(), (j.n + 1) * 4, cudaMemcpyHostToDevice, s));
-    BCU(cudaMemcpyAsync((uint32_t*)b->rowptr.p + j.rp_out, rp_out.data(), (j.n + 1) * 4, cudaMemcpyHostToDevice, s));
-    if (j.m_in) BCU(cudaMemcpyAsync((uint4*)b->ent.p + j.e_in, cin.ent.data(), j.m_in * 16, cudaMemcpyHostToDevice, s));
+    JCU(cudaMemcpyAsync((uint32_t*)b->rowptr.p + j.rp_in, rp_in.data(), (j.n + 1) * 4, cudaMemcpyHostToDevice, s));
+    JCU(cudaMemcpyAsync((uint32_t*)b->rowptr.p + j.rp_out, rp_out.data(), (j.n + 1) * 4, cudaMemcpyHostToDevice, s));
+    if (j.m_in) JCU(cudaMemcpyAsync((uint4*)b->ent.p + j.e_in, cin.ent.data(), j.m_in * 16, cudaMemcpyHostToDevice, s));
     if (j.m_out)
-      BCU(cudaMemcpyAsync((uint4*)b->ent.p + j.e_out, cout_.ent.data(), j.m_out * 16, cudaMemcpyHostToDevice, s));
+      JCU(cudaMemcpyAsync((uint4*)b->ent.p + j.e_out, cout_.ent.data(), j.m_out * 16, cudaMemcpyHostToDevice, s));
   }
-  BCU(cudaStreamSynchronize(s));
+  JCU(cudaStreamSynchronize(s));
+#undef JCU
   GraphDesc& D = j.desc;
   D.p_off = (uint32_t)j.p_off;
   D.n = (uint32_t)j.n;

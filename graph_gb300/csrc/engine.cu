@@ -479,6 +479,14 @@ cgl_status build_links_device(cgl_engine* e, uint64_t E64, size_t n) {
     return rc;
   };
   cgl_status rc;
+  // a CUDA error releases the temporaries before returning
+#define TCU(call)                                                                              \
+  do {                                                                                         \
+    cudaError_t _err = (call);                                                                 \
+    if (_err != cudaSuccess)                                                                   \
+      return done(fail(e, _err == cudaErrorMemoryAllocation ? CGL_OOM : CGL_CUDA_ERROR, "%s: %s", #call, \
+                       cudaGetErrorString(_err)));                                             \
+  } while (0)
   const uint64_t big = std::max<uint64_t>(E64 + 1, n + 1);
   const size_t tmp_words = std::max(sort_temp_words(big), scan_temp_words(big));
   if ((rc = dev_reserve(e, t_links, E64 * sizeof(float2), false)) ||
@@ -508,9 +516,9 @@ cgl_status build_links_device(cgl_engine* e, uint64_t E64, size_t n) {
   len_stats(len_in, N, stats, st);
   len_stats(len_out, N, stats + 2, st);
   uint32_t h[5];
-  CU(cudaMemcpyAsync(h, valid + E, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-  CU(cudaMemcpyAsync(h + 1, stats, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-  CU(cudaStreamSynchronize(st));
+  TCU(cudaMemcpyAsync(h, valid + E, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  TCU(cudaMemcpyAsync(h + 1, stats, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  TCU(cudaStreamSynchronize(st));
   const uint32_t M = h[0];
   const size_t pairs = std::max<size_t>(M, n);   // the pair buffers also hold the length sort
   if ((rc = dev_reserve(e, t_kin, pairs * sizeof(uint32_t), false)) ||
@@ -545,8 +553,8 @@ cgl_status build_links_device(cgl_engine* e, uint64_t E64, size_t n) {
   sort_pairs(kin, (uint32_t*)e->b_heavy_in.p, N, key_bits(h[1]), tmp, st);
   len_keys(len_out, N, stats + 2, kout, (uint32_t*)e->b_heavy_out.p, st);
   sort_pairs(kout, (uint32_t*)e->b_heavy_out.p, N, key_bits(h[3]), tmp, st);
-  CU(cudaGetLastError());
-  CU(cudaStreamSynchronize(st));
+  TCU(cudaGetLastError());
+  TCU(cudaStreamSynchronize(st));
   e->entries = M;
   e->max_deg_in = h[1];
   e->n_heavy_in = h[2];
@@ -554,6 +562,7 @@ cgl_status build_links_device(cgl_engine* e, uint64_t E64, size_t n) {
   e->n_heavy_out = h[4];
   return done(CGL_OK);
 }
+#undef TCU
 
 cgl_status apply_pinned(cgl_engine* e) {
   // Points.updatePinnedStatus (Points/index.ts:1264-1277) -> device flags
