@@ -21,7 +21,8 @@ Other workloads (--workload): ba10k (Barabasi-Albert 10,000 points), rmat
 (R-MAT scale 23 with collision, --rmat-scale to resize), batch (4,096
 independent jobs in one batched engine vs the plain engine job by job), serve
 (continuous batching vs a one-job-at-a-time queue under Poisson arrivals),
-ingest (Graph.render with the link lists built on the host and on the GPU).
+ingest (Graph.render with the link lists built on the host and on the GPU),
+repulsion (the reference's repulsion-benchmark story: 2k-200k points, ms/step).
 
 Multi-GPU (torchrun): replicas only — each rank lays out its own copy of the
 graph, no collective on the data path; value = all ranks' points x ticks over
@@ -232,7 +233,7 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="sbm1m", choices=["sbm1m", "ba10k", "rmat", "batch", "serve", "ingest"])
+    ap.add_argument("--workload", default="sbm1m", choices=["sbm1m", "ba10k", "rmat", "batch", "serve", "ingest", "repulsion"])
     ap.add_argument("--rmat-scale", type=int, default=23, help="R-MAT workload: 2^scale points, 40M * 2^(scale-23) links")
     ap.add_argument("--device-ingest-min", type=float, default=None,
                     help="batched workload: build link lists and jitter on the GPU from this many links/points up")
@@ -268,6 +269,9 @@ def main():
         return
     if args.workload == "ingest":
         run_ingest(args)
+        return
+    if args.workload == "repulsion":
+        run_repulsion(args)
         return
 
     import torch
@@ -396,6 +400,44 @@ def main():
     eng.close()
     if dist:
         dist.destroy_process_group()
+
+
+def run_repulsion(args):
+    """The reference's own benchmark story (src/stories/performance/
+    repulsion-benchmark.ts:13-16, 41-53, 80-88): pure points uniform in a
+    4096 space, gravity 0, repulsion 1, decay 1e12, pointDefaultSize 2; per
+    size, 12 warm-up steps, a read-back, then 40 steps and a read-back, timed
+    by the host clock (ms per step).  The oracle runs the same protocol on the
+    host cores beside it (the reference itself needs WebGL)."""
+    from graph_gb300.engine import Engine
+    from oracle import OracleEngine
+    sizes = [2_000, 5_000, 20_000, 50_000, 100_000, 200_000]
+    fields = dict(space_size=4096.0, point_default_size=2.0, simulation_decay=1e12, simulation_gravity=0.0,
+                  simulation_repulsion=1.0, random_seed=1)
+    rows = []
+    for n in sizes:
+        pos = generators.uniform_positions(n, 0, 4096, n)
+        row = {"size": n}
+        for name, cls in (("gb300_ms", Engine), ("oracle_ms", OracleEngine)):
+            eng = cls(**fields)
+            eng.set_point_positions(pos)
+            eng.render()
+            eng.start(1.0)
+            eng.step(12)
+            eng.get_point_positions()
+            t0 = time.perf_counter()
+            eng.step(40)
+            eng.get_point_positions()
+            row[name] = (time.perf_counter() - t0) * 1e3 / 40
+            eng.close()
+        row["speedup"] = row["oracle_ms"] / row["gb300_ms"]
+        rows.append(row)
+    print(json.dumps({"metric": "repulsion benchmark ms/step", "unit": "ms/step", "higher_is_better": False,
+                      "n_gpus": 1, "data": "synthetic",
+                      "config": {"workload": "repulsion-benchmark story: points only, uniform in 4096^2, gravity 0, "
+                                             "repulsion 1, decay 1e12; 12 warm-up + 40 timed steps, read-back "
+                                             "flush", "cores_oracle": os.cpu_count()},
+                      "rows": rows}))
 
 
 def run_ingest(args):
