@@ -1,7 +1,10 @@
 """The many-body kernels take their repulsion quotients from the reciprocal of
-the length (common.cuh: div_by_recip, Markstein's method).  This test builds
-a small CUDA program against the same header and checks the result equals the
-correctly rounded division (__fdiv_rn) bit for bit on 2^28 sampled pairs."""
+the length (common.cuh: div_by_recip, Markstein's method), and the length and
+its reciprocal from hardware approximations with one FMA correction each
+(sqrt_in_range, recip_in_range).  These tests build small CUDA programs
+against the same header and check the results equal the correctly rounded
+operations bit for bit: the division on 2^28 sampled pairs, the square root
+and the reciprocal on every float of their ranges."""
 import os
 import re
 import shutil
@@ -14,13 +17,27 @@ pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def test_markstein_quotient_equals_division(tmp_path):
+def _build(tmp_path, name):
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
-    exe = str(tmp_path / "check_quotient")
+    exe = str(tmp_path / name)
     subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-fmad=false",
                     "-prec-div=true", "-prec-sqrt=true", "-ftz=false", "-o", exe,
-                    os.path.join(HERE, "cuda", "check_quotient.cu")], check=True)
+                    os.path.join(HERE, "cuda", name + ".cu")], check=True)
+    return exe
+
+
+def test_markstein_quotient_equals_division(tmp_path):
+    exe = _build(tmp_path, "check_quotient")
     out = subprocess.run([exe, "16"], check=True, capture_output=True, text=True).stdout
     m = re.search(r"pairs=(\d+) mismatches=(\d+)", out)
     assert m and int(m.group(1)) == 1 << 28, out
     assert int(m.group(2)) == 0, out
+
+
+def test_in_range_sqrt_and_recip_equal_correctly_rounded(tmp_path):
+    exe = _build(tmp_path, "check_sqrt_recip")
+    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
+    m = re.search(r"sqrt=(\d+)/(\d+) recip=(\d+)/(\d+)", out)
+    assert m, out
+    assert int(m.group(1)) == (52 << 23) + 1 and int(m.group(3)) == (26 << 23) + 1, out
+    assert int(m.group(2)) == 0 and int(m.group(4)) == 0, out
