@@ -489,85 +489,22 @@ __global__ void __launch_bounds__(kBlock) kb_coarse(BatchView v) {
 // --------------------------------------------------------------- manybody --
 // FAST: the repulsion quotients come from the reciprocals (quotient_by_recip(k)).
 template <bool FAST>
-__device__ __forceinline__ void kb_manybody_point(const BatchView& v, const GraphDesc& D, uint32_t P, float2 p, float k) {
-  const float px = p.x, py = p.y;
+__device__ __forceinline__ void kb_manybody_point(const BatchView& v, const GraphDesc& D, uint32_t j, uint32_t P,
+                                                  float2 p, float k) {
   const int gf = D.gf, L = D.levels;
-  const int fcx = cell_index(px, D.csf, gf), fcy = cell_index(py, D.csf, gf);
+  const int fcx = cell_index(p.x, D.csf, gf), fcy = cell_index(p.y, D.csf, gf);
   const PairUnits pu = v.units;
   const float4* rec = v.rec + D.rec_off;
   float2 vel = make_float2(0.f, 0.f);
-  {   // level 0 (force-level.frag:70-79)
-    const int sh = L - 1;
-    const int ex = (fcx >> sh) - 1, ey = (fcy >> sh) - 1;
-    float2 lv2 = make_float2(0.f, 0.f);
 #pragma unroll 1
-    for (int jj = 0; jj < 4; ++jj) {
-      const bool row_in = (unsigned)(jj - ey) <= 2u;
-#pragma unroll 1
-      for (int ii = 0; ii < 4; ++ii) {
-        if (row_in && (unsigned)(ii - ex) <= 2u) continue;
-        cell_velocity<FAST>(__ldg(&rec[jj * 4 + ii]), p, k, lv2, pu);
-      }
-    }
-    vel = add2(vel, lv2, pu);
-  }
-#pragma unroll 1
-  for (int l = 1; l < L; ++l) {   // force-level.frag:80-95
-    const int G = 4 << l;
+  for (int l = 0; l < L; ++l) {   // force-level.frag:70-95
     const int sh = L - 1 - l;
-    const int pcx = fcx >> sh, pcy = fcy >> sh;
-    const int bx = (pcx & ~1) - 2, by = (pcy & ~1) - 2;
-    const int ex = pcx - 1, ey = pcy - 1;
-    const float4* lv = rec + level_base(l);
-    float2 lv2 = make_float2(0.f, 0.f);
-#pragma unroll 1
-    for (int jj = 0; jj < 6; ++jj) {
-      const int cy = by + jj;
-      if ((unsigned)cy >= (unsigned)G) continue;
-      const bool row_in = (unsigned)(cy - ey) <= 2u;
-      const float4* row = lv + cy * G;
-#pragma unroll 2   // two cells in flight; wider unrolling measured slower (instruction cache)
-      for (int ii = 0; ii < 6; ++ii) {
-        const int cx = bx + ii;
-        if ((unsigned)cx >= (unsigned)G) continue;
-        if (row_in && (unsigned)(cx - ex) <= 2u) continue;
-        cell_velocity<FAST>(__ldg(&row[cx]), p, k, lv2, pu);
-      }
-    }
-    vel = add2(vel, lv2, pu);
+    vel = add2(vel, level_terms<FAST>(rec + level_base(l), 4 << l, fcx >> sh, fcy >> sh, p, k, pu), pu);
   }
   // near field (force-nearfield.frag:199-263)
   const float2 rj = v.jitter[P];
-  const float4* fine = rec + level_base(L - 1);
-  float2 nf = make_float2(0.f, 0.f);
-#pragma unroll 1
-  for (int jj = -1; jj <= 1; ++jj)
-#pragma unroll 1
-    for (int ii = -1; ii <= 1; ++ii) {
-      const int cx = fcx + ii, cy = fcy + jj;
-      if (cx < 0 || cy < 0 || cx >= gf || cy >= gf) continue;
-      const uint32_t lc = (uint32_t)(cy * gf + cx);
-      const float4 r = __ldg(&fine[lc]);
-      const float others = __fsub_rn(r.z, (ii == 0 && jj == 0) ? 1.0f : 0.0f);
-      if (others <= 0.f) continue;
-      const int ns = (int)r.w;
-      const uint32_t b = __ldg(&v.cell_start[D.cell_off + lc]);
-      float2 sum = make_float2(0.f, 0.f);
-      float sampled = 0.f;
-#pragma unroll 1
-      for (int q = 0; q < kSlots; ++q) {
-        if (q >= ns) break;
-        const uint32_t oi = __ldg(&v.sorted_idx[b + q]);
-        if (oi == P) continue;   // the shader compares f32 indices; below 2^24 they are exact
-        const float2 o = __ldg(&v.sorted_pos[b + q]);
-        sampled = __fadd_rn(sampled, 1.0f);
-        pair_velocity<FAST>(p, o, rj, k, sum, pu);
-      }
-      if (sampled > 0.f) {
-        const float w = __fdiv_rn(others, sampled);
-        nf = add2(nf, mul2(splat(w), sum, pu), pu);
-      }
-    }
+  float2 nf = near_terms<FAST>(rec + level_base(L - 1), v.cell_start + D.cell_off, v.sorted_pos, gf, fcx, fcy, j, p, rj,
+                               k, pu);
   nf = add2(nf, mul2(nf, rj, pu), pu);
   const float max_step = __fmul_rn(2.0f, D.csf);
   const float2 nsq = mul2(nf, nf, pu);
@@ -587,8 +524,8 @@ __global__ void __launch_bounds__(kBlock) kb_manybody(BatchView v) {
   const BatchTick tp = tick_of(v, g);
   const float2 p = v.sorted_pos[j];
   const float k = __fmul_rn(tp.alpha, D.repulsion);
-  if (quotient_by_recip(k)) kb_manybody_point<true>(v, D, P, p, k);
-  else kb_manybody_point<false>(v, D, P, p, k);
+  if (quotient_by_recip(k)) kb_manybody_point<true>(v, D, j, P, p, k);
+  else kb_manybody_point<false>(v, D, j, P, p, k);
 }
 
 // ------------------------------------------------------------------- link --

@@ -603,84 +603,15 @@ __global__ void k_cells(DeviceView d, SimScalars s) {
 }
 
 // --------------------------------------------------------------- manybody --
-// Sum of level l's cell terms for the point at p (force-level.frag:70-95):
-// level 0, every cell of the 4x4 grid outside the 3x3 around the point's
-// cell; level l >= 1, the aligned 6x6 child block minus that 3x3; row order.
 // FAST: the repulsion quotients come from the reciprocals (quotient_by_recip(k),
 // the same for every point of a pass, so each launch runs one of the two).
+
+// Level l's sum for the point in finest cell (fcx, fcy).
 template <bool FAST>
 __device__ __forceinline__ float2 level_sum(const DeviceView& d, int L, int l, int fcx, int fcy, float2 p, float k,
                                             PairUnits pu) {
-  float2 lv2 = make_float2(0.f, 0.f);
-  if (l == 0) {
-    const int sh = L - 1;
-    const int ex = (fcx >> sh) - 1, ey = (fcy >> sh) - 1;   // first column / row of the 3x3
-#pragma unroll 1
-    for (int jj = 0; jj < 4; ++jj) {
-      const bool row_in = (unsigned)(jj - ey) <= 2u;
-#pragma unroll 1
-      for (int ii = 0; ii < 4; ++ii) {
-        if (row_in && (unsigned)(ii - ex) <= 2u) continue;
-        cell_velocity<FAST>(__ldg(&d.rec[jj * 4 + ii]), p, k, lv2, pu);
-      }
-    }
-    return lv2;
-  }
-  const int G = 4 << l;
   const int sh = L - 1 - l;
-  const int pcx = fcx >> sh, pcy = fcy >> sh;
-  const int bx = (pcx & ~1) - 2, by = (pcy & ~1) - 2;
-  const int ex = pcx - 1, ey = pcy - 1;
-  const float4* lv = d.rec + d.level_off[l];
-#pragma unroll 1
-  for (int jj = 0; jj < 6; ++jj) {
-    const int cy = by + jj;
-    if ((unsigned)cy >= (unsigned)G) continue;
-    const bool row_in = (unsigned)(cy - ey) <= 2u;
-    const float4* row = lv + cy * G;
-#pragma unroll 2   // two cells in flight; wider unrolling measured slower (instruction cache)
-    for (int ii = 0; ii < 6; ++ii) {
-      const int cx = bx + ii;
-      if ((unsigned)cx >= (unsigned)G) continue;
-      if (row_in && (unsigned)(cx - ex) <= 2u) continue;
-      cell_velocity<FAST>(__ldg(&row[cx]), p, k, lv2, pu);
-    }
-  }
-  return lv2;
-}
-
-// Near-field cell c of the 3x3 around the point's finest cell (row order,
-// force-nearfield.frag:199-263): (others / sampled) * the sum of its sampled
-// pair terms; adds = false when the cell contributes nothing.
-struct NearTerm {
-  float2 v;
-  bool adds;
-};
-template <bool FAST>
-__device__ __forceinline__ NearTerm near_cell(const DeviceView& d, int gf, int L, int c, int fcx, int fcy, uint32_t i,
-                                              float2 p, float2 rj, float k, PairUnits pu) {
-  const NearTerm none{make_float2(0.f, 0.f), false};
-  const int jj = c / 3 - 1, ii = c % 3 - 1;
-  const int cx = fcx + ii, cy = fcy + jj;
-  if (cx < 0 || cy < 0 || cx >= gf || cy >= gf) return none;
-  const uint32_t cell = (uint32_t)(cy * gf + cx);
-  const float4 r = __ldg(&d.rec[d.level_off[L - 1] + cell]);
-  const float others = __fsub_rn(r.z, (ii == 0 && jj == 0) ? 1.0f : 0.0f);
-  if (others <= 0.f) return none;
-  const int ns = (int)r.w;
-  const uint32_t b = __ldg(&d.cell_start[cell]);
-  float2 sum = make_float2(0.f, 0.f);
-  float sampled = 0.f;
-  for (int q = 0; q < kSlots; ++q) {
-    if (q >= ns) break;
-    const uint32_t oi = __ldg(&d.sorted_idx[b + q]);
-    if (oi == i) continue;   // (float)oi == (float)i: indices below 2^24 are exact in f32
-    const float2 o = __ldg(&d.sorted_pos[b + q]);
-    sampled = __fadd_rn(sampled, 1.0f);
-    pair_velocity<FAST>(p, o, rj, k, sum, pu);
-  }
-  if (!(sampled > 0.f)) return none;
-  return NearTerm{mul2(splat(__fdiv_rn(others, sampled)), sum, pu), true};
+  return level_terms<FAST>(d.rec + d.level_off[l], 4 << l, fcx >> sh, fcy >> sh, p, k, pu);
 }
 
 // force-nearfield.frag:151-157 (jitter, step clamp) and the update.
@@ -695,96 +626,20 @@ __device__ __forceinline__ void finish_point(const DeviceView& d, const SimScala
   if (!(d.flags[i] & kPinned)) d.pos[i] = integrate(p, vel.x, vel.y, s.friction, s.space);
 }
 
-// One point, all of its terms in order on one thread (the level sweep and
-// the near-field cells written out inline: through the helpers above this
-// kernel spills).
+// One point, all of its terms in order on one thread.
 template <bool FAST>
 __device__ __forceinline__ void manybody_point(const DeviceView& d, const SimScalars& s, uint32_t j, float k) {
   const uint32_t i = d.sorted_idx[j];
   const float2 p = d.sorted_pos[j];
-  const float px = p.x, py = p.y;
   const int gf = s.gf, L = s.levels;
-  const int fcx = cell_index(px, s.csf, gf), fcy = cell_index(py, s.csf, gf);
+  const int fcx = cell_index(p.x, s.csf, gf), fcy = cell_index(p.y, s.csf, gf);
   const PairUnits pu = s.units;
   float2 vel = make_float2(0.f, 0.f);
-  {   // level 0 (force-level.frag:70-79): every cell of the 4x4 grid outside the 3x3
-    const int sh = L - 1;
-    const int ex = (fcx >> sh) - 1, ey = (fcy >> sh) - 1;   // first column / row of the 3x3
-    const float4* lv = d.rec;
-    float2 lv2 = make_float2(0.f, 0.f);
 #pragma unroll 1
-    for (int jj = 0; jj < 4; ++jj) {
-      const bool row_in = (unsigned)(jj - ey) <= 2u;
-#pragma unroll 1
-      for (int ii = 0; ii < 4; ++ii) {
-        if (row_in && (unsigned)(ii - ex) <= 2u) continue;
-        cell_velocity<FAST>(__ldg(&lv[jj * 4 + ii]), p, k, lv2, pu);
-      }
-    }
-    vel = add2(vel, lv2, pu);
-  }
-  for (int l = 1; l < L; ++l) {   // force-level.frag:80-95: aligned 6x6 child block minus the 3x3
-    const int G = 4 << l;
-    const int sh = L - 1 - l;
-    const int pcx = fcx >> sh, pcy = fcy >> sh;
-    const int bx = (pcx & ~1) - 2, by = (pcy & ~1) - 2;
-    const int ex = pcx - 1, ey = pcy - 1;
-    const float4* lv = d.rec + d.level_off[l];
-    float2 lv2 = make_float2(0.f, 0.f);
-#pragma unroll 1
-    for (int jj = 0; jj < 6; ++jj) {
-      const int cy = by + jj;
-      if ((unsigned)cy >= (unsigned)G) continue;
-      const bool row_in = (unsigned)(cy - ey) <= 2u;
-      const float4* row = lv + cy * G;
-#pragma unroll 2   // two cells in flight; wider unrolling measured slower (instruction cache)
-      for (int ii = 0; ii < 6; ++ii) {
-        const int cx = bx + ii;
-        if ((unsigned)cx >= (unsigned)G) continue;
-        if (row_in && (unsigned)(cx - ex) <= 2u) continue;
-        cell_velocity<FAST>(__ldg(&row[cx]), p, k, lv2, pu);
-      }
-    }
-    vel = add2(vel, lv2, pu);
-  }
-  // near field (force-nearfield.frag:199-263)
+  for (int l = 0; l < L; ++l) vel = add2(vel, level_sum<FAST>(d, L, l, fcx, fcy, p, k, pu), pu);
   const float2 rj = d.jitter[i];
-  const float4* fine = d.rec + d.level_off[L - 1];
-  float2 nf = make_float2(0.f, 0.f);
-#pragma unroll 1
-  for (int jj = -1; jj <= 1; ++jj)
-#pragma unroll 1
-    for (int ii = -1; ii <= 1; ++ii) {
-      const int cx = fcx + ii, cy = fcy + jj;
-      if (cx < 0 || cy < 0 || cx >= gf || cy >= gf) continue;
-      const uint32_t c = (uint32_t)(cy * gf + cx);
-      const float4 r = __ldg(&fine[c]);
-      const float others = __fsub_rn(r.z, (ii == 0 && jj == 0) ? 1.0f : 0.0f);
-      if (others <= 0.f) continue;
-      const int ns = (int)r.w;
-      const uint32_t b = __ldg(&d.cell_start[c]);
-      float2 sum = make_float2(0.f, 0.f);
-      float sampled = 0.f;
-      for (int q = 0; q < kSlots; ++q) {
-        if (q >= ns) break;
-        const uint32_t oi = __ldg(&d.sorted_idx[b + q]);
-        if (oi == i) continue;   // (float)oi == (float)i: indices below 2^24 are exact in f32
-        const float2 o = __ldg(&d.sorted_pos[b + q]);
-        sampled = __fadd_rn(sampled, 1.0f);
-        pair_velocity<FAST>(p, o, rj, k, sum, pu);
-      }
-      if (sampled > 0.f) {
-        const float w = __fdiv_rn(others, sampled);
-        nf = add2(nf, mul2(splat(w), sum, pu), pu);
-      }
-    }
-  nf = add2(nf, mul2(nf, rj, pu), pu);
-  const float max_step = __fmul_rn(2.0f, s.csf);
-  const float2 nsq = mul2(nf, nf, pu);
-  const float speed = __fsqrt_rn(__fadd_rn(nsq.x, nsq.y));
-  if (speed > max_step) nf = mul2(nf, splat(__fdiv_rn(max_step, speed)), pu);
-  vel = add2(vel, nf, pu);
-  if (!(d.flags[i] & kPinned)) d.pos[i] = integrate(p, vel.x, vel.y, s.friction, s.space);
+  const float2 nf = near_terms<FAST>(d.rec + d.level_off[L - 1], d.cell_start, d.sorted_pos, gf, fcx, fcy, j, p, rj, k, pu);
+  finish_point(d, s, i, p, rj, vel, nf, pu);
 }
 
 // Small graphs: each point's level sums and near-field cells are independent
@@ -816,14 +671,11 @@ __device__ __forceinline__ void manybody_split(const DeviceView& d, const SimSca
       if (part < L) lvs[pt][part] = level_sum<FAST>(d, L, part, fcx, fcy, p, k, pu);
     } else {
       const float2 rj = d.jitter[i];
-      const NearTerm t = near_cell<FAST>(d, gf, L, part, fcx, fcy, i, p, rj, k, pu);
-      nfs[pt][part] = t.v;
-      nfa[pt][part] = t.adds;
-      if (part == 0) {
-        const NearTerm t8 = near_cell<FAST>(d, gf, L, 8, fcx, fcy, i, p, rj, k, pu);
-        nfs[pt][8] = t8.v;
-        nfa[pt][8] = t8.adds;
-      }
+      const float4* fine = d.rec + d.level_off[L - 1];
+#pragma unroll 1
+      for (int c = part; c < 9; c += 8)
+        nfa[pt][c] = near_cell_terms<FAST>(fine, d.cell_start, d.sorted_pos, gf, fcx, fcy, c % 3 - 1, c / 3 - 1, j, p,
+                                           rj, k, pu, nfs[pt][c]);
     }
   }
   __syncthreads();
@@ -852,7 +704,7 @@ __global__ void __launch_bounds__(kBlock) k_manybody_split(DeviceView d, SimScal
   else manybody_split<false>(d, s, k, lvs, nfs, nfa);
 }
 
-__global__ void __launch_bounds__(kBlock) k_manybody(DeviceView d, SimScalars s) {
+__global__ void __launch_bounds__(kBlock, 6) k_manybody(DeviceView d, SimScalars s) {
   const TickParams tp = tick_params(d);
   const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t total = d.cell_start[s.gf * s.gf];
