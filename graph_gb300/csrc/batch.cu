@@ -358,7 +358,7 @@ cgl_status cgl_batch_create(int32_t device, double hbm_budget_bytes, cgl_batch**
     return CGL_CUDA_ERROR;
   }
   cgl_status st;
-  if ((st = grow(b, b->big_count, 8, 0, 0)) || (st = grow(b, b->tick_ctr, 4, 0, 0)) ||
+  if ((st = grow(b, b->big_count, 16, 0, 0)) || (st = grow(b, b->tick_ctr, 4, 0, 0)) ||
       (st = reserve_cells(b, 1024)) || (st = reserve_points(b, 1024))) {
     cgl_batch_destroy(b);
     return st;

@@ -61,8 +61,9 @@ struct BatchView {
   uint32_t* cell_start;        // [cell arena + 1]
   uint32_t* scan1;             // scan partials per 1024 cells, then per 1024^2
   uint32_t* scan2;
-  uint32_t* big_list;          // [2 x cell arena] CTA cells, then warp cells
-  uint32_t* big_count;         // [2]
+  uint32_t* big_list;          // [2 x cell arena] CTA cells, then warp cells: those above
+                               // kWarpSmallCell from the front, the others from the back
+  uint32_t* big_count;         // [4] CTA cells, heavy and light warp cells, warp-cell ticket
   long long* big_sx;
   long long* big_sy;
   uint32_t* big_ns;

@@ -7,6 +7,7 @@
 // are graph-local, so a graph advances exactly as it would alone.
 #include "batch.cuh"
 #include "device_util.cuh"
+#include "warp_cells.cuh"
 
 namespace cgl {
 namespace {
@@ -115,7 +116,8 @@ __global__ void __launch_bounds__(kBlock) kb_scan_cells(BatchView v, const uint3
       v.cell_start[c] = o;
       v.counts[c] = 0;
       if (x[k] > kBigCell) v.big_list[atomicAdd(&v.big_count[0], 1u)] = c;
-      else if (x[k] > kSmallCell) v.big_list[n + atomicAdd(&v.big_count[1], 1u)] = c;
+      else if (x[k] > kWarpSmallCell) v.big_list[n + atomicAdd(&v.big_count[1], 1u)] = c;
+      else if (x[k] > kSmallCell) v.big_list[2 * n - 1 - atomicAdd(&v.big_count[2], 1u)] = c;
     }
     o += x[k];
   }
@@ -157,133 +159,6 @@ __device__ void kb_move_head(const BatchView& v, uint32_t b, int ns, uint32_t (&
       }
     }
   }
-}
-
-__device__ void kb_warp_cell(const BatchView& v, uint32_t c) {
-  const int lane = threadIdx.x & 31;
-  const uint32_t g = v.cell_gid[c];
-  const GraphDesc& D = v.desc[g];
-  const uint32_t seed = tick_of(v, g).seed_bits;
-  const uint32_t b = v.cell_start[c], e = v.cell_start[c + 1];
-  long long ax = 0, ay = 0;
-  uint32_t sel[kSlots];
-  int ns = 0;
-  if (e - b <= 128) {   // at most 4 points per lane: select from the keys in registers (kernels.cu warp_cell_small)
-    unsigned long long key[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const uint32_t j = b + lane + 32u * u;
-      key[u] = ~0ull;
-      if (j < e) {
-        const float2 p = v.sorted_pos[j];
-        ax += to_fixed(p.x, D.fx);
-        ay += to_fixed(p.y, D.fx);
-        key[u] = local_key(v.sorted_idx[j], D.p_off, seed);
-      }
-    }
-    ax = warp_sum_ll(ax);
-    ay = warp_sum_ll(ay);
-    unsigned long long last = 0;
-#pragma unroll
-    for (int k = 0; k < kSlots; ++k) {
-      unsigned long long m = ~0ull;
-      uint32_t mp = 0;
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-        if (key[u] != ~0ull && (k == 0 || (key[u] >> 32) > (last >> 32)) && key[u] < m) {
-          m = key[u];
-          mp = b + lane + 32u * u;
-        }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long om = __shfl_xor_sync(0xffffffffu, m, o);
-        const uint32_t op = __shfl_xor_sync(0xffffffffu, mp, o);
-        if (om < m) { m = om; mp = op; }
-      }
-      sel[k] = mp;
-      if (m != ~0ull) { ns = k + 1; last = m; }
-      else last = ~0ull;
-    }
-  } else {
-    unsigned long long best[kSlots];
-    uint32_t at[kSlots];
-#pragma unroll
-    for (int q = 0; q < kSlots; ++q) { best[q] = ~0ull; at[q] = 0; }
-    uint32_t j = b + lane;
-    for (; j + 96 < e; j += 128) {   // loads four points ahead of the selection
-      float2 p[4];
-      uint32_t ix[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) { p[u] = v.sorted_pos[j + 32 * u]; ix[u] = v.sorted_idx[j + 32 * u]; }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        ax += to_fixed(p[u].x, D.fx);
-        ay += to_fixed(p[u].y, D.fx);
-        top8_insert(best, at, local_key(ix[u], D.p_off, seed), j + 32 * u);
-      }
-    }
-    for (; j < e; j += 32) {
-      const float2 p = v.sorted_pos[j];
-      ax += to_fixed(p.x, D.fx);
-      ay += to_fixed(p.y, D.fx);
-      top8_insert(best, at, local_key(v.sorted_idx[j], D.p_off, seed), j);
-    }
-    ax = warp_sum_ll(ax);
-    ay = warp_sum_ll(ay);
-    unsigned long long last = 0;
-#pragma unroll
-    for (int k = 0; k < kSlots; ++k) {
-      unsigned long long m = ~0ull;
-      uint32_t mp = 0;
-#pragma unroll
-      for (int q = 0; q < kSlots; ++q)
-        if (best[q] != ~0ull && (k == 0 || (best[q] >> 32) > (last >> 32)) && best[q] < m) { m = best[q]; mp = at[q]; }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long om = __shfl_xor_sync(0xffffffffu, m, o);
-        const uint32_t op = __shfl_xor_sync(0xffffffffu, mp, o);
-        if (om < m) { m = om; mp = op; }
-      }
-      sel[k] = mp;
-      if (m != ~0ull) { ns = k + 1; last = m; }
-      else last = ~0ull;
-    }
-  }
-  // parallel move of the slots to the head (see kernels.cu warp_cell)
-  const uint32_t h = b + (uint32_t)lane;
-  bool h_selected = false, sel_outside = false;
-#pragma unroll
-  for (int k = 0; k < kSlots; ++k) {
-    if (k < ns && sel[k] == h) h_selected = true;
-    if (k == lane) sel_outside = k < ns && (sel[k] < b || sel[k] >= b + (uint32_t)ns);
-  }
-  const unsigned out_mask = __ballot_sync(0xffffffffu, sel_outside);
-  const bool in_head = lane < ns;
-  const bool displaced = in_head && !h_selected;
-  const unsigned disp_mask = __ballot_sync(0xffffffffu, displaced);
-  uint32_t take_idx = 0, disp_idx = 0, dest = 0;
-  float2 take_pos = make_float2(0.f, 0.f), disp_pos = make_float2(0.f, 0.f);
-  if (in_head) {
-    uint32_t src = 0;
-#pragma unroll
-    for (int k = 0; k < kSlots; ++k) if (k == lane) src = sel[k];
-    take_idx = v.sorted_idx[src];
-    take_pos = v.sorted_pos[src];
-  }
-  if (displaced) {
-    const int r = __popc(disp_mask & ((1u << lane) - 1u));
-    unsigned m = out_mask;
-    for (int t = 0; t < r; ++t) m &= m - 1u;
-    const int k = __ffs(m) - 1;
-#pragma unroll
-    for (int kk = 0; kk < kSlots; ++kk) if (kk == k) dest = sel[kk];
-    disp_idx = v.sorted_idx[h];
-    disp_pos = v.sorted_pos[h];
-  }
-  __syncwarp();
-  if (in_head) { v.sorted_idx[h] = take_idx; v.sorted_pos[h] = take_pos; }
-  if (displaced) { v.sorted_idx[dest] = disp_idx; v.sorted_pos[dest] = disp_pos; }
-  if (lane == 0) { v.big_sx[c] = ax; v.big_sy[c] = ay; v.big_ns[c] = (uint32_t)ns; }
 }
 
 __global__ void __launch_bounds__(kBlock) kb_bigcells(BatchView v) {
@@ -366,9 +241,21 @@ __global__ void __launch_bounds__(kBlock) kb_bigcells(BatchView v) {
     }
     __syncthreads();
   }
-  const uint32_t nmid = v.big_count[1];
-  const uint32_t wid = blockIdx.x * (blockDim.x >> 5) + w, nw = gridDim.x * (blockDim.x >> 5);
-  for (uint32_t wi = wid; wi < nmid; wi += nw) kb_warp_cell(v, v.big_list[v.cell_hwm + wi]);
+  // warp cells (warp_cells.cuh), one warp each, taken from a ticket: the heavy
+  // ones (above kWarpSmallCell points) first, so the longest start first
+  __shared__ uint32_t cand[kBlock / 32][3][kCandidates];
+  const uint32_t nheavy = v.big_count[1], nwarp = nheavy + v.big_count[2];
+  const uint32_t n = v.cell_hwm;
+  for (;;) {
+    uint32_t wi = 0;
+    if (lane == 0) wi = atomicAdd(&v.big_count[3], 1u);
+    wi = __shfl_sync(0xffffffffu, wi, 0);
+    if (wi >= nwarp) break;
+    const uint32_t c = wi < nheavy ? v.big_list[n + wi] : v.big_list[2 * n - 1 - (wi - nheavy)];
+    const uint32_t g = v.cell_gid[c];
+    const GraphDesc& D = v.desc[g];
+    warp_cell(v, D.fx, tick_of(v, g).seed_bits, D.p_off, c, cand[w]);
+  }
 }
 
 // One CTA per (graph, tile) of the work list; thread per finest cell of the
@@ -596,7 +483,7 @@ inline uint32_t blocks(uint32_t n) { return (n + kBlock - 1) / kBlock; }
 }  // namespace
 
 void batch_launch_tick(const BatchView& v, cudaStream_t st, cudaStream_t side, cudaEvent_t* fork, cudaEvent_t* join) {
-  cudaMemsetAsync(v.big_count, 0, 2 * sizeof(uint32_t), st);
+  cudaMemsetAsync(v.big_count, 0, 4 * sizeof(uint32_t), st);
   if (v.point_hwm) kb_prepass<<<blocks(v.point_hwm), kBlock, 0, st>>>(v);
   if (v.cell_hwm) {
     const uint32_t n1 = (v.cell_hwm + kChunk - 1) / kChunk;   // partials of 1024 cells

@@ -77,6 +77,43 @@ __device__ __forceinline__ void top8_insert(unsigned long long (&best)[kSlots], 
   }
 }
 
+// The slot selection of one warp cell from candidates held in registers, up
+// to 4 per lane: hash bits (~0u: none; hashes lie in [0, 1), so no hash has
+// those bits), point index and segment position.  Round k takes the smallest
+// hash above the last one taken, then the lowest index among the keys with
+// that hash: the order of the keys (hash << 32 | index) that top8_insert
+// keeps, found with two 32-bit warp minimums (redux) per round.
+__device__ __forceinline__ int warp_select_slots(const uint32_t (&hb)[4], const uint32_t (&ix)[4],
+                                                 const uint32_t (&at)[4], uint32_t (&sel)[kSlots]) {
+  int ns = 0;
+  uint32_t last = 0;
+#pragma unroll
+  for (int k = 0; k < kSlots; ++k) sel[k] = 0;
+#pragma unroll
+  for (int k = 0; k < kSlots; ++k) {
+    uint32_t mh = ~0u;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if ((k == 0 || hb[u] > last) && hb[u] < mh) mh = hb[u];
+    const uint32_t gh = __reduce_min_sync(0xffffffffu, mh);
+    if (gh == ~0u) break;   // warp-uniform: no hash left
+    uint32_t mi = ~0u;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (hb[u] == gh && ix[u] < mi) mi = ix[u];
+    const uint32_t gi = __reduce_min_sync(0xffffffffu, mi);
+    uint32_t mp = 0;
+    bool has = false;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (hb[u] == gh && ix[u] == gi) { mp = at[u]; has = true; }
+    sel[k] = __shfl_sync(0xffffffffu, mp, __ffs(__ballot_sync(0xffffffffu, has)) - 1);
+    ns = k + 1;
+    last = gh;
+  }
+  return ns;
+}
+
 __device__ __forceinline__ unsigned long long peel_key(uint32_t idx, uint32_t seed_bits) {
   return ((unsigned long long)__float_as_uint(peel_hash(idx, seed_bits)) << 32) | idx;
 }

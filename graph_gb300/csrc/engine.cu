@@ -304,7 +304,7 @@ cgl_status enqueue_tick(cgl_engine* e, cudaStream_t st, cudaEvent_t* ev) {
     if (ev) cudaEventRecord(ev[2 * stage + which], st);
   };
   if (p.cent) CU(cudaMemsetAsync(d.centroid, 0, 3 * sizeof(long long), st));
-  if (p.mb) CU(cudaMemsetAsync(d.big_count, 0, 2 * sizeof(uint32_t), st));
+  if (p.mb) CU(cudaMemsetAsync(d.big_count, 0, 4 * sizeof(uint32_t), st));
   uint32_t mode = 0;
   if (p.grav) mode |= kPreGravity;
   if (p.cent) mode |= kPreCentroid;
@@ -636,7 +636,7 @@ cgl_status do_render(cgl_engine* e, double alpha) {
       if ((st = dev_reserve(e, e->b_acc, 3 * (size_t)aoff * sizeof(long long), true))) return st;
       if ((st = dev_reserve(e, e->b_centroid, 3 * sizeof(long long), true))) return st;
       if ((st = dev_reserve(e, e->b_big_list, 2 * (size_t)cells * sizeof(uint32_t), false))) return st;
-      if ((st = dev_reserve(e, e->b_big_count, 2 * sizeof(uint32_t), true))) return st;
+      if ((st = dev_reserve(e, e->b_big_count, 4 * sizeof(uint32_t), true))) return st;
       if ((st = dev_reserve(e, e->b_big_sx, cells * sizeof(long long), false))) return st;
       if ((st = dev_reserve(e, e->b_big_sy, cells * sizeof(long long), false))) return st;
       if ((st = dev_reserve(e, e->b_big_ns, cells * sizeof(uint32_t), false))) return st;

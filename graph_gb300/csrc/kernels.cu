@@ -24,6 +24,7 @@
 // renderer's position texture.
 #include "device_util.cuh"
 #include "kernels.cuh"
+#include "warp_cells.cuh"
 
 namespace cgl {
 
@@ -189,7 +190,8 @@ __global__ void __launch_bounds__(kBlock) k_scan_down(DeviceView d, uint32_t cel
       d.cell_start[c] = off;
       d.counts[c] = 0;   // histogram ready for the next tick
       if (v[k] > kBigCell) d.big_list[atomicAdd(&d.big_count[0], 1u)] = c;
-      else if (v[k] > kSmallCell) d.big_list[cells + atomicAdd(&d.big_count[1], 1u)] = c;
+      else if (v[k] > kWarpSmallCell) d.big_list[cells + atomicAdd(&d.big_count[1], 1u)] = c;
+      else if (v[k] > kSmallCell) d.big_list[2 * cells - 1 - atomicAdd(&d.big_count[2], 1u)] = c;
     }
     off += v[k];
   }
@@ -229,166 +231,10 @@ __device__ __forceinline__ void move_slots_to_head(const DeviceView& d, uint32_t
 }
 
 // Cells holding more than kSmallCell points (lists built by the scan): above
-// kBigCell one CTA per cell, otherwise one warp per cell, so a dense hub cell
-// does not serialise on one thread.  Exact sums by warp/block reduction; slots
-// by per-thread top-8 lists merged in 8 rounds of a minimum over keys whose
-// hash is larger than the previous slot's.  Every global top-8 key is in the
-// top-8 of the thread that holds it, so the merge is exact.
-// The end of a warp cell: move the selected slots to the head of its segment
-// and write its sums and slot count (lane-parallel, see warp_cell).
-__device__ __forceinline__ void warp_finish_cell(const DeviceView& d, uint32_t c, uint32_t b, int ns,
-                                                 const uint32_t (&sel)[kSlots], long long ax, long long ay) {
-  const int lane = threadIdx.x & 31;
-  // Move the slots to the head [b, b + ns) in slot order, in parallel: lane q
-  // takes slot q's entry; a head entry that is not a slot moves to the place
-  // of the r-th slot that lies outside the head (r = its rank among them).
-  uint32_t take_idx = 0, disp_idx = 0, dest = 0;
-  float2 take_pos = make_float2(0.f, 0.f), disp_pos = make_float2(0.f, 0.f);
-  bool displaced = false;
-  const uint32_t h = b + (uint32_t)lane;
-  bool h_selected = false, sel_outside = false;
-#pragma unroll
-  for (int k = 0; k < kSlots; ++k) {
-    if (k < ns && sel[k] == h) h_selected = true;
-    if (k == lane) sel_outside = k < ns && (sel[k] < b || sel[k] >= b + (uint32_t)ns);
-  }
-  const unsigned out_mask = __ballot_sync(0xffffffffu, sel_outside);
-  const bool in_head = lane < ns;
-  displaced = in_head && !h_selected;
-  const unsigned disp_mask = __ballot_sync(0xffffffffu, displaced);
-  if (in_head) {
-    uint32_t src = 0;
-#pragma unroll
-    for (int k = 0; k < kSlots; ++k) if (k == lane) src = sel[k];
-    take_idx = d.sorted_idx[src];
-    take_pos = d.sorted_pos[src];
-  }
-  if (displaced) {
-    const int r = __popc(disp_mask & ((1u << lane) - 1u));
-    unsigned m = out_mask;
-    for (int t = 0; t < r; ++t) m &= m - 1u;
-    const int k = __ffs(m) - 1;
-#pragma unroll
-    for (int kk = 0; kk < kSlots; ++kk) if (kk == k) dest = sel[kk];
-    disp_idx = d.sorted_idx[h];
-    disp_pos = d.sorted_pos[h];
-  }
-  __syncwarp();
-  if (in_head) {
-    d.sorted_idx[h] = take_idx;
-    d.sorted_pos[h] = take_pos;
-  }
-  if (displaced) {
-    d.sorted_idx[dest] = disp_idx;
-    d.sorted_pos[dest] = disp_pos;
-  }
-  if (lane == 0) {
-    d.big_sx[c] = ax;
-    d.big_sy[c] = ay;
-    d.big_ns[c] = (uint32_t)ns;
-  }
-}
-
-__device__ void warp_cell(const DeviceView& d, const SimScalars& s, uint32_t seed_bits, uint32_t c) {
-  const int lane = threadIdx.x & 31;
-  const uint32_t b = d.cell_start[c], e = d.cell_start[c + 1];
-  long long ax = 0, ay = 0;
-  unsigned long long best[kSlots];
-  uint32_t at[kSlots];
-#pragma unroll
-  for (int q = 0; q < kSlots; ++q) { best[q] = ~0ull; at[q] = 0; }
-  uint32_t j = b + lane;
-  for (; j + 96 < e; j += 128) {   // loads four points ahead of the selection
-    float2 p[4];
-    uint32_t ix[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) { p[u] = d.sorted_pos[j + 32 * u]; ix[u] = d.sorted_idx[j + 32 * u]; }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      ax += to_fixed(p[u].x, s.fx);
-      ay += to_fixed(p[u].y, s.fx);
-      top8_insert(best, at, peel_key(ix[u], seed_bits), j + 32 * u);
-    }
-  }
-  for (; j < e; j += 32) {
-    const float2 p = d.sorted_pos[j];
-    ax += to_fixed(p.x, s.fx);
-    ay += to_fixed(p.y, s.fx);
-    top8_insert(best, at, peel_key(d.sorted_idx[j], seed_bits), j);
-  }
-  ax = warp_sum_ll(ax);
-  ay = warp_sum_ll(ay);
-  uint32_t sel[kSlots];
-  int ns = 0;
-  unsigned long long last = 0;
-#pragma unroll
-  for (int k = 0; k < kSlots; ++k) {
-    unsigned long long m = ~0ull;
-    uint32_t mp = 0;
-#pragma unroll
-    for (int q = 0; q < kSlots; ++q)
-      if (best[q] != ~0ull && (k == 0 || (best[q] >> 32) > (last >> 32)) && best[q] < m) { m = best[q]; mp = at[q]; }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const unsigned long long om = __shfl_xor_sync(0xffffffffu, m, o);
-      const uint32_t op = __shfl_xor_sync(0xffffffffu, mp, o);
-      if (om < m) { m = om; mp = op; }
-    }
-    sel[k] = mp;
-    if (m != ~0ull) { ns = k + 1; last = m; }
-    else last = ~0ull;
-  }
-  warp_finish_cell(d, c, b, ns, sel, ax, ay);
-}
-
-// A cell of at most 128 points: each lane holds at most 4 keys in registers,
-// so the 8 selection rounds scan them directly (the smallest key whose hash
-// exceeds the last one taken, then the warp minimum) instead of keeping a
-// sorted list per lane; the slots and sums are the same.
-__device__ void warp_cell_small(const DeviceView& d, const SimScalars& s, uint32_t seed_bits, uint32_t c, uint32_t b,
-                                uint32_t e) {
-  const int lane = threadIdx.x & 31;
-  unsigned long long key[4];
-  long long ax = 0, ay = 0;
-#pragma unroll
-  for (int u = 0; u < 4; ++u) {
-    const uint32_t j = b + lane + 32u * u;
-    key[u] = ~0ull;
-    if (j < e) {
-      const float2 p = d.sorted_pos[j];
-      ax += to_fixed(p.x, s.fx);
-      ay += to_fixed(p.y, s.fx);
-      key[u] = peel_key(d.sorted_idx[j], seed_bits);
-    }
-  }
-  ax = warp_sum_ll(ax);
-  ay = warp_sum_ll(ay);
-  uint32_t sel[kSlots];
-  int ns = 0;
-  unsigned long long last = 0;
-#pragma unroll
-  for (int k = 0; k < kSlots; ++k) {
-    unsigned long long m = ~0ull;
-    uint32_t mp = 0;
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-      if (key[u] != ~0ull && (k == 0 || (key[u] >> 32) > (last >> 32)) && key[u] < m) {
-        m = key[u];
-        mp = b + lane + 32u * u;
-      }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const unsigned long long om = __shfl_xor_sync(0xffffffffu, m, o);
-      const uint32_t op = __shfl_xor_sync(0xffffffffu, mp, o);
-      if (om < m) { m = om; mp = op; }
-    }
-    sel[k] = mp;
-    if (m != ~0ull) { ns = k + 1; last = m; }
-    else last = ~0ull;
-  }
-  warp_finish_cell(d, c, b, ns, sel, ax, ay);
-}
-
+// kBigCell one CTA per cell, otherwise one warp per cell (warp_cells.cuh), so a
+// dense hub cell does not serialise on one thread.  The CTA cells: exact sums
+// by block reduction; slots by per-thread top-8 lists merged in 8 rounds of a
+// block minimum over keys whose hash is larger than the previous slot's.
 __global__ void __launch_bounds__(kBlock) k_bigcells(DeviceView d, SimScalars s) {
   __shared__ unsigned long long skey[kBlock * kSlots];
   __shared__ uint32_t spos[kBlock * kSlots];
@@ -467,15 +313,18 @@ __global__ void __launch_bounds__(kBlock) k_bigcells(DeviceView d, SimScalars s)
     }
     __syncthreads();
   }
-  // medium cells: one warp each
-  const uint32_t nmid = d.big_count[1];
+  // warp cells, one warp each, taken from a ticket: the heavy ones (above
+  // kWarpSmallCell points) first, so the longest start first
+  __shared__ uint32_t cand[kBlock / 32][3][kCandidates];
+  const uint32_t nheavy = d.big_count[1], nwarp = nheavy + d.big_count[2];
   const uint32_t cells = (uint32_t)(s.gf * s.gf);
-  const uint32_t wid = blockIdx.x * (blockDim.x >> 5) + w, nw = gridDim.x * (blockDim.x >> 5);
-  for (uint32_t wi = wid; wi < nmid; wi += nw) {
-    const uint32_t c = d.big_list[cells + wi];
-    const uint32_t b = d.cell_start[c], e = d.cell_start[c + 1];
-    if (e - b <= 128) warp_cell_small(d, s, tp.seed_bits, c, b, e);   // warp-uniform
-    else warp_cell(d, s, tp.seed_bits, c);
+  for (;;) {
+    uint32_t wi = 0;
+    if (lane == 0) wi = atomicAdd(&d.big_count[3], 1u);
+    wi = __shfl_sync(0xffffffffu, wi, 0);
+    if (wi >= nwarp) break;
+    const uint32_t c = wi < nheavy ? d.big_list[cells + wi] : d.big_list[2 * cells - 1 - (wi - nheavy)];
+    warp_cell(d, s.fx, tp.seed_bits, 0u, c, cand[w]);
   }
 }
 

@@ -34,8 +34,10 @@ struct DeviceView {
   long long* acc;             // coarse-level integer sums (x, y, count) per cell, levels < tile level
   uint32_t acc_off[10];       // offset (in cells) of level l in acc
   uint32_t* cells_ticket;     // last-block ticket of the cell kernel
-  uint32_t* big_list;         // [G^2] cells above kBigCell, then [G^2] cells above kSmallCell
-  uint32_t* big_count;        // entries of the two lists this tick (zeroed at tick start)
+  uint32_t* big_list;         // [G^2] cells above kBigCell, then [G^2] warp cells: those above
+                              // kWarpSmallCell from the front, the others above kSmallCell from the back
+  uint32_t* big_count;        // [4] CTA cells, heavy and light warp cells this tick, warp-cell
+                              // ticket (zeroed at tick start)
   long long* big_sx;          // exact sums of big cells [G^2]
   long long* big_sy;
   uint32_t* big_ns;           // slots of big cells [G^2]
