@@ -94,6 +94,7 @@ struct cgl_engine {
   DevBuf b_big_list, b_big_count, b_big_sx, b_big_sy, b_big_ns;
   DevBuf b_params, b_tick_ctr;
   DevBuf b_rowptr_in, b_rowptr_out, b_ent_in, b_ent_out, b_heavy_in, b_heavy_out;
+  DevBuf b_woff_in, b_woff_out, b_lane_ent_in, b_lane_ent_out;   // light rows by warps (kernels.cuh)
   uint32_t n_heavy_in = 0, n_heavy_out = 0;
   DevBuf b_size, b_cgrid_acc, b_cgrid;
   DevBuf b_cl_of, b_cl_coeff, b_cl_custom, b_cl_acc;
@@ -177,7 +178,8 @@ void dev_free_all(cgl_engine* e) {
                    &e->b_rowptr_in, &e->b_rowptr_out, &e->b_ent_in, &e->b_ent_out, &e->b_size,
                    &e->b_cgrid_acc, &e->b_cgrid, &e->b_big_list, &e->b_big_count,
                    &e->b_big_sx, &e->b_big_sy, &e->b_big_ns, &e->b_heavy_in, &e->b_heavy_out,
-                   &e->b_cl_of, &e->b_cl_coeff, &e->b_cl_custom, &e->b_cl_acc, &e->b_texture};
+                   &e->b_cl_of, &e->b_cl_coeff, &e->b_cl_custom, &e->b_cl_acc, &e->b_texture,
+                   &e->b_woff_in, &e->b_woff_out, &e->b_lane_ent_in, &e->b_lane_ent_out};
   for (DevBuf* b : all) {
     if (b->p) cudaFree(b->p);
     b->p = nullptr;
@@ -236,6 +238,10 @@ void refresh_view(cgl_engine* e) {
   d.heavy_out = (const uint32_t*)e->b_heavy_out.p;
   d.n_heavy_in = e->n_heavy_in;
   d.n_heavy_out = e->n_heavy_out;
+  d.woff_in = (const uint32_t*)e->b_woff_in.p;
+  d.lane_ent_in = (const uint4*)e->b_lane_ent_in.p;
+  d.woff_out = (const uint32_t*)e->b_woff_out.p;
+  d.lane_ent_out = (const uint4*)e->b_lane_ent_out.p;
   d.size = (const float*)e->b_size.p;
   d.cgrid_acc = (long long*)e->b_cgrid_acc.p;
   d.cgrid = (float4*)e->b_cgrid.p;
@@ -564,6 +570,45 @@ cgl_status build_links_device(cgl_engine* e, uint64_t E64, size_t n) {
 }
 #undef TCU
 
+// The light rows of both directions by warps (DeviceView::woff_*, lane_ent_*),
+// from the CSR and the order: a warp's block holds entry k of its 32 lists at
+// 32 k + lane, so the link pass loads one entry of every lane at once.
+cgl_status build_link_warps(cgl_engine* e) {
+  const uint32_t n = (uint32_t)e->N;
+  cudaStream_t st = e->stream;
+  DevBuf t_tmp;
+  cgl_status rc = CGL_OK;
+  for (int dir = 0; dir < 2 && rc == CGL_OK; ++dir) {
+    const uint32_t nhub = dir == 0 ? e->n_heavy_in : e->n_heavy_out;
+    const uint32_t nw = (n - nhub + 31) / 32;
+    DevBuf& woff = dir == 0 ? e->b_woff_in : e->b_woff_out;
+    DevBuf& lanes = dir == 0 ? e->b_lane_ent_in : e->b_lane_ent_out;
+    const uint32_t* order = (const uint32_t*)(dir == 0 ? e->b_heavy_in.p : e->b_heavy_out.p);
+    const uint32_t* rowptr = (const uint32_t*)(dir == 0 ? e->b_rowptr_in.p : e->b_rowptr_out.p);
+    const uint4* ent = (const uint4*)(dir == 0 ? e->b_ent_in.p : e->b_ent_out.p);
+    if ((rc = dev_reserve(e, woff, (nw + 1) * sizeof(uint32_t), true))) break;
+    if ((rc = dev_reserve(e, t_tmp, dingest::scan_temp_words(nw + 1) * sizeof(uint32_t), false))) break;
+    uint32_t total = 0;
+    if (nw) {
+      launch_warp_lengths(order, rowptr, nhub, n, (uint32_t*)woff.p, st);
+      dingest::scan_exclusive((uint32_t*)woff.p, nw + 1, (uint32_t*)t_tmp.p, st);
+      cudaError_t err = cudaMemcpyAsync(&total, (uint32_t*)woff.p + nw, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+      if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+      if (err != cudaSuccess) { rc = fail(e, CGL_CUDA_ERROR, "link warp layout: %s", cudaGetErrorString(err)); break; }
+    }
+    if ((rc = dev_reserve(e, lanes, std::max<size_t>(total, 1) * sizeof(uint4), false))) break;
+    if (total) launch_fill_lanes(order, rowptr, ent, nhub, n, (const uint32_t*)woff.p, (uint4*)lanes.p, st);
+    const cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) rc = fail(e, CGL_CUDA_ERROR, "link warp layout: %s", cudaGetErrorString(err));
+  }
+  if (rc == CGL_OK) {
+    const cudaError_t err = cudaStreamSynchronize(st);
+    if (err != cudaSuccess) rc = fail(e, CGL_CUDA_ERROR, "link warp layout: %s", cudaGetErrorString(err));
+  }
+  dev_release(e, t_tmp);
+  return rc;
+}
+
 cgl_status apply_pinned(cgl_engine* e) {
   // Points.updatePinnedStatus (Points/index.ts:1264-1277) -> device flags
   e->pinned.assign(e->N, 0);
@@ -706,6 +751,7 @@ cgl_status do_render(cgl_engine* e, double alpha) {
       CU(cudaMemcpyAsync(e->b_ent_out.p, en_out.data(), en_out.size() * sizeof(uint4), cudaMemcpyHostToDevice, e->stream));
     CU(cudaStreamSynchronize(e->stream));
     }
+    if ((st = build_link_warps(e))) return st;
   }
   if (e->clusters_dirty || pos_changed) {
     // Clusters.create (Clusters/index.ts:54-100), src/index.ts:1668

@@ -611,7 +611,8 @@ __device__ __forceinline__ int hub_fill(HubStage& st, int buf, uint32_t at, uint
 // rows[nhub..nrows): the rest of the points by list length, so the lanes of a
 // warp walk lists of (nearly) the same length.
 __global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, const uint32_t* __restrict__ rowptr,
-                                                 const uint4* __restrict__ ent, const float2* __restrict__ src,
+                                                 const uint4* __restrict__ ent, const uint32_t* __restrict__ woff,
+                                                 const uint4* __restrict__ lane_ent, const float2* __restrict__ src,
                                                  float2* __restrict__ dst, const uint32_t* __restrict__ rows,
                                                  uint32_t nrows, uint32_t nhub) {
   // ForceLink.run (ForceLink/index.ts:221-263), force-spring.ts:38-96
@@ -679,7 +680,11 @@ __global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, con
   const float2 pp = src[p];
   const uint8_t f = d.flags[p];
   if (f & kAbsent) { dst[p] = pp; return; }
-  const uint32_t e0 = rowptr[p], e1 = rowptr[p + 1];
+  // This lane's list in its warp's block: entry k at 32 k (one coalesced load
+  // per entry for the warp), padded with absent entries to the warp's longest.
+  const uint32_t lt = t - nhub;
+  const uint32_t o0 = woff[lt >> 5], cnt = (woff[(lt >> 5) + 1] - o0) >> 5;
+  const uint4* col = lane_ent + o0 + (lt & 31);
   // The loads do not depend on the running velocity: issue them kLinkBatch
   // links ahead, then apply the springs strictly in list order.
   float2 vel = make_float2(0.f, 0.f);
@@ -690,25 +695,53 @@ __global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, con
   };
 
   constexpr int kLinkBatch = 4;
-  uint32_t at = e0;
-  for (; at + kLinkBatch <= e1; at += kLinkBatch) {
+  uint32_t at = 0;
+  for (; at + kLinkBatch <= cnt; at += kLinkBatch) {
     uint4 en[kLinkBatch];
     float2 q[kLinkBatch];
 #pragma unroll
-    for (int u = 0; u < kLinkBatch; ++u) en[u] = __ldg(&ent[at + u]);
+    for (int u = 0; u < kLinkBatch; ++u) en[u] = __ldg(&col[32 * (at + u)]);
 #pragma unroll
     for (int u = 0; u < kLinkBatch; ++u) q[u] = en[u].x != kAbsentTarget ? __ldg(&src[en[u].x]) : make_float2(0.f, 0.f);
 #pragma unroll
     for (int u = 0; u < kLinkBatch; ++u)
       if (en[u].x != kAbsentTarget) spring(en[u], q[u]);
   }
-  for (; at < e1; ++at) {
-    const uint4 en = __ldg(&ent[at]);
+  for (; at < cnt; ++at) {
+    const uint4 en = __ldg(&col[32 * at]);
     if (en.x == kAbsentTarget) continue;
     spring(en, __ldg(&src[en.x]));
   }
   dst[p] = (f & kPinned) ? pp : integrate(pp, vel.x, vel.y, s.friction, s.space);
 }
+
+__global__ void __launch_bounds__(kBlock) k_warp_lengths(const uint32_t* __restrict__ order,
+                                                         const uint32_t* __restrict__ rowptr, uint32_t nhub,
+                                                         uint32_t n, uint32_t* __restrict__ woff) {
+  const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t nw = (n - nhub + 31) / 32;
+  if (w > nw) return;
+  uint32_t len = 0;
+  if (w < nw) {   // the first row of a warp has its longest list
+    const uint32_t p = order[nhub + 32 * w];
+    len = rowptr[p + 1] - rowptr[p];
+  }
+  woff[w] = 32 * len;
+}
+
+__global__ void __launch_bounds__(kBlock) k_fill_lanes(const uint32_t* __restrict__ order,
+                                                       const uint32_t* __restrict__ rowptr,
+                                                       const uint4* __restrict__ ent, uint32_t nhub, uint32_t n,
+                                                       const uint32_t* __restrict__ woff, uint4* __restrict__ lane_ent) {
+  const uint32_t lt = blockIdx.x * blockDim.x + threadIdx.x;
+  if (lt >= n - nhub) return;
+  const uint32_t p = order[nhub + lt];
+  const uint32_t e0 = rowptr[p], len = rowptr[p + 1] - e0;
+  const uint32_t o0 = woff[lt >> 5], cnt = (woff[(lt >> 5) + 1] - o0) >> 5;
+  uint4* col = lane_ent + o0 + (lt & 31);
+  for (uint32_t k = 0; k < cnt; ++k) col[32 * k] = k < len ? ent[e0 + k] : make_uint4(kAbsentTarget, 0u, 0u, 0u);
+}
+
 
 // -------------------------------------------------------------- collision --
 __device__ __forceinline__ float coll_bin(float p, float o, float cs, float gm1) {
@@ -1074,10 +1107,24 @@ void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool s
   const uint4* en = direction == 0 ? d.ent_in : d.ent_out;
   const uint32_t* order = direction == 0 ? d.heavy_in : d.heavy_out;   // all points, longest lists first
   const uint32_t nhub = direction == 0 ? d.n_heavy_in : d.n_heavy_out;
+  const uint32_t* woff = direction == 0 ? d.woff_in : d.woff_out;
+  const uint4* lane_ent = direction == 0 ? d.lane_ent_in : d.lane_ent_out;
   const float2* src = swap_back ? d.pos_alt : d.pos;
   float2* dst = swap_back ? d.pos : d.pos_alt;
   const uint32_t nb = nhub + blocks_for(d.n - nhub);
-  k_link<<<nb, kBlock, nhub ? sizeof(HubStage) : 0, st>>>(d, s, rp, en, src, dst, order, d.n, nhub);
+  k_link<<<nb, kBlock, nhub ? sizeof(HubStage) : 0, st>>>(d, s, rp, en, woff, lane_ent, src, dst, order, d.n, nhub);
+}
+
+void launch_warp_lengths(const uint32_t* order, const uint32_t* rowptr, uint32_t nhub, uint32_t n, uint32_t* woff,
+                         cudaStream_t st) {
+  const uint32_t nw = (n - nhub + 31) / 32;
+  k_warp_lengths<<<blocks_for(nw + 1), kBlock, 0, st>>>(order, rowptr, nhub, n, woff);
+}
+
+void launch_fill_lanes(const uint32_t* order, const uint32_t* rowptr, const uint4* ent, uint32_t nhub, uint32_t n,
+                       const uint32_t* woff, uint4* lane_ent, cudaStream_t st) {
+  const uint32_t nb = blocks_for(n - nhub);
+  if (nb) k_fill_lanes<<<nb, kBlock, 0, st>>>(order, rowptr, ent, nhub, n, woff, lane_ent);
 }
 
 void launch_cluster_sum(const DeviceView& d, const SimScalars& s, cudaStream_t st) {

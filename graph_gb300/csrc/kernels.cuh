@@ -52,6 +52,13 @@ struct DeviceView {
   const uint32_t* heavy_in;   // all points by incoming list length, longest first;
   const uint32_t* heavy_out;  // the first n_heavy_* have lists longer than kHeavyDegree
   uint32_t n_heavy_in, n_heavy_out;
+  // The rows after the first n_heavy_* of the order, by warps of 32: warp w's
+  // entries at lane_ent[woff[w] .. woff[w + 1]), entry k of lane l at
+  // 32 k + l, each lane's list padded to its warp's longest with absent entries.
+  const uint32_t* woff_in;
+  const uint4* lane_ent_in;
+  const uint32_t* woff_out;
+  const uint4* lane_ent_out;
   // collision
   const float* size;          // resolved point sizes [n]
   long long* cgrid_acc;       // 4 grids x G_c^2 x (x, y, size, count)
@@ -99,6 +106,14 @@ void launch_manybody(const DeviceView& d, const SimScalars& s, cudaStream_t st);
 // direction 0 = incoming (reads pos, writes pos_alt), 1 = outgoing (pos_alt -> pos)
 // The first n_heavy_* rows of the order each get a CTA of their own.
 void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool swap_back, cudaStream_t st);
+// The warp layout of one direction's light rows (woff, lane_ent above):
+// warp_lengths writes 32 x the longest list of each of the nw warps to
+// woff[0 .. nw) and 0 to woff[nw] (an exclusive scan then gives the offsets);
+// fill_lanes copies the lists into place.
+void launch_warp_lengths(const uint32_t* order, const uint32_t* rowptr, uint32_t nhub, uint32_t n, uint32_t* woff,
+                         cudaStream_t st);
+void launch_fill_lanes(const uint32_t* order, const uint32_t* rowptr, const uint4* ent, uint32_t nhub, uint32_t n,
+                       const uint32_t* woff, uint4* lane_ent, cudaStream_t st);
 // `order`: the live points in cell order (sorted_idx of this tick's many-body
 // pass, `count` of them), or nullptr to take all points in index order.
 void launch_collision_grid(const DeviceView& d, const SimScalars& s, const uint32_t* order, uint32_t count,
