@@ -443,16 +443,7 @@ __global__ void __launch_bounds__(kBlock) kb_link(BatchView v, int direction, co
   auto spring = [&](const uint4 en, const float2 q) {
     float dd = __fadd_rn(__fmul_rn(__uint_as_float(en.y), span), D.link_r0);
     dd = __fmul_rn(dd, D.link_distance);
-    const float2 t = add2(pp, vel, pu);                     // p + v, then q - (p + v)
-    const float2 d = add2(q, make_float2(-t.x, -t.y), pu);
-    const float2 sq = mul2(d, d, pu);
-    float l = __fsqrt_rn(__fadd_rn(sq.x, sq.y));
-    l = gmax(l, __fmul_rn(dd, 0.99f));
-    l = __fdiv_rn(__fsub_rn(l, dd), l);
-    l = __fmul_rn(l, sa);
-    l = __fmul_rn(l, __uint_as_float(en.w));
-    l = __fmul_rn(l, __uint_as_float(en.z));
-    vel = add2(vel, mul2(d, splat(l), pu), pu);
+    spring_step(pp, vel, q, dd, __fmul_rn(dd, 0.99f), sa, __uint_as_float(en.w), __uint_as_float(en.z), pu);
   };
 
   constexpr int kLinkBatch = 4;

@@ -564,23 +564,6 @@ __global__ void __launch_bounds__(kBlock, 6) k_manybody(DeviceView d, SimScalars
 }
 
 // ------------------------------------------------------------------- link --
-// One spring (force-spring.ts:61-91) against the running velocity `vel`:
-// dx = q - (p + v); l = max(|dx|, 0.99 d); v += dx * ((l - d) / l * spring *
-// alpha * strength * bias).  `dd99` = d * 0.99, rounded, as the shader has it.
-__device__ __forceinline__ void spring_step(float2 pp, float2& vel, float2 q, float dd, float dd99, float sa,
-                                            float strength, float bias, PairUnits pu) {
-  const float2 t = add2(pp, vel, pu);                     // p + v, then q - (p + v)
-  const float2 d = add2(q, make_float2(-t.x, -t.y), pu);
-  const float2 sq = mul2(d, d, pu);
-  float l = __fsqrt_rn(__fadd_rn(sq.x, sq.y));
-  l = gmax(l, dd99);
-  l = __fdiv_rn(__fsub_rn(l, dd), l);
-  l = __fmul_rn(l, sa);
-  l = __fmul_rn(l, strength);
-  l = __fmul_rn(l, bias);
-  vel = add2(vel, mul2(d, splat(l), pu), pu);
-}
-
 // Hub rows: a list of thousands of links is one strictly sequential chain
 // (each spring reads the velocity the previous one left).  One CTA per hub:
 // warps 1..7 gather the next kHubChunk links (entry, neighbour position,
@@ -644,26 +627,33 @@ __global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, con
           next = hub_fill(hub, buf ^ 1, e0 + (c + 1) * kHubChunk, e1, ent, src, span, s.link_r0, s.link_distance);
       } else if (threadIdx.x == 0) {
         const uint32_t len = min((uint32_t)kHubChunk, e1 - e0 - c * kHubChunk);
-        if (!absent && len == (uint32_t)kHubChunk) {   // a full chunk: constant trip count
-          const float4* A = hub.a[buf];
-          const float4* B = hub.b[buf];
+        const float4* A = hub.a[buf];
+        const float4* B = hub.b[buf];
+        bool exact = absent != 0;
+        if (!absent) {   // no per-link branch: the chain runs back to back
+          const float2 v0 = vel;
+          bool out = false;
+          if (len == (uint32_t)kHubChunk) {   // a full chunk: constant trip count
 #pragma unroll 4
-          for (int k = 0; k < kHubChunk; ++k) {
+            for (int k = 0; k < kHubChunk; ++k) {
+              const float4 a = A[k];
+              const float4 b = B[k];
+              spring_step_fast(pp, vel, make_float2(a.x, a.y), a.z, a.w, sa, b.x, b.y, pu, out);
+            }
+          } else {
+#pragma unroll 4
+            for (uint32_t k = 0; k < len; ++k) {
+              const float4 a = A[k];
+              const float4 b = B[k];
+              spring_step_fast(pp, vel, make_float2(a.x, a.y), a.z, a.w, sa, b.x, b.y, pu, out);
+            }
+          }
+          if (out) { vel = v0; exact = true; }
+        }
+        if (exact) {   // absent targets, or operands outside the in-range sequences
+          for (uint32_t k = 0; k < len; ++k) {
             const float4 a = A[k];
             const float4 b = B[k];
-            spring_step(pp, vel, make_float2(a.x, a.y), a.z, a.w, sa, b.x, b.y, pu);
-          }
-        } else if (!absent) {   // no per-link branch: the chain runs back to back
-#pragma unroll 4
-          for (uint32_t k = 0; k < len; ++k) {
-            const float4 a = hub.a[buf][k];
-            const float4 b = hub.b[buf][k];
-            spring_step(pp, vel, make_float2(a.x, a.y), a.z, a.w, sa, b.x, b.y, pu);
-          }
-        } else {
-          for (uint32_t k = 0; k < len; ++k) {
-            const float4 a = hub.a[buf][k];
-            const float4 b = hub.b[buf][k];
             if (b.z != 0.f) continue;
             spring_step(pp, vel, make_float2(a.x, a.y), a.z, a.w, sa, b.x, b.y, pu);
           }
@@ -687,6 +677,8 @@ __global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, con
   const uint4* col = lane_ent + o0 + (lt & 31);
   // The loads do not depend on the running velocity: issue them kLinkBatch
   // links ahead, then apply the springs strictly in list order.
+  // Short lists on many threads: the correctly rounded springs (spring_step);
+  // the in-range sequences save latency on a hub's long chain, not here.
   float2 vel = make_float2(0.f, 0.f);
   auto spring = [&](const uint4 en, const float2 q) {
     float dd = __fadd_rn(__fmul_rn(__uint_as_float(en.y), span), s.link_r0);

@@ -156,6 +156,27 @@ def test_hub_lists():
         _assert_same(eng, orc, ("hub", t))
 
 
+def test_springs_outside_the_in_range_sequences():
+    # A hub whose list holds neighbours on top of it and well under one unit
+    # away, with rest lengths under one unit: springs of length 0 and below 1
+    # leave the in-range square root and quotient of the hub chain, so the link
+    # pass runs those hub chunks again with the correctly rounded springs.
+    n = 1500
+    rng = np.random.default_rng(33)
+    pos = rng.uniform(1000, 1400, size=2 * n).astype(np.float32)
+    pos[2:62] = np.repeat(pos[0:2][None, :], 30, axis=0).reshape(-1)            # 30 points on the hub
+    pos[62:262] = (pos[0:2][None, :] + rng.uniform(-0.4, 0.4, size=(100, 2))).reshape(-1).astype(np.float32)
+    star = np.stack([np.zeros(n - 1), np.arange(1, n)], axis=1)
+    close = rng.integers(1, 131, size=(600, 2))                                  # light rows among them
+    links = np.concatenate([star, close]).astype(np.float32).reshape(-1)
+    eng, orc = make_pair(pos, links, dict(random_seed=33, simulation_link_distance=0.3))
+    assert eng.layout().max_degree_in > 256 or eng.layout().max_degree_out > 256
+    for t in range(4):
+        eng.step(1)
+        orc.step(1)
+        _assert_same(eng, orc, ("short springs", t))
+
+
 def test_coincident_points_and_outside_space():
     n = 400
     rng = np.random.default_rng(9)

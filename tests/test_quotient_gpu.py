@@ -29,9 +29,10 @@ def _build(tmp_path, name):
 def test_markstein_quotient_equals_division(tmp_path):
     exe = _build(tmp_path, "check_quotient")
     out = subprocess.run([exe, "16"], check=True, capture_output=True, text=True).stdout
-    m = re.search(r"pairs=(\d+) mismatches=(\d+)", out)
-    assert m and int(m.group(1)) == 1 << 28, out
-    assert int(m.group(2)) == 0, out
+    m = re.search(r"pairs=(\d+) mismatches=(\d+) spring=(\d+)/(\d+)", out)
+    # spring operands: about 26/34 of the lengths lie in [1, 2^26]
+    assert m and int(m.group(1)) == 1 << 28 and int(m.group(3)) > 1 << 27, out
+    assert int(m.group(2)) == 0 and int(m.group(4)) == 0, out
 
 
 def test_in_range_sqrt_and_recip_equal_correctly_rounded(tmp_path):
