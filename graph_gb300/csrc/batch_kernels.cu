@@ -241,20 +241,20 @@ __global__ void __launch_bounds__(kBlock) kb_bigcells(BatchView v) {
     }
     __syncthreads();
   }
-  // warp cells (warp_cells.cuh), one warp each, taken from a ticket: the heavy
-  // ones (above kWarpSmallCell points) first, so the longest start first
+  // warp cells (warp_cells.cuh), one warp each, the heavy ones (above
+  // kWarpSmallCell points) first, so the longest start first
   __shared__ uint32_t cand[kBlock / 32][3][kCandidates];
   const uint32_t nheavy = v.big_count[1], nwarp = nheavy + v.big_count[2];
   const uint32_t n = v.cell_hwm;
-  for (;;) {
-    uint32_t wi = 0;
-    if (lane == 0) wi = atomicAdd(&v.big_count[3], 1u);
-    wi = __shfl_sync(0xffffffffu, wi, 0);
-    if (wi >= nwarp) break;
+  // the first cell by warp id, the next ones from the ticket
+  const uint32_t nw_grid = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t wi = blockIdx.x * (blockDim.x >> 5) + w; wi < nwarp;) {
     const uint32_t c = wi < nheavy ? v.big_list[n + wi] : v.big_list[2 * n - 1 - (wi - nheavy)];
     const uint32_t g = v.cell_gid[c];
     const GraphDesc& D = v.desc[g];
     warp_cell(v, D.fx, tick_of(v, g).seed_bits, D.p_off, c, cand[w]);
+    if (lane == 0) wi = nw_grid + atomicAdd(&v.big_count[3], 1u);
+    wi = __shfl_sync(0xffffffffu, wi, 0);
   }
 }
 

@@ -313,18 +313,18 @@ __global__ void __launch_bounds__(kBlock) k_bigcells(DeviceView d, SimScalars s)
     }
     __syncthreads();
   }
-  // warp cells, one warp each, taken from a ticket: the heavy ones (above
-  // kWarpSmallCell points) first, so the longest start first
+  // warp cells, one warp each, the heavy ones (above kWarpSmallCell points)
+  // first, so the longest start first
   __shared__ uint32_t cand[kBlock / 32][3][kCandidates];
   const uint32_t nheavy = d.big_count[1], nwarp = nheavy + d.big_count[2];
   const uint32_t cells = (uint32_t)(s.gf * s.gf);
-  for (;;) {
-    uint32_t wi = 0;
-    if (lane == 0) wi = atomicAdd(&d.big_count[3], 1u);
-    wi = __shfl_sync(0xffffffffu, wi, 0);
-    if (wi >= nwarp) break;
+  // the first cell by warp id, the next ones from the ticket
+  const uint32_t nw_grid = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t wi = blockIdx.x * (blockDim.x >> 5) + w; wi < nwarp;) {
     const uint32_t c = wi < nheavy ? d.big_list[cells + wi] : d.big_list[2 * cells - 1 - (wi - nheavy)];
     warp_cell(d, s.fx, tp.seed_bits, 0u, c, cand[w]);
+    if (lane == 0) wi = nw_grid + atomicAdd(&d.big_count[3], 1u);
+    wi = __shfl_sync(0xffffffffu, wi, 0);
   }
 }
 
@@ -456,11 +456,11 @@ __global__ void k_cells(DeviceView d, SimScalars s) {
 // the same for every point of a pass, so each launch runs one of the two).
 
 // Level l's sum for the point in finest cell (fcx, fcy).
-template <bool FAST>
+template <bool FAST, bool UNCHECKED = FAST>
 __device__ __forceinline__ float2 level_sum(const DeviceView& d, int L, int l, int fcx, int fcy, float2 p, float k,
                                             PairUnits pu) {
   const int sh = L - 1 - l;
-  return level_terms<FAST>(d.rec + d.level_off[l], 4 << l, fcx >> sh, fcy >> sh, p, k, pu);
+  return level_terms<FAST, UNCHECKED>(d.rec + d.level_off[l], 4 << l, fcx >> sh, fcy >> sh, p, k, pu);
 }
 
 // force-nearfield.frag:151-157 (jitter, step clamp) and the update.
@@ -517,7 +517,7 @@ __device__ __forceinline__ void manybody_split(const DeviceView& d, const SimSca
     const float2 p = d.sorted_pos[j];
     const int fcx = cell_index(p.x, s.csf, gf), fcy = cell_index(p.y, s.csf, gf);
     if (level_role) {
-      if (part < L) lvs[pt][part] = level_sum<FAST>(d, L, part, fcx, fcy, p, k, pu);
+      if (part < L) lvs[pt][part] = level_sum<FAST, false>(d, L, part, fcx, fcy, p, k, pu);
     } else {
       const float2 rj = d.jitter[i];
       const float4* fine = d.rec + d.level_off[L - 1];

@@ -177,6 +177,21 @@ def test_springs_outside_the_in_range_sequences():
         _assert_same(eng, orc, ("short springs", t))
 
 
+def test_level_terms_under_one_unit():
+    # Space 32 and a 128-cell finest grid: cells 0.25 units wide, so level
+    # centroids within one unit of a point are common and those levels are
+    # summed again with the length tested per term.
+    n = 3000
+    rng = np.random.default_rng(34)
+    pos = rng.uniform(0, 32, size=2 * n).astype(np.float32)
+    links = generators.erdos_renyi(n, 2, 34)
+    eng, orc = make_pair(pos, links, dict(space_size=32.0, random_seed=34, simulation_link_distance=0.5))
+    for t in range(3):
+        eng.step(1)
+        orc.step(1)
+        _assert_same(eng, orc, ("space 32", t))
+
+
 def test_coincident_points_and_outside_space():
     n = 400
     rng = np.random.default_rng(9)
