@@ -575,7 +575,9 @@ struct HubStage {
   float4 b[2][kHubChunk];   // strength, bias, absent flag, -
 };
 
-// Stages link at + (thread - 32); returns whether its target is absent.
+// Stages link at + (thread - 32); returns kStagedAbsent when its target is
+// absent and kStagedStrength when its strength is not 1.
+constexpr int kStagedAbsent = 1, kStagedStrength = 2;
 __device__ __forceinline__ int hub_fill(HubStage& st, int buf, uint32_t at, uint32_t e1, const uint4* __restrict__ ent,
                                         const float2* __restrict__ src, float span, float r0, float dist) {
   const int k = threadIdx.x - 32;
@@ -586,7 +588,31 @@ __device__ __forceinline__ int hub_fill(HubStage& st, int buf, uint32_t at, uint
   const float dd = __fmul_rn(__fadd_rn(__fmul_rn(__uint_as_float(en.y), span), r0), dist);
   st.a[buf][k] = make_float4(q.x, q.y, dd, __fmul_rn(dd, 0.99f));
   st.b[buf][k] = make_float4(__uint_as_float(en.w), __uint_as_float(en.z), absent ? 1.f : 0.f, 0.f);
-  return absent;
+  return (absent ? kStagedAbsent : 0) | (__uint_as_float(en.w) != 1.0f ? kStagedStrength : 0);
+}
+
+// The fast chain over one staged chunk without absent targets (a full chunk
+// with a constant trip count); returns spring_step_fast's flag.
+template <bool UNIT_STRENGTH>
+__device__ __forceinline__ bool hub_chunk_fast(const float4* A, const float4* B, uint32_t len, float2 pp, float2& vel,
+                                               float sa, PairUnits pu) {
+  bool out = false;
+  if (len == (uint32_t)kHubChunk) {
+#pragma unroll 4
+    for (int k = 0; k < kHubChunk; ++k) {
+      const float4 a = A[k];
+      const float4 b = B[k];
+      spring_step_fast<UNIT_STRENGTH>(pp, vel, make_float2(a.x, a.y), a.z, a.w, sa, b.x, b.y, pu, out);
+    }
+  } else {
+#pragma unroll 4
+    for (uint32_t k = 0; k < len; ++k) {
+      const float4 a = A[k];
+      const float4 b = B[k];
+      spring_step_fast<UNIT_STRENGTH>(pp, vel, make_float2(a.x, a.y), a.z, a.w, sa, b.x, b.y, pu, out);
+    }
+  }
+  return out;
 }
 
 // Blocks [0, nhub) take the hub rows rows[0..nhub) (longest first, so the
@@ -615,9 +641,10 @@ __global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, con
     }
     const uint32_t e0 = rowptr[p], e1 = rowptr[p + 1];
     const uint32_t chunks = (e1 - e0 + kHubChunk - 1) / kHubChunk;
-    int absent = 0;   // some link of the staged chunk has an absent target
-    if (threadIdx.x >= 32) absent = hub_fill(hub, 0, e0, e1, ent, src, span, s.link_r0, s.link_distance);
-    absent = __syncthreads_or(absent);
+    int staged = 0;
+    if (threadIdx.x >= 32) staged = hub_fill(hub, 0, e0, e1, ent, src, span, s.link_r0, s.link_distance);
+    int absent = __syncthreads_or(staged & kStagedAbsent);       // some target of the chunk is absent
+    int strengths = __syncthreads_or(staged & kStagedStrength);  // some strength of the chunk is not 1
     float2 vel = make_float2(0.f, 0.f);
     for (uint32_t c = 0; c < chunks; ++c) {
       const int buf = c & 1;
@@ -632,22 +659,8 @@ __global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, con
         bool exact = absent != 0;
         if (!absent) {   // no per-link branch: the chain runs back to back
           const float2 v0 = vel;
-          bool out = false;
-          if (len == (uint32_t)kHubChunk) {   // a full chunk: constant trip count
-#pragma unroll 4
-            for (int k = 0; k < kHubChunk; ++k) {
-              const float4 a = A[k];
-              const float4 b = B[k];
-              spring_step_fast(pp, vel, make_float2(a.x, a.y), a.z, a.w, sa, b.x, b.y, pu, out);
-            }
-          } else {
-#pragma unroll 4
-            for (uint32_t k = 0; k < len; ++k) {
-              const float4 a = A[k];
-              const float4 b = B[k];
-              spring_step_fast(pp, vel, make_float2(a.x, a.y), a.z, a.w, sa, b.x, b.y, pu, out);
-            }
-          }
+          const bool out = strengths ? hub_chunk_fast<false>(A, B, len, pp, vel, sa, pu)
+                                     : hub_chunk_fast<true>(A, B, len, pp, vel, sa, pu);
           if (out) { vel = v0; exact = true; }
         }
         if (exact) {   // absent targets, or operands outside the in-range sequences
@@ -659,7 +672,8 @@ __global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, con
           }
         }
       }
-      absent = __syncthreads_or(next);
+      absent = __syncthreads_or(next & kStagedAbsent);
+      strengths = __syncthreads_or(next & kStagedStrength);
     }
     if (threadIdx.x == 0) dst[p] = (f & kPinned) ? pp : integrate(pp, vel.x, vel.y, s.friction, s.space);
     return;

@@ -192,6 +192,25 @@ def test_level_terms_under_one_unit():
         _assert_same(eng, orc, ("space 32", t))
 
 
+def test_hub_lists_with_strengths():
+    # Hub chunks whose strengths are all 1 leave out the strength product;
+    # the star's first 300 links have strength 1 and the rest random ones, so
+    # one chain runs both kinds of chunk.
+    n = 3000
+    rng = np.random.default_rng(22)
+    pos = rng.uniform(1000, 3000, size=2 * n).astype(np.float32)
+    star = np.stack([np.zeros(n - 1), np.arange(1, n)], axis=1)
+    links = np.concatenate([star, rng.integers(0, n, size=(3000, 2))]).astype(np.float32).reshape(-1)
+    strength = rng.uniform(0.2, 2.0, size=links.size // 2).astype(np.float32)
+    strength[:300] = 1.0
+    eng, orc = make_pair(pos, links, dict(random_seed=22, simulation_link_distance=3.0), strength=strength)
+    assert max(eng.layout().max_degree_in, eng.layout().max_degree_out) > 256
+    for t in range(4):
+        eng.step(1)
+        orc.step(1)
+        _assert_same(eng, orc, ("hub strengths", t))
+
+
 def test_coincident_points_and_outside_space():
     n = 400
     rng = np.random.default_rng(9)
