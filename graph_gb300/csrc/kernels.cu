@@ -9,11 +9,15 @@
 //   scatter      counting-sort scatter of live points into cell order
 //   cells        per finest cell: exact sums, the 8-slot near-field peel
 //                (build-nearfield-slots.vert), and the pyramid of coarser
-//                levels (calculate-level.vert for every level)
+//                levels (calculate-level.vert for every level); dense cells
+//                get a warp (warp_cells.cuh) or a CTA first (k_bigcells)
 //   manybody     level passes + near field + update (force-level.frag,
-//                force-nearfield.frag, update-position.frag)
+//                force-nearfield.frag, update-position.frag); one thread per
+//                point, or 16 per point for small graphs (k_manybody_split)
 //   link in/out  spring force over each direction's link lists + update
-//                (force-spring.ts); hub lists get a CTA each
+//                (force-spring.ts); hub lists get a CTA each, the other
+//                lists are read by warps (k_warp_lengths and k_fill_lanes
+//                lay them out at render)
 //   clusters     centre of mass per cluster + cluster pull + update
 //                (calculate-centermass.vert, force-cluster.frag)   [if set]
 //   collision    4 offset grids + spatial collision force + update
