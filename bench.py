@@ -106,6 +106,23 @@ def stage_bytes(stage, n, m, c, cl):
     }[stage]
 
 
+# The whole tick's algorithmic bytes (the survey's model): gravity, binning,
+# scan, many-body and both link passes over N points and E links, the finest
+# grid's C_f cells, and with collision its four grids of C_c cells.
+def tick_bytes(n, e, cf, cc=None):
+    b = 112 * n + 48 * e + 107 * cf
+    if cc is not None:
+        b += 144 * n + 128 * cc
+    return b
+
+
+def ran_stages(stages, fields):
+    """Stage times of the stages that launched work: the engine times every
+    stage of the tick, and one whose force is off reads as a short gap."""
+    center_on = float(fields.get("simulation_center", 0.0)) != 0.0
+    return {k: v for k, v in stages.items() if v > 0 and (k != "center" or center_on)}
+
+
 def load_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -331,7 +348,7 @@ def main():
         return
 
     # per-stage device times (events between the tick's kernels, no graph)
-    stages = eng.profile_stages(20)
+    stages = ran_stages(eng.profile_stages(20), fields)
     m = lay.link_entries_in
     c = lay.finest_grid ** 2
     cl = sum((4 << l) ** 2 for l in range(lay.levels))
@@ -344,6 +361,9 @@ def main():
     per_stage = {k: round(v * 1e3, 2) for k, v in stages.items() if v > 0}
     stage_gbs = {k: round(stage_bytes(k, live, m, c, cl) / (stages[k] / 1e3) / 1e9, 1)
                  for k in stages if stages[k] > 0}
+    coll_on = float(fields.get("simulation_collision", 0.0)) != 0.0
+    tb = tick_bytes(live, int(lay.links_number), c, int(lay.collision_grid) ** 2 if coll_on else None)
+    tick_gbs = tb / (ms / args.steps / 1e3) / 1e9
 
     # end to end through the C ABI with host buffers
     pinned = torch.empty(2 * lay.points_number, dtype=torch.float32, pin_memory=True)
@@ -386,6 +406,11 @@ def main():
                                   "reciprocal per term for bit-exact parity), not by HBM; issue_active_ncu is its "
                                   "share of busy issue slots from the committed ncu summary")
                          if dom == "manybody" else None},
+            "tick_roofline": {"bytes_model": "112 N + 48 E + 107 C_f" + (" + 144 N + 128 C_c" if coll_on else ""),
+                              "bytes": tb, "achieved": tick_gbs, "peak": peak, "unit": "GB/s",
+                              "frac": tick_gbs / peak,
+                              "note": "whole tick against HBM; the many-body pass is issue-bound, so the tick "
+                                      "sits well below this roof"},
             "stage_us": per_stage,
             "stage_alg_gbs": stage_gbs,
             "cpu_baseline": cpu,

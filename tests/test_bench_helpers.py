@@ -1,0 +1,36 @@
+"""bench.py's byte models and stage filter (host code, no GPU)."""
+import importlib.util
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _bench():
+    spec = importlib.util.spec_from_file_location("bench", os.path.join(HERE, "..", "bench.py"))
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    return b
+
+
+def test_tick_bytes_model():
+    b = _bench()
+    # the 1M-point SBM: N = 1e6, E = 4,976,035 links, 512^2 finest cells
+    assert b.tick_bytes(1_000_000, 4_976_035, 512 * 512) == 112_000_000 + 48 * 4_976_035 + 107 * 262_144
+    assert b.tick_bytes(10, 20, 16, cc=4) == 112 * 10 + 48 * 20 + 107 * 16 + 144 * 10 + 128 * 4
+
+
+def test_stages_without_work_are_left_out():
+    b = _bench()
+    timed = {"prepass": 0.0235, "center": 0.0021, "manybody": 0.37, "clusters": 0.0}
+    assert b.ran_stages(timed, {"simulation_center": 0.0}) == {"prepass": 0.0235, "manybody": 0.37}
+    assert b.ran_stages(timed, {"simulation_center": 0.1}) == {"prepass": 0.0235, "center": 0.0021,
+                                                               "manybody": 0.37}
+
+
+def test_stage_bytes_cover_every_timed_stage():
+    b = _bench()
+    from graph_gb300 import _abi
+    for name in _abi.STAGE_TIME_NAMES:
+        if name.startswith("collision") or name in ("prepass", "center", "scan", "scatter", "cells", "manybody",
+                                                    "link_in", "link_out", "clusters"):
+            assert b.stage_bytes(name, 10, 20, 16, 21) > 0
