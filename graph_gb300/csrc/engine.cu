@@ -411,7 +411,10 @@ cgl_status prepare_tick(cgl_engine* e) {
 // (ForceManyBody/index.ts:521), then Store.addAlpha (Store/index.ts:328-332).
 // Right-click repulsion is on (src/index.ts:2011, 2083)
 bool mouse_active(const cgl_engine* e) { return e->right_button && e->cfg.enable_right_click_repulsion; }
-bool interactive(const cgl_engine* e) { return mouse_active(e) || (e->drag_index >= 0 && e->cfg.enable_drag); }
+bool dragging(const cgl_engine* e) {
+  return e->drag_index >= 0 && e->drag_index < (int64_t)e->N && e->cfg.enable_drag;   // the index of this graph
+}
+bool interactive(const cgl_engine* e) { return mouse_active(e) || dragging(e); }
 
 void launch_pointer_force(cgl_engine* e) {
   launch_mouse(e->view, make_scalars(e), make_float2((float)e->mouse_x, (float)e->mouse_y),
@@ -623,6 +626,34 @@ cgl_status apply_pinned(cgl_engine* e) {
   return CGL_OK;
 }
 
+// A render that fails part way (a refused or failed allocation, a CUDA error)
+// can leave buffers of the old graph's sizes under the new graph's counts.
+// The engine then forgets the graph, as before its first render: no tick,
+// read-back or texture touches a buffer until a render succeeds, and every
+// staged input stays dirty, so the next render builds all of it again.  The
+// random stream goes back to where the failed render found it, so the next
+// render draws what an uninterrupted one would have.
+void forget_graph(cgl_engine* e) {
+  e->N = e->E = 0;
+  e->T = e->W = 0;
+  e->Gf = e->L = 0;
+  e->live = 0;
+  e->entries = 0;
+  e->max_deg_in = e->max_deg_out = 0;
+  e->n_heavy_in = e->n_heavy_out = 0;
+  e->mb_ready = false;
+  e->collision_ready = false;
+  e->point_clusters = e->cluster_positions = false;
+  e->n_clusters = 0;
+  e->running = false;
+  e->drag_index = -1;
+  e->pos_dirty = e->links_dirty = e->sizes_dirty = e->clusters_dirty = true;
+  e->graph_dirty = true;
+  refresh_view(e);
+}
+
+cgl_status build_graph(cgl_engine* e, double alpha, uint64_t N, uint64_t E);
+
 cgl_status do_render(cgl_engine* e, double alpha) {
   // GraphData.update (GraphData/index.ts:443-462)
   const uint64_t N = e->have_pos_input ? e->in_pos.size() / 2 : 0;
@@ -630,6 +661,16 @@ cgl_status do_render(cgl_engine* e, double alpha) {
   if (N == 0 && E == 0) return CGL_OK;   // empty render (src/index.ts:941-955)
   if (N > (1ull << 24)) return fail(e, CGL_INVALID_ARG, "%llu points: point indices must stay exact in f32 (max 2^24)", (unsigned long long)N);
   if (E > 0xFFFFFFF0ull) return fail(e, CGL_INVALID_ARG, "too many links");
+  const uint64_t rng_ctr = e->rng_ctr;
+  const cgl_status st = build_graph(e, alpha, N, E);
+  if (st != CGL_OK) {
+    e->rng_ctr = rng_ctr;
+    forget_graph(e);
+  }
+  return st;
+}
+
+cgl_status build_graph(cgl_engine* e, double alpha, uint64_t N, uint64_t E) {
   const bool pos_changed = e->pos_dirty;
   const bool links_changed = e->links_dirty || pos_changed;
   cgl_status st;
@@ -1120,7 +1161,7 @@ cgl_status one_frame(cgl_engine* e, uint32_t* ticks) {
       CU(cudaGetLastError());
     }
   }
-  if (e->drag_index >= 0 && e->cfg.enable_drag) {
+  if (dragging(e)) {
     launch_drag(e->view, (uint32_t)e->drag_index, make_float2((float)e->mouse_x, (float)e->mouse_y), e->stream);
     CU(cudaGetLastError());
   }
