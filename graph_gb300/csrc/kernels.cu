@@ -1094,8 +1094,11 @@ void launch_scatter(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
 void launch_cells(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
   // grid-stride over the dense cells; blocks beyond one resident wave (3 per SM)
   // start as others finish and even out the cells' unequal sizes (measured
-  // best at 8 per SM)
-  k_bigcells<<<8 * sm_count(), kBlock, 0, st>>>(d, s);
+  // best at 8 per SM).  A graph of n points has at most n / (kSmallCell + 1)
+  // dense cells: small graphs launch a warp for each, not 8 idle blocks per SM.
+  const uint32_t most = d.n / (kSmallCell + 1);
+  const uint32_t nb = std::min(8u * sm_count(), std::max(1u, (most + kBlock / 32 - 1) / (kBlock / 32)));
+  k_bigcells<<<nb, kBlock, 0, st>>>(d, s);
   const int tiles = (s.gf / s.tile) * (s.gf / s.tile);
   const size_t smem = 3 * sizeof(long long) * s.tile * s.tile;
   k_cells<<<tiles, s.tile * s.tile, smem, st>>>(d, s);
