@@ -44,6 +44,22 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
+
+def _reference_arm(argv):
+    for k, a in enumerate(argv):
+        if a == "--impl" and k + 1 < len(argv):
+            return argv[k + 1] == "reference"
+        if a.startswith("--impl="):
+            return a.split("=", 1)[1] == "reference"
+    return False
+
+
+# torchrun gives each process OMP_NUM_THREADS=1.  The reference arm runs on
+# rank 0 alone, so that rank takes every host core; the count must be set
+# before torch or the oracle loads an OpenMP runtime, which reads it once.
+if _reference_arm(sys.argv[1:]) and int(os.environ.get("WORLD_SIZE", "1")) > 1:
+    os.environ["OMP_NUM_THREADS"] = str(os.cpu_count() or 1)
+
 from graph_gb300 import _abi, generators, replicas  # noqa: E402
 
 METRIC = "point-iterations/s"

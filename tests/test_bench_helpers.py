@@ -34,3 +34,11 @@ def test_stage_bytes_cover_every_timed_stage():
         if name.startswith("collision") or name in ("prepass", "center", "scan", "scatter", "cells", "manybody",
                                                     "link_in", "link_out", "clusters"):
             assert b.stage_bytes(name, 10, 20, 16, 21) > 0
+
+
+def test_reference_arm_is_recognised_before_imports():
+    b = _bench()
+    assert b._reference_arm(["--impl", "reference", "--gpus", "2"])
+    assert b._reference_arm(["--steps", "3", "--impl=reference"])
+    assert not b._reference_arm(["--impl", "gb300"])
+    assert not b._reference_arm(["--gpus", "2"])
