@@ -57,8 +57,16 @@ def _reference_arm(argv):
 # torchrun gives each process OMP_NUM_THREADS=1.  The reference arm runs on
 # rank 0 alone, so that rank takes every host core; the count must be set
 # before torch or the oracle loads an OpenMP runtime, which reads it once.
+def _host_cores():
+    # the cores this process may run on (a cgroup or taskset mask can allow fewer than the host has)
+    try:
+        return len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1
+
+
 if _reference_arm(sys.argv[1:]) and int(os.environ.get("WORLD_SIZE", "1")) > 1:
-    os.environ["OMP_NUM_THREADS"] = str(os.cpu_count() or 1)
+    os.environ["OMP_NUM_THREADS"] = str(_host_cores())
 
 from graph_gb300 import _abi, generators, replicas  # noqa: E402
 
@@ -243,7 +251,7 @@ def time_oracle(pos, links, fields, budget_s, max_ticks, warmup=1, sizes=None):
     ticks += max(more, 0)
     live = o.layout().live_points
     o.close()
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    cores = int(os.environ.get("OMP_NUM_THREADS", _host_cores()))
     return live * ticks / t, ticks, t, cores
 
 
@@ -477,7 +485,7 @@ def run_repulsion(args):
                       "n_gpus": 1, "data": "synthetic",
                       "config": {"workload": "repulsion-benchmark story: points only, uniform in 4096^2, gravity 0, "
                                              "repulsion 1, decay 1e12; 12 warm-up + 40 timed steps, read-back "
-                                             "flush", "cores_oracle": os.cpu_count()},
+                                             "flush", "cores_oracle": _host_cores()},
                       "rows": rows}))
 
 
@@ -716,7 +724,7 @@ def run_reference(args):
             break
     secs = time.perf_counter() - t_start
     value = live * ticks / secs
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    cores = int(os.environ.get("OMP_NUM_THREADS", _host_cores()))
     sample = ("%d of %d requested ticks (after %d warm-up) of the %s workload on the oracle port "
               "(C++ restatement of the reference's per-tick algorithm, OpenMP on %s); the reference itself "
               "is TypeScript + WebGL2 and cannot execute on this machine" % (ticks, args.steps, warm, desc,

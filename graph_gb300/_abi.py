@@ -59,7 +59,14 @@ class Config(C.Structure):
         ("enable_right_click_repulsion", C.c_int32),
         ("enable_drag", C.c_int32),
         ("device_ingest_min_links", C.c_double),
+        ("random_stream", C.c_int32),
+        ("rescale_positions", C.c_int32),
+        ("random_seed_text", C.c_char_p),
     ]
+
+
+RANDOM_REFERENCE = 0
+RANDOM_COUNTER = 1
 
 
 class State(C.Structure):
@@ -124,6 +131,9 @@ DEFAULTS = dict(
     enable_right_click_repulsion=0,
     enable_drag=0,
     device_ingest_min_links=65536.0,
+    random_stream=RANDOM_REFERENCE,
+    rescale_positions=-1,
+    random_seed_text=None,
 )
 
 # Reference config keys (camelCase, src/config.ts) -> C field names.
@@ -148,28 +158,71 @@ CAMEL_TO_FIELD = {
     "simulationRepulsionFromMouse": "simulation_repulsion_from_mouse",
     "enableRightClickRepulsion": "enable_right_click_repulsion",
     "enableDrag": "enable_drag",
+    "rescalePositions": "rescale_positions",
 }
 
 
-def seed_to_u64(seed):
-    """randomSeed accepts a number or a string (src/config.ts:771); map it to 64 bits.
+def js_number_to_string(x):
+    """JavaScript's String(x) for a number (ECMA-262 Number::toString, radix 10)."""
+    import decimal
+    x = float(x)
+    if x != x:
+        return "NaN"
+    if x == 0:
+        return "0"
+    if x < 0:
+        return "-" + js_number_to_string(-x)
+    if x == math.inf:
+        return "Infinity"
+    # shortest round-trip digits s (k of them) and n with x = 0.s * 10^n
+    t = decimal.Decimal(repr(x)).normalize().as_tuple()
+    digits = "".join(str(d) for d in t.digits)
+    k = len(digits)
+    n = t.exponent + k
+    if k <= n <= 21:
+        return digits + "0" * (n - k)
+    if 0 < n <= 21:
+        return digits[:n] + "." + digits[n:]
+    if -6 < n <= 0:
+        return "0." + "0" * (-n) + digits
+    e = n - 1
+    sign = "+" if e >= 0 else "-"
+    mant = digits[0] + ("." + digits[1:] if k > 1 else "")
+    return "%se%s%d" % (mant, sign, abs(e))
 
-    Integers are taken modulo 2^64; floats by their IEEE-754 bits; strings by FNV-1a 64.
+
+def seed_fields(seed):
+    """randomSeed (a number or a string, src/config.ts:771) as config fields.
+
+    The reference seeds its generator with String(randomSeed) (random@4.1.0's
+    clone over seedrandom@3.0.5): random_seed_text carries that text whenever it
+    is not simply random_seed in decimal.  random_seed also keys the engine's
+    opt-in counter stream: integers modulo 2^64, other numbers by their
+    IEEE-754 bits, strings by FNV-1a 64.
     """
     if isinstance(seed, bool):
         seed = int(seed)
     if isinstance(seed, int):
-        return seed % (1 << 64)
+        if 0 <= seed < (1 << 64):
+            return seed, None
+        return seed % (1 << 64), str(seed)
     if isinstance(seed, float):
-        if seed.is_integer():
-            return int(seed) % (1 << 64)
+        text = js_number_to_string(seed)
+        if seed.is_integer() and 0 <= seed < 2.0 ** 53:
+            return int(seed), None
         import struct
-        return struct.unpack("<Q", struct.pack("<d", seed))[0]
+        return struct.unpack("<Q", struct.pack("<d", seed))[0], text
+    text = str(seed)
     h = 0xCBF29CE484222325
-    for b in str(seed).encode("utf-8"):
+    for b in text.encode("utf-8"):
         h ^= b
         h = (h * 0x100000001B3) % (1 << 64)
-    return h
+    return h, text
+
+
+def seed_to_u64(seed):
+    """The 64-bit random_seed field for a randomSeed value (see seed_fields)."""
+    return seed_fields(seed)[0]
 
 
 def make_config(**fields) -> Config:
@@ -181,10 +234,15 @@ def make_config(**fields) -> Config:
         vals[k] = v
     if "random_seed" in fields and fields["random_seed"] is not None:
         vals["has_random_seed"] = 1
-        vals["random_seed"] = seed_to_u64(fields["random_seed"])
+        u64, text = seed_fields(fields["random_seed"])
+        vals["random_seed"] = u64
+        if "random_seed_text" not in fields:
+            vals["random_seed_text"] = text
     elif "random_seed" in fields:
         vals["has_random_seed"] = 0
         vals["random_seed"] = 0
+    if isinstance(vals.get("random_seed_text"), str):
+        vals["random_seed_text"] = vals["random_seed_text"].encode("utf-8")
     cfg = Config()
     for k, v in vals.items():
         if k == "simulation_link_dist_random_variation_range":
@@ -201,6 +259,8 @@ def config_to_dict(cfg: Config) -> dict:
         v = getattr(cfg, name)
         if name == "simulation_link_dist_random_variation_range":
             v = (v[0], v[1])
+        elif name == "random_seed_text" and v is not None:
+            v = v.decode("utf-8")
         out[name] = v
     return out
 
@@ -211,6 +271,7 @@ def declare(lib, prefix: str, engine_t=C.c_void_p):
     f = C.POINTER(C.c_float)
     spec = {
         "set_point_positions": ([E, f, C.c_uint64], C.c_int),
+        "set_point_positions_ex": ([E, f, C.c_uint64, C.c_int32], C.c_int),
         "set_links": ([E, f, C.c_uint64], C.c_int),
         "set_link_strength": ([E, f, C.c_uint64], C.c_int),
         "set_point_sizes": ([E, f, C.c_uint64], C.c_int),

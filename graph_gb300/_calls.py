@@ -53,6 +53,10 @@ class EngineCalls:
         a = _f32(xy)
         return self._call("set_point_positions", _fptr(a), a.size)
 
+    def set_point_positions_ex(self, xy, dont_rescale):
+        a = _f32(xy)
+        return self._call("set_point_positions_ex", _fptr(a), a.size, 1 if dont_rescale else 0)
+
     def set_links(self, st):
         a = _f32(st)
         return self._call("set_links", _fptr(a), a.size)

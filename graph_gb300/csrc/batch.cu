@@ -410,13 +410,19 @@ cgl_status cgl_batch_add(cgl_batch* b, const cgl_config* cfg, const float* xy, u
   j.E = n_link_floats / 2;
   if (j.n == 0) return bfail(b, CGL_INVALID_ARG, "a job needs points");
   if (j.n > (1ull << 24)) return bfail(b, CGL_INVALID_ARG, "%llu points exceed 2^24", (unsigned long long)j.n);
-  if (cfg->has_random_seed) j.rng.seed = cfg->random_seed;
-  else { std::random_device rd; j.rng.seed = ((uint64_t)rd() << 32) ^ rd(); }
+  ingest::seed_rng(*cfg, j.rng);
+  j.cfg.random_seed_text = nullptr;   // the seed is used here only
   const double space = ingest::adjusted_space(*cfg);
   // ingest exactly as cgl_render does for a fresh plain engine
   std::vector<float2> pos;
   std::vector<uint8_t> absent;
-  j.live = ingest::canonical_positions(xy, j.n, pos, absent);
+  if (ingest::should_rescale(*cfg, false)) {
+    std::vector<float> scaled(xy, xy + 2 * j.n);
+    ingest::rescale_positions(scaled.data(), j.n, cfg->space_size);
+    j.live = ingest::canonical_positions(scaled.data(), j.n, pos, absent);
+  } else {
+    j.live = ingest::canonical_positions(xy, j.n, pos, absent);
+  }
   int fbits = 0;
   const FixedScale fx = ingest::fixed_for(j.n, space, &fbits);
   const ingest::Grid grid = ingest::grid_for(j.n);
@@ -425,7 +431,7 @@ cgl_status cgl_batch_add(cgl_batch* b, const cgl_config* cfg, const float* xy, u
   j.tile = std::min(16, j.gf);
   // the jitter draws come first (ForceManyBody.create), then the link draws
   const uint64_t T = (uint64_t)std::ceil(std::sqrt((double)j.n));
-  const bool dev_jitter = !(cfg->device_ingest_min_links > (double)j.n);
+  const bool dev_jitter = j.rng.counter && !(cfg->device_ingest_min_links > (double)j.n);
   const uint64_t jitter_base = j.rng.ctr;
   std::vector<float2> jit;
   if (dev_jitter) j.rng.ctr += 2 * T * T;
@@ -438,13 +444,16 @@ cgl_status cgl_batch_add(cgl_batch* b, const cgl_config* cfg, const float* xy, u
   bool dev_links = has_links && j.E < 0xFFFFFFF0ull && !(cfg->device_ingest_min_links > (double)j.E);
   const uint64_t big = std::max<uint64_t>(j.E + 1, j.n + 1);
   const size_t tmp_words = std::max(dingest::sort_temp_words(big), dingest::scan_temp_words(big));
+  const double draw_bytes = j.rng.counter ? 0.0 : 8.0 * j.E;   // host draws of the reference's stream
   if (dev_links && b->budget > 0 &&
-      (double)b->dev_bytes + 8.0 * j.E + 4.0 * (j.E + 1) + 8.0 * (j.n + 1) + 16.0 * big + 4.0 * tmp_words > b->budget)
+      (double)b->dev_bytes + 8.0 * j.E + 4.0 * (j.E + 1) + 8.0 * (j.n + 1) + 16.0 * big + 4.0 * tmp_words + draw_bytes >
+          b->budget)
     dev_links = false;
   float2* d_links = nullptr;
   uint32_t *d_valid = nullptr, *d_len_in = nullptr, *d_len_out = nullptr, *d_tmp = nullptr, *d_stats = nullptr;
   uint32_t *d_kin = nullptr, *d_kout = nullptr, *d_vin = nullptr, *d_vout = nullptr;
   uint32_t dev_m = 0, dev_stats[4] = {0, 0, 0, 0};
+  float* d_draws = nullptr;
   const uint64_t links_base = j.rng.ctr;
   if (dev_links) {
     d_links = tmp.get<float2>(j.E);
@@ -475,7 +484,17 @@ cgl_status cgl_batch_add(cgl_batch* b, const cgl_config* cfg, const float* xy, u
     BCU(cudaMemcpyAsync(dev_stats, d_stats, 16, cudaMemcpyDeviceToHost, s));
     BCU(cudaStreamSynchronize(s));
     j.m_in = j.m_out = dev_m;
-    j.rng.ctr += 2 * (uint64_t)dev_m;
+    if (!j.rng.counter && dev_m) {
+      // the reference's stream is sequential: both directions' draws on the host
+      std::vector<float> h_draws(2 * (size_t)dev_m);
+      j.rng.fill_unit_f32(h_draws.data(), 2 * (uint64_t)dev_m);
+      d_draws = tmp.get<float>(2 * (size_t)dev_m);
+      if (!d_draws) return bfail(b, CGL_OOM, "link draw buffer");
+      BCU(cudaMemcpyAsync(d_draws, h_draws.data(), 2 * (size_t)dev_m * sizeof(float), cudaMemcpyHostToDevice, s));
+      BCU(cudaStreamSynchronize(s));
+    } else {
+      j.rng.ctr += 2 * (uint64_t)dev_m;
+    }
   } else {
     if (has_links) ingest::build_links(links, j.E, j.n, nullptr, absent, j.rng, cin, cout_);
     else { cin.rowptr.assign(j.n + 1, 0); cout_.rowptr.assign(j.n + 1, 0); }
@@ -584,10 +603,11 @@ cgl_status cgl_batch_add(cgl_batch* b, const cgl_config* cfg, const float* xy, u
     const int row_bits = dingest::key_bits(j.n - 1);
     dingest::sort_pairs(d_kin, d_vin, M, row_bits, d_tmp, s);
     dingest::sort_pairs(d_kout, d_vout, M, row_bits, d_tmp, s);
-    dingest::fill_csr(d_kin, d_vin, M, d_links, true, d_len_in, d_len_out, nullptr, flags_j, j.rng.seed, links_base,
-                      (uint32_t)j.p_off, (uint4*)b->ent.p + j.e_in, s);
-    dingest::fill_csr(d_kout, d_vout, M, d_links, false, d_len_in, d_len_out, nullptr, flags_j, j.rng.seed,
-                      links_base + M, (uint32_t)j.p_off, (uint4*)b->ent.p + j.e_out, s);
+    dingest::fill_csr(d_kin, d_vin, M, d_links, true, d_len_in, d_len_out, nullptr, flags_j, d_draws, j.rng.seed,
+                      links_base, (uint32_t)j.p_off, (uint4*)b->ent.p + j.e_in, s);
+    dingest::fill_csr(d_kout, d_vout, M, d_links, false, d_len_in, d_len_out, nullptr, flags_j,
+                      d_draws ? d_draws + M : nullptr, j.rng.seed, links_base + M, (uint32_t)j.p_off,
+                      (uint4*)b->ent.p + j.e_out, s);
     // the long lists (rows by length, longest first; the first stats[1] / stats[3])
     j.heavy_in.resize(dev_stats[1]);
     j.heavy_out.resize(dev_stats[3]);

@@ -46,6 +46,7 @@ struct cgl_engine {
   bool pinned_set = false;
   std::vector<double> pinned_input;
   bool pos_dirty = false, links_dirty = false, sizes_dirty = false;
+  bool skip_rescale = false;   // Points.shouldSkipRescale (setPointPositions(…, dontRescale))
   bool have_clusters = false, have_cluster_pos = false, have_cluster_strength = false;
   std::vector<float> in_clusters, in_cluster_pos, in_cluster_strength;
   bool clusters_dirty = false;
@@ -84,7 +85,8 @@ struct cgl_engine {
   double alpha = 1.0;
   double progress = 0.0;
   bool running = false;
-  uint64_t rng_seed = 0, rng_ctr = 0;
+  ingest::Rng rng;             // Store.random: the graph's random draws
+  std::string seed_text;       // the copied cgl_config.random_seed_text
   uint64_t tick = 0;
 
   // device state
@@ -111,12 +113,7 @@ struct cgl_engine {
   bool graph_dirty = true;
   bool use_graph = true;
 
-  double rnd(double mn, double mx) {
-    ingest::Rng r{rng_seed, rng_ctr};
-    const double v = r.uniform(mn, mx);
-    rng_ctr = r.ctr;
-    return v;
-  }
+  double rnd(double mn, double mx) { return rng.uniform(mn, mx); }
 };
 
 namespace {
@@ -480,9 +477,9 @@ cgl_status build_links_device(cgl_engine* e, uint64_t E64, size_t n) {
   using namespace dingest;
   cudaStream_t st = e->stream;
   const uint32_t E = (uint32_t)E64, N = (uint32_t)n;
-  DevBuf t_links, t_str, t_valid, t_len_in, t_len_out, t_kin, t_kout, t_vin, t_vout, t_tmp, t_stats;
+  DevBuf t_links, t_str, t_valid, t_len_in, t_len_out, t_kin, t_kout, t_vin, t_vout, t_tmp, t_stats, t_draws;
   DevBuf* temps[] = {&t_links, &t_str, &t_valid, &t_len_in, &t_len_out, &t_kin, &t_kout, &t_vin, &t_vout, &t_tmp,
-                     &t_stats};
+                     &t_stats, &t_draws};
   auto done = [&](cgl_status rc) {
     for (DevBuf* b : temps) dev_release(e, *b);
     return rc;
@@ -546,12 +543,26 @@ cgl_status build_links_device(cgl_engine* e, uint64_t E64, size_t n) {
   const int row_bits = key_bits(n ? n - 1 : 0);
   sort_pairs(kin, vin, M, row_bits, tmp, st);
   sort_pairs(kout, vout, M, row_bits, tmp, st);
-  const uint64_t base = e->rng_ctr;
-  fill_csr(kin, vin, M, links, true, len_in, len_out, strength, (const uint8_t*)e->b_flags.p, e->rng_seed, base,
-           0, (uint4*)e->b_ent_in.p, st);
-  fill_csr(kout, vout, M, links, false, len_in, len_out, strength, (const uint8_t*)e->b_flags.p, e->rng_seed,
-           base + M, 0, (uint4*)e->b_ent_out.p, st);
-  e->rng_ctr += 2 * (uint64_t)M;
+  const uint64_t base = e->rng.ctr;
+  const float* draws_in = nullptr;
+  const float* draws_out = nullptr;
+  if (!e->rng.counter && M) {
+    // The reference's stream is sequential: draw both directions' values on the
+    // host (entry order, incoming first) while the sorts run, then upload them.
+    std::vector<float> h_draws(2 * (size_t)M);
+    e->rng.fill_unit_f32(h_draws.data(), 2 * (uint64_t)M);
+    if ((rc = dev_reserve(e, t_draws, 2 * (size_t)M * sizeof(float), false))) return done(rc);
+    TCU(cudaMemcpyAsync(t_draws.p, h_draws.data(), 2 * (size_t)M * sizeof(float), cudaMemcpyHostToDevice, st));
+    TCU(cudaStreamSynchronize(st));   // h_draws is pageable and about to go
+    draws_in = (const float*)t_draws.p;
+    draws_out = draws_in + M;
+  } else {
+    e->rng.ctr += 2 * (uint64_t)M;
+  }
+  fill_csr(kin, vin, M, links, true, len_in, len_out, strength, (const uint8_t*)e->b_flags.p, draws_in, e->rng.seed,
+           base, 0, (uint4*)e->b_ent_in.p, st);
+  fill_csr(kout, vout, M, links, false, len_in, len_out, strength, (const uint8_t*)e->b_flags.p, draws_out,
+           e->rng.seed, base + M, 0, (uint4*)e->b_ent_out.p, st);
   // rowptr = exclusive scan of the list lengths (len[n] = 0 makes rowptr[n] = M)
   copy_u32(len_in, (uint32_t*)e->b_rowptr_in.p, N + 1, st);
   scan_exclusive((uint32_t*)e->b_rowptr_in.p, N + 1, tmp, st);
@@ -646,7 +657,6 @@ void forget_graph(cgl_engine* e) {
   e->point_clusters = e->cluster_positions = false;
   e->n_clusters = 0;
   e->running = false;
-  e->drag_index = -1;
   e->pos_dirty = e->links_dirty = e->sizes_dirty = e->clusters_dirty = true;
   e->graph_dirty = true;
   refresh_view(e);
@@ -661,10 +671,10 @@ cgl_status do_render(cgl_engine* e, double alpha) {
   if (N == 0 && E == 0) return CGL_OK;   // empty render (src/index.ts:941-955)
   if (N > (1ull << 24)) return fail(e, CGL_INVALID_ARG, "%llu points: point indices must stay exact in f32 (max 2^24)", (unsigned long long)N);
   if (E > 0xFFFFFFF0ull) return fail(e, CGL_INVALID_ARG, "too many links");
-  const uint64_t rng_ctr = e->rng_ctr;
+  const ingest::Rng rng = e->rng;
   const cgl_status st = build_graph(e, alpha, N, E);
   if (st != CGL_OK) {
-    e->rng_ctr = rng_ctr;
+    e->rng = rng;
     forget_graph(e);
   }
   return st;
@@ -685,9 +695,16 @@ cgl_status build_graph(cgl_engine* e, double alpha, uint64_t N, uint64_t E) {
   const size_t n = e->N;
   if (pos_changed) {
     e->graph_dirty = true;
-    // Points.updatePositions (Points/index.ts:390-592)
+    // Points.updatePositions (Points/index.ts:390-592): the optional rescale
+    // (:396-413), then absence and the position texture
     std::vector<float2> pos;
-    e->live = ingest::canonical_positions(e->in_pos.data(), n, pos, e->absent);
+    if (ingest::should_rescale(e->cfg, e->skip_rescale)) {
+      std::vector<float> xy(e->in_pos);
+      ingest::rescale_positions(xy.data(), n, e->cfg.space_size);
+      e->live = ingest::canonical_positions(xy.data(), n, pos, e->absent);
+    } else {
+      e->live = ingest::canonical_positions(e->in_pos.data(), n, pos, e->absent);
+    }
     if ((st = dev_reserve(e, e->b_pos, n * sizeof(float2), false))) return st;
     if ((st = dev_reserve(e, e->b_pos_alt, n * sizeof(float2), false))) return st;
     if ((st = dev_reserve(e, e->b_flags, n, false))) return st;
@@ -727,15 +744,13 @@ cgl_status build_graph(cgl_engine* e, double alpha, uint64_t N, uint64_t E) {
       if ((st = dev_reserve(e, e->b_big_sy, cells * sizeof(long long), false))) return st;
       if ((st = dev_reserve(e, e->b_big_ns, cells * sizeof(uint32_t), false))) return st;
       const uint64_t texels = (uint64_t)e->T * e->T;
-      if (!(e->cfg.device_ingest_min_links > (double)n)) {   // drawn on the device, same draws
-        dingest::jitter(e->rng_seed, e->rng_ctr, (uint32_t)n, (float2*)e->b_jitter.p, e->stream);
+      if (e->rng.counter && !(e->cfg.device_ingest_min_links > (double)n)) {   // drawn on the device, same draws
+        dingest::jitter(e->rng.seed, e->rng.ctr, (uint32_t)n, (float2*)e->b_jitter.p, e->stream);
         CU(cudaGetLastError());
-        e->rng_ctr += 2 * texels;
+        e->rng.ctr += 2 * texels;
       } else {
         std::vector<float2> jit;
-        ingest::Rng rng{e->rng_seed, e->rng_ctr};
-        ingest::jitter(rng, n, jit);
-        e->rng_ctr = rng.ctr;
+        ingest::jitter(e->rng, n, jit);
         if (n) CU(cudaMemcpyAsync(e->b_jitter.p, jit.data(), n * sizeof(float2), cudaMemcpyHostToDevice, e->stream));
       }
       CU(cudaStreamSynchronize(e->stream));
@@ -753,10 +768,8 @@ cgl_status build_graph(cgl_engine* e, double alpha, uint64_t N, uint64_t E) {
     } else {
     ingest::Csr cin, cout_;
     if (e->T && e->W) {
-      ingest::Rng rng{e->rng_seed, e->rng_ctr};
-      ingest::build_links(e->in_links.data(), E, n, e->has_strength ? e->in_strength.data() : nullptr, e->absent, rng,
-                          cin, cout_);
-      e->rng_ctr = rng.ctr;
+      ingest::build_links(e->in_links.data(), E, n, e->has_strength ? e->in_strength.data() : nullptr, e->absent,
+                          e->rng, cin, cout_);
     } else {
       cin.rowptr.assign(n + 1, 0);
       cout_.rowptr.assign(n + 1, 0);
@@ -817,6 +830,7 @@ cgl_status build_graph(cgl_engine* e, double alpha, uint64_t N, uint64_t E) {
   }
   refresh_view(e);
   e->pos_dirty = e->links_dirty = e->sizes_dirty = e->clusters_dirty = false;
+  if (pos_changed) e->skip_rescale = false;   // Points/index.ts:412-413
   if (!std::isnan(alpha)) e->alpha = alpha;
   return CGL_OK;
 }
@@ -856,6 +870,9 @@ void cgl_config_defaults(cgl_config* c) {
   c->enable_right_click_repulsion = 0;
   c->enable_drag = 0;
   c->device_ingest_min_links = 65536;
+  c->random_stream = CGL_RANDOM_REFERENCE;
+  c->rescale_positions = -1;
+  c->random_seed_text = nullptr;
 }
 
 cgl_status cgl_create(const cgl_config* cfg, cgl_engine** out) {
@@ -864,8 +881,10 @@ cgl_status cgl_create(const cgl_config* cfg, cgl_engine** out) {
   cgl_engine* e = new cgl_engine();
   e->cfg = *cfg;
   e->device = cfg->device;
-  if (cfg->has_random_seed) e->rng_seed = cfg->random_seed;
-  else { std::random_device rd; e->rng_seed = ((uint64_t)rd() << 32) ^ rd(); }
+  // Store.addRandomSeed (src/index.ts:452): the seed text is copied and kept
+  if (cfg->has_random_seed && cfg->random_seed_text) e->seed_text = cfg->random_seed_text;
+  e->cfg.random_seed_text = (cfg->has_random_seed && cfg->random_seed_text) ? e->seed_text.c_str() : nullptr;
+  ingest::seed_rng(e->cfg, e->rng);
   adjust_space_size(e);
   const char* g = getenv("CGL_NO_GRAPH");
   e->use_graph = !(g && g[0] == '1');
@@ -922,6 +941,8 @@ cgl_status cgl_set_config(cgl_engine* e, const cgl_config* cfg) {
   e->cfg = *cfg;
   e->cfg.has_random_seed = prev.has_random_seed;   // init-only (src/index.ts:1720-1724)
   e->cfg.random_seed = prev.random_seed;
+  e->cfg.random_seed_text = prev.random_seed_text;
+  e->cfg.random_stream = prev.random_stream;
   e->cfg.device = prev.device;
   e->graph_dirty = true;
   if (prev.space_size != e->cfg.space_size) {
@@ -942,6 +963,10 @@ cgl_status cgl_get_config(cgl_engine* e, cgl_config* out) {
 }
 
 cgl_status cgl_set_point_positions(cgl_engine* e, const float* xy, uint64_t n) {
+  return cgl_set_point_positions_ex(e, xy, n, 0);
+}
+
+cgl_status cgl_set_point_positions_ex(cgl_engine* e, const float* xy, uint64_t n, int32_t dont_rescale) {
   CHECK_E(e);
   if (!xy && n) return CGL_INVALID_ARG;
   cgl_status st = CGL_OK;
@@ -952,6 +977,7 @@ cgl_status cgl_set_point_positions(cgl_engine* e, const float* xy, uint64_t n) {
   }
   e->in_pos.assign(xy, xy + n);
   e->have_pos_input = true;
+  e->skip_rescale = dont_rescale != 0;   // src/index.ts:553
   e->pos_dirty = e->links_dirty = e->sizes_dirty = true;
   e->clusters_dirty = true;   // src/index.ts:570
   return st;
@@ -1254,11 +1280,19 @@ cgl_status cgl_get_state(cgl_engine* e, cgl_state* s) {
   s->tick = e->tick;
   s->points_number = e->N;
   s->links_number = e->E;
-  s->rng_draws = e->rng_ctr;
+  s->rng_draws = e->rng.ctr;
   return CGL_OK;
 }
 
 const char* cgl_last_error(cgl_engine* e) { return e ? e->err.c_str() : "null engine"; }
+
+cgl_status cgl_random_draws(const char* seed_text, uint64_t n, double* out) {
+  if (!seed_text || (!out && n)) return CGL_INVALID_ARG;
+  RandomStream r;
+  r.seed_utf8(seed_text);
+  for (uint64_t k = 0; k < n; ++k) out[k] = r.next();
+  return CGL_OK;
+}
 
 cgl_status cgl_set_stream(cgl_engine* e, void* cuda_stream) {
   CHECK_E(e);

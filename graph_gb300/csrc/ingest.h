@@ -10,30 +10,92 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <random>
+#include <string>
 #include <vector>
 
 #include "../../include/cgl.h"
 #include "common.cuh"
+#include "random_stream.h"
 
 namespace cgl {
 namespace ingest {
 
-// SplitMix64 draw k (0-based) of seed s; u = top 53 bits / 2^53, and
-// Random.float(min, max) = min + (max - min) * u (Store/index.ts:200-202).
+// SplitMix64 draw k (0-based) of seed s (the counter stream, below).
 inline uint64_t splitmix_draw(uint64_t seed, uint64_t k) {
   uint64_t z = seed + (k + 1) * 0x9E3779B97F4A7C15ull;
   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
   z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
   return z ^ (z >> 31);
 }
+inline double splitmix_unit(uint64_t seed, uint64_t k) { return (double)(splitmix_draw(seed, k) >> 11) * 0x1.0p-53; }
 
+// The random draws of one graph, in the reference's order and count
+// (Store.getRandomFloat, Store/index.ts:200-202).  By default they are the
+// reference's own stream (random_stream.h: random@4.1.0 over seedrandom@3.0.5,
+// seeded with String(randomSeed)).  cgl_config.random_stream =
+// CGL_RANDOM_COUNTER selects SplitMix64 instead (draw k of seed s =
+// splitmix(s + (k + 1) * golden gamma), u = top 53 bits / 2^53): not the
+// reference's values, but draw k needs no earlier draw, so the device builds
+// large graphs' jitter and link draws itself.
 struct Rng {
-  uint64_t seed = 0, ctr = 0;
-  double uniform(double mn, double mx) {
-    const double u = (double)(splitmix_draw(seed, ctr++) >> 11) * 0x1.0p-53;
-    return mn + (mx - mn) * u;
+  bool counter = false;
+  RandomStream ref;        // the reference's stream
+  uint64_t seed = 0;       // the counter stream's seed
+  uint64_t ctr = 0;        // draws so far
+
+  double unit() {
+    const double u = counter ? splitmix_unit(seed, ctr) : ref.next();
+    ++ctr;
+    return u;
+  }
+  // Random.float(min, max) = next() * (max - min) + min
+  double uniform(double mn, double mx) { return unit() * (mx - mn) + mn; }
+
+  // out[k] = f32(float(0, 1)), n draws (ForceLink/index.ts:76)
+  void fill_unit_f32(float* out, uint64_t n) {
+    if (counter) {
+      for (uint64_t k = 0; k < n; ++k) out[k] = (float)splitmix_unit(seed, ctr + k);
+    } else {
+      ref.fill_unit_f32(out, n);
+    }
+    ctr += n;
+  }
+  // ForceManyBody.create jitter (ForceManyBody/index.ts:133-138): two draws per
+  // texel of `texels`, f32(float(-1, 1) * 0.00001); the first `keep` texels kept.
+  void fill_jitter(float* out_xy, uint64_t keep, uint64_t texels) {
+    if (counter) {
+      for (uint64_t t = 0; t < texels; ++t) {
+        const double ux = splitmix_unit(seed, ctr + 2 * t), uy = splitmix_unit(seed, ctr + 2 * t + 1);
+        if (t < keep) {
+          out_xy[2 * t] = (float)((ux * 2.0 + -1.0) * 0.00001);
+          out_xy[2 * t + 1] = (float)((uy * 2.0 + -1.0) * 0.00001);
+        }
+      }
+    } else {
+      ref.fill_jitter(out_xy, keep, texels);
+    }
+    ctr += 2 * texels;
   }
 };
+
+// Store.addRandomSeed(randomSeed) (Store/index.ts:196-198, src/index.ts:452):
+// the seed text is random_seed_text when given, else random_seed in decimal
+// (JavaScript's String(n) for an integer below 2^53).  Without a seed the
+// reference draws from Math.random; the engine seeds from the host's entropy.
+inline void seed_rng(const cgl_config& c, Rng& r) {
+  r = Rng{};
+  r.counter = c.random_stream == CGL_RANDOM_COUNTER;
+  if (c.has_random_seed) {
+    r.seed = c.random_seed;
+    if (c.random_seed_text) r.ref.seed_utf8(c.random_seed_text);
+    else r.ref.seed_utf8(std::to_string(c.random_seed).c_str());
+  } else {
+    std::random_device rd;
+    r.seed = ((uint64_t)rd() << 32) ^ rd();
+    r.ref.seed_utf8(std::to_string(r.seed).c_str());
+  }
+}
 
 // Store.adjustSpaceSize (Store/index.ts:209-233)
 inline double adjusted_space(const cgl_config& c) {
@@ -83,6 +145,69 @@ inline Grid grid_for(uint64_t n) {
 // cells of all levels of a pyramid with `levels` levels, and the offset of level l
 inline uint32_t level_base(int l) { uint32_t o = 0; for (int m = 0; m < l; ++m) o += (uint32_t)((4 << m) * (4 << m)); return o; }
 
+// Math.min / Math.max of two doubles: NaN if either is NaN, -0 below +0.
+inline double js_min(double a, double b) {
+  if (std::isnan(a) || std::isnan(b)) return NAN;
+  if (a == b) return std::signbit(a) ? a : b;
+  return a < b ? a : b;
+}
+inline double js_max(double a, double b) {
+  if (std::isnan(a) || std::isnan(b)) return NAN;
+  if (a == b) return std::signbit(a) ? b : a;
+  return a > b ? a : b;
+}
+
+// Points.updatePositions' rescale decision (Points/index.ts:396-402):
+// rescalePositions, or true when it is undefined and the simulation is off;
+// setPointPositions(…, dontRescale) skips it once.
+inline bool should_rescale(const cgl_config& c, bool dont_rescale) {
+  bool r = c.rescale_positions == 1;
+  if (c.rescale_positions < 0 && !c.enable_simulation) r = true;
+  return r && !dont_rescale;
+}
+
+// Points.rescaleInitialNodePositions (Points/index.ts:3134-3218) on the staged
+// positions, in place: the extent of the live points (absent = NaN in either
+// coordinate, left as they are), then x' = (x - minX) * scale + offsetX in FP64
+// as in JavaScript, stored as f32 like the reference's Float32Array.  `space` is
+// the configured spaceSize (not the adjusted one).
+inline void rescale_positions(float* xy, uint64_t n, double space) {
+  if (space == 0 || std::isnan(space)) return;
+  double minX = INFINITY, maxX = -INFINITY, minY = INFINITY, maxY = -INFINITY;
+  for (uint64_t i = 0; i < n; ++i) {
+    const float x = xy[2 * i], y = xy[2 * i + 1];
+    if (std::isnan(x) || std::isnan(y)) continue;
+    minX = js_min(minX, x);
+    maxX = js_max(maxX, x);
+    minY = js_min(minY, y);
+    maxY = js_max(maxY, y);
+  }
+  if (!std::isfinite(minX)) return;   // no live point (or an infinite extent): no scale
+  const double w = maxX - minX, h = maxY - minY;
+  const double range = js_max(w, h);
+  if (range == 0) {   // one point or all coincident: centre them, keeping offsets
+    const double center = space / 2;
+    for (uint64_t i = 0; i < n; ++i) {
+      if (std::isnan(xy[2 * i]) || std::isnan(xy[2 * i + 1])) continue;
+      xy[2 * i] = (float)((double)xy[2 * i] - minX + center);
+      xy[2 * i + 1] = (float)((double)xy[2 * i + 1] - minY + center);
+    }
+    return;
+  }
+  if (range > space) return;
+  const double density = space * space * 0.001;
+  const double effective = (double)n > density ? space * js_max(1.2, std::sqrt((double)n) / space) : space * 0.1;
+  const double scale = effective / range;
+  const double center_off = (space - effective) / 2;
+  const double offX = ((range - w) / 2) * scale + center_off;
+  const double offY = ((range - h) / 2) * scale + center_off;
+  for (uint64_t i = 0; i < n; ++i) {
+    if (std::isnan(xy[2 * i]) || std::isnan(xy[2 * i + 1])) continue;
+    xy[2 * i] = (float)(((double)xy[2 * i] - minX) * scale + offX);
+    xy[2 * i + 1] = (float)(((double)xy[2 * i + 1] - minY) * scale + offY);
+  }
+}
+
 // Points.updatePositions (Points/index.ts:390-592, position-utils.ts:9-27):
 // a NaN in either coordinate makes the point absent (both coordinates NaN).
 inline uint64_t canonical_positions(const float* xy, uint64_t n, std::vector<float2>& pos, std::vector<uint8_t>& absent) {
@@ -104,12 +229,7 @@ inline uint64_t canonical_positions(const float* xy, uint64_t n, std::vector<flo
 inline void jitter(Rng& rng, uint64_t n, std::vector<float2>& out) {
   out.resize(n);
   const uint64_t T = (uint64_t)std::ceil(std::sqrt((double)n));
-  const uint64_t texels = T * T;
-  for (uint64_t t = 0; t < texels; ++t) {
-    const float jx = (float)(rng.uniform(-1, 1) * 0.00001);
-    const float jy = (float)(rng.uniform(-1, 1) * 0.00001);
-    if (t < n) out[t] = make_float2(jx, jy);
-  }
+  rng.fill_jitter((float*)out.data(), n, T * T);
 }
 
 struct Csr {

@@ -191,13 +191,16 @@ __device__ __forceinline__ uint64_t splitmix_draw(uint64_t seed, uint64_t k) {
 }
 
 // One entry of a direction's CSR (ForceLink/index.ts:57-76): neighbour (or the
-// absent sentinel), the f32 random rest-length draw, bias and strength.
+// absent sentinel), the f32 random rest-length draw, bias and strength.  The
+// draw is draws[at] when the host drew the graph's values (the reference's
+// sequential stream), else counter draw draw_base + at of `seed`.
 __global__ void __launch_bounds__(kBlock) k_csr_fill(const uint32_t* __restrict__ rows, const uint32_t* __restrict__ lidx,
                                                      uint32_t M, const float2* __restrict__ links, int incoming,
                                                      const uint32_t* __restrict__ len_in,
                                                      const uint32_t* __restrict__ len_out,
                                                      const float* __restrict__ strength,
-                                                     const uint8_t* __restrict__ flags, uint64_t seed,
+                                                     const uint8_t* __restrict__ flags,
+                                                     const float* __restrict__ draws, uint64_t seed,
                                                      uint64_t draw_base, uint32_t point_off, uint4* __restrict__ ent) {
   const uint32_t at = blockIdx.x * blockDim.x + threadIdx.x;
   if (at >= M) return;
@@ -213,9 +216,15 @@ __global__ void __launch_bounds__(kBlock) k_csr_fill(const uint32_t* __restrict_
   if (!strength || !isfinite(si) || si < 0.0) st = __ddiv_rn(1.0, mind < 1.0 ? 1.0 : mind);
   else st = si;
   st = __dsqrt_rn(st);
-  // Random.float(0, 1) = 0 + (1 - 0) * u, u = top 53 bits / 2^53 (exact), rounded to f32
-  const double u = (double)(splitmix_draw(seed, draw_base + at) >> 11) * 0x1.0p-53;
-  ent[at] = make_uint4((flags[q] & kAbsent) ? kAbsentTarget : q + point_off, __float_as_uint(__double2float_rn(u)),
+  float r;
+  if (draws) {
+    r = draws[at];
+  } else {
+    // Random.float(0, 1) = u * (1 - 0) + 0, u = top 53 bits / 2^53 (exact), rounded to f32
+    const double u = (double)(splitmix_draw(seed, draw_base + at) >> 11) * 0x1.0p-53;
+    r = __double2float_rn(u);
+  }
+  ent[at] = make_uint4((flags[q] & kAbsent) ? kAbsentTarget : q + point_off, __float_as_uint(r),
                        __float_as_uint(__double2float_rn(bias)), __float_as_uint(__double2float_rn(st)));
 }
 
@@ -339,10 +348,10 @@ void compact_links(const float2* links, uint32_t E, const uint32_t* pos, uint32_
 
 void fill_csr(const uint32_t* rows, const uint32_t* lidx, uint32_t M, const float2* links, bool incoming,
               const uint32_t* len_in, const uint32_t* len_out, const float* strength, const uint8_t* flags,
-              uint64_t seed, uint64_t draw_base, uint32_t point_off, uint4* ent, cudaStream_t st) {
+              const float* draws, uint64_t seed, uint64_t draw_base, uint32_t point_off, uint4* ent, cudaStream_t st) {
   if (M)
     k_csr_fill<<<ceil_div(M, kBlock), kBlock, 0, st>>>(rows, lidx, M, links, incoming ? 1 : 0, len_in, len_out,
-                                                        strength, flags, seed, draw_base, point_off, ent);
+                                                        strength, flags, draws, seed, draw_base, point_off, ent);
 }
 
 void len_stats(const uint32_t* len, uint32_t N, uint32_t* stats, cudaStream_t st) {

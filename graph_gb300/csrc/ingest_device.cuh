@@ -29,16 +29,17 @@ void count_links(const float2* links, uint32_t E, uint32_t N, uint32_t* valid, u
 void compact_links(const float2* links, uint32_t E, const uint32_t* pos, uint32_t* key_in, uint32_t* key_out,
                    uint32_t* val_in, uint32_t* val_out, cudaStream_t st);
 // Entries of one direction from its row-sorted (row, link) pairs; entry `at`
-// draws random number draw_base + at of `seed`; neighbours are written as
+// takes draws[at] (device memory, drawn on the host) or, when draws is null,
+// counter draw draw_base + at of `seed`; neighbours are written as
 // point_off + index (flags indexed by the graph's own point index).
 void fill_csr(const uint32_t* rows, const uint32_t* lidx, uint32_t M, const float2* links, bool incoming,
               const uint32_t* len_in, const uint32_t* len_out, const float* strength, const uint8_t* flags,
-              uint64_t seed, uint64_t draw_base, uint32_t point_off, uint4* ent, cudaStream_t st);
+              const float* draws, uint64_t seed, uint64_t draw_base, uint32_t point_off, uint4* ent, cudaStream_t st);
 // stats[0] = longest list, stats[1] = lists longer than kHeavyDegree (stats zeroed by the caller)
 void len_stats(const uint32_t* len, uint32_t N, uint32_t* stats, cudaStream_t st);
 // key[p] = stats[0] - len[p], val[p] = p: sorted stably, the points by list length, longest first
 void len_keys(const uint32_t* len, uint32_t N, const uint32_t* stats, uint32_t* key, uint32_t* val, cudaStream_t st);
-// The many-body jitter of points [0, n): draws base + 2t, base + 2t + 1.
+// The many-body jitter of points [0, n) from the counter stream: draws base + 2t, base + 2t + 1.
 void jitter(uint64_t seed, uint64_t base, uint32_t n, float2* out, cudaStream_t st);
 // b[i] = a[i] + add
 void copy_u32(const uint32_t* a, uint32_t* b, uint32_t n, cudaStream_t st, uint32_t add = 0);

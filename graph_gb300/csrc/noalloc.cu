@@ -16,7 +16,10 @@
 // Every call shares that array and it keeps the last call's contents; the
 // first kernel of each call clears what must start at zero.  Calls whose work
 // overlaps on the GPU (different streams, or different host threads without
-// ordering) race on the array.
+// ordering) race on the array.  The array's device address is looked up once
+// per device and kept; a device reset (cudaDeviceReset) unloads the library's
+// device code, after which that address is stale, so a process that resets a
+// device must not call this entry point on that device again.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -26,6 +29,7 @@
 
 #include "../../include/cgl.h"
 #include "common.cuh"
+#include "ingest.h"
 
 namespace cgl {
 namespace {
@@ -111,11 +115,10 @@ extern "C" cgl_status cgl_levels_noalloc(const float* d_xy, uint64_t n_points, d
   if (!d_xy || !d_cells) return na_fail(err, err_len, CGL_INVALID_ARG, "null device pointer");
   if (!(space_size >= 2) || !std::isfinite(space_size))
     return na_fail(err, err_len, CGL_INVALID_ARG, "space size %g must be a finite number >= 2", space_size);
-  // grid sizes as ForceManyBody.createLevels (ForceManyBody/index.ts:646-667)
-  const double target = 2 * std::sqrt((double)n_points);
-  const double g = std::fmin((double)kMaxGrid, std::fmax(8.0, std::pow(2.0, std::ceil(std::log2(target)))));
-  const int gf = (int)g;
-  const int L = (int)std::log2(g) - 1;
+  // grid sizes as the engine's (ForceManyBody.createLevels, ForceManyBody/index.ts:646-667)
+  const ingest::Grid grid = ingest::grid_for(n_points);
+  const int gf = grid.gf;
+  const int L = grid.levels;
   uint32_t off[kNaLevelsMax + 1];
   off[0] = 0;
   for (int l = 0; l < L; ++l) off[l + 1] = off[l] + (uint32_t)((4 << l) * (4 << l));
@@ -126,18 +129,8 @@ extern "C" cgl_status cgl_levels_noalloc(const float* d_xy, uint64_t n_points, d
   if (cells_capacity_floats < 4ull * cells)
     return na_fail(err, err_len, CGL_INVALID_ARG, "output holds %llu floats, %u levels need %llu",
                    (unsigned long long)cells_capacity_floats, L, 4ull * cells);
-  // exact-sum scale as the engine's: B = power of two >= 2*S, F = 62 - ceil(log2 n) - log2 B
-  const float S = (float)space_size;
-  int lb = 0;
-  while (std::ldexp(1.0, lb) < 2.0 * (double)S) ++lb;
-  int ln = 0;
-  while ((1ull << ln) < n_points) ++ln;
-  int F = 62 - ln - lb;
-  if (F > 60) F = 60;
-  FixedScale fx;
-  fx.bound = (float)std::ldexp(1.0, lb);
-  fx.scale = std::ldexp(1.0f, F);
-  fx.inv = std::ldexp(1.0f, -F);
+  // exact-sum scale as the engine's
+  const FixedScale fx = ingest::fixed_for(n_points, space_size, nullptr);
 
   int dev = 0;
   cudaError_t ce = cudaGetDevice(&dev);

@@ -50,6 +50,8 @@ def load_library(build_if_missing: bool = True):
     lib.cgl_levels_noalloc.argtypes = [C.c_void_p, C.c_uint64, C.c_double, C.c_void_p, C.c_uint64, C.c_void_p,
                                        C.c_char_p, C.c_size_t]
     lib.cgl_levels_noalloc.restype = C.c_int
+    lib.cgl_random_draws.argtypes = [C.c_char_p, C.c_uint64, C.POINTER(C.c_double)]
+    lib.cgl_random_draws.restype = C.c_int
     _abi.declare(lib, "cgl")
     _LIB = lib
     return lib

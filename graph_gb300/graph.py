@@ -37,6 +37,8 @@ def _to_fields(config):
             v = math.nan
         if f in ("enable_simulation", "enable_right_click_repulsion", "enable_drag"):
             v = 1 if v else 0
+        if f == "rescale_positions":
+            v = -1 if v is None else (1 if v else 0)
         fields[f] = v
     return fields
 
@@ -47,11 +49,8 @@ class Graph:
         self._callbacks = {k: config.get(k) for k in _CALLBACKS}
         self._config = dict(config)
         fields = _to_fields(config)
-        seed = fields.pop("random_seed", None)
+        # randomSeed seeds the reference's stream with String(randomSeed) (src/index.ts:452)
         cfg = _abi.make_config(device=device, **fields)
-        if seed is not None:
-            cfg.has_random_seed = 1
-            cfg.random_seed = _abi.seed_to_u64(seed)
         self._engine = Engine(cfg)
         self._destroyed = False
         self._staged = {}
@@ -92,9 +91,11 @@ class Graph:
 
     # --- data (staged by reference, read at render) -------------------------
     def setPointPositions(self, pointPositions, dontRescale=None):
+        """Stage positions; dontRescale skips the next render's rescale (src/index.ts:548-553)."""
         if self._destroyed:
             return
         self._staged["positions"] = pointPositions
+        self._staged["dont_rescale"] = bool(dontRescale)
 
     def setLinks(self, links):
         if self._destroyed:
@@ -139,8 +140,13 @@ class Graph:
         if self._destroyed:
             return
         s = self._staged
+        rescaled = None
         if "positions" in s:
-            self._engine.set_point_positions(s.pop("positions"))
+            positions = s.pop("positions")
+            dont = s.pop("dont_rescale", False)
+            self._engine.set_point_positions_ex(positions, dont)
+            if self._rescales(dont):
+                rescaled = positions
         if "links" in s:
             self._engine.set_links(s.pop("links"))
         if "strength" in s:
@@ -154,6 +160,22 @@ class Graph:
         if "cluster_strength" in s:
             self._engine.set_point_cluster_strength(s.pop("cluster_strength"))
         self._engine.render(simulationAlpha)
+        if isinstance(rescaled, np.ndarray) and rescaled.dtype == np.float32 and rescaled.flags.writeable:
+            # the reference rescales the caller's Float32Array in place
+            # (Points/index.ts:3211-3216): copy the rescaled live positions back
+            now = self._engine.get_point_positions()
+            if now.size == rescaled.size:
+                flat = rescaled.reshape(-1)
+                live = ~(np.isnan(flat[0::2]) | np.isnan(flat[1::2]))
+                flat[0::2][live] = now[0::2][live]
+                flat[1::2][live] = now[1::2][live]
+
+    def _rescales(self, dont_rescale):
+        # Points.updatePositions (Points/index.ts:396-402)
+        r = self._config.get("rescalePositions")
+        if r is None and not self._config.get("enableSimulation", True):
+            r = True
+        return bool(r) and not dont_rescale
 
     # --- control (src/index.ts:1457-1540) ------------------------------------
     def _cb(self, name, *args):

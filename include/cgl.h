@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define CGL_ABI_VERSION 1u
+#define CGL_ABI_VERSION 2u
 
 typedef enum cgl_status {
   CGL_OK = 0,
@@ -52,6 +52,15 @@ enum {
   CGL_STAGE_COLLISION = 1u << 5,
   CGL_STAGE_CLUSTERS = 1u << 6,
   CGL_STAGE_ALL = 0x7Fu
+};
+
+/* cgl_config.random_stream: where the random draws come from.  Both give the
+ * reference's draw order and count (the jitter, one draw per link entry
+ * incoming then outgoing, one peel seed per tick). */
+enum {
+  CGL_RANDOM_REFERENCE = 0, /* the reference's stream: random@4.1.0 float(min, max) over
+                               seedrandom@3.0.5 seeded with String(randomSeed) (default) */
+  CGL_RANDOM_COUNTER = 1    /* SplitMix64 by draw index: other values, but large graphs draw on the GPU */
 };
 
 /* Simulation configuration.  Field meanings and defaults follow the reference:
@@ -85,9 +94,17 @@ typedef struct cgl_config {
   double simulation_repulsion_from_mouse;    /* simulationRepulsionFromMouse, default 2 (variables.ts:77) */
   int32_t enable_right_click_repulsion;      /* enableRightClickRepulsion, default 0 (variables.ts:83) */
   int32_t enable_drag;                       /* enableDrag, default 0 (variables.ts:132) */
-  double device_ingest_min_links;            /* the link lists (from this many links up) and the many-body jitter
-                                                (from this many points up) are built on the GPU; default 65536,
-                                                0 = always, +inf = never; both builds give the same data */
+  double device_ingest_min_links;            /* the link lists (from this many links up) and, with the counter
+                                                stream, the many-body jitter (from this many points up) are built
+                                                on the GPU; default 65536, 0 = always, +inf = never; both builds
+                                                give the same data */
+  int32_t random_stream;                     /* CGL_RANDOM_REFERENCE (default) or CGL_RANDOM_COUNTER; init-only */
+  int32_t rescale_positions;                 /* rescalePositions (config.ts:798): -1 undefined (default), 0 false,
+                                                1 true; undefined rescales when enable_simulation is 0
+                                                (Points/index.ts:396-398) */
+  const char* random_seed_text;              /* with has_random_seed: randomSeed as text (UTF-8), for string seeds
+                                                and non-integer numbers (the reference seeds with String(seed));
+                                                NULL = random_seed in decimal.  Copied at cgl_create; init-only */
 } cgl_config;
 
 typedef struct cgl_state {
@@ -121,8 +138,17 @@ cgl_status cgl_get_config(cgl_engine* e, cgl_config* out);
 
 /* Graph.setPointPositions(Float32Array) — src/index.ts:548-574.  xy = [x0,y0,x1,y1,...];
  * a NaN in either coordinate marks the point absent (helper.ts:157-159).  An odd
- * length drops the trailing value with CGL_WARNING (GraphData/index.ts:117-120). */
+ * length drops the trailing value with CGL_WARNING (GraphData/index.ts:117-120).
+ * At render the positions are rescaled into the space when rescale_positions is
+ * 1, or when it is -1 and enable_simulation is 0 (Points.updatePositions,
+ * Points/index.ts:390-413; rescaleInitialNodePositions :3134-3218).  The
+ * reference rescales the caller's array in place; here the caller's array is not
+ * written (cgl_get_point_positions after cgl_render returns the rescaled values). */
 cgl_status cgl_set_point_positions(cgl_engine* e, const float* xy, uint64_t n_floats);
+/* Graph.setPointPositions(pointPositions, dontRescale) — src/index.ts:548-553:
+ * dont_rescale != 0 skips the rescale at the next render only
+ * (Points.shouldSkipRescale, Points/index.ts:399-413). */
+cgl_status cgl_set_point_positions_ex(cgl_engine* e, const float* xy, uint64_t n_floats, int32_t dont_rescale);
 
 /* Graph.setLinks(Float32Array) — src/index.ts:723-734.  st = [s0,t0,s1,t1,...] of
  * point indices as floats; links with an invalid endpoint are skipped but keep
@@ -245,6 +271,12 @@ const char* cgl_last_error(cgl_engine* e);
 
 /* --- Engine extensions (no counterpart in the reference) ------------------- */
 
+/* The reference's random stream without a GPU: the first n values of
+ * seedrandom(seed_text) (random@4.1.0's next(), in [0, 1)) into out.  The
+ * engine seeds its stream with String(randomSeed); this lets a host or a test
+ * reproduce the draws.  seed_text is UTF-8. */
+cgl_status cgl_random_draws(const char* seed_text, uint64_t n, double* out);
+
 /* Run the engine's kernels on a caller-owned cudaStream_t (NULL = engine's own). */
 cgl_status cgl_set_stream(cgl_engine* e, void* cuda_stream);
 /* Block until all queued work on the engine stream finished. */
@@ -329,14 +361,17 @@ const char* cgl_batch_last_error(cgl_batch* b);
  * code recording a CUDA graph (cudaMalloc is not allowed during capture), and
  * frame loops that cannot absorb cudaMalloc's implicit synchronisation.
  * d_xy: device positions [x0,y0,x1,y1,...] of n_points points (NaN = absent);
+ * space_size: the space the engine simulates in (the configured spaceSize
+ * unless max_texture_dimension reduced it, Store.adjustSpaceSize);
  * d_cells: device output, every level's cells (centroid x, centroid y, count,
  * 0), level 0 first, row-major — the cells the engine's many-body pass builds
  * for the same positions (engine levels via cgl_debug_get_cells).  Scratch is
  * a fixed 8.4 MB static device array (the largest pyramid: finest grid 512, 8
  * levels); n_points above 2^24 is rejected with CGL_INVALID_ARG.  The first
  * call on a device looks up that array's device address, so make it before any
- * stream capture.  All calls share the array: calls that overlap on the GPU
- * race.  err (optional) receives the error text.  Runs on cuda_stream
+ * stream capture; the address is kept, so after a device reset (cudaDeviceReset)
+ * this entry point must not be called on that device again.  All calls share
+ * the array: calls that overlap on the GPU race.  err (optional) receives the error text.  Runs on cuda_stream
  * (NULL = default stream) of the current device; calls no allocator. */
 cgl_status cgl_levels_noalloc(const float* d_xy, uint64_t n_points, double space_size, float* d_cells,
                               uint64_t cells_capacity_floats, void* cuda_stream, char* err, size_t err_len);

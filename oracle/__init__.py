@@ -38,6 +38,8 @@ def load():
         lib.orc_peel_hash.restype = C.c_float
         lib.orc_splitmix_draw.argtypes = [C.c_uint64, C.c_uint64]
         lib.orc_splitmix_draw.restype = C.c_uint64
+        lib.orc_seedrandom.argtypes = [C.c_char_p, C.c_uint64, C.POINTER(C.c_double)]
+        lib.orc_seedrandom.restype = None
         lib.orc_sincos.argtypes = [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]
         lib.orc_sincos.restype = None
         lib.orc_cell_index.argtypes = [C.c_float, C.c_float, C.c_int]
@@ -117,6 +119,13 @@ def peel_hash(index, seed_bits):
 
 def splitmix_draw(seed, k):
     return load().orc_splitmix_draw(seed, k)
+
+
+def seedrandom(seed_text, n):
+    """The oracle's restatement of seedrandom@3.0.5: its first n values for seed_text."""
+    out = np.zeros(n, dtype=np.float64)
+    load().orc_seedrandom(str(seed_text).encode("utf-8"), n, out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out
 
 
 def sincos(a):

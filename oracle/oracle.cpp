@@ -37,13 +37,21 @@
 //    f32 adds in draw order; that variant is kept as sum_mode 1 to put the
 //    difference on record.  Blending of full-screen passes into the velocity
 //    target is restated as f32 adds in pass order.
-//  * random numbers: SplitMix64 (Steele, Lea, Flood 2014; Vigna's reference
-//    constants), draw k of seed s = mix(s + (k+1)*0x9E3779B97F4A7C15),
-//    u = (mix >> 11) * 2^-53, Random.float(min,max) = min + (max-min)*u.  The
-//    reference's generator is random@4.1.0 over seedrandom@3.0.5
-//    (package-lock.json:8264-8274, 8687-8690), absent here; the restatement
-//    keeps its draw ORDER and COUNT (Store/index.ts:200-202 call sites:
-//    ForceManyBody/index.ts:133-138, :521; ForceLink/index.ts:76).
+//  * random numbers: the reference's generator, random@4.1.0 over
+//    seedrandom@3.0.5 (package-lock.json:8264-8274, 8687-8690; neither is
+//    vendored in the reference), restated from their published algorithms in
+//    Arc4Seed below: Random.clone(seed) seeds seedrandom with String(seed);
+//    seedrandom mixes the string's UTF-16 code units into an RC4 key, drops
+//    256 bytes and builds each double from 7+ bytes; Random.float(min, max) =
+//    next() * (max - min) + min.  Pinned by seedrandom's README known answers
+//    (tests/test_oracle.py).  Draw ORDER and COUNT follow the call sites of
+//    Store.getRandomFloat (Store/index.ts:200-202): ForceManyBody/index.ts:133-138,
+//    :521; ForceLink/index.ts:76.  The one step no available source pins is
+//    random's own glue (that it seeds with `seed + ''` and scales next() as
+//    above); it is the package's documented behaviour.  random_stream =
+//    CGL_RANDOM_COUNTER selects SplitMix64 instead (Steele, Lea, Flood 2014;
+//    draw k of seed s = mix(s + (k+1)*0x9E3779B97F4A7C15), u = (mix >> 11) *
+//    2^-53), the engine's opt-in stream for device-side draws.
 //  * near-field peel ties (build-nearfield-slots.vert:146-162): slot k of a
 //    cell holds the lowest-index point among those with the k-th smallest
 //    DISTINCT f32 hash (the depth test keeps the first-drawn of equal depths;
@@ -90,6 +98,93 @@ inline uint64_t splitmix_draw(uint64_t seed, uint64_t k) {
 }
 inline double splitmix_unit(uint64_t seed, uint64_t k) {
   return (double)(splitmix_draw(seed, k) >> 11) * 0x1.0p-53;
+}
+
+// seedrandom@3.0.5's default generator, restated from its published source
+// description in the arithmetic it uses (JavaScript doubles):
+//   mixkey(seed, key): for j over the seed string's UTF-16 code units,
+//     key[j & 255] = 255 & ((smear ^= key[j & 255] * 19) + code[j]);
+//   ARC4(key): RC4 key schedule over key (empty key = [0]), then g(256) drops
+//     256 output bytes; g(count) = the next `count` output bytes as a base-256
+//     number;
+//   prng(): n = g(6), d = 2^48, x = 0; while (n < 2^52) { n = (n + x) * 256;
+//     d *= 256; x = g(1) }; while (n >= 2^53) { n /= 2; d /= 2; x >>>= 1 };
+//     return (n + x) / d.
+struct Arc4Seed {
+  int S[256];
+  int i = 0, j = 0;
+  void seed(const std::vector<uint16_t>& code) {
+    std::vector<int> key;
+    double smear = 0;   // `undefined` before the first ^=, which reads as 0
+    for (size_t k = 0; k < code.size(); ++k) {
+      const size_t at = k & 255;
+      const int prev = at < key.size() ? key[at] : 0;   // undefined * 19 -> NaN -> 0 under ^
+      smear = (double)((int32_t)smear ^ (int32_t)(prev * 19));
+      const int v = 255 & (int)(smear + code[k]);
+      if (at < key.size()) key[at] = v; else key.push_back(v);
+    }
+    if (key.empty()) key.push_back(0);
+    for (int k = 0; k < 256; ++k) S[k] = k;
+    int jj = 0;
+    for (int k = 0; k < 256; ++k) {
+      const int t = S[k];
+      jj = 255 & (jj + key[k % key.size()] + t);
+      S[k] = S[jj];
+      S[jj] = t;
+    }
+    i = j = 0;
+    g(256);
+  }
+  double g(int count) {
+    double r = 0;
+    while (count--) {
+      i = 255 & (i + 1);
+      const int t = S[i];
+      j = 255 & (j + t);
+      S[i] = S[j];
+      S[j] = t;
+      r = r * 256 + S[255 & (S[i] + t)];
+    }
+    return r;
+  }
+  double prng() {
+    double n = g(6), d = 281474976710656.0, x = 0;   // 2^48
+    while (n < 4503599627370496.0) {                  // 2^52
+      n = (n + x) * 256;
+      d *= 256;
+      x = g(1);
+    }
+    while (n >= 9007199254740992.0) {                 // 2^53
+      n /= 2;
+      d /= 2;
+      x = (double)((uint32_t)x >> 1);
+    }
+    return (n + x) / d;
+  }
+};
+
+// A UTF-8 string as UTF-16 code units (JavaScript's string of the same text).
+std::vector<uint16_t> utf16_units(const char* s) {
+  std::vector<uint16_t> u;
+  const unsigned char* p = (const unsigned char*)s;
+  while (p && *p) {
+    uint32_t c = *p++;
+    int more = c >= 0xF0 ? 3 : c >= 0xE0 ? 2 : c >= 0xC0 ? 1 : 0;
+    if (more) c &= (0x3F >> more);
+    bool ok = c < 0x80 || more > 0;
+    for (int k = 0; k < more && ok; ++k) {
+      if ((*p & 0xC0) != 0x80) ok = false;
+      else c = (c << 6) | (*p++ & 0x3F);
+    }
+    if (!ok || c > 0x10FFFF || (c >= 0xD800 && c < 0xE000)) { u.push_back(0xFFFD); continue; }
+    if (c >= 0x10000) {
+      u.push_back((uint16_t)(0xD800 + ((c - 0x10000) >> 10)));
+      u.push_back((uint16_t)(0xDC00 + ((c - 0x10000) & 0x3FF)));
+    } else {
+      u.push_back((uint16_t)c);
+    }
+  }
+  return u;
 }
 
 // lowbias32 (build-nearfield-slots.vert:130-135).
@@ -203,6 +298,7 @@ struct orc_engine {
   bool pinned_set = false;
   std::vector<double> pinned_input;
   bool pos_dirty = false, links_dirty = false, sizes_dirty = false;
+  bool skip_rescale = false;       // Points.shouldSkipRescale
 
   // applied data
   uint64_t N = 0, E = 0;           // pointsNumber, linksNumber
@@ -246,16 +342,21 @@ struct orc_engine {
   double alpha = 1.0;
   double progress = 0.0;
   bool running = false;
-  uint64_t rng_seed = 0, rng_ctr = 0;
+  uint64_t rng_seed = 0, rng_ctr = 0;   // counter stream seed; draws so far (both streams)
+  bool counter_stream = false;
+  Arc4Seed arc;                          // the reference's stream
+  std::string seed_text;
   uint64_t tick = 0;
 
   // retained from the last many-body pass (test hooks)
   std::vector<std::vector<CellRec>> levels;
   std::vector<int32_t> slots;      // Gf^2 * 8
 
+  // Store.getRandomFloat(min, max) = random.float(min, max)
   double rnd(double mn, double mx) {
-    double u = splitmix_unit(rng_seed, rng_ctr++);
-    return mn + (mx - mn) * u;
+    const double u = counter_stream ? splitmix_unit(rng_seed, rng_ctr) : arc.prng();
+    ++rng_ctr;
+    return u * (mx - mn) + mn;
   }
 };
 
@@ -324,6 +425,62 @@ void build_csr(orc_engine* e, bool incoming, Csr& c, const std::vector<uint32_t>
       c.strength[at] = (float)strength;
       c.rnd[at] = (float)e->rnd(0, 1);
     }
+  }
+}
+
+// Math.min / Math.max (NaN if either is NaN; -0 < +0).
+double js_min(double a, double b) {
+  if (std::isnan(a) || std::isnan(b)) return NAN;
+  if (a == b) return std::signbit(a) ? a : b;
+  return a < b ? a : b;
+}
+double js_max(double a, double b) {
+  if (std::isnan(a) || std::isnan(b)) return NAN;
+  if (a == b) return std::signbit(a) ? b : a;
+  return a > b ? a : b;
+}
+
+// Points.rescaleInitialNodePositions (Points/index.ts:3134-3218): FP64 as in
+// JavaScript, written back into the Float32Array (rounded to f32).
+void rescale_initial_positions(std::vector<float>& points, double spaceSize) {
+  if (spaceSize == 0 || std::isnan(spaceSize)) return;   // `!spaceSize`
+  const size_t pointsNumber = points.size() / 2;
+  auto absent = [&](size_t i) { return std::isnan(points[2 * i]) || std::isnan(points[2 * i + 1]); };
+  double minX = INFINITY, maxX = -INFINITY, minY = INFINITY, maxY = -INFINITY;
+  for (size_t i = 0; i < pointsNumber; ++i) {
+    if (absent(i)) continue;
+    const double x = points[2 * i], y = points[2 * i + 1];
+    minX = js_min(minX, x);
+    maxX = js_max(maxX, x);
+    minY = js_min(minY, y);
+    maxY = js_max(maxY, y);
+  }
+  if (!std::isfinite(minX)) return;
+  const double w = maxX - minX;
+  const double h = maxY - minY;
+  const double range = js_max(w, h);
+  if (range == 0) {
+    const double center = spaceSize / 2;
+    for (size_t i = 0; i < pointsNumber; ++i) {
+      if (absent(i)) continue;
+      points[2 * i] = (float)((double)points[2 * i] - minX + center);
+      points[2 * i + 1] = (float)((double)points[2 * i + 1] - minY + center);
+    }
+    return;
+  }
+  if (range > spaceSize) return;
+  const double densityThreshold = spaceSize * spaceSize * 0.001;
+  const double effectiveSpaceSize = (double)pointsNumber > densityThreshold
+                                        ? spaceSize * js_max(1.2, std::sqrt((double)pointsNumber) / spaceSize)
+                                        : spaceSize * 0.1;
+  const double scaleFactor = effectiveSpaceSize / range;
+  const double centerOffset = (spaceSize - effectiveSpaceSize) / 2;
+  const double offsetX = ((range - w) / 2) * scaleFactor + centerOffset;
+  const double offsetY = ((range - h) / 2) * scaleFactor + centerOffset;
+  for (size_t i = 0; i < pointsNumber; ++i) {
+    if (absent(i)) continue;
+    points[2 * i] = (float)(((double)points[2 * i] - minX) * scaleFactor + offsetX);
+    points[2 * i + 1] = (float)(((double)points[2 * i + 1] - minY) * scaleFactor + offsetY);
   }
 }
 
@@ -967,8 +1124,14 @@ extern "C" {
 orc_engine* orc_create(const cgl_config* cfg) {
   orc_engine* e = new orc_engine();
   e->cfg = *cfg;
+  // Store.addRandomSeed (Store/index.ts:196-198, src/index.ts:452)
   if (cfg->has_random_seed) e->rng_seed = cfg->random_seed;
   else { std::random_device rd; e->rng_seed = ((uint64_t)rd() << 32) ^ rd(); }
+  e->counter_stream = cfg->random_stream == CGL_RANDOM_COUNTER;
+  if (cfg->has_random_seed && cfg->random_seed_text) e->seed_text = cfg->random_seed_text;
+  else e->seed_text = std::to_string(e->rng_seed);   // String(n) of an integer seed
+  e->cfg.random_seed_text = (cfg->has_random_seed && cfg->random_seed_text) ? e->seed_text.c_str() : nullptr;
+  e->arc.seed(utf16_units(e->seed_text.c_str()));
   adjust_space_size(e);
   return e;
 }
@@ -982,6 +1145,8 @@ int orc_set_config(orc_engine* e, const cgl_config* cfg) {
   e->cfg = *cfg;
   e->cfg.has_random_seed = prev.has_random_seed;   // init-only (src/index.ts:1720-1724)
   e->cfg.random_seed = prev.random_seed;
+  e->cfg.random_seed_text = prev.random_seed_text;
+  e->cfg.random_stream = prev.random_stream;
   if (prev.space_size != e->cfg.space_size) {
     adjust_space_size(e);
     e->collision_ready = false;
@@ -991,14 +1156,19 @@ int orc_set_config(orc_engine* e, const cgl_config* cfg) {
   return 0;
 }
 
-int orc_set_point_positions(orc_engine* e, const float* xy, uint64_t n) {
+int orc_set_point_positions_ex(orc_engine* e, const float* xy, uint64_t n, int dont_rescale) {
   int st = 0;
   if (n % 2) { n -= 1; st = CGL_WARNING; }
   e->in_pos.assign(xy, xy + n);
   e->have_pos_input = true;
+  e->skip_rescale = dont_rescale != 0;   // src/index.ts:553
   e->pos_dirty = true; e->links_dirty = true; e->sizes_dirty = true;
   e->clusters_dirty = true;   // src/index.ts:570
   return st;
+}
+
+int orc_set_point_positions(orc_engine* e, const float* xy, uint64_t n) {
+  return orc_set_point_positions_ex(e, xy, n, 0);
 }
 
 int orc_set_point_clusters(orc_engine* e, const float* v, uint64_t n) {
@@ -1077,6 +1247,13 @@ int orc_render(orc_engine* e, double alpha) {
   if (pos_changed) {
     e->N = N;
     e->data_pos = e->in_pos;
+    // Points.updatePositions (Points/index.ts:396-413): rescale the input
+    // (in place in the reference, on the applied copy here)
+    bool rescale = e->cfg.rescale_positions == 1;
+    if (e->cfg.rescale_positions < 0 && !e->cfg.enable_simulation) rescale = true;
+    if (e->skip_rescale) rescale = false;
+    e->skip_rescale = false;
+    if (rescale) rescale_initial_positions(e->data_pos, e->cfg.space_size);
   }
   e->E = E;
   e->data_links = e->in_links;
@@ -1255,6 +1432,12 @@ int orc_debug_get_jitter(orc_engine* e, float* out, uint64_t cap) {
 uint32_t orc_lowbias32(uint32_t h) { return lowbias32(h); }
 float orc_peel_hash(uint32_t index, uint32_t seed_bits) { return peel_hash(index, seed_bits); }
 uint64_t orc_splitmix_draw(uint64_t seed, uint64_t k) { return splitmix_draw(seed, k); }
+// The first n values of seedrandom(seed_text) (random's next()).
+void orc_seedrandom(const char* seed_text, uint64_t n, double* out) {
+  Arc4Seed a;
+  a.seed(utf16_units(seed_text));
+  for (uint64_t k = 0; k < n; ++k) out[k] = a.prng();
+}
 void orc_sincos(float a, float* s, float* c) { portable_sincos(a, s, c); }
 int orc_cell_index(float p, float cs, int G) { return cell_index(p, cs, G); }
 
@@ -1295,8 +1478,10 @@ int orc_manybody_velocity(orc_engine* e, int precision, double* out) {
     return 0;
   }
   const uint64_t saved_ctr = e->rng_ctr;
+  const Arc4Seed saved_arc = e->arc;
   const float seed = (float)e->rnd(0, 1);
   e->rng_ctr = saved_ctr;
+  e->arc = saved_arc;
   std::vector<std::vector<double>> f64;
   std::vector<float> prev = e->pos;
   build_pyramid_and_slots(e, prev, fbits(seed), precision == 1, &f64);

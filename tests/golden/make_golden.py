@@ -9,26 +9,28 @@ collision pair (force-collision-spatial.frag:103-168), and the cluster pull
 towards a centre of mass or a given cluster position (force-cluster.frag:28-53,
 calculate-centermass.vert:22-52).  The update is
 update-position.frag:52-57 and alpha follows Store/index.ts:328-332.  Random
-draws follow the project's SplitMix64 stream in the reference's order.
+draws are the reference's stream (random@4.1.0 over seedrandom@3.0.5, restated
+in tests/seedrandom_ref.py) in the reference's order.
 Run:  python tests/golden/make_golden.py
 """
 import json
 import math
 import os
 
-M64 = (1 << 64) - 1
+import sys
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+from seedrandom_ref import SeedRandom  # noqa: E402
+
 STAGE = dict(gravity=1, center=2, manybody=4, link_in=8, link_out=16, collision=32, clusters=64)
 
 
-def splitmix(seed, k):
-    z = (seed + (k + 1) * 0x9E3779B97F4A7C15) & M64
-    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M64
-    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M64
-    return z ^ (z >> 31)
-
-
 def unit(seed, k):
-    return (splitmix(seed, k) >> 11) * 2.0 ** -53
+    """Draw k (0-based) of the reference's stream for randomSeed = seed."""
+    r = SeedRandom(str(seed))
+    for _ in range(k):
+        r.next()
+    return r.next()
 
 
 def alpha_next(a, decay=5000):
@@ -102,7 +104,7 @@ def case_repulsion_pair():
     seed, S, fr, rep = 14, 4096.0, 0.85, 1.0
     p = [[1000.0, 1000.0], [1003.0, 1004.0]]
     # jitter of point i = draws (2i, 2i+1) scaled U(-1,1) * 1e-5
-    jit = [[(-1 + 2 * unit(seed, 2 * i)) * 1e-5, (-1 + 2 * unit(seed, 2 * i + 1)) * 1e-5] for i in range(2)]
+    jit = [[(unit(seed, 2 * i) * 2 - 1) * 1e-5, (unit(seed, 2 * i + 1) * 2 - 1) * 1e-5] for i in range(2)]
     a = 1.0
     out = []
     for i in range(2):

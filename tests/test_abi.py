@@ -48,7 +48,7 @@ def test_config_defaults_match_reference(engine_lib):
 
 def test_struct_sizes_match_header():
     # natural C layout: doubles and uint64 aligned to 8
-    assert C.sizeof(_abi.Config) == 192
+    assert C.sizeof(_abi.Config) == 208
     assert C.sizeof(_abi.State) == 56
     assert C.sizeof(_abi.Layout) == 88
 

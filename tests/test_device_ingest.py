@@ -6,7 +6,7 @@ import math
 import numpy as np
 import pytest
 
-from graph_gb300 import generators
+from graph_gb300 import _abi, generators
 
 from helpers import first_mismatch, make_pair, same_bits, scenario
 
@@ -27,7 +27,6 @@ def _awkward_links(n, seed):
 
 def _pair(pos, links, fields, dmin, **kw):
     from graph_gb300.engine import Engine
-    from graph_gb300 import _abi
     e = Engine(_abi.make_config(**dict(fields, device_ingest_min_links=dmin)))
     e.set_point_positions(pos)
     e.set_links(links)
@@ -38,9 +37,14 @@ def _pair(pos, links, fields, dmin, **kw):
     return e
 
 
+STREAMS = [_abi.RANDOM_REFERENCE, _abi.RANDOM_COUNTER]
+
+
+@pytest.mark.parametrize("stream", STREAMS)
 @pytest.mark.parametrize("with_strength", [False, True])
-def test_device_and_host_builds_agree(with_strength):
+def test_device_and_host_builds_agree(with_strength, stream):
     pos, _, fields = scenario("ba_small")
+    fields = dict(fields, random_stream=stream)
     n = pos.size // 2
     pos = pos.copy()
     pos[2 * 9: 2 * 12] = np.nan                      # links to absent points keep their draws
@@ -65,11 +69,12 @@ def test_device_and_host_builds_agree(with_strength):
         assert same_bits(a, b), (t, first_mismatch(a, b))
 
 
-def test_device_build_matches_oracle():
+@pytest.mark.parametrize("stream", STREAMS)
+def test_device_build_matches_oracle(stream):
     pos, _, fields = scenario("collision")
     n = pos.size // 2
     links = _awkward_links(n, 5)
-    eng, orc = make_pair(pos, links, dict(fields, device_ingest_min_links=0.0))
+    eng, orc = make_pair(pos, links, dict(fields, device_ingest_min_links=0.0, random_stream=stream))
     for t in range(3):
         eng.step(1)
         orc.step(1)

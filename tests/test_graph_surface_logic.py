@@ -35,6 +35,10 @@ class StandInEngine:
     def set_point_positions(self, a):
         self._log("positions", np.array(a, copy=True))
 
+    def set_point_positions_ex(self, a, dont_rescale):
+        self.dont_rescale = dont_rescale
+        self._log("positions", np.array(a, copy=True))
+
     def set_links(self, a):
         self._log("links", np.array(a, copy=True))
 
@@ -95,7 +99,7 @@ class StandInEngine:
         return self.run(n)
 
     def get_point_positions(self):
-        return np.zeros(4, np.float32)
+        return getattr(self, "current", np.zeros(4, np.float32))
 
     def set_pointer(self, x, y, right):
         self._log("pointer", x, y, right)
@@ -208,3 +212,28 @@ def test_everything_is_a_no_op_after_destroy(make):
     assert g.getPointPositions().size == 0
     assert not g.isSimulationRunning and g.progress == 0.0
     assert eng.calls == [("close",)]
+
+
+def test_rescale_flags_and_write_back(make):
+    # rescalePositions true: the engine rescales at render and the caller's
+    # Float32Array receives the rescaled live positions (the reference writes it
+    # in place, Points/index.ts:3211-3216); absent points stay as they were
+    g = make({"rescalePositions": True})
+    assert g.engine.cfgs[0].rescale_positions == 1
+    pos = np.array([1.0, 2.0, np.nan, 5.0, 3.0, 4.0], np.float32)
+    g.setPointPositions(pos)
+    g.engine.current = np.array([10.0, 20.0, np.nan, np.nan, 30.0, 40.0], np.float32)
+    g.render()
+    assert g.engine.dont_rescale is False
+    assert pos[0] == 10.0 and pos[5] == 40.0 and np.isnan(pos[2]) and pos[3] == 5.0
+    # dontRescale skips it once (src/index.ts:553); nothing is written back
+    pos2 = np.array([1.0, 2.0, 3.0, 4.0], np.float32)
+    g.setPointPositions(pos2, True)
+    g.engine.current = np.array([9.0, 9.0, 9.0, 9.0], np.float32)
+    g.render()
+    assert g.engine.dont_rescale is True and pos2[0] == 1.0
+    # undefined rescales when the simulation is off (Points/index.ts:396-398)
+    assert make({"enableSimulation": False})._rescales(False)
+    assert not make({})._rescales(False)
+    assert not make({"rescalePositions": False, "enableSimulation": False})._rescales(False)
+    assert make({}).engine.cfgs[0].rescale_positions == -1

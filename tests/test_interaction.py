@@ -144,7 +144,7 @@ def test_frame_loop_end_matches():
 
 @pytest.mark.gpu
 def test_graph_surface_clusters_pointer_texture():
-    # the flow INTEGRATION.md shows, through the camelCase Graph
+    # clusters, the pointer and the position texture through the camelCase Graph
     from graph_gb300 import Graph, generators
     n = 2000
     pos = generators.uniform_positions(n, 1000, 3000, 4)

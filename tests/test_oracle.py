@@ -17,6 +17,7 @@ import oracle
 from graph_gb300 import _abi, generators
 from oracle import OracleEngine
 
+from seedrandom_ref import SeedRandom
 from helpers import mass_seen, scenario
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -96,9 +97,9 @@ def test_rng_draw_order_and_count():
     o.start()
     o.step(7)
     assert o.state().rng_draws == 2 * t * t + 2 * m + 7
-    # the first jitter value is draw 0 scaled: U(-1,1) * 1e-5
-    u0 = (oracle.splitmix_draw(fields["random_seed"], 0) >> 11) * 2.0 ** -53
-    assert o.jitter()[0] == np.float32((-1 + 2 * u0) * 1e-5)
+    # the first jitter value is draw 0 scaled: float(-1, 1) * 1e-5 of seedrandom(String(seed))
+    u0 = SeedRandom(str(fields["random_seed"])).next()
+    assert o.jitter()[0] == np.float32((u0 * 2 - 1) * 1e-5)
     # re-setting only the links consumes only link draws
     before = o.state().rng_draws
     o.set_links(links)
@@ -329,3 +330,81 @@ def test_golden_fixtures():
         o.step(case["ticks"])
         got = o.get_point_positions().astype(np.float64)
         np.testing.assert_allclose(got, np.array(case["expected"]), rtol=0, atol=case["atol"], err_msg=case["name"])
+
+
+def _rescale_py(pos, space):
+    """rescaleInitialNodePositions (Points/index.ts:3134-3218) in Python floats."""
+    p = pos.astype(np.float64).reshape(-1, 2)
+    live = ~np.isnan(p).any(axis=1)
+    if not live.any():
+        return pos.copy()
+    mnx, mxx = p[live, 0].min(), p[live, 0].max()
+    mny, mxy = p[live, 1].min(), p[live, 1].max()
+    w, h = mxx - mnx, mxy - mny
+    rng = max(w, h)
+    out = p.copy()
+    if rng == 0:
+        c = space / 2
+        out[live, 0] = p[live, 0] - mnx + c
+        out[live, 1] = p[live, 1] - mny + c
+        return out.astype(np.float32).reshape(-1)
+    if rng > space:
+        return pos.copy()
+    n = p.shape[0]
+    eff = space * max(1.2, math.sqrt(n) / space) if n > space * space * 0.001 else space * 0.1
+    sf = eff / rng
+    co = (space - eff) / 2
+    ox = ((rng - w) / 2) * sf + co
+    oy = ((rng - h) / 2) * sf + co
+    out[live, 0] = (p[live, 0] - mnx) * sf + ox
+    out[live, 1] = (p[live, 1] - mny) * sf + oy
+    return out.astype(np.float32).reshape(-1)
+
+
+@pytest.mark.parametrize("case", ["sparse", "dense", "one_point", "coincident", "too_wide", "all_absent", "absent"])
+def test_rescale_initial_positions(case):
+    space = 4096.0
+    rng = np.random.default_rng(7)
+    if case == "sparse":
+        pos = rng.uniform(-50, 80, size=200).astype(np.float32)
+    elif case == "dense":   # more points than spaceSize^2 * 0.001
+        space = 64.0
+        pos = rng.uniform(0, 1, size=2 * 5000).astype(np.float32)
+    elif case == "one_point":
+        pos = np.array([12.5, -3.0], np.float32)
+    elif case == "coincident":
+        pos = np.array([7.0, 7.0, 7.0, 7.0, 7.0, 7.0], np.float32)
+    elif case == "too_wide":
+        pos = np.array([0.0, 0.0, 5000.0, 10.0], np.float32)
+    elif case == "all_absent":
+        pos = np.array([np.nan, 1.0, 2.0, np.nan], np.float32)
+    else:
+        pos = rng.uniform(100, 300, size=100).astype(np.float32)
+        pos[10] = np.nan
+    want = _rescale_py(pos, space)
+    o = OracleEngine(random_seed=1, space_size=space, rescale_positions=1, stage_mask=0)
+    o.set_point_positions(pos)
+    o.render()
+    got = o.get_point_positions()
+    live = ~(np.isnan(want[0::2]) | np.isnan(want[1::2]))
+    assert np.array_equal(np.repeat(live, 2), ~np.isnan(got))
+    assert np.array_equal(got[np.repeat(live, 2)], want[np.repeat(live, 2)])
+
+
+def test_rescale_defaults_and_dont_rescale():
+    pos = np.array([1.0, 1.0, 3.0, 2.0], np.float32)
+    # rescalePositions undefined: only when the simulation is disabled
+    on = OracleEngine(random_seed=1)
+    off = OracleEngine(random_seed=1, enable_simulation=0)
+    for e in (on, off):
+        e.set_point_positions(pos)
+        e.render()
+    assert np.array_equal(on.get_point_positions(), pos)
+    assert not np.array_equal(off.get_point_positions(), pos)
+    # dontRescale skips one render's rescale only
+    off.set_point_positions_ex(pos, True)
+    off.render()
+    assert np.array_equal(off.get_point_positions(), pos)
+    off.set_point_positions(pos)
+    off.render()
+    assert not np.array_equal(off.get_point_positions(), pos)

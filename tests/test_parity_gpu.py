@@ -314,19 +314,42 @@ def test_graph_api_surface():
     assert g.getPointPositions().size == 0
 
 
-def test_sbm_million_two_ticks_bit_exact():
+def _sbm_config1(seed=1):
     # config 1 shape: SBM 1,000,000 points / ~5M links, S = 8192
     n = 1_000_000
-    links = generators.sbm_zipf(n, 200, 1.2, 10, 0.9, seed=1)
-    pos = generators.uniform_positions(n, 0, 8192, 1)
+    links = generators.sbm_zipf(n, 200, 1.2, 10, 0.9, seed=seed)
+    pos = generators.uniform_positions(n, 0, 8192, seed)
     fields = dict(space_size=8192, simulation_repulsion=0.1, simulation_gravity=0.25, simulation_friction=0.85,
-                  simulation_link_spring=1.0, simulation_link_distance=2.0, simulation_decay=5000, random_seed=1)
+                  simulation_link_spring=1.0, simulation_link_distance=2.0, simulation_decay=5000, random_seed=seed)
+    return pos, links, fields
+
+
+def test_sbm_million_ten_ticks_bit_exact():
+    # the first 10 ticks: positions after every tick, cells and slots after ticks 1 and 10
+    pos, links, fields = _sbm_config1()
     eng, orc = make_pair(pos, links, fields)
-    for t in range(2):
+    assert eng.state().rng_draws == orc.state().rng_draws
+    for t in range(10):
         eng.step(1)
         orc.step(1)
         _assert_same(eng, orc, ("sbm1M", t))
-    _assert_cells_and_slots(eng, orc)
+        if t in (0, 9):
+            _assert_cells_and_slots(eng, orc)
+
+
+def test_sbm_million_full_run_agreement():
+    # all 500 ticks of config 1: bit-exact at ticks 250 and 500, agreement figures on record
+    from graph_gb300 import agreement
+    pos, links, fields = _sbm_config1()
+    eng, orc = make_pair(pos, links, fields)
+    for block in (250, 250):
+        eng.step(block)
+        orc.step(block)
+        a, b = orc.get_point_positions(), eng.get_point_positions()
+        fig = agreement.agreement(a, b, links)
+        print("sbm1M tick", eng.state().tick, fig)
+        assert fig == dict(procrustes_rms=0.0, procrustes_rms_relative=0.0, edge_length_stress=0.0)
+        _assert_same(eng, orc, ("sbm1M tick", eng.state().tick))
 
 
 def test_full_size_properties():
@@ -358,10 +381,11 @@ def test_full_size_properties():
     assert np.all(outs[0] >= 0) and np.all(outs[0] <= 8192)
 
 
-def test_rmat_scale23_collision_bit_exact():
+def test_rmat_scale23_collision_ten_ticks_bit_exact():
     # config 2 shape: R-MAT scale 23 (a,b,c,d = .57,.19,.19,.05), 40M links after
     # self-loop and duplicate removal, radius U[1,8] (pointSizes = 2r), collision
     # 0.5, spaceSize 16384.  Hub lists (up to ~57,000 links) get a CTA each.
+    # Positions after each of the first 10 ticks, cells and slots after 1 and 10.
     n = 1 << 23
     links = generators.rmat(23, 40_000_000, 0.57, 0.19, 0.19, seed=3)
     pos = generators.uniform_positions(n, 0, 16384, 3)
@@ -371,10 +395,12 @@ def test_rmat_scale23_collision_bit_exact():
                   simulation_decay=5000, random_seed=3)
     eng, orc = make_pair(pos, links, fields, sizes=2 * radius)
     assert eng.layout().max_degree_in > 1000 and eng.layout().collision_grid == 0
-    for t in range(2):
+    for t in range(10):
         eng.step(1)
         orc.step(1)
         _assert_same(eng, orc, ("rmat23", t))
+        if t in (0, 9):
+            _assert_cells_and_slots(eng, orc)
     lay = eng.layout()
     assert lay.collision_grid == orc.layout().collision_grid == 512
     orc.close()
@@ -382,3 +408,79 @@ def test_rmat_scale23_collision_bit_exact():
     p = eng.get_point_positions()
     assert np.all(p >= 0) and np.all(p <= 16384)
     assert eng.cells(lay.levels - 1)[..., 2].sum() == n
+
+
+def test_cfg0_late_ticks_bit_exact():
+    # config 0 well past its 300 ticks: bit-exact at ticks 300, 600 and 1000
+    from graph_gb300 import agreement
+    pos, links, fields = scenario("cfg0")
+    eng, orc = make_pair(pos, links, fields)
+    for block in (300, 300, 400):
+        eng.step(block)
+        orc.step(block)
+        fig = agreement.agreement(orc.get_point_positions(), eng.get_point_positions(), links)
+        print("cfg0 tick", eng.state().tick, fig)
+        _assert_same(eng, orc, ("cfg0 tick", eng.state().tick))
+
+
+@pytest.mark.parametrize("mode", ["sim_off_default", "rescale_true", "dont_rescale"])
+def test_rescale_positions(mode):
+    # Points.updatePositions' rescale (Points/index.ts:390-413, 3134-3218)
+    rng = np.random.default_rng(12)
+    n = 3000
+    pos = rng.uniform(-40, 90, size=2 * n).astype(np.float32)
+    pos[2 * 5] = np.nan
+    links = generators.erdos_renyi(n, 4, 12)
+    from graph_gb300.engine import Engine
+    from oracle import OracleEngine
+    fields = dict(random_seed=12, space_size=4096)
+    if mode == "sim_off_default":
+        fields["enable_simulation"] = 0
+    else:
+        fields["rescale_positions"] = 1
+    cfg = _abi.make_config(**fields)
+    pair = []
+    for cls in (Engine, OracleEngine):
+        e = cls(cfg)
+        if mode == "dont_rescale":
+            e.set_point_positions_ex(pos, True)
+        else:
+            e.set_point_positions(pos)
+        e.set_links(links)
+        e.render()
+        e.start(1.0)
+        pair.append(e)
+    eng, orc = pair
+    _assert_same(eng, orc, (mode, "render"))
+    p = eng.get_point_positions()
+    if mode == "dont_rescale":
+        assert same_bits(p, np.where(np.isnan(pos.reshape(-1, 2)).any(axis=1, keepdims=True), np.nan,
+                                     pos.reshape(-1, 2)).reshape(-1))
+    else:
+        assert not same_bits(p, pos) and np.nanmin(p) >= 0 and np.nanmax(p) <= 4096
+    for t in range(4):
+        eng.step(1)
+        orc.step(1)
+        _assert_same(eng, orc, (mode, t))
+
+
+@pytest.mark.parametrize("stream", [_abi.RANDOM_REFERENCE, _abi.RANDOM_COUNTER])
+def test_random_streams_match_oracle(stream):
+    # both streams: jitter and link draws (on the device for the counter
+    # stream, from the host for the reference's), then a few ticks
+    pos, links, fields = scenario("ba_small")
+    eng, orc = make_pair(pos, links, dict(fields, random_stream=stream, device_ingest_min_links=0.0))
+    assert eng.state().rng_draws == orc.state().rng_draws
+    for t in range(4):
+        eng.step(1)
+        orc.step(1)
+        _assert_same(eng, orc, (stream, t))
+
+
+def test_string_seed_matches_oracle():
+    pos, links, fields = scenario("ba_small")
+    eng, orc = make_pair(pos, links, dict(fields, random_seed="layout-α"))
+    for t in range(3):
+        eng.step(1)
+        orc.step(1)
+        _assert_same(eng, orc, ("string seed", t))

@@ -69,6 +69,15 @@ def test_noalloc_matches_engine_on_two_calls():
         for l, (w, g) in enumerate(zip(want, got)):
             assert same_bits(w, g), ("level", l)
     assert got_a[0][:, 2].sum() == 200_000 and got_b[0][:, 2].sum() == 200_000 - 1
+    # a third call with fewer levels: its finest level sits elsewhere in the
+    # shared array, and only that part is cleared, so the 200k-point sums left
+    # there must not leak into it
+    pos_c = generators.uniform_positions(3_000, 0, space, 13)
+    want_c = _engine_levels(pos_c, space)
+    got_c = _noalloc_levels(lib, pos_c, space, len(want_c), stream)
+    assert len(want_c) == len(got_c) == 6   # finest grid 128 against the first calls' 512
+    for l, (w, g) in enumerate(zip(want_c, got_c)):
+        assert same_bits(w, g), ("small call, level", l)
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch():
