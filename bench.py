@@ -157,16 +157,80 @@ def load_peaks():
         return 6800.0, "fallback"
 
 
-def load_ncu(workload, stage):
-    """From the committed ncu summary of `workload` (profiles/ncu_<workload>.json):
-    DRAM bytes per launch of `stage` and its issue-slot utilisation, or Nones."""
+def load_ncu(workload):
+    """The committed ncu summary of `workload` (profiles/ncu_<workload>.json):
+    per kernel stage, per-launch counters of the launches it captured (the
+    bench's timed state: ticks 5-7 of the seeded layout), or {}."""
     path = os.path.join(ROOT, "profiles", "ncu_%s.json" % workload)
     try:
         with open(path) as f:
-            t = json.load(f)
-        return t.get("dram_bytes", {}).get(stage), t.get("issue_active", {}).get(stage)
+            return json.load(f)
     except Exception:
-        return None, None
+        return {}
+
+
+# Launch shares and issue peaks.  An SM issues at most one warp instruction per
+# scheduler per cycle: 4 schedulers per SM.
+ISSUE_PER_SM_CYCLE = 4
+
+
+def issue_roofline(dom, dom_ms, ncu, sm_count, sm_mhz, alg_bytes, hbm_peak, hbm_kind):
+    """Roofline of an issue-bound kernel: warp instructions per launch (ncu, on
+    the benched state) over its event-timed launch, against 4 x SMs x the
+    median SM clock of the timed region; the HBM view is kept beside it."""
+    k = ncu.get("kernels", {}).get(dom, {})
+    inst = k.get("inst_executed")
+    peak = ISSUE_PER_SM_CYCLE * sm_count * sm_mhz * 1e6
+    achieved = inst / (dom_ms / 1e3) if inst and dom_ms > 0 else None
+    hbm = alg_bytes / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
+    return {"bound": "issue", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "warp-inst/s",
+            "frac": achieved / peak if achieved else None, "traffic": k.get("dram_bytes"),
+            "launch_ms": dom_ms, "inst_per_launch": inst,
+            "peak_source": "architectural: %d issue slots per SM cycle x %d SMs x %.0f MHz (median SM clock of "
+                           "the timed region)" % (ISSUE_PER_SM_CYCLE, sm_count, sm_mhz),
+            "fp32_pipe_frac_ncu": k.get("fp32_pipe"), "l2_throughput_frac_ncu": k.get("l2_throughput"),
+            "issue_active_frac_ncu": k.get("issue_active"),
+            "hbm": {"achieved": hbm, "peak": hbm_peak, "unit": "GB/s", "frac": hbm / hbm_peak,
+                    "algorithmic_bytes": alg_bytes, "peak_source": hbm_kind},
+            "ncu_state": ncu.get("state"), "ncu_source": "profiles/" + ncu.get("file", "")}
+
+
+def rel_errors(v, ref):
+    """Relative error of velocities v against ref (flat x, y pairs): the largest
+    and 99th-percentile per-point |dv| / |ref| (points with ref != 0) and the
+    norm-wise RMS(|dv|) / RMS(|ref|)."""
+    d = np.hypot(v[0::2] - ref[0::2], v[1::2] - ref[1::2])
+    r = np.hypot(ref[0::2], ref[1::2])
+    ok = r > 0
+    q = d[ok] / r[ok]
+    return {"max_rel": float(q.max()) if q.size else 0.0, "p99_rel": float(np.percentile(q, 99)) if q.size else 0.0,
+            "rms_rel": float(math.sqrt((d * d).mean() / max((r * r).mean(), 1e-300))), "points": int(ok.sum())}
+
+
+def approximation_error(oracle_engine, tick_note):
+    """The many-body velocity of one tick, FP32 (what the engine computes: it is
+    bit-exact with the oracle's FP32 restatement) against (1) the same
+    grid-pyramid approximation in FP64 at this workload's state and (2) exact
+    all-pairs FP64 repulsion at 20,000 points of config 1's density."""
+    from oracle import OracleEngine
+    v32 = oracle_engine.manybody_velocity(0)
+    v64 = oracle_engine.manybody_velocity(1)
+    out = {"fp32_vs_fp64_pyramid": dict(rel_errors(v32, v64), state=tick_note)}
+    n, space = 20_000, 8192.0
+    side = space * math.sqrt(n / 1_000_000)   # 3.8 points per finest cell, as 1M points in 8192^2
+    pos = generators.uniform_positions(n, 0, side, 7)
+    o = OracleEngine(space_size=space, simulation_repulsion=0.1, random_seed=7)
+    o.set_point_positions(pos)
+    o.render()
+    o.start(1.0)
+    exact = o.manybody_velocity(2)
+    out["pyramid_vs_exact_20k"] = {
+        "fp32": rel_errors(o.manybody_velocity(0), exact),
+        "fp64": rel_errors(o.manybody_velocity(1), exact),
+        "state": "20,000 points uniform in a %.0f x %.0f square of the 8192 space (config 1's density), tick 0; "
+                 "exact = all-pairs FP64 with the same falloff, no jitter" % (side, side)}
+    o.close()
+    return out
 
 
 # ------------------------------------------------------------------- clocks --
@@ -227,8 +291,8 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- CPU side --
-def time_oracle(pos, links, fields, budget_s, max_ticks, warmup=1, sizes=None):
-    """Oracle ticks on all host cores; returns (point-iter/s, ticks timed, seconds, cores)."""
+def time_oracle(pos, links, fields, budget_s, max_ticks, warmup=1, sizes=None, keep=False):
+    """Oracle ticks on all host cores; returns (point-iter/s, ticks timed, seconds, cores[, engine])."""
     from oracle import OracleEngine
     o = OracleEngine(**fields)
     o.set_point_positions(pos)
@@ -250,8 +314,10 @@ def time_oracle(pos, links, fields, budget_s, max_ticks, warmup=1, sizes=None):
     t = t1 + (time.perf_counter() - t0)
     ticks += max(more, 0)
     live = o.layout().live_points
-    o.close()
     cores = int(os.environ.get("OMP_NUM_THREADS", _host_cores()))
+    if keep:
+        return live * ticks / t, ticks, t, cores, o
+    o.close()
     return live * ticks / t, ticks, t, cores
 
 
@@ -381,7 +447,16 @@ def main():
     alg = stage_bytes(dom, live, m, c, cl)
     peak, peak_kind = load_peaks()
     achieved = alg / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
-    traffic, issue = load_ncu(args.workload if not args.positions_from else "none", dom)
+    ncu = load_ncu(args.workload) if not args.positions_from else {}
+    dom_ncu = ncu.get("kernels", {}).get(dom, {})
+    sm_count = torch.cuda.get_device_properties(local_rank).multi_processor_count
+    sm_mhz = clk.get("sm_mhz") or 2070.0
+    if dom == "manybody":
+        roofline = issue_roofline(dom, dom_ms, ncu, sm_count, sm_mhz, alg, peak, peak_kind)
+    else:
+        roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "traffic": dom_ncu.get("dram_bytes"), "algorithmic_bytes": alg,
+                    "launch_ms": dom_ms, "peak_source": peak_kind}
     per_stage = {k: round(v * 1e3, 2) for k, v in stages.items() if v > 0}
     stage_gbs = {k: round(stage_bytes(k, live, m, c, cl) / (stages[k] / 1e3) / 1e9, 1)
                  for k in stages if stages[k] > 0}
@@ -405,11 +480,15 @@ def main():
     e2e_value = live_all * e2e_steps / e2e_s
 
     cpu = None
+    approx = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, ticks, secs, cores = time_oracle(pos, links, fields, args.cpu_budget, 50, sizes=sizes)
+        v, ticks, secs, cores, o = time_oracle(pos, links, fields, args.cpu_budget, 50, sizes=sizes, keep=True)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": "%d ticks of the same %s workload on the oracle (C++ restatement, OpenMP, %s), %.1f s"
                          % (ticks, args.workload, cpu_model(), secs)}
+        # the oracle as the checker: the approximation error of the tick the engine computes
+        approx = approximation_error(o, "tick %d of the seeded layout" % (ticks + 1))
+        o.close()
 
     if rank == 0:
         out = {
@@ -422,14 +501,7 @@ def main():
                        "l2": "inputs larger than L2 (per-tick working set ~%d MB > 129 MB)"
                              % int((29 * live + 24 * 2 * m + 60 * live) / 1e6),
                        "parallelism": "replicas" if world > 1 else "single GPU"},
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic,
-                         "algorithmic_bytes": alg, "launch_ms": dom_ms, "peak_source": peak_kind,
-                         "issue_active_ncu": issue,
-                         "note": ("k_manybody is bound by instruction issue (correctly rounded sqrt, division and "
-                                  "reciprocal per term for bit-exact parity), not by HBM; issue_active_ncu is its "
-                                  "share of busy issue slots from the committed ncu summary")
-                         if dom == "manybody" else None},
+            "roofline": roofline,
             "tick_roofline": {"bytes_model": "112 N + 48 E + 107 C_f" + (" + 144 N + 128 C_c" if coll_on else ""),
                               "bytes": tb, "achieved": tick_gbs, "peak": peak, "unit": "GB/s",
                               "frac": tick_gbs / peak,
@@ -438,6 +510,7 @@ def main():
             "stage_us": per_stage,
             "stage_alg_gbs": stage_gbs,
             "cpu_baseline": cpu,
+            "approximation_error": approx,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8,
                     "d2h_bytes_per_step": 8 * int(lay.points_number), "steps": e2e_steps},
             "gpu_launches": int(lay.kernels_per_tick) * args.steps,

@@ -1,6 +1,9 @@
 """bench.py's byte models and stage filter (host code, no GPU)."""
 import importlib.util
+import math
 import os
+
+import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
@@ -42,3 +45,25 @@ def test_reference_arm_is_recognised_before_imports():
     assert b._reference_arm(["--steps", "3", "--impl=reference"])
     assert not b._reference_arm(["--impl", "gb300"])
     assert not b._reference_arm(["--gpus", "2"])
+
+
+def test_rel_errors():
+    b = _bench()
+    ref = np.array([1.0, 0.0, 0.0, 2.0, 0.0, 0.0])
+    v = np.array([1.1, 0.0, 0.0, 2.0, 0.5, 0.0])
+    e = b.rel_errors(v, ref)
+    assert e["points"] == 2 and abs(e["max_rel"] - 0.1) < 1e-12
+    assert abs(e["rms_rel"] - math.sqrt((0.01 + 0.25) / 3 / (5 / 3))) < 1e-12
+
+
+def test_issue_roofline_uses_the_ncu_instruction_count():
+    b = _bench()
+    ncu = {"file": "ncu_x.json", "state": "ticks 5-7", "kernels": {"manybody": {"inst_executed": 1.0e8,
+                                                                                "dram_bytes": 2.0e7}}}
+    r = b.issue_roofline("manybody", 0.5, ncu, 152, 2000.0, 29e6, 6000.0, "measured")
+    assert r["bound"] == "issue" and r["unit"] == "warp-inst/s"
+    assert abs(r["achieved"] - 2.0e11) < 1 and abs(r["peak"] - 4 * 152 * 2.0e9) < 1
+    assert abs(r["frac"] - 2.0e11 / (4 * 152 * 2.0e9)) < 1e-12
+    assert r["traffic"] == 2.0e7 and abs(r["hbm"]["achieved"] - 58.0) < 1e-9
+    r = b.issue_roofline("manybody", 0.5, {}, 152, 2000.0, 29e6, 6000.0, "measured")
+    assert r["achieved"] is None and r["frac"] is None
