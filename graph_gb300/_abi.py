@@ -99,8 +99,13 @@ class Layout(C.Structure):
         ("collision_cell_size", C.c_float),
         ("device_bytes", C.c_uint64),
         ("kernels_per_tick", C.c_uint32),
-        ("reserved", C.c_uint32),
+        ("manybody_kernel", C.c_uint32),
     ]
+
+
+MANYBODY_ONE_POINT = 0
+MANYBODY_SPLIT = 1
+MANYBODY_TWO_POINTS = 2
 
 
 # Reference defaults (src/variables.ts:10,15,19,69-82,147-148) mapped to C field names.

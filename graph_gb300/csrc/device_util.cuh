@@ -52,6 +52,34 @@ static __device__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total) {
   return before + x - v;
 }
 
+// The same for 64-bit values (the scan of packed (count, pairs) cell words).
+static __device__ unsigned long long block_exclusive_scan64(unsigned long long v, unsigned long long* total) {
+  __shared__ unsigned long long warp_tot64[kBlock / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned long long x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot64[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    unsigned long long t = lane < (kBlock / 32) ? warp_tot64[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned long long y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    if (lane < (kBlock / 32)) warp_tot64[lane] = t;
+  }
+  __syncthreads();
+  const unsigned long long before = w > 0 ? warp_tot64[w - 1] : 0;
+  *total = warp_tot64[kBlock / 32 - 1];
+  __syncthreads();
+  return before + x - v;
+}
+
 // Insert (hash bits, index) into a sorted list of the 8 smallest DISTINCT
 // hashes, each kept with its lowest index (the peel's tie rule,
 // build-nearfield-slots.vert:146-162); `at` tracks segment positions.

@@ -92,7 +92,7 @@ struct cgl_engine {
   // device state
   size_t dev_bytes = 0;
   DevBuf b_pos, b_pos_alt, b_flags, b_jitter, b_key, b_rank, b_sorted_idx, b_sorted_pos;
-  DevBuf b_counts, b_cell_start, b_block_sums, b_tickets, b_rec, b_acc, b_centroid;
+  DevBuf b_counts, b_cell_start, b_block_sums, b_tickets, b_rec, b_acc, b_centroid, b_pair_start, b_pair_list;
   DevBuf b_big_list, b_big_count, b_big_sx, b_big_sy, b_big_ns;
   DevBuf b_params, b_tick_ctr;
   DevBuf b_rowptr_in, b_rowptr_out, b_ent_in, b_ent_out, b_heavy_in, b_heavy_out;
@@ -176,7 +176,8 @@ void dev_free_all(cgl_engine* e) {
                    &e->b_cgrid_acc, &e->b_cgrid, &e->b_big_list, &e->b_big_count,
                    &e->b_big_sx, &e->b_big_sy, &e->b_big_ns, &e->b_heavy_in, &e->b_heavy_out,
                    &e->b_cl_of, &e->b_cl_coeff, &e->b_cl_custom, &e->b_cl_acc, &e->b_texture,
-                   &e->b_woff_in, &e->b_woff_out, &e->b_lane_ent_in, &e->b_lane_ent_out};
+                   &e->b_woff_in, &e->b_woff_out, &e->b_lane_ent_in, &e->b_lane_ent_out, &e->b_pair_start,
+                   &e->b_pair_list};
   for (DevBuf* b : all) {
     if (b->p) cudaFree(b->p);
     b->p = nullptr;
@@ -212,7 +213,9 @@ void refresh_view(cgl_engine* e) {
   d.sorted_pos = (float2*)e->b_sorted_pos.p;
   d.counts = (uint32_t*)e->b_counts.p;
   d.cell_start = (uint32_t*)e->b_cell_start.p;
-  d.block_sums = (uint32_t*)e->b_block_sums.p;
+  d.block_sums = (unsigned long long*)e->b_block_sums.p;
+  d.pair_start = (uint32_t*)e->b_pair_start.p;
+  d.pair_list = (uint32_t*)e->b_pair_list.p;
   d.scan_ticket = (uint32_t*)e->b_tickets.p;
   d.cells_ticket = d.scan_ticket ? d.scan_ticket + 1 : nullptr;
   d.big_list = (uint32_t*)e->b_big_list.p;
@@ -273,6 +276,13 @@ SimScalars make_scalars(const cgl_engine* e) {
   s.fx = e->fx;
   s.units = PairUnits{1.0f, -0.0f};
   s.cluster = (float)e->cfg.simulation_cluster;
+  // two points of a cell per thread once the cells hold one point on average
+  // and the graph fills the GPU with one thread per point
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  s.pairs = e->Gf > 0 && e->live >= (uint64_t)e->Gf * e->Gf && e->N >= 2ull * 256 * (uint64_t)sms;
+  s.level_guard = s.csf >= 2.0f && s.space <= 33554432.0f;   // 2^25
   return s;
 }
 
@@ -307,7 +317,7 @@ cgl_status enqueue_tick(cgl_engine* e, cudaStream_t st, cudaEvent_t* ev) {
     if (ev) cudaEventRecord(ev[2 * stage + which], st);
   };
   if (p.cent) CU(cudaMemsetAsync(d.centroid, 0, 3 * sizeof(long long), st));
-  if (p.mb) CU(cudaMemsetAsync(d.big_count, 0, 4 * sizeof(uint32_t), st));
+  if (p.mb) CU(cudaMemsetAsync(d.big_count, 0, 8 * sizeof(uint32_t), st));
   uint32_t mode = 0;
   if (p.grav) mode |= kPreGravity;
   if (p.cent) mode |= kPreCentroid;
@@ -733,13 +743,16 @@ cgl_status build_graph(cgl_engine* e, double alpha, uint64_t N, uint64_t E) {
       const uint32_t cells = (uint32_t)(e->Gf * e->Gf);
       if ((st = dev_reserve(e, e->b_counts, cells * sizeof(uint32_t), true))) return st;
       if ((st = dev_reserve(e, e->b_cell_start, (cells + 1) * sizeof(uint32_t), false))) return st;
-      if ((st = dev_reserve(e, e->b_block_sums, (scan_blocks(cells) + 1) * sizeof(uint32_t), false))) return st;
+      if ((st = dev_reserve(e, e->b_block_sums, (scan_blocks(cells) + 1) * sizeof(unsigned long long), false)))
+        return st;
+      if ((st = dev_reserve(e, e->b_pair_start, (cells + 1) * sizeof(uint32_t), true))) return st;
+      if ((st = dev_reserve(e, e->b_pair_list, std::max<size_t>(n, 1) * sizeof(uint32_t), false))) return st;
       if ((st = dev_reserve(e, e->b_tickets, 4 * sizeof(uint32_t), true))) return st;
       if ((st = dev_reserve(e, e->b_rec, off * sizeof(float4), true))) return st;
       if ((st = dev_reserve(e, e->b_acc, 3 * (size_t)aoff * sizeof(long long), true))) return st;
       if ((st = dev_reserve(e, e->b_centroid, 3 * sizeof(long long), true))) return st;
       if ((st = dev_reserve(e, e->b_big_list, 2 * (size_t)cells * sizeof(uint32_t), false))) return st;
-      if ((st = dev_reserve(e, e->b_big_count, 4 * sizeof(uint32_t), true))) return st;
+      if ((st = dev_reserve(e, e->b_big_count, 8 * sizeof(uint32_t), true))) return st;
       if ((st = dev_reserve(e, e->b_big_sx, cells * sizeof(long long), false))) return st;
       if ((st = dev_reserve(e, e->b_big_sy, cells * sizeof(long long), false))) return st;
       if ((st = dev_reserve(e, e->b_big_ns, cells * sizeof(uint32_t), false))) return st;
@@ -1339,6 +1352,13 @@ cgl_status cgl_get_layout(cgl_engine* e, cgl_layout* o) {
   o->collision_grid = (uint32_t)e->cgrid;
   o->collision_cell_size = e->ccell;
   o->device_bytes = e->dev_bytes;
+  if (e->mb_ready && e->N) {
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    o->manybody_kernel = make_scalars(e).pairs ? CGL_MANYBODY_TWO_POINTS
+                         : e->N < 2ull * 256 * (uint64_t)sms ? CGL_MANYBODY_SPLIT : CGL_MANYBODY_ONE_POINT;
+  }
   const TickPlan p = plan_tick(e);
   uint32_t k = 1;                                      // tick end
   if (p.grav || p.cent || p.mb) k += 1;                // prepass

@@ -28,6 +28,7 @@
 // renderer's position texture.
 #include "device_util.cuh"
 #include "kernels.cuh"
+#include "manybody_duo.cuh"
 #include "warp_cells.cuh"
 
 namespace cgl {
@@ -62,6 +63,12 @@ __device__ __forceinline__ void bin_point(const DeviceView& d, const SimScalars&
   const uint32_t key = (uint32_t)(cy * s.gf + cx);
   d.key[i] = key;
   d.rank[i] = atomicAdd(&d.counts[key], 1u);
+  // a point outside [0, space] (a pinned point, or input positions before
+  // their first update) can put a cell's centroid outside its cell
+  const bool outside = !(p.x >= 0.f && p.x <= s.space && p.y >= 0.f && p.y <= s.space);
+  const unsigned am = __activemask();
+  if (__ballot_sync(am, outside) && (threadIdx.x & 31) == (unsigned)(__ffs(am) - 1))
+    atomicOr(&d.big_count[kOutsideFlag], 1u);
 }
 
 // ---------------------------------------------------------------- prepass --
@@ -133,16 +140,25 @@ __global__ void __launch_bounds__(kBlock) k_center(DeviceView d, SimScalars s) {
 constexpr int kScanItems = 4;
 constexpr int kScanChunk = kBlock * kScanItems;   // cells per scan block
 
+// A cell's scan word: its count, and with PAIRS the number of work items of
+// the paired many-body pass, ceil(count / 2), in the high 32 bits (no sum of
+// either exceeds 2^32, so one 64-bit add adds both).
+template <bool PAIRS>
+__device__ __forceinline__ unsigned long long scan_word(uint32_t count) {
+  return PAIRS ? ((unsigned long long)((count + 1) >> 1) << 32) | count : count;
+}
+
+template <bool PAIRS>
 __global__ void __launch_bounds__(kBlock) k_scan_reduce(DeviceView d, uint32_t cells) {
   const uint32_t base = blockIdx.x * kScanChunk;
-  uint32_t sum = 0;
+  unsigned long long sum = 0;
 #pragma unroll
   for (int k = 0; k < kScanItems; ++k) {
     uint32_t c = base + k * kBlock + threadIdx.x;
-    if (c < cells) sum += d.counts[c];
+    if (c < cells) sum += scan_word<PAIRS>(d.counts[c]);
   }
-  uint32_t total;
-  block_exclusive_scan(sum, &total);
+  unsigned long long total;
+  block_exclusive_scan64(sum, &total);
   __shared__ bool last;
   if (threadIdx.x == 0) {
     d.block_sums[blockIdx.x] = total;
@@ -153,16 +169,16 @@ __global__ void __launch_bounds__(kBlock) k_scan_reduce(DeviceView d, uint32_t c
   if (!last) return;
   // Last block: exclusive scan of the block totals (gridDim.x <= kScanChunk).
   __threadfence();
-  uint32_t v[kScanItems];
-  uint32_t run = 0;
+  unsigned long long v[kScanItems];
+  unsigned long long run = 0;
 #pragma unroll
   for (int k = 0; k < kScanItems; ++k) {
     uint32_t b = threadIdx.x * kScanItems + k;
     v[k] = b < gridDim.x ? __ldcg(&d.block_sums[b]) : 0;
     run += v[k];
   }
-  uint32_t grand;
-  uint32_t off = block_exclusive_scan(run, &grand);
+  unsigned long long grand;
+  unsigned long long off = block_exclusive_scan64(run, &grand);
 #pragma unroll
   for (int k = 0; k < kScanItems; ++k) {
     uint32_t b = threadIdx.x * kScanItems + k;
@@ -175,42 +191,59 @@ __global__ void __launch_bounds__(kBlock) k_scan_reduce(DeviceView d, uint32_t c
   }
 }
 
+template <bool PAIRS>
 __global__ void __launch_bounds__(kBlock) k_scan_down(DeviceView d, uint32_t cells) {
   const uint32_t base = blockIdx.x * kScanChunk + threadIdx.x * kScanItems;
   uint32_t v[kScanItems];
-  uint32_t run = 0;
+  unsigned long long run = 0;
 #pragma unroll
   for (int k = 0; k < kScanItems; ++k) {
     uint32_t c = base + k;
     v[k] = c < cells ? d.counts[c] : 0;
-    run += v[k];
+    run += scan_word<PAIRS>(v[k]);
   }
-  uint32_t total;
-  uint32_t off = block_exclusive_scan(run, &total) + __ldcg(&d.block_sums[blockIdx.x]);
+  unsigned long long total;
+  unsigned long long off = block_exclusive_scan64(run, &total) + __ldcg(&d.block_sums[blockIdx.x]);
 #pragma unroll
   for (int k = 0; k < kScanItems; ++k) {
     uint32_t c = base + k;
     if (c < cells) {
-      d.cell_start[c] = off;
+      d.cell_start[c] = (uint32_t)off;
+      if (PAIRS) d.pair_start[c] = (uint32_t)(off >> 32);
       d.counts[c] = 0;   // histogram ready for the next tick
       if (v[k] > kBigCell) d.big_list[atomicAdd(&d.big_count[0], 1u)] = c;
       else if (v[k] > kWarpSmallCell) d.big_list[cells + atomicAdd(&d.big_count[1], 1u)] = c;
       else if (v[k] > kSmallCell) d.big_list[2 * cells - 1 - atomicAdd(&d.big_count[2], 1u)] = c;
     }
-    off += v[k];
+    off += scan_word<PAIRS>(v[k]);
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) d.cell_start[cells] = __ldcg(&d.block_sums[gridDim.x]);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const unsigned long long g = __ldcg(&d.block_sums[gridDim.x]);
+    d.cell_start[cells] = (uint32_t)g;
+    if (PAIRS) d.pair_start[cells] = (uint32_t)(g >> 32);
+  }
 }
 
 // ---------------------------------------------------------------- scatter --
+// With PAIRS, the point at an even position of its cell's segment also writes
+// the paired pass's work item: positions (dst, dst + 1), or dst alone when it
+// is the segment's last point.  Positions, not points: the cell kernel later
+// moves the slots to the segment's head, and a pair stays within its cell.
+template <bool PAIRS>
 __global__ void __launch_bounds__(kBlock) k_scatter(DeviceView d) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.n) return;
   const uint32_t k = d.key[i];
   if (k == kNoCell) return;
-  const uint32_t dst = d.cell_start[k] + d.rank[i];
+  const uint32_t r = d.rank[i];
+  const uint32_t b = d.cell_start[k];
+  const uint32_t dst = b + r;
   d.sorted_idx[dst] = i;
   d.sorted_pos[dst] = d.pos[i];
+  if (PAIRS && !(r & 1u)) {
+    const uint32_t m = d.cell_start[k + 1] - b;
+    d.pair_list[d.pair_start[k] + (r >> 1)] = dst | (r + 1 == m ? kSingleBit : 0u);
+  }
 }
 
 // ------------------------------------------------------------------ cells --
@@ -555,6 +588,74 @@ __global__ void __launch_bounds__(kBlock) k_manybody_split(DeviceView d, SimScal
   const float k = __fmul_rn(tp.alpha, s.repulsion);
   if (quotient_by_recip(k)) manybody_split<true>(d, s, k, lvs, nfs, nfa);
   else manybody_split<false>(d, s, k, lvs, nfs, nfa);
+}
+
+// Two points of one finest cell per thread (manybody_duo.cuh): every result
+// is the one manybody_point gives that point.  GUARD (the host's
+// level_guard): when no binned point lies outside the space this tick, no
+// level term's length can leave [1, 2^52], and the level terms run without
+// the range flag.
+template <bool GUARD>
+__device__ __forceinline__ void manybody_duo(const DeviceView& d, const SimScalars& s, uint32_t jA, uint32_t jB,
+                                             bool single, float k) {
+  const uint32_t iA = d.sorted_idx[jA], iB = d.sorted_idx[jB];
+  const float2 pA = d.sorted_pos[jA], pB = d.sorted_pos[jB];
+  const int gf = s.gf, L = s.levels;
+  const int fcx = cell_index(pA.x, s.csf, gf), fcy = cell_index(pA.y, s.csf, gf);
+  const PairUnits pu = s.units;
+  const Duo P = {make_float2(pA.x, pB.x), make_float2(pA.y, pB.y)};
+  Duo vel = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll 1
+  for (int l = 0; l < L; ++l) {
+    const int sh = L - 1 - l;
+    const float4* lv = d.rec + d.level_off[l];
+    bool out = false;
+    Duo v = level_terms_duo<!GUARD>(lv, 4 << l, fcx >> sh, fcy >> sh, P, k, pu, out);
+    if (!GUARD && out) {   // a length outside the sequences: each point's level with the tested terms
+      const float2 a = level_terms<true, false>(lv, 4 << l, fcx >> sh, fcy >> sh, pA, k, pu);
+      const float2 b = level_terms<true, false>(lv, 4 << l, fcx >> sh, fcy >> sh, pB, k, pu);
+      v.x = make_float2(a.x, b.x);
+      v.y = make_float2(a.y, b.y);
+    }
+    vel.x = add2(vel.x, v.x, pu);
+    vel.y = add2(vel.y, v.y, pu);
+  }
+  const float2 rA = d.jitter[iA], rB = d.jitter[iB];
+  const Duo R = {make_float2(rA.x, rB.x), make_float2(rA.y, rB.y)};
+  Duo nf = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+  const float4* fine = d.rec + d.level_off[L - 1];
+  // the 3x3 near field in row order; the own cell is the middle one
+#pragma unroll 1
+  for (int c = 0; c < 4; ++c)
+    near_cell_duo<false>(fine, d.cell_start, d.sorted_pos, gf, fcx, fcy, c % 3 - 1, c / 3 - 1, jA, jB, P, R, k, pu, nf);
+  near_cell_duo<true>(fine, d.cell_start, d.sorted_pos, gf, fcx, fcy, 0, 0, jA, jB, P, R, k, pu, nf);
+#pragma unroll 1
+  for (int c = 5; c < 9; ++c)
+    near_cell_duo<false>(fine, d.cell_start, d.sorted_pos, gf, fcx, fcy, c % 3 - 1, c / 3 - 1, jA, jB, P, R, k, pu, nf);
+  finish_point(d, s, iA, pA, rA, make_float2(vel.x.x, vel.y.x), make_float2(nf.x.x, nf.y.x), pu);
+  if (!single) finish_point(d, s, iB, pB, rB, make_float2(vel.x.y, vel.y.y), make_float2(nf.x.y, nf.y.y), pu);
+}
+
+// Four blocks per SM (62 registers): five spill and run 13% slower, three
+// leave warps short and run 6% slower (1M-point SBM, GB300).
+template <bool GUARD>
+__global__ void __launch_bounds__(kBlock, 4) k_manybody_duo(DeviceView d, SimScalars s) {
+  const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= d.pair_start[s.gf * s.gf]) return;
+  const TickParams tp = tick_params(d);
+  const float k = __fmul_rn(tp.alpha, s.repulsion);
+  const uint32_t e = d.pair_list[w];
+  const uint32_t jA = e & ~kSingleBit;
+  const bool single = (e & kSingleBit) != 0;
+  const uint32_t jB = single ? jA : jA + 1;
+  if (!quotient_by_recip(k)) {   // quotients outside the reciprocal method's range: one point at a time
+    manybody_point<false>(d, s, jA, k);
+    if (!single) manybody_point<false>(d, s, jB, k);
+  } else if (GUARD && __ldg(&d.big_count[kOutsideFlag]) == 0) {
+    manybody_duo<true>(d, s, jA, jB, single, k);
+  } else {
+    manybody_duo<false>(d, s, jA, jB, single, k);
+  }
 }
 
 __global__ void __launch_bounds__(kBlock, 6) k_manybody(DeviceView d, SimScalars s) {
@@ -1081,14 +1182,20 @@ void launch_center(const DeviceView& d, const SimScalars& s, bool bin, cudaStrea
 void launch_scan(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
   const uint32_t cells = (uint32_t)(s.gf * s.gf);
   const uint32_t nb = scan_blocks(cells);
-  k_scan_reduce<<<nb, kBlock, 0, st>>>(d, cells);
-  k_scan_down<<<nb, kBlock, 0, st>>>(d, cells);
+  if (s.pairs) {
+    k_scan_reduce<true><<<nb, kBlock, 0, st>>>(d, cells);
+    k_scan_down<true><<<nb, kBlock, 0, st>>>(d, cells);
+  } else {
+    k_scan_reduce<false><<<nb, kBlock, 0, st>>>(d, cells);
+    k_scan_down<false><<<nb, kBlock, 0, st>>>(d, cells);
+  }
 }
 
 void launch_scatter(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
-  (void)s;
   const uint32_t nb = blocks_for(d.n);
-  if (nb) k_scatter<<<nb, kBlock, 0, st>>>(d);
+  if (!nb) return;
+  if (s.pairs) k_scatter<true><<<nb, kBlock, 0, st>>>(d);
+  else k_scatter<false><<<nb, kBlock, 0, st>>>(d);
 }
 
 void launch_cells(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
@@ -1108,10 +1215,20 @@ void launch_cells(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
 // warps and each point's serial chain of terms sets the pass time; below that
 // the split kernel spreads a point over 16 threads (2k-50k points: 1.2-2x
 // faster; at 100k it is 16% slower).
+// Graphs with at least one point per finest cell on average (the finest grid
+// is capped at 512, so from 262,144 points) take two points of a cell per
+// thread: at most (n + cells) / 2 work items.
 void launch_manybody(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
   if (!d.n) return;
-  if (d.n < 2u * kBlock * sm_count()) k_manybody_split<<<(d.n + kSplitPoints - 1) / kSplitPoints, kBlock, 0, st>>>(d, s);
-  else k_manybody<<<blocks_for(d.n), kBlock, 0, st>>>(d, s);
+  if (s.pairs) {
+    const uint32_t items = (uint32_t)(((uint64_t)d.n + (uint64_t)s.gf * s.gf) / 2 + 1);
+    if (s.level_guard) k_manybody_duo<true><<<blocks_for(items), kBlock, 0, st>>>(d, s);
+    else k_manybody_duo<false><<<blocks_for(items), kBlock, 0, st>>>(d, s);
+  } else if (d.n < 2u * kBlock * sm_count()) {
+    k_manybody_split<<<(d.n + kSplitPoints - 1) / kSplitPoints, kBlock, 0, st>>>(d, s);
+  } else {
+    k_manybody<<<blocks_for(d.n), kBlock, 0, st>>>(d, s);
+  }
 }
 
 void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool swap_back, cudaStream_t st) {

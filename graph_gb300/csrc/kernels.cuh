@@ -27,7 +27,10 @@ struct DeviceView {
   float2* sorted_pos;         // positions in the same order (snapshot for the many-body pass) [n]
   uint32_t* counts;           // finest-cell histogram [G^2] (zeroed by the scan)
   uint32_t* cell_start;       // exclusive scan [G^2 + 1]
-  uint32_t* block_sums;       // scan partials
+  unsigned long long* block_sums;  // scan partials: (count, pairs) packed as low and high 32 bits
+  uint32_t* pair_start;       // exclusive scan of ceil(count / 2) per finest cell [G^2 + 1]
+  uint32_t* pair_list;        // per pair of one cell's consecutive sorted positions (j, j + 1): j,
+                              // with the top bit set when j is the cell's last point alone [<= n]
   uint32_t* scan_ticket;      // last-block ticket of the scan
   float4* rec;                // cell records of all levels (cx, cy, count, nslot)
   uint32_t level_off[10];     // offset of level l in rec
@@ -36,8 +39,9 @@ struct DeviceView {
   uint32_t* cells_ticket;     // last-block ticket of the cell kernel
   uint32_t* big_list;         // [G^2] cells above kBigCell, then [G^2] warp cells: those above
                               // kWarpSmallCell from the front, the others above kSmallCell from the back
-  uint32_t* big_count;        // [4] CTA cells, heavy and light warp cells this tick, warp-cell
-                              // ticket (zeroed at tick start)
+  uint32_t* big_count;        // [8] CTA cells, heavy and light warp cells this tick, warp-cell
+                              // ticket, then [4] = 1 when a binned point lies outside [0, space]
+                              // (zeroed at tick start)
   long long* big_sx;          // exact sums of big cells [G^2]
   long long* big_sy;
   uint32_t* big_ns;           // slots of big cells [G^2]
@@ -92,7 +96,13 @@ struct SimScalars {
   FixedScale fx;
   PairUnits units;            // {1, -0}: operands of the paired sums and products
   float cluster;              // simulationCluster
+  int pairs;                  // the many-body pass takes two points of a cell per thread (k_manybody_duo);
+                              // the scan and scatter then build the pair list
+  int level_guard;            // finest cell >= 2 units and space <= 2^25: a level term's length is
+                              // then in [1, 2^52] whenever every binned point lies in [0, space]
 };
+constexpr uint32_t kOutsideFlag = 4;   // big_count word of the outside-the-space flag
+constexpr uint32_t kSingleBit = 0x80000000u;
 
 
 enum PrepassMode : uint32_t { kPreGravity = 1, kPreCentroid = 2, kPreBin = 4 };

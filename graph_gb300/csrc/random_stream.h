@@ -22,8 +22,12 @@
 //
 // The stream is sequential (each byte permutes the generator's state), so the
 // engines draw on the host and upload what the kernels need.  The bulk fills
-// below keep the generator's state in locals; every value is exact: n + x is an
-// integer below 2^53 and d a power of two.
+// below keep the generator's state in locals.  seedrandom's double is, exactly,
+// the integer M of the first 6 + k bytes (k >= 1 the fewest with M >= 2^52)
+// cut to its top 53 bits and scaled by 2^-(48 + 8k): its loop appends bytes to
+// n and shifts n, x and d right together, so (n + x) / d is M with the bits
+// below the top 53 dropped; that is computed here with one count of leading
+// zeros, in exact integer and power-of-two arithmetic.
 #pragma once
 #include <cstddef>
 #include <cstdint>
@@ -48,10 +52,10 @@ class RandomStream {
     }
     size_t keylen = n < 256 ? n : 256;
     if (keylen == 0) { key[0] = 0; keylen = 1; }
-    for (int i = 0; i < 256; ++i) S_[i] = (uint8_t)i;
+    for (int i = 0; i < 256; ++i) S_[i] = (uint32_t)i;
     uint32_t j = 0;
     for (int i = 0; i < 256; ++i) {
-      const uint8_t t = S_[i];
+      const uint32_t t = S_[i];
       j = (j + key[i % keylen] + t) & 255u;
       S_[i] = S_[j];
       S_[j] = t;
@@ -141,37 +145,33 @@ class RandomStream {
     j_ = j;
     return b;
   }
-  static inline uint32_t step(uint8_t* __restrict S, uint32_t& i, uint32_t& j) {
+  // RC4's output step; the state is kept in 32-bit words (faster here than bytes).
+  static inline uint32_t step(uint32_t* __restrict S, uint32_t& i, uint32_t& j) {
     i = (i + 1) & 255u;
     const uint32_t t = S[i];
     j = (j + t) & 255u;
     const uint32_t sj = S[j];
-    S[i] = (uint8_t)sj;
-    S[j] = (uint8_t)t;
+    S[i] = sj;
+    S[j] = t;
     return S[(sj + t) & 255u];
   }
-  static inline double unit(uint8_t* S, uint32_t& i, uint32_t& j) {
-    uint64_t n = 0;
-    for (int k = 0; k < 6; ++k) n = (n << 8) | step(S, i, j);
-    int e = 48;   // d = 2^e
-    uint64_t x = 0;
-    while (n < (1ull << 52)) {
-      n = (n + x) << 8;
+  static inline double unit(uint32_t* S, uint32_t& i, uint32_t& j) {
+    uint64_t m = 0;
+    for (int k = 0; k < 7; ++k) m = (m << 8) | step(S, i, j);
+    int e = 56;   // the value is m / 2^e before the cut to 53 bits
+    while ((m >> 8) < (1ull << 44)) {   // seedrandom's loop runs again: one more byte
+      m = (m << 8) | step(S, i, j);
       e += 8;
-      x = step(S, i, j);
     }
-    while (n >= (1ull << 53)) {   // n is a multiple of 256 here: the shifts are exact
-      n >>= 1;
-      --e;
-      x >>= 1;
-    }
-    // (n + x) < 2^53 is exact in a double; dividing by 2^e is exact too
-    double v = (double)(n + x);
+    // here 2^52 <= m < 2^60: keep the top 53 bits (exact in a double)
+    const int h = 11 - __builtin_clzll(m);   // bit length - 53
+    double v = (double)(m >> h);
+    e -= h;
     while (e > 60) { v *= 0x1.0p-60; e -= 60; }
     return v * (1.0 / (double)(1ull << e));
   }
 
-  uint8_t S_[256] = {};
+  uint32_t S_[256] = {};
   uint32_t i_ = 0, j_ = 0;
   uint64_t draws_ = 0;
 };

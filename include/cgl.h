@@ -305,8 +305,13 @@ typedef struct cgl_layout {
   float collision_cell_size;
   uint64_t device_bytes;       /* device memory held by the handle */
   uint32_t kernels_per_tick;   /* kernel launches one tick makes with the current data and config */
-  uint32_t reserved;
+  uint32_t manybody_kernel;    /* CGL_MANYBODY_*: how the many-body pass spreads points over threads */
 } cgl_layout;
+enum {
+  CGL_MANYBODY_ONE_POINT = 0,   /* a thread per point */
+  CGL_MANYBODY_SPLIT = 1,       /* small graphs: a point's terms over 16 threads */
+  CGL_MANYBODY_TWO_POINTS = 2   /* two points of one finest cell per thread (cells of >= 1 point on average) */
+};
 cgl_status cgl_get_layout(cgl_engine* e, cgl_layout* out);
 
 /* Test hooks: state retained from the last tick's many-body pass. */

@@ -68,3 +68,11 @@ def test_seed_mapping():
     assert _abi.seed_to_u64(-1) == (1 << 64) - 1
     assert _abi.seed_to_u64("abc") == _abi.seed_to_u64("abc") != _abi.seed_to_u64("abd")
     assert _abi.seed_to_u64(2.0) == 2
+
+
+def test_layout_names_the_many_body_kernels():
+    src = open(HEADER).read()
+    for name, value in (("CGL_MANYBODY_ONE_POINT", 0), ("CGL_MANYBODY_SPLIT", 1), ("CGL_MANYBODY_TWO_POINTS", 2)):
+        assert re.search(r"%s = %d" % (name, value), src)
+    assert (_abi.MANYBODY_ONE_POINT, _abi.MANYBODY_SPLIT, _abi.MANYBODY_TWO_POINTS) == (0, 1, 2)
+    assert [f for f, _ in _abi.Layout._fields_][-1] == "manybody_kernel"
