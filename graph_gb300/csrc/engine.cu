@@ -93,6 +93,7 @@ struct cgl_engine {
   size_t dev_bytes = 0;
   DevBuf b_pos, b_pos_alt, b_flags, b_jitter, b_key, b_rank, b_sorted_idx, b_sorted_pos;
   DevBuf b_counts, b_cell_start, b_block_sums, b_tickets, b_rec, b_acc, b_centroid, b_pair_start, b_pair_list;
+  DevBuf b_idx_s, b_pos_s, b_bin_state;
   DevBuf b_big_list, b_big_count, b_big_sx, b_big_sy, b_big_ns;
   DevBuf b_params, b_tick_ctr;
   DevBuf b_rowptr_in, b_rowptr_out, b_ent_in, b_ent_out, b_heavy_in, b_heavy_out;
@@ -177,7 +178,7 @@ void dev_free_all(cgl_engine* e) {
                    &e->b_big_sx, &e->b_big_sy, &e->b_big_ns, &e->b_heavy_in, &e->b_heavy_out,
                    &e->b_cl_of, &e->b_cl_coeff, &e->b_cl_custom, &e->b_cl_acc, &e->b_texture,
                    &e->b_woff_in, &e->b_woff_out, &e->b_lane_ent_in, &e->b_lane_ent_out, &e->b_pair_start,
-                   &e->b_pair_list};
+                   &e->b_pair_list, &e->b_idx_s, &e->b_pos_s, &e->b_bin_state};
   for (DevBuf* b : all) {
     if (b->p) cudaFree(b->p);
     b->p = nullptr;
@@ -215,6 +216,9 @@ void refresh_view(cgl_engine* e) {
   d.cell_start = (uint32_t*)e->b_cell_start.p;
   d.block_sums = (unsigned long long*)e->b_block_sums.p;
   d.pair_start = (uint32_t*)e->b_pair_start.p;
+  d.idx_s = (uint32_t*)e->b_idx_s.p;
+  d.pos_s = (float2*)e->b_pos_s.p;
+  d.bin_state = (uint32_t*)e->b_bin_state.p;
   d.pair_list = (uint32_t*)e->b_pair_list.p;
   d.scan_ticket = (uint32_t*)e->b_tickets.p;
   d.cells_ticket = d.scan_ticket ? d.scan_ticket + 1 : nullptr;
@@ -723,6 +727,10 @@ cgl_status build_graph(cgl_engine* e, double alpha, uint64_t N, uint64_t E) {
     if ((st = dev_reserve(e, e->b_rank, n * sizeof(uint32_t), false))) return st;
     if ((st = dev_reserve(e, e->b_sorted_idx, n * sizeof(uint32_t), false))) return st;
     if ((st = dev_reserve(e, e->b_sorted_pos, n * sizeof(float2), false))) return st;
+    if ((st = dev_reserve(e, e->b_idx_s, n * sizeof(uint32_t), false))) return st;
+    if ((st = dev_reserve(e, e->b_pos_s, n * sizeof(float2), false))) return st;
+    // a new point set: the first tick bins in index order (no cell order yet)
+    if ((st = dev_reserve(e, e->b_bin_state, 4 * sizeof(uint32_t), true))) return st;
     if (n) CU(cudaMemcpyAsync(e->b_pos.p, pos.data(), n * sizeof(float2), cudaMemcpyHostToDevice, e->stream));
     CU(cudaStreamSynchronize(e->stream));
     refresh_view(e);

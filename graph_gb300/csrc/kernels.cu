@@ -72,27 +72,74 @@ __device__ __forceinline__ void bin_point(const DeviceView& d, const SimScalars&
 }
 
 // ---------------------------------------------------------------- prepass --
+// force-gravity.frag:24-40 for point p (the velocity, before the update).
+__device__ __forceinline__ float2 gravity_velocity(const SimScalars& s, float alpha, float2 p) {
+  const float c = __fmul_rn(s.space, 0.5f);
+  const float dx = __fsub_rn(c, p.x), dy = __fsub_rn(c, p.y);
+  const float dist = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
+  float vx = 0.f, vy = 0.f;
+  if (dist > 0.f) {
+    const float add = __fmul_rn(__fmul_rn(__fmul_rn(alpha, s.gravity), dist), 0.1f);
+    vx = __fadd_rn(vx, __fmul_rn(add, __fdiv_rn(dx, dist)));
+    vy = __fadd_rn(vy, __fmul_rn(add, __fdiv_rn(dy, dist)));
+  }
+  return make_float2(vx, vy);
+}
+
+// Binning in the previous tick's cell order (bin_state[0]): points move little
+// in a tick, so the lanes of a warp mostly fall in a few cells, and one atomic
+// per cell and warp (__match_any_sync) ranks them all.  Keys, ranks, points and
+// positions are written by position j; the scatter reads them in that order.
+// The order of the points within a cell is free (every use of it is), so the
+// ranks need not follow j.
+template <uint32_t MODE>
+__device__ __forceinline__ void prepass_in_cell_order(const DeviceView& d, const SimScalars& s, const TickParams& tp) {
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j == 0) d.bin_state[1] = 1;
+  if (j >= d.cell_start[s.gf * s.gf]) return;   // the live points, binned last tick
+  const uint32_t i = d.sorted_idx[j];
+  float2 p = d.pos[i];
+  if (MODE & kPreGravity) {
+    const float2 v = gravity_velocity(s, tp.alpha, p);
+    if (!(d.flags[i] & kPinned)) {
+      p = integrate(p, v.x, v.y, s.friction, s.space);
+      d.pos[i] = p;
+    }
+  }
+  const int cx = cell_index(p.x, s.csf, s.gf), cy = cell_index(p.y, s.csf, s.gf);
+  const uint32_t key = (uint32_t)(cy * s.gf + cx);
+  const bool outside = !(p.x >= 0.f && p.x <= s.space && p.y >= 0.f && p.y <= s.space);
+  const unsigned am = __activemask();
+  const int lane = threadIdx.x & 31;
+  if (__ballot_sync(am, outside) && lane == __ffs(am) - 1) atomicOr(&d.big_count[kOutsideFlag], 1u);
+  const unsigned peers = __match_any_sync(am, key);
+  const int leader = __ffs(peers) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(&d.counts[key], (uint32_t)__popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  d.key[j] = key;
+  d.rank[j] = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+  d.idx_s[j] = i;
+  d.pos_s[j] = p;
+}
+
 template <uint32_t MODE>
 __global__ void __launch_bounds__(kBlock) k_prepass(DeviceView d, SimScalars s) {
   const TickParams tp = tick_params(d);
+  if ((MODE & kPreBin) && !(MODE & kPreCentroid) && d.bin_state[0]) {
+    prepass_in_cell_order<MODE>(d, s, tp);
+    return;
+  }
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((MODE & kPreBin) && i == 0) d.bin_state[1] = 0;
   long long sx = 0, sy = 0, sn = 0;
   if (i < d.n) {
     const uint8_t f = d.flags[i];
     float2 p = d.pos[i];
     if (MODE & kPreGravity) {
-      // force-gravity.frag:24-40
-      const float c = __fmul_rn(s.space, 0.5f);
-      const float dx = __fsub_rn(c, p.x), dy = __fsub_rn(c, p.y);
-      const float dist = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
-      float vx = 0.f, vy = 0.f;
-      if (dist > 0.f) {
-        const float add = __fmul_rn(__fmul_rn(__fmul_rn(tp.alpha, s.gravity), dist), 0.1f);
-        vx = __fadd_rn(vx, __fmul_rn(add, __fdiv_rn(dx, dist)));
-        vy = __fadd_rn(vy, __fmul_rn(add, __fdiv_rn(dy, dist)));
-      }
+      const float2 v = gravity_velocity(s, tp.alpha, p);
       if (!(f & (kPinned | kAbsent))) {
-        p = integrate(p, vx, vy, s.friction, s.space);
+        p = integrate(p, v.x, v.y, s.friction, s.space);
         d.pos[i] = p;
       }
     }
@@ -131,6 +178,7 @@ __global__ void __launch_bounds__(kBlock) k_center(DeviceView d, SimScalars s) {
     d.pos[i] = p;
   }
   if (BIN) {
+    if (i == 0) d.bin_state[1] = 0;
     if (!(f & kAbsent)) bin_point(d, s, i, p);
     else d.key[i] = kNoCell;
   }
@@ -229,17 +277,32 @@ __global__ void __launch_bounds__(kBlock) k_scan_down(DeviceView d, uint32_t cel
 // the paired pass's work item: positions (dst, dst + 1), or dst alone when it
 // is the segment's last point.  Positions, not points: the cell kernel later
 // moves the slots to the segment's head, and a pair stays within its cell.
+// Keys and ranks by point (index order) or by last tick's position
+// (bin_state[1]); either way every live point lands at cell_start + rank, and
+// sorted_idx then holds a cell order of the live points (bin_state[0]).
 template <bool PAIRS>
-__global__ void __launch_bounds__(kBlock) k_scatter(DeviceView d) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.n) return;
-  const uint32_t k = d.key[i];
-  if (k == kNoCell) return;
-  const uint32_t r = d.rank[i];
+__global__ void __launch_bounds__(kBlock) k_scatter(DeviceView d, uint32_t cells) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t == 0) d.bin_state[0] = 1;
+  uint32_t i, k;
+  float2 p;
+  if (d.bin_state[1]) {
+    if (t >= d.cell_start[cells]) return;
+    i = d.idx_s[t];
+    k = d.key[t];
+    p = d.pos_s[t];
+  } else {
+    if (t >= d.n) return;
+    i = t;
+    k = d.key[t];
+    if (k == kNoCell) return;
+    p = d.pos[t];
+  }
+  const uint32_t r = d.rank[t];
   const uint32_t b = d.cell_start[k];
   const uint32_t dst = b + r;
   d.sorted_idx[dst] = i;
-  d.sorted_pos[dst] = d.pos[i];
+  d.sorted_pos[dst] = p;
   if (PAIRS && !(r & 1u)) {
     const uint32_t m = d.cell_start[k + 1] - b;
     d.pair_list[d.pair_start[k] + (r >> 1)] = dst | (r + 1 == m ? kSingleBit : 0u);
@@ -1194,8 +1257,9 @@ void launch_scan(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
 void launch_scatter(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
   const uint32_t nb = blocks_for(d.n);
   if (!nb) return;
-  if (s.pairs) k_scatter<true><<<nb, kBlock, 0, st>>>(d);
-  else k_scatter<false><<<nb, kBlock, 0, st>>>(d);
+  const uint32_t cells = (uint32_t)(s.gf * s.gf);
+  if (s.pairs) k_scatter<true><<<nb, kBlock, 0, st>>>(d, cells);
+  else k_scatter<false><<<nb, kBlock, 0, st>>>(d, cells);
 }
 
 void launch_cells(const DeviceView& d, const SimScalars& s, cudaStream_t st) {

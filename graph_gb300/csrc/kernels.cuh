@@ -21,13 +21,18 @@ struct DeviceView {
   float2* pos_alt;            // ping-pong target of the link passes [n]
   const uint8_t* flags;       // kPinned | kAbsent [n]
   const float2* jitter;       // per-point random vector (ForceManyBody/index.ts:133-138) [n]
-  uint32_t* key;              // finest cell of each point, kNoCell if absent [n]
-  uint32_t* rank;             // rank within its cell from the histogram atomics [n]
+  uint32_t* key;              // finest cell of each point, kNoCell if absent [n] (of position j when
+                              // bin_state[1]: see idx_s)
+  uint32_t* rank;             // rank within its cell from the histogram atomics [n] (likewise)
   uint32_t* sorted_idx;       // points grouped by finest cell; head of each cell = slots in hash order [n]
   float2* sorted_pos;         // positions in the same order (snapshot for the many-body pass) [n]
   uint32_t* counts;           // finest-cell histogram [G^2] (zeroed by the scan)
   uint32_t* cell_start;       // exclusive scan [G^2 + 1]
   unsigned long long* block_sums;  // scan partials: (count, pairs) packed as low and high 32 bits
+  uint32_t* idx_s;            // binning in the previous cell order: the point at position j [n]
+  float2* pos_s;              // and its position after the prepass [n]
+  uint32_t* bin_state;        // [0] = 1 once sorted_idx holds a cell order of the live points (zeroed at
+                              // render); [1] = 1 when this tick's keys and ranks are by that order
   uint32_t* pair_start;       // exclusive scan of ceil(count / 2) per finest cell [G^2 + 1]
   uint32_t* pair_list;        // per pair of one cell's consecutive sorted positions (j, j + 1): j,
                               // with the top bit set when j is the cell's last point alone [<= n]

@@ -484,3 +484,32 @@ def test_string_seed_matches_oracle():
         eng.step(1)
         orc.step(1)
         _assert_same(eng, orc, ("string seed", t))
+
+
+def test_binning_order_switches():
+    # From the second tick the pass bins in the previous tick's cell order; a
+    # tick with the center force bins in point order (its centroid pass does
+    # the binning), a render of new positions starts over in point order, and
+    # pin changes apply in either order.
+    pos, links, fields = scenario("ba_small")
+    eng, orc = make_pair(pos, links, dict(fields, simulation_gravity=0.2))
+    plan = [({}, 2), ({"simulation_center": 0.4}, 2), ({}, 2), ("pin", 2), ("render", 3), ({"simulation_gravity": 0.0}, 2)]
+    base = dict(fields, simulation_gravity=0.2)
+    for change, ticks in plan:
+        if change == "pin":
+            for e in (eng, orc):
+                e.set_pinned_points([1, 5, 9, 300])
+        elif change == "render":
+            new_pos = generators.uniform_positions(pos.size // 2, 100, 4000, 8)
+            for e in (eng, orc):
+                e.set_point_positions(new_pos)
+                e.render()
+        else:
+            cfg = _abi.make_config(**dict(base, **change))
+            eng.set_config(cfg)
+            orc.set_config(cfg)
+        for t in range(ticks):
+            eng.step(1)
+            orc.step(1)
+            _assert_same(eng, orc, (change, t))
+    _assert_cells_and_slots(eng, orc)
