@@ -59,6 +59,7 @@ struct cgl_engine {
   bool has_data_sizes = false;
   std::vector<uint8_t> absent, pinned;
   uint64_t live = 0;
+  bool any_pinned = false;     // some live point is pinned (a tick-graph constant)
   uint64_t entries = 0;
   uint32_t max_deg_in = 0, max_deg_out = 0;
   bool mb_ready = false;
@@ -287,6 +288,7 @@ SimScalars make_scalars(const cgl_engine* e) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   s.pairs = e->Gf > 0 && e->live >= (uint64_t)e->Gf * e->Gf && e->N >= 2ull * 256 * (uint64_t)sms;
   s.level_guard = s.csf >= 2.0f && s.space <= 33554432.0f;   // 2^25
+  s.any_pinned = e->any_pinned;
   return s;
 }
 
@@ -643,6 +645,10 @@ cgl_status apply_pinned(cgl_engine* e) {
   if (e->pinned_set)
     for (double v : e->pinned_input)
       if (v >= 0 && v < (double)e->N && v == std::floor(v)) e->pinned[(size_t)v] = 1;
+  bool any = false;
+  for (uint64_t i = 0; i < e->N; ++i) any |= e->pinned[i] && !e->absent[i];
+  if (any != e->any_pinned) e->graph_dirty = true;   // the tick kernels take it as a constant
+  e->any_pinned = any;
   if (!e->N) return CGL_OK;
   std::vector<uint8_t> flags(e->N);
   for (uint64_t i = 0; i < e->N; ++i) flags[i] = (e->pinned[i] ? kPinned : 0) | (e->absent[i] ? kAbsent : 0);

@@ -91,7 +91,11 @@ __device__ __forceinline__ float2 gravity_velocity(const SimScalars& s, float al
 // per cell and warp (__match_any_sync) ranks them all.  Keys, ranks, points and
 // positions are written by position j; the scatter reads them in that order.
 // The order of the points within a cell is free (every use of it is), so the
-// ranks need not follow j.
+// ranks need not follow j.  The gravity-updated position is not written back
+// to pos: the many-body pass that follows this binning starts from it (through
+// the scatter's sorted_pos) and writes every live point that is not pinned,
+// and a pinned point does not move.  Without pinned points (s.any_pinned = 0)
+// no flag is read either: absent points are not in the cell order.
 template <uint32_t MODE>
 __device__ __forceinline__ void prepass_in_cell_order(const DeviceView& d, const SimScalars& s, const TickParams& tp) {
   const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -101,10 +105,7 @@ __device__ __forceinline__ void prepass_in_cell_order(const DeviceView& d, const
   float2 p = d.pos[i];
   if (MODE & kPreGravity) {
     const float2 v = gravity_velocity(s, tp.alpha, p);
-    if (!(d.flags[i] & kPinned)) {
-      p = integrate(p, v.x, v.y, s.friction, s.space);
-      d.pos[i] = p;
-    }
+    if (!s.any_pinned || !(d.flags[i] & kPinned)) p = integrate(p, v.x, v.y, s.friction, s.space);
   }
   const int cx = cell_index(p.x, s.csf, s.gf), cy = cell_index(p.y, s.csf, s.gf);
   const uint32_t key = (uint32_t)(cy * s.gf + cx);

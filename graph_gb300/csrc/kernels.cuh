@@ -105,6 +105,7 @@ struct SimScalars {
                               // the scan and scatter then build the pair list
   int level_guard;            // finest cell >= 2 units and space <= 2^25: a level term's length is
                               // then in [1, 2^52] whenever every binned point lies in [0, space]
+  int any_pinned;             // some live point is pinned
 };
 constexpr uint32_t kOutsideFlag = 4;   // big_count word of the outside-the-space flag
 constexpr uint32_t kSingleBit = 0x80000000u;
