@@ -611,7 +611,7 @@ def run_batch(args):
     # batched
     t0 = time.perf_counter()
     b = Batch()
-    ids = [b.add(p, l, max_ticks=args.ticks, **f) for p, l, f in jobs]
+    ids = b.add_many([dict(positions=p, links=l, max_ticks=args.ticks, **f) for p, l, f in jobs])
     b.synchronize()
     t1 = time.perf_counter()
     b.step(args.ticks)

@@ -320,3 +320,18 @@ class BatchInfo(C.Structure):
         ("kernels_per_tick", C.c_uint32),
         ("reserved", C.c_uint32),
     ]
+
+
+class BatchJob(C.Structure):
+    """cgl_batch_job (include/cgl.h): one job of cgl_batch_add_many."""
+    _fields_ = [
+        ("cfg", C.POINTER(Config)),
+        ("xy", C.POINTER(C.c_float)),
+        ("n_floats", C.c_uint64),
+        ("links", C.POINTER(C.c_float)),
+        ("n_link_floats", C.c_uint64),
+        ("sizes", C.POINTER(C.c_float)),
+        ("n_sizes", C.c_uint64),
+        ("max_ticks", C.c_uint32),
+        ("stop_below_alpha_min", C.c_int32),
+    ]

@@ -23,6 +23,8 @@ def _declare(lib):
     lib.cgl_batch_destroy.argtypes = [B]
     lib.cgl_batch_add.argtypes = [B, C.POINTER(_abi.Config), f, C.c_uint64, f, C.c_uint64, C.c_uint32, C.c_int32,
                                   C.POINTER(C.c_uint32)]
+    lib.cgl_batch_add_many.argtypes = [B, C.c_uint32, C.POINTER(_abi.BatchJob), C.POINTER(C.c_uint32), C.c_uint32,
+                                       C.POINTER(C.c_uint32)]
     lib.cgl_batch_remove.argtypes = [B, C.c_uint32]
     lib.cgl_batch_step.argtypes = [B, C.c_uint32]
     lib.cgl_batch_synchronize.argtypes = [B]
@@ -31,8 +33,8 @@ def _declare(lib):
     lib.cgl_batch_get_info.argtypes = [B, C.POINTER(_abi.BatchInfo)]
     lib.cgl_batch_last_error.argtypes = [B]
     lib.cgl_batch_last_error.restype = C.c_char_p
-    for fn in ("create", "destroy", "add", "remove", "step", "synchronize", "get_point_positions", "get_state",
-               "get_info"):
+    for fn in ("create", "destroy", "add", "add_many", "remove", "step", "synchronize", "get_point_positions",
+               "get_state", "get_info"):
         getattr(lib, "cgl_batch_" + fn).restype = C.c_int
     lib._batch_declared = True
 
@@ -54,7 +56,11 @@ class Batch:
             raise StatusError("cgl_batch_" + name, st, t.decode() if t else "")
         return st
 
-    def add(self, positions, links=None, max_ticks=0, stop_below_alpha_min=False, cfg=None, **fields):
+    def add(self, positions, links=None, max_ticks=0, stop_below_alpha_min=False, cfg=None, sizes=None, **fields):
+        """Add one job; `sizes` are its per-point sizes (the collision radii, Graph.setPointSizes)."""
+        if sizes is not None:
+            return self.add_many([dict(positions=positions, links=links, max_ticks=max_ticks,
+                                       stop_below_alpha_min=stop_below_alpha_min, cfg=cfg, sizes=sizes, **fields)])[0]
         if cfg is None:
             cfg = _abi.make_config(**fields)
         xy = _f32(positions)
@@ -64,6 +70,42 @@ class Batch:
                                                    int(max_ticks), int(bool(stop_below_alpha_min)), C.byref(gid)))
         self._n[gid.value] = xy.size // 2
         return gid.value
+
+    def add_many(self, jobs, threads=0):
+        """Add jobs (dicts of add()'s arguments) with their host work on `threads` host threads
+        (0 = one per core); returns their ids in order."""
+        keep = []
+        arr = (_abi.BatchJob * len(jobs))()
+        for k, jb in enumerate(jobs):
+            jb = dict(jb)
+            cfg = jb.pop("cfg", None)
+            pos = _f32(jb.pop("positions"))
+            links = jb.pop("links", None)
+            ln = _f32(links) if links is not None else np.zeros(0, dtype=np.float32)
+            sizes = jb.pop("sizes", None)
+            sz = _f32(sizes) if sizes is not None else None
+            max_ticks = jb.pop("max_ticks", 0)
+            stop = jb.pop("stop_below_alpha_min", False)
+            if cfg is None:
+                cfg = _abi.make_config(**jb)
+            keep += [cfg, pos, ln, sz]
+            arr[k].cfg = C.pointer(cfg)
+            arr[k].xy = _fptr(pos)
+            arr[k].n_floats = pos.size
+            arr[k].links = _fptr(ln)
+            arr[k].n_link_floats = ln.size
+            if sz is not None:
+                arr[k].sizes = _fptr(sz)
+                arr[k].n_sizes = sz.size
+            arr[k].max_ticks = int(max_ticks)
+            arr[k].stop_below_alpha_min = int(bool(stop))
+        ids = (C.c_uint32 * len(jobs))()
+        added = C.c_uint32()
+        st = self._lib.cgl_batch_add_many(self._h, len(jobs), arr, ids, int(threads), C.byref(added))
+        for k in range(added.value):
+            self._n[ids[k]] = int(arr[k].n_floats) // 2
+        self._check("add_many", st)
+        return [ids[k] for k in range(len(jobs))]
 
     def remove(self, job):
         self._check("remove", self._lib.cgl_batch_remove(self._h, int(job)))

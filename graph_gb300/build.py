@@ -17,7 +17,7 @@ OBJ_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcgl_gb300.so")
 SOURCES = ["kernels.cu", "engine.cu", "noalloc.cu", "ingest_device.cu", "batch_kernels.cu", "batch.cu"]
 HEADERS = ["common.cuh", "kernels.cuh", "ingest.h", "device_util.cuh", "batch.cuh", "ingest_device.cuh",
-           "warp_cells.cuh", "random_stream.h"]
+           "warp_cells.cuh", "random_stream.h", "manybody_duo.cuh", "collision.cuh"]
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

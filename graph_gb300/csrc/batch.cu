@@ -12,8 +12,13 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
+#include <condition_variable>
 #include <map>
+#include <memory>
+#include <mutex>
 #include <random>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -73,6 +78,7 @@ struct Job {
   uint64_t n = 0, live = 0, E = 0, m_in = 0, m_out = 0;
   uint64_t p_off = 0, cell_off = 0, cells = 0, rec_off = 0, recs = 0, acc_off = 0, accs = 0;
   uint64_t rp_in = 0, rp_out = 0, e_in = 0, e_out = 0;
+  uint64_t coll_off = 0, coll_cells = 0;   // collision grids: 4 x coll_grid^2 cells
   int gf = 0, levels = 0, tile = 0;
   uint32_t stages = 0;
   ingest::Rng rng;
@@ -94,7 +100,7 @@ struct cgl_batch {
   cudaStream_t stream = nullptr, side = nullptr;
   cudaEvent_t fork[2] = {}, join[2] = {}, params_copied = nullptr;
   bool params_pending = false;
-  Arena pts, cells, recs, accs, rows, ents;
+  Arena pts, cells, recs, accs, rows, ents, colls;
   std::vector<Job> jobs;
   size_t dev_bytes = 0;
   // point arena
@@ -103,6 +109,8 @@ struct cgl_batch {
   Buf counts, cell_start, cell_gid, big_list, big_sx, big_sy, big_ns, scan1, scan2;
   Buf big_count, tick_ctr;
   Buf rec, acc, rowptr, ent, desc, tiles, heavy_in, heavy_out, ticks;
+  Buf size, cgrid_acc, cgrid, coll_gid, centroid;   // collision and center
+  bool any_center = false, any_collision = false;
   uint32_t n_tiles = 0, n_heavy_in = 0, n_heavy_out = 0, slots_cap = 0;
   BatchTick* h_ticks = nullptr;
   cudaGraphExec_t graph = nullptr;
@@ -181,7 +189,7 @@ cgl_status reserve_points(cgl_batch* b, uint64_t cap) {
       (st = grow(b, b->pos_alt, cap * 8, keep * 8, -1)) || (st = grow(b, b->flags, cap, keep, 0)) ||
       (st = grow(b, b->jitter, cap * 8, keep * 8, -1)) || (st = grow(b, b->key, cap * 4, 0, -1)) ||
       (st = grow(b, b->rank, cap * 4, 0, -1)) || (st = grow(b, b->sorted_idx, cap * 4, 0, -1)) ||
-      (st = grow(b, b->sorted_pos, cap * 8, 0, -1)))
+      (st = grow(b, b->sorted_pos, cap * 8, 0, -1)) || (st = grow(b, b->size, cap * 4, keep * 4, 0)))
     return st;
   b->pts.cap = cap;
   return CGL_OK;
@@ -199,6 +207,18 @@ cgl_status reserve_cells(cgl_batch* b, uint64_t cap) {
       (st = grow(b, b->scan2, n2 * 4, 0, -1)))
     return st;
   b->cells.cap = cap;
+  return CGL_OK;
+}
+
+// The collision arena: integer sums (zero between ticks), grids, graph of each cell.
+cgl_status reserve_colls(cgl_batch* b, uint64_t cap) {
+  if (cap <= b->colls.cap) return CGL_OK;
+  const uint64_t keep = b->colls.hwm;
+  cgl_status st;
+  if ((st = grow(b, b->cgrid_acc, cap * 32, keep * 32, 0)) || (st = grow(b, b->cgrid, cap * 16, 0, 0)) ||
+      (st = grow(b, b->coll_gid, cap * 4, keep * 4, 0xFF)))
+    return st;
+  b->colls.cap = cap;
   return CGL_OK;
 }
 
@@ -240,6 +260,14 @@ void refresh_view(cgl_batch* b) {
   v.n_heavy_out = b->n_heavy_out;
   v.ticks = (const BatchTick*)b->ticks.p;
   v.tick_ctr = (uint32_t*)b->tick_ctr.p;
+  v.centroid = (long long*)b->centroid.p;
+  v.size = (const float*)b->size.p;
+  v.cgrid_acc = (long long*)b->cgrid_acc.p;
+  v.cgrid = (float4*)b->cgrid.p;
+  v.coll_gid = (const uint32_t*)b->coll_gid.p;
+  v.coll_hwm = (uint32_t)b->colls.hwm;
+  v.any_center = b->any_center ? 1 : 0;
+  v.any_collision = b->any_collision ? 1 : 0;
 }
 
 // Descriptors, the cell-kernel work list and the long-list rows of all jobs.
@@ -250,10 +278,13 @@ cgl_status rebuild_tables(cgl_batch* b) {
   std::vector<GraphDesc> descs(slots);
   std::vector<uint2> tiles;
   std::vector<uint32_t> hin, hout;
+  b->any_center = b->any_collision = false;
   for (size_t g = 0; g < slots; ++g) {
     const Job& j = b->jobs[g];
     if (!j.used) { std::memset(&descs[g], 0, sizeof(GraphDesc)); continue; }
     descs[g] = j.desc;
+    b->any_center |= (j.stages & kGCenter) != 0;
+    b->any_collision |= (j.stages & kGCollision) != 0;
     if (j.stages & kGManybody) {
       const int per_row = j.gf / j.tile;
       for (int t = 0; t < per_row * per_row; ++t) tiles.push_back(make_uint2((uint32_t)g, (uint32_t)t));
@@ -266,6 +297,7 @@ cgl_status rebuild_tables(cgl_batch* b) {
   if ((st = grow(b, b->tiles, std::max<size_t>(tiles.size(), 1) * sizeof(uint2), 0, -1))) return st;
   if ((st = grow(b, b->heavy_in, std::max<size_t>(hin.size(), 1) * 4, 0, -1))) return st;
   if ((st = grow(b, b->heavy_out, std::max<size_t>(hout.size(), 1) * 4, 0, -1))) return st;
+  if ((st = grow(b, b->centroid, std::max<size_t>(slots, 1) * 3 * sizeof(long long), 0, 0))) return st;
   if (slots) BCU(cudaMemcpyAsync(b->desc.p, descs.data(), slots * sizeof(GraphDesc), cudaMemcpyHostToDevice, b->stream));
   if (!tiles.empty())
     BCU(cudaMemcpyAsync(b->tiles.p, tiles.data(), tiles.size() * sizeof(uint2), cudaMemcpyHostToDevice, b->stream));
@@ -332,6 +364,373 @@ void release(cgl_batch* b, Job& j) {
   b->rows.release(j.rp_out, j.n + 1);
   b->ents.release(j.e_in, j.m_in);
   b->ents.release(j.e_out, j.m_out);
+  b->colls.release(j.coll_off, j.coll_cells);
+}
+
+// ---------------------------------------------------------------- ingest --
+// A job's ingest in two steps.  prepare_job is host work only (no CUDA call,
+// nothing shared): positions and their rescale, the random draws (the
+// reference's stream is sequential per job), the host link lists of small
+// jobs, point sizes and collision grid.  Many jobs prepare on many host
+// threads at once (cgl_batch_add_many).  commit_job then takes the arena
+// ranges and uploads, in job order on the batch's stream.
+struct HostJob {
+  Job j;
+  cgl_status status = CGL_OK;
+  std::string err;
+  double space = 0;
+  FixedScale fx{};
+  std::vector<float2> pos;
+  std::vector<uint8_t> absent;
+  bool dev_jitter = false;     // counter stream: the device draws the jitter
+  uint64_t jitter_base = 0;
+  std::vector<float2> jit;
+  const float* links = nullptr;   // the caller's array (read again at commit)
+  bool has_links = false;
+  bool dev_links = false;      // the device builds the link lists (commit may fall back)
+  uint32_t m = 0;              // valid links
+  ingest::Rng rng_links;       // the stream where the link draws start
+  std::vector<float> draws;    // reference stream, device build: 2m rest-length draws
+  ingest::Csr cin, cout_;      // host build
+  std::vector<float> sizes;    // collision: resolved point sizes
+};
+
+cgl_status prep_fail(HostJob& h, cgl_status st, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  h.err = buf;
+  h.status = st;
+  return st;
+}
+
+cgl_status prepare_job(const cgl_batch_job& in, HostJob& h) {
+  const cgl_config* cfg = in.cfg;
+  if (!cfg || (!in.xy && in.n_floats) || (!in.links && in.n_link_floats) || (!in.sizes && in.n_sizes))
+    return prep_fail(h, CGL_INVALID_ARG, "null array");
+  if (!cfg->enable_simulation) return prep_fail(h, CGL_INVALID_ARG, "enableSimulation is off");
+  Job& j = h.j;
+  j.used = true;
+  j.cfg = *cfg;
+  j.cfg.random_seed_text = nullptr;   // the seed is used here only
+  j.n = in.n_floats / 2;
+  j.E = in.n_link_floats / 2;
+  if (j.n == 0) return prep_fail(h, CGL_INVALID_ARG, "a job needs points");
+  if (j.n > (1ull << 24)) return prep_fail(h, CGL_INVALID_ARG, "%llu points exceed 2^24", (unsigned long long)j.n);
+  const uint32_t mask = cfg->stage_mask;
+  ingest::seed_rng(*cfg, j.rng);
+  h.space = ingest::adjusted_space(*cfg);
+  // Points.updatePositions (Points/index.ts:390-413), as cgl_render for a fresh engine
+  if (ingest::should_rescale(*cfg, false)) {
+    std::vector<float> scaled(in.xy, in.xy + 2 * j.n);
+    ingest::rescale_positions(scaled.data(), j.n, cfg->space_size);
+    j.live = ingest::canonical_positions(scaled.data(), j.n, h.pos, h.absent);
+  } else {
+    j.live = ingest::canonical_positions(in.xy, j.n, h.pos, h.absent);
+  }
+  int fbits = 0;
+  h.fx = ingest::fixed_for(j.n, h.space, &fbits);
+  const ingest::Grid grid = ingest::grid_for(j.n);
+  j.gf = grid.gf;
+  j.levels = grid.levels;
+  j.tile = std::min(16, j.gf);
+  // the jitter draws come first (ForceManyBody.create), then the link draws
+  const uint64_t T = (uint64_t)std::ceil(std::sqrt((double)j.n));
+  h.dev_jitter = j.rng.counter && !(cfg->device_ingest_min_links > (double)j.n);
+  h.jitter_base = j.rng.ctr;
+  if (h.dev_jitter) j.rng.ctr += 2 * T * T;
+  else ingest::jitter(j.rng, j.n, h.jit);
+  h.links = in.links;
+  h.has_links = j.E > 0;
+  h.dev_links = h.has_links && j.E < 0xFFFFFFF0ull && !(cfg->device_ingest_min_links > (double)j.E);
+  h.rng_links = j.rng;
+  if (h.dev_links) {
+    // GraphData.isPointIndex of both ends (GraphData/index.ts:286-289): one draw per list entry
+    uint64_t m = 0;
+    for (uint64_t i = 0; i < j.E; ++i)
+      m += ingest::is_point_index(in.links[2 * i], j.n) && ingest::is_point_index(in.links[2 * i + 1], j.n);
+    h.m = (uint32_t)m;
+    if (!j.rng.counter && m) {
+      h.draws.resize(2 * (size_t)m);
+      j.rng.fill_unit_f32(h.draws.data(), 2 * m);
+    } else {
+      j.rng.ctr += 2 * m;
+    }
+    j.m_in = j.m_out = m;
+  } else {
+    if (h.has_links) ingest::build_links(in.links, j.E, j.n, nullptr, h.absent, j.rng, h.cin, h.cout_);
+    else { h.cin.rowptr.assign(j.n + 1, 0); h.cout_.rowptr.assign(j.n + 1, 0); }
+    j.m_in = h.cin.ent.size();
+    j.m_out = h.cout_.ent.size();
+    j.heavy_in = h.cin.heavy;
+    j.heavy_out = h.cout_.heavy;
+  }
+  j.stages = 0;
+  if (cfg->simulation_gravity != 0 && (mask & CGL_STAGE_GRAVITY)) j.stages |= kGGravity;
+  if (cfg->simulation_center != 0 && (mask & CGL_STAGE_CENTER)) j.stages |= kGCenter;
+  if (mask & CGL_STAGE_MANYBODY) j.stages |= kGManybody;
+  if (h.has_links && (mask & CGL_STAGE_LINK_IN)) j.stages |= kGLinkIn;
+  if (h.has_links && (mask & CGL_STAGE_LINK_OUT)) j.stages |= kGLinkOut;
+  if (cfg->simulation_collision != 0 && (mask & CGL_STAGE_COLLISION)) j.stages |= kGCollision;
+  j.decay_factor = 1 - std::pow(kAlphaMin, 1 / cfg->simulation_decay);
+  j.max_ticks = in.max_ticks;
+  j.stop_below_min = in.stop_below_alpha_min != 0;
+  j.cells = (uint64_t)j.gf * j.gf;
+  j.recs = ingest::level_base(j.levels);
+  int lv_tile = j.levels - 1;
+  for (int g = j.tile; g > 1 && lv_tile > 0; g >>= 1) --lv_tile;
+  j.accs = ingest::level_base(lv_tile);
+  GraphDesc& D = j.desc;
+  std::memset(&D, 0, sizeof(D));
+  if (j.stages & kGCollision) {
+    // GraphData.getResolvedPointSize (GraphData/index.ts:189-194) and
+    // ForceCollision.create (ForceCollision/index.ts:61-95)
+    const bool has = in.sizes != nullptr;
+    h.sizes.resize(j.n);
+    double max_size = cfg->point_default_size;
+    for (uint64_t i = 0; i < j.n; ++i) {
+      float r = NAN;
+      if (has && i < in.n_sizes) r = in.sizes[i];
+      if (std::isnan(r)) r = h.absent[i] ? 0.f : (float)cfg->point_default_size;
+      h.sizes[i] = r;
+      if (has) max_size = std::max(max_size, (double)r);
+    }
+    const double cr = std::isnan(cfg->simulation_collision_radius) ? 0 : cfg->simulation_collision_radius;
+    const double eff = (cr > 0 ? cr : max_size * 0.5) + cfg->simulation_collision_padding;
+    const double cell = std::max(eff * 2, 8.0);
+    const int cgrid = (int)std::min(512.0, std::max(1.0, std::floor(h.space / cell)));
+    D.coll_grid = cgrid;
+    D.coll_cell = (float)(h.space / cgrid);
+    D.coll_strength = (float)cfg->simulation_collision;
+    D.coll_radius = (float)cr;
+    D.coll_padding = (float)cfg->simulation_collision_padding;
+    j.coll_cells = 4ull * (uint64_t)cgrid * (uint64_t)cgrid;
+  }
+  return CGL_OK;
+}
+
+cgl_status commit_job(cgl_batch* b, HostJob& h, uint32_t* id) {
+  Job& j = h.j;
+  const cgl_config* cfg = &j.cfg;
+  // link lists on the device when asked for and when its transient buffers fit the budget
+  Temp tmp{b};
+  bool dev_links = h.dev_links;
+  const uint64_t big = std::max<uint64_t>(j.E + 1, j.n + 1);
+  const size_t tmp_words = std::max(dingest::sort_temp_words(big), dingest::scan_temp_words(big));
+  if (dev_links && b->budget > 0 &&
+      (double)b->dev_bytes + 8.0 * j.E + 4.0 * (j.E + 1) + 8.0 * (j.n + 1) + 16.0 * big + 4.0 * tmp_words +
+              4.0 * h.draws.size() > b->budget)
+    dev_links = false;
+  float2* d_links = nullptr;
+  float* d_draws = nullptr;
+  uint32_t *d_valid = nullptr, *d_len_in = nullptr, *d_len_out = nullptr, *d_tmp = nullptr, *d_stats = nullptr;
+  uint32_t *d_kin = nullptr, *d_kout = nullptr, *d_vin = nullptr, *d_vout = nullptr;
+  if (dev_links) {
+    d_links = tmp.get<float2>(j.E);
+    d_valid = tmp.get<uint32_t>(j.E + 1);
+    d_len_in = tmp.get<uint32_t>(j.n + 1);
+    d_len_out = tmp.get<uint32_t>(j.n + 1);
+    d_tmp = tmp.get<uint32_t>(tmp_words);
+    d_stats = tmp.get<uint32_t>(4);
+    d_kin = tmp.get<uint32_t>(big);
+    d_kout = tmp.get<uint32_t>(big);
+    d_vin = tmp.get<uint32_t>(big);
+    d_vout = tmp.get<uint32_t>(big);
+    if (!h.draws.empty()) d_draws = tmp.get<float>(h.draws.size());
+    dev_links = d_links && d_valid && d_len_in && d_len_out && d_tmp && d_stats && d_kin && d_kout && d_vin &&
+                d_vout && (h.draws.empty() || d_draws);
+  }
+  if (h.dev_links && !dev_links) {
+    // the device build did not fit: the host build, from the same point of the
+    // stream (it draws the same 2m values prepare_job drew)
+    j.rng = h.rng_links;
+    ingest::build_links(h.links, j.E, j.n, nullptr, h.absent, j.rng, h.cin, h.cout_);
+    j.m_in = h.cin.ent.size();
+    j.m_out = h.cout_.ent.size();
+    j.heavy_in = h.cin.heavy;
+    j.heavy_out = h.cout_.heavy;
+  }
+  uint32_t dev_stats[4] = {0, 0, 0, 0};
+  if (dev_links) {
+    cudaStream_t s = b->stream;
+    const uint32_t E32 = (uint32_t)j.E, N32 = (uint32_t)j.n;
+    uint32_t dev_m = 0;
+    BCU(cudaMemcpyAsync(d_links, h.links, j.E * sizeof(float2), cudaMemcpyHostToDevice, s));
+    if (d_draws) BCU(cudaMemcpyAsync(d_draws, h.draws.data(), h.draws.size() * 4, cudaMemcpyHostToDevice, s));
+    BCU(cudaMemsetAsync(d_valid, 0, (j.E + 1) * 4, s));
+    BCU(cudaMemsetAsync(d_len_in, 0, (j.n + 1) * 4, s));
+    BCU(cudaMemsetAsync(d_len_out, 0, (j.n + 1) * 4, s));
+    BCU(cudaMemsetAsync(d_stats, 0, 16, s));
+    dingest::count_links(d_links, E32, N32, d_valid, d_len_in, d_len_out, s);
+    dingest::scan_exclusive(d_valid, E32 + 1, d_tmp, s);
+    dingest::len_stats(d_len_in, N32, d_stats, s);
+    dingest::len_stats(d_len_out, N32, d_stats + 2, s);
+    BCU(cudaMemcpyAsync(&dev_m, d_valid + j.E, 4, cudaMemcpyDeviceToHost, s));
+    BCU(cudaMemcpyAsync(dev_stats, d_stats, 16, cudaMemcpyDeviceToHost, s));
+    BCU(cudaStreamSynchronize(s));
+    if (dev_m != h.m) return bfail(b, CGL_CUDA_ERROR, "link count %u on the device, %u on the host", dev_m, h.m);
+  }
+  // arena ranges (grow the arenas when full)
+  cgl_status st;
+  auto take = [&](Arena& a, uint64_t n, uint64_t* off, int kind) -> cgl_status {
+    if (a.alloc(n, off)) return CGL_OK;
+    const uint64_t cap = grown(a.cap, a.hwm + n);
+    cgl_status s2 = CGL_OK;
+    if (kind == 0) s2 = reserve_points(b, cap);
+    else if (kind == 1) s2 = reserve_cells(b, cap);
+    else if (kind == 2) s2 = grow(b, b->rec, cap * sizeof(float4), a.hwm * sizeof(float4), 0);
+    else if (kind == 3) s2 = grow(b, b->acc, cap * 3 * sizeof(long long), a.hwm * 3 * sizeof(long long), 0);
+    else if (kind == 4) s2 = grow(b, b->rowptr, cap * 4, a.hwm * 4, -1);
+    else if (kind == 5) s2 = grow(b, b->ent, cap * sizeof(uint4), a.hwm * sizeof(uint4), -1);
+    else s2 = reserve_colls(b, cap);
+    if (s2) return s2;
+    if (kind >= 2 && kind <= 5) a.cap = cap;
+    b->dirty = true;
+    return a.alloc(n, off) ? CGL_OK : bfail(b, CGL_OOM, "arena allocation failed");
+  };
+  // Take every range; on a refusal give back exactly the ranges already taken.
+  struct Want { Arena* a; uint64_t n; uint64_t* off; int kind; };
+  const Want wants[] = {{&b->pts, j.n, &j.p_off, 0},        {&b->cells, j.cells, &j.cell_off, 1},
+                        {&b->recs, j.recs, &j.rec_off, 2},   {&b->accs, j.accs, &j.acc_off, 3},
+                        {&b->rows, j.n + 1, &j.rp_in, 4},    {&b->rows, j.n + 1, &j.rp_out, 4},
+                        {&b->ents, j.m_in, &j.e_in, 5},      {&b->ents, j.m_out, &j.e_out, 5},
+                        {&b->colls, j.coll_cells, &j.coll_off, 6}};
+  int taken = 0;
+  st = CGL_OK;
+  for (const Want& w : wants) {
+    if ((st = take(*w.a, w.n, w.off, w.kind))) break;
+    ++taken;
+  }
+  if (!st && (b->pts.hwm > 0xFFFFFF00ull || b->cells.hwm > 0xFFFFFF00ull || b->ents.hwm > 0xFFFFFF00ull ||
+              b->colls.hwm > 0xFFFFFF00ull))
+    st = bfail(b, CGL_OOM, "arena index space (32 bits) exhausted");
+  if (st) {
+    for (int k = 0; k < taken; ++k) wants[k].a->release(*wants[k].off, wants[k].n);
+    return st;
+  }
+  // From here on a CUDA error gives the job's arena ranges back before returning.
+  auto give_back = [&]() {
+    for (const Want& w : wants) w.a->release(*w.off, w.n);
+  };
+#define JCU(call)                                                                                    \
+  do {                                                                                               \
+    cudaError_t _e = (call);                                                                         \
+    if (_e != cudaSuccess) {                                                                         \
+      give_back();                                                                                   \
+      return bfail(b, _e == cudaErrorMemoryAllocation ? CGL_OOM : CGL_CUDA_ERROR, "%s: %s", #call,  \
+                   cudaGetErrorString(_e));                                                          \
+    }                                                                                                \
+  } while (0)
+  // upload: absolute indices for rows and neighbours
+  std::vector<uint32_t> rp_in, rp_out;
+  if (!dev_links) {
+    rp_in.resize(j.n + 1);
+    rp_out.resize(j.n + 1);
+    for (uint64_t i = 0; i <= j.n; ++i) {
+      rp_in[i] = (uint32_t)(j.e_in + h.cin.rowptr[i]);
+      rp_out[i] = (uint32_t)(j.e_out + h.cout_.rowptr[i]);
+    }
+    for (auto& e : h.cin.ent) if (e.x != kAbsentTarget) e.x += (uint32_t)j.p_off;
+    for (auto& e : h.cout_.ent) if (e.x != kAbsentTarget) e.x += (uint32_t)j.p_off;
+  }
+  std::vector<uint8_t> flags(j.n);
+  for (uint64_t i = 0; i < j.n; ++i) flags[i] = h.absent[i] ? kAbsent : 0;
+  const uint32_t g = [&]() {
+    for (uint32_t sl = 0; sl < b->jobs.size(); ++sl)
+      if (!b->jobs[sl].used) return sl;
+    b->jobs.emplace_back();
+    return (uint32_t)(b->jobs.size() - 1);
+  }();
+  std::vector<uint32_t> gids(j.n, g), cgids(j.cells, g);
+  cudaStream_t s = b->stream;
+  JCU(cudaMemcpyAsync((float2*)b->pos.p + j.p_off, h.pos.data(), j.n * 8, cudaMemcpyHostToDevice, s));
+  if (h.dev_jitter) dingest::jitter(j.rng.seed, h.jitter_base, (uint32_t)j.n, (float2*)b->jitter.p + j.p_off, s);
+  else JCU(cudaMemcpyAsync((float2*)b->jitter.p + j.p_off, h.jit.data(), j.n * 8, cudaMemcpyHostToDevice, s));
+  JCU(cudaMemcpyAsync((uint8_t*)b->flags.p + j.p_off, flags.data(), j.n, cudaMemcpyHostToDevice, s));
+  JCU(cudaMemcpyAsync((uint32_t*)b->gid.p + j.p_off, gids.data(), j.n * 4, cudaMemcpyHostToDevice, s));
+  JCU(cudaMemcpyAsync((uint32_t*)b->cell_gid.p + j.cell_off, cgids.data(), j.cells * 4, cudaMemcpyHostToDevice, s));
+  JCU(cudaMemsetAsync((uint32_t*)b->counts.p + j.cell_off, 0, j.cells * 4, s));
+  JCU(cudaMemsetAsync((long long*)b->acc.p + 3 * j.acc_off, 0, j.accs * 3 * sizeof(long long), s));
+  std::vector<uint32_t> coll_gids;
+  if (j.coll_cells) {
+    coll_gids.assign(j.coll_cells, g);
+    JCU(cudaMemcpyAsync((float*)b->size.p + j.p_off, h.sizes.data(), j.n * 4, cudaMemcpyHostToDevice, s));
+    JCU(cudaMemcpyAsync((uint32_t*)b->coll_gid.p + j.coll_off, coll_gids.data(), j.coll_cells * 4,
+                        cudaMemcpyHostToDevice, s));
+    JCU(cudaMemsetAsync((long long*)b->cgrid_acc.p + 4 * j.coll_off, 0, j.coll_cells * 32, s));
+  }
+  if (dev_links) {
+    // (row, link) pairs sorted by row, entries filled in place with arena
+    // indices; the flags of this job are already queued above
+    const uint32_t E32 = (uint32_t)j.E, N32 = (uint32_t)j.n, M = h.m;
+    const uint8_t* flags_j = (const uint8_t*)b->flags.p + j.p_off;
+    dingest::compact_links(d_links, E32, d_valid, d_kin, d_kout, d_vin, d_vout, s);
+    const int row_bits = dingest::key_bits(j.n - 1);
+    dingest::sort_pairs(d_kin, d_vin, M, row_bits, d_tmp, s);
+    dingest::sort_pairs(d_kout, d_vout, M, row_bits, d_tmp, s);
+    const uint64_t links_base = h.rng_links.ctr;
+    dingest::fill_csr(d_kin, d_vin, M, d_links, true, d_len_in, d_len_out, nullptr, flags_j, d_draws, j.rng.seed,
+                      links_base, (uint32_t)j.p_off, (uint4*)b->ent.p + j.e_in, s);
+    dingest::fill_csr(d_kout, d_vout, M, d_links, false, d_len_in, d_len_out, nullptr, flags_j,
+                      d_draws ? d_draws + M : nullptr, j.rng.seed, links_base + M, (uint32_t)j.p_off,
+                      (uint4*)b->ent.p + j.e_out, s);
+    // the long lists (rows by length, longest first; the first stats[1] / stats[3])
+    j.heavy_in.resize(dev_stats[1]);
+    j.heavy_out.resize(dev_stats[3]);
+    for (int dir = 0; dir < 2; ++dir) {
+      std::vector<uint32_t>& hv = dir == 0 ? j.heavy_in : j.heavy_out;
+      if (hv.empty()) continue;
+      dingest::len_keys(dir == 0 ? d_len_in : d_len_out, N32, d_stats + 2 * dir, d_kin, d_vin, s);
+      dingest::sort_pairs(d_kin, d_vin, N32, dingest::key_bits(dev_stats[2 * dir]), d_tmp, s);
+      JCU(cudaMemcpyAsync(hv.data(), d_vin, hv.size() * 4, cudaMemcpyDeviceToHost, s));
+    }
+    // row pointers: exclusive scan of the lengths, offset by the entry range
+    dingest::scan_exclusive(d_len_in, N32 + 1, d_tmp, s);
+    dingest::copy_u32(d_len_in, (uint32_t*)b->rowptr.p + j.rp_in, N32 + 1, s, (uint32_t)j.e_in);
+    dingest::scan_exclusive(d_len_out, N32 + 1, d_tmp, s);
+    dingest::copy_u32(d_len_out, (uint32_t*)b->rowptr.p + j.rp_out, N32 + 1, s, (uint32_t)j.e_out);
+    JCU(cudaGetLastError());
+  } else {
+    JCU(cudaMemcpyAsync((uint32_t*)b->rowptr.p + j.rp_in, rp_in.data(), (j.n + 1) * 4, cudaMemcpyHostToDevice, s));
+    JCU(cudaMemcpyAsync((uint32_t*)b->rowptr.p + j.rp_out, rp_out.data(), (j.n + 1) * 4, cudaMemcpyHostToDevice, s));
+    if (j.m_in)
+      JCU(cudaMemcpyAsync((uint4*)b->ent.p + j.e_in, h.cin.ent.data(), j.m_in * 16, cudaMemcpyHostToDevice, s));
+    if (j.m_out)
+      JCU(cudaMemcpyAsync((uint4*)b->ent.p + j.e_out, h.cout_.ent.data(), j.m_out * 16, cudaMemcpyHostToDevice, s));
+  }
+  JCU(cudaStreamSynchronize(s));
+#undef JCU
+  GraphDesc& D = j.desc;
+  D.p_off = (uint32_t)j.p_off;
+  D.n = (uint32_t)j.n;
+  D.cell_off = (uint32_t)j.cell_off;
+  D.rec_off = (uint32_t)j.rec_off;
+  D.acc_off = (uint32_t)j.acc_off;
+  D.acc_cells = (uint32_t)j.accs;
+  D.rp_in = (uint32_t)j.rp_in;
+  D.rp_out = (uint32_t)j.rp_out;
+  D.gf = j.gf;
+  D.levels = j.levels;
+  D.tile = j.tile;
+  D.stages = j.stages;
+  D.space = (float)h.space;
+  D.csf = (float)(h.space / j.gf);
+  D.friction = (float)cfg->simulation_friction;
+  D.gravity = (float)cfg->simulation_gravity;
+  D.repulsion = (float)cfg->simulation_repulsion;
+  D.link_spring = (float)cfg->simulation_link_spring;
+  D.link_distance = (float)cfg->simulation_link_distance;
+  D.link_r0 = (float)cfg->simulation_link_dist_random_variation_range[0];
+  D.link_r1 = (float)cfg->simulation_link_dist_random_variation_range[1];
+  D.fx = h.fx;
+  D.center = (float)cfg->simulation_center;
+  D.coll_off = (uint32_t)j.coll_off;
+  b->jobs[g] = std::move(j);
+  b->dirty = true;
+  *id = g;
+  return CGL_OK;
 }
 
 }  // namespace
@@ -376,7 +775,8 @@ cgl_status cgl_batch_destroy(cgl_batch* b) {
   Buf* all[] = {&b->gid, &b->pos, &b->pos_alt, &b->flags, &b->jitter, &b->key, &b->rank, &b->sorted_idx,
                 &b->sorted_pos, &b->counts, &b->cell_start, &b->cell_gid, &b->big_list, &b->big_sx, &b->big_sy,
                 &b->big_ns, &b->scan1, &b->scan2, &b->big_count, &b->tick_ctr, &b->rec, &b->acc, &b->rowptr,
-                &b->ent, &b->desc, &b->tiles, &b->heavy_in, &b->heavy_out, &b->ticks};
+                &b->ent, &b->desc, &b->tiles, &b->heavy_in, &b->heavy_out, &b->ticks, &b->size, &b->cgrid_acc,
+                &b->cgrid, &b->coll_gid, &b->centroid};
   for (Buf* x : all)
     if (x->p) cudaFree(x->p);
   if (b->h_ticks) cudaFreeHost(b->h_ticks);
@@ -398,269 +798,81 @@ cgl_status cgl_batch_add(cgl_batch* b, const cgl_config* cfg, const float* xy, u
   if (!b || !cfg || !id || (!xy && n_floats) || (!links && n_link_floats)) return CGL_INVALID_ARG;
   b->err.clear();
   if (cudaSetDevice(b->device) != cudaSuccess) return bfail(b, CGL_CUDA_ERROR, "cudaSetDevice");
-  const uint32_t mask = cfg->stage_mask;
-  if ((cfg->simulation_center != 0 && (mask & CGL_STAGE_CENTER)) ||
-      (cfg->simulation_collision != 0 && (mask & CGL_STAGE_COLLISION)))
-    return bfail(b, CGL_INVALID_ARG, "batched jobs run gravity, many-body and link forces; center and collision need a plain engine");
-  if (!cfg->enable_simulation) return bfail(b, CGL_INVALID_ARG, "enableSimulation is off");
-  Job j;
-  j.used = true;
-  j.cfg = *cfg;
-  j.n = n_floats / 2;
-  j.E = n_link_floats / 2;
-  if (j.n == 0) return bfail(b, CGL_INVALID_ARG, "a job needs points");
-  if (j.n > (1ull << 24)) return bfail(b, CGL_INVALID_ARG, "%llu points exceed 2^24", (unsigned long long)j.n);
-  ingest::seed_rng(*cfg, j.rng);
-  j.cfg.random_seed_text = nullptr;   // the seed is used here only
-  const double space = ingest::adjusted_space(*cfg);
-  // ingest exactly as cgl_render does for a fresh plain engine
-  std::vector<float2> pos;
-  std::vector<uint8_t> absent;
-  if (ingest::should_rescale(*cfg, false)) {
-    std::vector<float> scaled(xy, xy + 2 * j.n);
-    ingest::rescale_positions(scaled.data(), j.n, cfg->space_size);
-    j.live = ingest::canonical_positions(scaled.data(), j.n, pos, absent);
-  } else {
-    j.live = ingest::canonical_positions(xy, j.n, pos, absent);
-  }
-  int fbits = 0;
-  const FixedScale fx = ingest::fixed_for(j.n, space, &fbits);
-  const ingest::Grid grid = ingest::grid_for(j.n);
-  j.gf = grid.gf;
-  j.levels = grid.levels;
-  j.tile = std::min(16, j.gf);
-  // the jitter draws come first (ForceManyBody.create), then the link draws
-  const uint64_t T = (uint64_t)std::ceil(std::sqrt((double)j.n));
-  const bool dev_jitter = j.rng.counter && !(cfg->device_ingest_min_links > (double)j.n);
-  const uint64_t jitter_base = j.rng.ctr;
-  std::vector<float2> jit;
-  if (dev_jitter) j.rng.ctr += 2 * T * T;
-  else ingest::jitter(j.rng, j.n, jit);
-  ingest::Csr cin, cout_;
-  const bool has_links = j.E > 0;
-  // link lists on the device when asked for and when its transient buffers fit
-  // the budget (ingest_device.cu; the same lists as ingest::build_links)
-  Temp tmp{b};
-  bool dev_links = has_links && j.E < 0xFFFFFFF0ull && !(cfg->device_ingest_min_links > (double)j.E);
-  const uint64_t big = std::max<uint64_t>(j.E + 1, j.n + 1);
-  const size_t tmp_words = std::max(dingest::sort_temp_words(big), dingest::scan_temp_words(big));
-  const double draw_bytes = j.rng.counter ? 0.0 : 8.0 * j.E;   // host draws of the reference's stream
-  if (dev_links && b->budget > 0 &&
-      (double)b->dev_bytes + 8.0 * j.E + 4.0 * (j.E + 1) + 8.0 * (j.n + 1) + 16.0 * big + 4.0 * tmp_words + draw_bytes >
-          b->budget)
-    dev_links = false;
-  float2* d_links = nullptr;
-  uint32_t *d_valid = nullptr, *d_len_in = nullptr, *d_len_out = nullptr, *d_tmp = nullptr, *d_stats = nullptr;
-  uint32_t *d_kin = nullptr, *d_kout = nullptr, *d_vin = nullptr, *d_vout = nullptr;
-  uint32_t dev_m = 0, dev_stats[4] = {0, 0, 0, 0};
-  float* d_draws = nullptr;
-  const uint64_t links_base = j.rng.ctr;
-  if (dev_links) {
-    d_links = tmp.get<float2>(j.E);
-    d_valid = tmp.get<uint32_t>(j.E + 1);
-    d_len_in = tmp.get<uint32_t>(j.n + 1);
-    d_len_out = tmp.get<uint32_t>(j.n + 1);
-    d_tmp = tmp.get<uint32_t>(tmp_words);
-    d_stats = tmp.get<uint32_t>(4);
-    d_kin = tmp.get<uint32_t>(big);
-    d_kout = tmp.get<uint32_t>(big);
-    d_vin = tmp.get<uint32_t>(big);
-    d_vout = tmp.get<uint32_t>(big);
-    dev_links = d_links && d_valid && d_len_in && d_len_out && d_tmp && d_stats && d_kin && d_kout && d_vin && d_vout;
-  }
-  if (dev_links) {
-    cudaStream_t s = b->stream;
-    const uint32_t E32 = (uint32_t)j.E, N32 = (uint32_t)j.n;
-    BCU(cudaMemcpyAsync(d_links, links, j.E * sizeof(float2), cudaMemcpyHostToDevice, s));
-    BCU(cudaMemsetAsync(d_valid, 0, (j.E + 1) * 4, s));
-    BCU(cudaMemsetAsync(d_len_in, 0, (j.n + 1) * 4, s));
-    BCU(cudaMemsetAsync(d_len_out, 0, (j.n + 1) * 4, s));
-    BCU(cudaMemsetAsync(d_stats, 0, 16, s));
-    dingest::count_links(d_links, E32, N32, d_valid, d_len_in, d_len_out, s);
-    dingest::scan_exclusive(d_valid, E32 + 1, d_tmp, s);
-    dingest::len_stats(d_len_in, N32, d_stats, s);
-    dingest::len_stats(d_len_out, N32, d_stats + 2, s);
-    BCU(cudaMemcpyAsync(&dev_m, d_valid + j.E, 4, cudaMemcpyDeviceToHost, s));
-    BCU(cudaMemcpyAsync(dev_stats, d_stats, 16, cudaMemcpyDeviceToHost, s));
-    BCU(cudaStreamSynchronize(s));
-    j.m_in = j.m_out = dev_m;
-    if (!j.rng.counter && dev_m) {
-      // the reference's stream is sequential: both directions' draws on the host
-      std::vector<float> h_draws(2 * (size_t)dev_m);
-      j.rng.fill_unit_f32(h_draws.data(), 2 * (uint64_t)dev_m);
-      d_draws = tmp.get<float>(2 * (size_t)dev_m);
-      if (!d_draws) return bfail(b, CGL_OOM, "link draw buffer");
-      BCU(cudaMemcpyAsync(d_draws, h_draws.data(), 2 * (size_t)dev_m * sizeof(float), cudaMemcpyHostToDevice, s));
-      BCU(cudaStreamSynchronize(s));
-    } else {
-      j.rng.ctr += 2 * (uint64_t)dev_m;
-    }
-  } else {
-    if (has_links) ingest::build_links(links, j.E, j.n, nullptr, absent, j.rng, cin, cout_);
-    else { cin.rowptr.assign(j.n + 1, 0); cout_.rowptr.assign(j.n + 1, 0); }
-    j.m_in = cin.ent.size();
-    j.m_out = cout_.ent.size();
-    j.heavy_in = cin.heavy;
-    j.heavy_out = cout_.heavy;
-  }
-  j.stages = 0;
-  if (cfg->simulation_gravity != 0 && (mask & CGL_STAGE_GRAVITY)) j.stages |= kGGravity;
-  if (mask & CGL_STAGE_MANYBODY) j.stages |= kGManybody;
-  if (has_links && (mask & CGL_STAGE_LINK_IN)) j.stages |= kGLinkIn;
-  if (has_links && (mask & CGL_STAGE_LINK_OUT)) j.stages |= kGLinkOut;
-  j.decay_factor = 1 - std::pow(kAlphaMin, 1 / cfg->simulation_decay);
-  j.max_ticks = max_ticks;
-  j.stop_below_min = stop_below_alpha_min != 0;
-  j.cells = (uint64_t)j.gf * j.gf;
-  j.recs = ingest::level_base(j.levels);
-  int lv_tile = j.levels - 1;
-  for (int g = j.tile; g > 1 && lv_tile > 0; g >>= 1) --lv_tile;
-  j.accs = ingest::level_base(lv_tile);
-  // arena ranges (grow the arenas when full)
-  cgl_status st;
-  auto take = [&](Arena& a, uint64_t n, uint64_t* off, int kind) -> cgl_status {
-    if (a.alloc(n, off)) return CGL_OK;
-    const uint64_t cap = grown(a.cap, a.hwm + n);
-    cgl_status s2 = CGL_OK;
-    if (kind == 0) s2 = reserve_points(b, cap);
-    else if (kind == 1) s2 = reserve_cells(b, cap);
-    else if (kind == 2) s2 = grow(b, b->rec, cap * sizeof(float4), a.hwm * sizeof(float4), 0);
-    else if (kind == 3) s2 = grow(b, b->acc, cap * 3 * sizeof(long long), a.hwm * 3 * sizeof(long long), 0);
-    else if (kind == 4) s2 = grow(b, b->rowptr, cap * 4, a.hwm * 4, -1);
-    else s2 = grow(b, b->ent, cap * sizeof(uint4), a.hwm * sizeof(uint4), -1);
-    if (s2) return s2;
-    if (kind >= 2) a.cap = cap;
-    b->dirty = true;
-    return a.alloc(n, off) ? CGL_OK : bfail(b, CGL_OOM, "arena allocation failed");
-  };
-  // Take every range; on a refusal give back exactly the ranges already taken.
-  struct Want { Arena* a; uint64_t n; uint64_t* off; int kind; };
-  const Want wants[] = {{&b->pts, j.n, &j.p_off, 0},        {&b->cells, j.cells, &j.cell_off, 1},
-                        {&b->recs, j.recs, &j.rec_off, 2},   {&b->accs, j.accs, &j.acc_off, 3},
-                        {&b->rows, j.n + 1, &j.rp_in, 4},    {&b->rows, j.n + 1, &j.rp_out, 4},
-                        {&b->ents, j.m_in, &j.e_in, 5},      {&b->ents, j.m_out, &j.e_out, 5}};
-  int taken = 0;
-  st = CGL_OK;
-  for (const Want& w : wants) {
-    if ((st = take(*w.a, w.n, w.off, w.kind))) break;
-    ++taken;
-  }
-  if (!st && (b->pts.hwm > 0xFFFFFF00ull || b->cells.hwm > 0xFFFFFF00ull || b->ents.hwm > 0xFFFFFF00ull))
-    st = bfail(b, CGL_OOM, "arena index space (32 bits) exhausted");
-  if (st) {
-    for (int k = 0; k < taken; ++k) wants[k].a->release(*wants[k].off, wants[k].n);
-    return st;
-  }
-  // From here on a CUDA error gives the job's arena ranges back before returning.
-  auto give_back = [&]() {
-    for (const Want& w : wants) w.a->release(*w.off, w.n);
-  };
-#define JCU(call)                                                                                    \
-  do {                                                                                               \
-    cudaError_t _e = (call);                                                                         \
-    if (_e != cudaSuccess) {                                                                         \
-      give_back();                                                                                   \
-      return bfail(b, _e == cudaErrorMemoryAllocation ? CGL_OOM : CGL_CUDA_ERROR, "%s: %s", #call,  \
-                   cudaGetErrorString(_e));                                                          \
-    }                                                                                                \
-  } while (0)
-  // upload: absolute indices for rows and neighbours
-  std::vector<uint32_t> rp_in, rp_out;
-  if (!dev_links) {
-    rp_in.resize(j.n + 1);
-    rp_out.resize(j.n + 1);
-    for (uint64_t i = 0; i <= j.n; ++i) {
-      rp_in[i] = (uint32_t)(j.e_in + cin.rowptr[i]);
-      rp_out[i] = (uint32_t)(j.e_out + cout_.rowptr[i]);
-    }
-    for (auto& e : cin.ent) if (e.x != kAbsentTarget) e.x += (uint32_t)j.p_off;
-    for (auto& e : cout_.ent) if (e.x != kAbsentTarget) e.x += (uint32_t)j.p_off;
-  }
-  std::vector<uint8_t> flags(j.n);
-  for (uint64_t i = 0; i < j.n; ++i) flags[i] = absent[i] ? kAbsent : 0;
-  const uint32_t g = [&]() {
-    for (uint32_t s = 0; s < b->jobs.size(); ++s)
-      if (!b->jobs[s].used) return s;
-    b->jobs.emplace_back();
-    return (uint32_t)(b->jobs.size() - 1);
-  }();
-  std::vector<uint32_t> gids(j.n, g), cgids(j.cells, g);
-  cudaStream_t s = b->stream;
-  JCU(cudaMemcpyAsync((float2*)b->pos.p + j.p_off, pos.data(), j.n * 8, cudaMemcpyHostToDevice, s));
-  if (dev_jitter) dingest::jitter(j.rng.seed, jitter_base, (uint32_t)j.n, (float2*)b->jitter.p + j.p_off, s);
-  else JCU(cudaMemcpyAsync((float2*)b->jitter.p + j.p_off, jit.data(), j.n * 8, cudaMemcpyHostToDevice, s));
-  JCU(cudaMemcpyAsync((uint8_t*)b->flags.p + j.p_off, flags.data(), j.n, cudaMemcpyHostToDevice, s));
-  JCU(cudaMemcpyAsync((uint32_t*)b->gid.p + j.p_off, gids.data(), j.n * 4, cudaMemcpyHostToDevice, s));
-  JCU(cudaMemcpyAsync((uint32_t*)b->cell_gid.p + j.cell_off, cgids.data(), j.cells * 4, cudaMemcpyHostToDevice, s));
-  JCU(cudaMemsetAsync((uint32_t*)b->counts.p + j.cell_off, 0, j.cells * 4, s));
-  JCU(cudaMemsetAsync((long long*)b->acc.p + 3 * j.acc_off, 0, j.accs * 3 * sizeof(long long), s));
-  if (dev_links) {
-    // (row, link) pairs sorted by row, entries filled in place with arena
-    // indices; the flags of this job are already queued above
-    const uint32_t E32 = (uint32_t)j.E, N32 = (uint32_t)j.n, M = dev_m;
-    const uint8_t* flags_j = (const uint8_t*)b->flags.p + j.p_off;
-    dingest::compact_links(d_links, E32, d_valid, d_kin, d_kout, d_vin, d_vout, s);
-    const int row_bits = dingest::key_bits(j.n - 1);
-    dingest::sort_pairs(d_kin, d_vin, M, row_bits, d_tmp, s);
-    dingest::sort_pairs(d_kout, d_vout, M, row_bits, d_tmp, s);
-    dingest::fill_csr(d_kin, d_vin, M, d_links, true, d_len_in, d_len_out, nullptr, flags_j, d_draws, j.rng.seed,
-                      links_base, (uint32_t)j.p_off, (uint4*)b->ent.p + j.e_in, s);
-    dingest::fill_csr(d_kout, d_vout, M, d_links, false, d_len_in, d_len_out, nullptr, flags_j,
-                      d_draws ? d_draws + M : nullptr, j.rng.seed, links_base + M, (uint32_t)j.p_off,
-                      (uint4*)b->ent.p + j.e_out, s);
-    // the long lists (rows by length, longest first; the first stats[1] / stats[3])
-    j.heavy_in.resize(dev_stats[1]);
-    j.heavy_out.resize(dev_stats[3]);
-    for (int dir = 0; dir < 2; ++dir) {
-      std::vector<uint32_t>& hv = dir == 0 ? j.heavy_in : j.heavy_out;
-      if (hv.empty()) continue;
-      dingest::len_keys(dir == 0 ? d_len_in : d_len_out, N32, d_stats + 2 * dir, d_kin, d_vin, s);
-      dingest::sort_pairs(d_kin, d_vin, N32, dingest::key_bits(dev_stats[2 * dir]), d_tmp, s);
-      JCU(cudaMemcpyAsync(hv.data(), d_vin, hv.size() * 4, cudaMemcpyDeviceToHost, s));
-    }
-    // row pointers: exclusive scan of the lengths, offset by the entry range
-    dingest::scan_exclusive(d_len_in, N32 + 1, d_tmp, s);
-    dingest::copy_u32(d_len_in, (uint32_t*)b->rowptr.p + j.rp_in, N32 + 1, s, (uint32_t)j.e_in);
-    dingest::scan_exclusive(d_len_out, N32 + 1, d_tmp, s);
-    dingest::copy_u32(d_len_out, (uint32_t*)b->rowptr.p + j.rp_out, N32 + 1, s, (uint32_t)j.e_out);
-    JCU(cudaGetLastError());
-  } else {
-    JCU(cudaMemcpyAsync((uint32_t*)b->rowptr.p + j.rp_in, rp_in.data(), (j.n + 1) * 4, cudaMemcpyHostToDevice, s));
-    JCU(cudaMemcpyAsync((uint32_t*)b->rowptr.p + j.rp_out, rp_out.data(), (j.n + 1) * 4, cudaMemcpyHostToDevice, s));
-    if (j.m_in) JCU(cudaMemcpyAsync((uint4*)b->ent.p + j.e_in, cin.ent.data(), j.m_in * 16, cudaMemcpyHostToDevice, s));
-    if (j.m_out)
-      JCU(cudaMemcpyAsync((uint4*)b->ent.p + j.e_out, cout_.ent.data(), j.m_out * 16, cudaMemcpyHostToDevice, s));
-  }
-  JCU(cudaStreamSynchronize(s));
-#undef JCU
-  GraphDesc& D = j.desc;
-  D.p_off = (uint32_t)j.p_off;
-  D.n = (uint32_t)j.n;
-  D.cell_off = (uint32_t)j.cell_off;
-  D.rec_off = (uint32_t)j.rec_off;
-  D.acc_off = (uint32_t)j.acc_off;
-  D.acc_cells = (uint32_t)j.accs;
-  D.rp_in = (uint32_t)j.rp_in;
-  D.rp_out = (uint32_t)j.rp_out;
-  D.gf = j.gf;
-  D.levels = j.levels;
-  D.tile = j.tile;
-  D.stages = j.stages;
-  D.space = (float)space;
-  D.csf = (float)(space / j.gf);
-  D.friction = (float)cfg->simulation_friction;
-  D.gravity = (float)cfg->simulation_gravity;
-  D.repulsion = (float)cfg->simulation_repulsion;
-  D.link_spring = (float)cfg->simulation_link_spring;
-  D.link_distance = (float)cfg->simulation_link_distance;
-  D.link_r0 = (float)cfg->simulation_link_dist_random_variation_range[0];
-  D.link_r1 = (float)cfg->simulation_link_dist_random_variation_range[1];
-  D.fx = fx;
-  b->jobs[g] = std::move(j);
-  b->dirty = true;
-  *id = g;
-  return CGL_OK;
+  cgl_batch_job in{};
+  in.cfg = cfg;
+  in.xy = xy;
+  in.n_floats = n_floats;
+  in.links = links;
+  in.n_link_floats = n_link_floats;
+  in.max_ticks = max_ticks;
+  in.stop_below_alpha_min = stop_below_alpha_min;
+  HostJob h;
+  if (prepare_job(in, h)) return bfail(b, h.status, "%s", h.err.c_str());
+  return commit_job(b, h, id);
 }
+
+cgl_status cgl_batch_add_many(cgl_batch* b, uint32_t count, const cgl_batch_job* jobs, uint32_t* ids,
+                              uint32_t threads, uint32_t* added) {
+  if (added) *added = 0;
+  if (!b || (!jobs && count) || (!ids && count)) return CGL_INVALID_ARG;
+  b->err.clear();
+  if (cudaSetDevice(b->device) != cudaSuccess) return bfail(b, CGL_CUDA_ERROR, "cudaSetDevice");
+  if (count == 0) return CGL_OK;
+  unsigned nt = threads ? threads : std::max(1u, std::thread::hardware_concurrency());
+  nt = std::min<unsigned>(nt, count);
+  // Prepare in a sliding window of jobs (bounded host memory) on nt threads,
+  // commit in job order as each becomes ready.
+  const uint32_t window = std::max<uint32_t>(4 * nt, 16);
+  std::vector<std::unique_ptr<HostJob>> ready(count);
+  std::vector<std::atomic<bool>> done(count);
+  for (auto& d : done) d.store(false);
+  std::atomic<uint32_t> next{0};
+  std::atomic<uint32_t> committed{0};
+  std::atomic<bool> stop{false};
+  std::mutex mu;
+  std::condition_variable cv;
+  auto worker = [&]() {
+    for (;;) {
+      uint32_t k = next.fetch_add(1);
+      if (k >= count || stop.load()) return;
+      {   // stay within the window ahead of the commits
+        std::unique_lock<std::mutex> lock(mu);
+        cv.wait(lock, [&] { return k < committed.load() + window || stop.load(); });
+      }
+      if (stop.load()) return;
+      auto h = std::make_unique<HostJob>();
+      prepare_job(jobs[k], *h);
+      {
+        std::lock_guard<std::mutex> lock(mu);
+        ready[k] = std::move(h);
+        done[k].store(true);
+      }
+      cv.notify_all();
+    }
+  };
+  std::vector<std::thread> pool;
+  for (unsigned t = 0; t < nt; ++t) pool.emplace_back(worker);
+  cgl_status st = CGL_OK;
+  for (uint32_t k = 0; k < count; ++k) {
+    std::unique_ptr<HostJob> h;
+    {
+      std::unique_lock<std::mutex> lock(mu);
+      cv.wait(lock, [&] { return done[k].load(); });
+      h = std::move(ready[k]);
+    }
+    if (h->status) st = bfail(b, h->status, "job %u: %s", k, h->err.c_str());
+    else st = commit_job(b, *h, &ids[k]);
+    if (st) break;
+    committed.store(k + 1);
+    if (added) *added = k + 1;
+    cv.notify_all();
+  }
+  stop.store(true);
+  cv.notify_all();
+  for (auto& t : pool) t.join();
+  return st;
+}
+
 
 cgl_status cgl_batch_remove(cgl_batch* b, uint32_t id) {
   if (!b || id >= b->jobs.size() || !b->jobs[id].used) return CGL_INVALID_ARG;

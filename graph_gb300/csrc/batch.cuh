@@ -26,7 +26,7 @@ struct BatchTick {
   uint32_t pad;
 };
 
-enum : uint32_t { kGGravity = 1, kGManybody = 4, kGLinkIn = 8, kGLinkOut = 16 };
+enum : uint32_t { kGGravity = 1, kGCenter = 2, kGManybody = 4, kGLinkIn = 8, kGLinkOut = 16, kGCollision = 32 };
 
 struct GraphDesc {
   uint32_t p_off, n;           // points [p_off, p_off + n) of the point arena
@@ -40,6 +40,11 @@ struct GraphDesc {
   float space, csf, friction, gravity, repulsion;
   float link_spring, link_distance, link_r0, link_r1;
   FixedScale fx;
+  float center;                // simulationCenter (kGCenter)
+  // collision (kGCollision): four coll_grid^2 grids from cell coll_off of the collision arena
+  uint32_t coll_off;
+  int32_t coll_grid;
+  float coll_cell, coll_strength, coll_radius, coll_padding;
 };
 
 struct BatchView {
@@ -80,6 +85,15 @@ struct BatchView {
   const BatchTick* ticks;      // [tick][slot]
   uint32_t* tick_ctr;
   PairUnits units;             // {1, -0}: operands of the paired sums and products
+  // center: exact (x, y, count) sums per slot, zeroed at tick start
+  long long* centroid;
+  // collision: resolved point sizes; grid sums and grids of the collision arena
+  const float* size;           // [point arena]
+  long long* cgrid_acc;        // 4 per collision cell, zero between ticks
+  float4* cgrid;
+  const uint32_t* coll_gid;    // graph of each collision cell, kNoGraph if free
+  uint32_t coll_hwm;           // collision cells in use
+  int any_center, any_collision;   // some job runs the force (its kernels are launched)
 };
 
 void batch_launch_tick(const BatchView& v, cudaStream_t st, cudaStream_t side, cudaEvent_t* fork, cudaEvent_t* join);

@@ -6,6 +6,7 @@
 // Point indices that enter the arithmetic (peel hash, tie-break, self test)
 // are graph-local, so a graph advances exactly as it would alone.
 #include "batch.cuh"
+#include "collision.cuh"
 #include "device_util.cuh"
 #include "warp_cells.cuh"
 
@@ -24,39 +25,112 @@ __device__ __forceinline__ uint32_t level_base(int l) {
 }
 
 // ---------------------------------------------------------------- prepass --
+__device__ __forceinline__ void kb_bin(const BatchView& v, const GraphDesc& D, uint32_t P, float2 p) {
+  const int cx = cell_index(p.x, D.csf, D.gf), cy = cell_index(p.y, D.csf, D.gf);
+  const uint32_t key = D.cell_off + (uint32_t)(cy * D.gf + cx);
+  v.key[P] = key;
+  v.rank[P] = atomicAdd(&v.counts[key], 1u);
+}
+
+// Adds each `live` lane's exact (x, y, 1) into its graph's centroid sums; all
+// 32 lanes take part.  The lanes of one graph (points of a graph are
+// contiguous in the arena, so a warp holds one or two) sum first and one lane
+// adds the totals.  Integer sums: the order does not matter.
+__device__ __forceinline__ void centroid_accumulate(const BatchView& v, uint32_t g, bool live, long long sx,
+                                                    long long sy) {
+  const int lane = threadIdx.x & 31;
+  unsigned todo = __ballot_sync(0xffffffffu, live);
+  while (todo) {
+    const int l = __ffs(todo) - 1;
+    const uint32_t gl = __shfl_sync(0xffffffffu, g, l);
+    const bool mine = ((todo >> lane) & 1u) && g == gl;
+    const unsigned grp = __ballot_sync(0xffffffffu, mine);
+    const long long tx = warp_sum64(mine ? sx : 0), ty = warp_sum64(mine ? sy : 0);
+    if (lane == l) {
+      long long* c = v.centroid + 3 * (size_t)gl;
+      atomicAdd((unsigned long long*)&c[0], (unsigned long long)tx);
+      atomicAdd((unsigned long long*)&c[1], (unsigned long long)ty);
+      atomicAdd((unsigned long long*)&c[2], (unsigned long long)__popc(grp));
+    }
+    todo &= ~grp;
+  }
+}
+
+// Gravity and binning (k_prepass); a graph with the center force sums its
+// centroid here instead and bins in kb_center, after the pull.
 __global__ void __launch_bounds__(kBlock) kb_prepass(BatchView v) {
+  const uint32_t P = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t g = kNoGraph;
+  bool centre = false;
+  long long sx = 0, sy = 0;
+  if (P < v.point_hwm && (g = v.gid[P]) != kNoGraph) {
+    const GraphDesc& D = v.desc[g];
+    const BatchTick tp = tick_of(v, g);
+    if (!tp.active) {
+      v.key[P] = kNoCell;
+    } else {
+      const uint8_t f = v.flags[P];
+      float2 p = v.pos[P];
+      if (D.stages & kGGravity) {   // force-gravity.frag:24-40
+        const float c = __fmul_rn(D.space, 0.5f);
+        const float dx = __fsub_rn(c, p.x), dy = __fsub_rn(c, p.y);
+        const float dist = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
+        float vx = 0.f, vy = 0.f;
+        if (dist > 0.f) {
+          const float add = __fmul_rn(__fmul_rn(__fmul_rn(tp.alpha, D.gravity), dist), 0.1f);
+          vx = __fadd_rn(vx, __fmul_rn(add, __fdiv_rn(dx, dist)));
+          vy = __fadd_rn(vy, __fmul_rn(add, __fdiv_rn(dy, dist)));
+        }
+        if (!(f & (kPinned | kAbsent))) {
+          p = integrate(p, vx, vy, D.friction, D.space);
+          v.pos[P] = p;
+        }
+      }
+      if (D.stages & kGCenter) {
+        // calculate-centermass.vert:18-28 over the live points
+        centre = !(f & kAbsent);
+        if (centre) { sx = to_fixed(p.x, D.fx); sy = to_fixed(p.y, D.fx); }
+      } else if ((D.stages & kGManybody) && !(f & kAbsent)) {
+        kb_bin(v, D, P, p);
+      } else {
+        v.key[P] = kNoCell;
+      }
+    }
+  }
+  if (v.any_center) centroid_accumulate(v, g, centre, sx, sy);
+}
+
+// ForceCenter.run (ForceCenter/index.ts:149-199): force-center.frag:22-36 from
+// the graph's centroid, the update, then the binning.
+__global__ void __launch_bounds__(kBlock) kb_center(BatchView v) {
   const uint32_t P = blockIdx.x * blockDim.x + threadIdx.x;
   if (P >= v.point_hwm) return;
   const uint32_t g = v.gid[P];
   if (g == kNoGraph) return;
   const GraphDesc& D = v.desc[g];
+  if (!(D.stages & kGCenter)) return;
   const BatchTick tp = tick_of(v, g);
-  if (!tp.active) { v.key[P] = kNoCell; return; }
+  if (!tp.active) return;
+  const long long* cs = v.centroid + 3 * (size_t)g;
+  const float sx = from_fixed(cs[0], D.fx), sy = from_fixed(cs[1], D.fx);
+  const float cnt = (float)cs[2];
+  const float cmx = __fdiv_rn(sx, cnt), cmy = __fdiv_rn(sy, cnt);
   const uint8_t f = v.flags[P];
   float2 p = v.pos[P];
-  if (D.stages & kGGravity) {   // force-gravity.frag:24-40
-    const float c = __fmul_rn(D.space, 0.5f);
-    const float dx = __fsub_rn(c, p.x), dy = __fsub_rn(c, p.y);
-    const float dist = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
-    float vx = 0.f, vy = 0.f;
-    if (dist > 0.f) {
-      const float add = __fmul_rn(__fmul_rn(__fmul_rn(tp.alpha, D.gravity), dist), 0.1f);
-      vx = __fadd_rn(vx, __fmul_rn(add, __fdiv_rn(dx, dist)));
-      vy = __fadd_rn(vy, __fmul_rn(add, __fdiv_rn(dy, dist)));
-    }
-    if (!(f & (kPinned | kAbsent))) {
-      p = integrate(p, vx, vy, D.friction, D.space);
-      v.pos[P] = p;
-    }
+  const float dx = __fsub_rn(cmx, p.x), dy = __fsub_rn(cmy, p.y);
+  const float dist = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
+  float vx = 0.f, vy = 0.f;
+  if (dist > 0.f) {
+    const float add = __fmul_rn(__fmul_rn(__fmul_rn(tp.alpha, D.center), dist), 0.01f);
+    vx = __fadd_rn(vx, __fmul_rn(add, __fdiv_rn(dx, dist)));
+    vy = __fadd_rn(vy, __fmul_rn(add, __fdiv_rn(dy, dist)));
   }
-  if ((D.stages & kGManybody) && !(f & kAbsent)) {
-    const int cx = cell_index(p.x, D.csf, D.gf), cy = cell_index(p.y, D.csf, D.gf);
-    const uint32_t key = D.cell_off + (uint32_t)(cy * D.gf + cx);
-    v.key[P] = key;
-    v.rank[P] = atomicAdd(&v.counts[key], 1u);
-  } else {
-    v.key[P] = kNoCell;
+  if (!(f & (kPinned | kAbsent))) {
+    p = integrate(p, vx, vy, D.friction, D.space);
+    v.pos[P] = p;
   }
+  if ((D.stages & kGManybody) && !(f & kAbsent)) kb_bin(v, D, P, p);
+  else v.key[P] = kNoCell;
 }
 
 // ------------------------------------------------------------------- scan --
@@ -467,6 +541,54 @@ __global__ void __launch_bounds__(kBlock) kb_link(BatchView v, int direction, co
   dst[P] = (f & kPinned) ? pp : integrate(pp, vel.x, vel.y, D.friction, D.space);
 }
 
+// -------------------------------------------------------------- collision --
+// ForceCollision.run per graph (collision.cuh's arithmetic, the plain
+// engine's): grid sums of the four offset grids, their conversion, the force.
+__global__ void __launch_bounds__(kBlock) kb_coll_grid(BatchView v) {
+  const uint32_t P = blockIdx.x * blockDim.x + threadIdx.x;
+  bool live = false;
+  const GraphDesc* D = nullptr;
+  float2 p = make_float2(0.f, 0.f);
+  float sz = 0.f;
+  if (P < v.point_hwm) {
+    const uint32_t g = v.gid[P];
+    if (g != kNoGraph) {
+      D = &v.desc[g];
+      live = (D->stages & kGCollision) && tick_of(v, g).active && !(v.flags[P] & kAbsent);
+      if (live) { p = v.pos[P]; sz = v.size[P]; }
+    }
+  }
+  if (!__any_sync(0xffffffffu, live)) return;   // warp-uniform
+  const FixedScale none{1.f, 1.f, 1.f};
+  coll_accumulate(live ? v.cgrid_acc + 4 * (size_t)D->coll_off : v.cgrid_acc, live ? D->coll_grid : 1,
+                  live ? D->coll_cell : 1.f, live ? D->fx : none, p, sz, live);
+}
+
+__global__ void __launch_bounds__(kBlock) kb_coll_convert(BatchView v) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= v.coll_hwm) return;
+  const uint32_t g = v.coll_gid[c];
+  if (g == kNoGraph) return;
+  coll_convert_cell(v.cgrid_acc + 4 * (size_t)c, v.cgrid + c, v.desc[g].fx);
+}
+
+__global__ void __launch_bounds__(kBlock) kb_coll_force(BatchView v) {
+  const uint32_t P = blockIdx.x * blockDim.x + threadIdx.x;
+  if (P >= v.point_hwm) return;
+  const uint32_t g = v.gid[P];
+  if (g == kNoGraph) return;
+  const GraphDesc& D = v.desc[g];
+  if (!(D.stages & kGCollision)) return;
+  const BatchTick tp = tick_of(v, g);
+  if (!tp.active) return;
+  const uint8_t f = v.flags[P];
+  if (f & kAbsent) return;
+  const float2 p = v.pos[P];
+  const CollParams cp{D.coll_grid, D.coll_cell, D.coll_radius, D.coll_padding, __fmul_rn(tp.alpha, D.coll_strength)};
+  const float2 w = coll_velocity(v.cgrid + D.coll_off, cp, p, v.size[P], P - D.p_off, D.n);
+  if (!(f & kPinned)) v.pos[P] = integrate(p, w.x, w.y, D.friction, D.space);
+}
+
 __global__ void kb_tick_end(BatchView v) { *v.tick_ctr += 1; }
 
 inline uint32_t blocks(uint32_t n) { return (n + kBlock - 1) / kBlock; }
@@ -475,7 +597,9 @@ inline uint32_t blocks(uint32_t n) { return (n + kBlock - 1) / kBlock; }
 
 void batch_launch_tick(const BatchView& v, cudaStream_t st, cudaStream_t side, cudaEvent_t* fork, cudaEvent_t* join) {
   cudaMemsetAsync(v.big_count, 0, 4 * sizeof(uint32_t), st);
+  if (v.any_center) cudaMemsetAsync(v.centroid, 0, 3 * sizeof(long long) * (size_t)v.slots, st);
   if (v.point_hwm) kb_prepass<<<blocks(v.point_hwm), kBlock, 0, st>>>(v);
+  if (v.any_center && v.point_hwm) kb_center<<<blocks(v.point_hwm), kBlock, 0, st>>>(v);
   if (v.cell_hwm) {
     const uint32_t n1 = (v.cell_hwm + kChunk - 1) / kChunk;   // partials of 1024 cells
     const uint32_t n2 = (n1 + kChunk - 1) / kChunk;           // partials of 1024^2 cells (<= 1024)
@@ -504,6 +628,11 @@ void batch_launch_tick(const BatchView& v, cudaStream_t st, cudaStream_t side, c
     if (v.point_hwm) kb_link<<<blocks(v.point_hwm), kBlock, 0, st>>>(v, dir, src, dst, nullptr, v.point_hwm);
     if (nh) cudaStreamWaitEvent(st, join[dir], 0);
   }
+  if (v.any_collision && v.point_hwm) {   // after the links, as in runSimulationStep (src/index.ts:2068-2078)
+    kb_coll_grid<<<blocks(v.point_hwm), kBlock, 0, st>>>(v);
+    if (v.coll_hwm) kb_coll_convert<<<blocks(v.coll_hwm), kBlock, 0, st>>>(v);
+    kb_coll_force<<<blocks(v.point_hwm), kBlock, 0, st>>>(v);
+  }
   kb_tick_end<<<1, 1, 0, st>>>(v);
 }
 
@@ -512,6 +641,8 @@ uint32_t batch_kernels_per_tick(const BatchView& v) {
   if (v.cell_hwm) k += 5;
   if (v.n_tiles) k += 1;
   k += (v.n_heavy_in > 0) + (v.n_heavy_out > 0);
+  if (v.any_center) k += 1;
+  if (v.any_collision) k += 2 + (v.coll_hwm > 0);
   return k + 1;                          // tick end
 }
 

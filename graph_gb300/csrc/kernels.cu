@@ -27,6 +27,7 @@
 // repulsion and drag passes (force-mouse.frag, drag-point.frag) and the
 // renderer's position texture.
 #include "device_util.cuh"
+#include "collision.cuh"
 #include "kernels.cuh"
 #include "manybody_duo.cuh"
 #include "warp_cells.cuh"
@@ -919,34 +920,13 @@ __global__ void __launch_bounds__(kBlock) k_fill_lanes(const uint32_t* __restric
 
 
 // -------------------------------------------------------------- collision --
-__device__ __forceinline__ float coll_bin(float p, float o, float cs, float gm1) {
-  const float off = __fadd_rn(p, __fmul_rn(o, cs));
-  float c = gclamp(floorf(__fdiv_rn(off, cs)), 0.f, gm1);
-  if (!(c == c)) c = 0.f;
-  return c;
-}
-
-__constant__ float kOffX[4] = {0.f, 0.5f, 0.f, 0.5f};
-__constant__ float kOffY[4] = {0.f, 0.f, 0.5f, 0.5f};
-
-// Warp-wide sum of a 64-bit value (all 32 lanes take part).
-__device__ __forceinline__ long long warp_sum64(long long v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
+// The arithmetic is collision.cuh's, shared with the batched engine.
 // Points are taken in `order` (the many-body pass's cell order) when given,
-// so the lanes of a warp fall into a few grid cells; the lanes of each cell
-// sum their integer terms first and one lane adds the cell's total (at most
-// kCollRounds cells per warp and grid, the rest add their own terms).
-// Integer sums are order-free, so the grid is the same in any order.
-constexpr int kCollRounds = 6;
+// so the lanes of a warp fall into a few grid cells.
 __global__ void __launch_bounds__(kBlock) k_coll_grid(DeviceView d, SimScalars s, const uint32_t* __restrict__ order,
                                                       uint32_t count) {
   // build-grid.vert:28-62 for the 4 offsets (ForceCollision/index.ts:19-24)
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int lane = threadIdx.x & 31;
   uint32_t i = 0;
   bool live = t < count;
   if (live) {
@@ -957,51 +937,14 @@ __global__ void __launch_bounds__(kBlock) k_coll_grid(DeviceView d, SimScalars s
   float2 p = make_float2(0.f, 0.f);
   float sz = 0.f;
   if (live) { p = d.pos[i]; sz = d.size[i]; }
-  const float gm1 = (float)s.coll_grid - 1.0f;
-  const long long fx = live ? to_fixed(p.x, s.fx) : 0, fy = live ? to_fixed(p.y, s.fx) : 0;
-  const long long fs = live ? to_fixed(sz, s.fx) : 0;
-  const uint32_t G2 = (uint32_t)(s.coll_grid * s.coll_grid);
-  const unsigned active = __ballot_sync(0xffffffffu, live);
-#pragma unroll 1
-  for (int g = 0; g < 4; ++g) {
-    const int cx = (int)coll_bin(p.x, kOffX[g], s.coll_cell, gm1);
-    const int cy = (int)coll_bin(p.y, kOffY[g], s.coll_cell, gm1);
-    const uint32_t key = (uint32_t)(cy * s.coll_grid + cx);
-    long long* a = d.cgrid_acc + 4 * ((size_t)g * G2 + key);
-    unsigned todo = active;
-#pragma unroll 1
-    for (int r = 0; r < kCollRounds && todo; ++r) {
-      const int l = __ffs(todo) - 1;
-      const uint32_t kl = __shfl_sync(0xffffffffu, key, l);
-      const bool mine = ((todo >> lane) & 1u) && key == kl;
-      const unsigned grp = __ballot_sync(0xffffffffu, mine);
-      const long long sx = warp_sum64(mine ? fx : 0);
-      const long long sy = warp_sum64(mine ? fy : 0);
-      const long long ss = warp_sum64(mine ? fs : 0);
-      if (lane == l) {
-        atomicAdd((unsigned long long*)&a[0], (unsigned long long)sx);
-        atomicAdd((unsigned long long*)&a[1], (unsigned long long)sy);
-        atomicAdd((unsigned long long*)&a[2], (unsigned long long)ss);
-        atomicAdd((unsigned long long*)&a[3], (unsigned long long)__popc(grp));
-      }
-      todo &= ~grp;
-    }
-    if ((todo >> lane) & 1u) {
-      atomicAdd((unsigned long long*)&a[0], (unsigned long long)fx);
-      atomicAdd((unsigned long long*)&a[1], (unsigned long long)fy);
-      atomicAdd((unsigned long long*)&a[2], (unsigned long long)fs);
-      atomicAdd((unsigned long long*)&a[3], 1ull);
-    }
-  }
+  coll_accumulate(d.cgrid_acc, s.coll_grid, s.coll_cell, s.fx, p, sz, live);
 }
 
 __global__ void __launch_bounds__(kBlock) k_coll_convert(DeviceView d, SimScalars s) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t total = 4u * (uint32_t)(s.coll_grid * s.coll_grid);
   if (k >= total) return;
-  long long* a = d.cgrid_acc + 4 * (size_t)k;
-  d.cgrid[k] = make_float4(from_fixed(a[0], s.fx), from_fixed(a[1], s.fx), from_fixed(a[2], s.fx), (float)a[3]);
-  a[0] = 0; a[1] = 0; a[2] = 0; a[3] = 0;
+  coll_convert_cell(d.cgrid_acc + 4 * (size_t)k, d.cgrid + k, s.fx);
 }
 
 __global__ void __launch_bounds__(kBlock) k_coll_force(DeviceView d, SimScalars s, const uint32_t* __restrict__ order,
@@ -1014,76 +957,9 @@ __global__ void __launch_bounds__(kBlock) k_coll_force(DeviceView d, SimScalars 
   const uint8_t f = d.flags[i];
   if (f & kAbsent) return;
   const float2 p = d.pos[i];
-  const float cs = s.coll_cell;
-  const int G = s.coll_grid;
-  const float Gf = (float)G;
-  const float gm1 = Gf - 1.0f;
-  const uint32_t G2 = (uint32_t)(G * G);
-  const float cur = (float)i;
-  const float csz = d.size[i];
-  const float cr = s.coll_radius, pad = s.coll_padding;
-  const float R = __fadd_rn(cr > 0.f ? cr : __fmul_rn(csz, 0.5f), pad);
-  float vx = 0.f, vy = 0.f;
-  if (!(cur < 0.f || cur >= (float)d.n)) {
-    for (int g = 0; g < 4; ++g) {
-      const float mx = coll_bin(p.x, kOffX[g], cs, gm1);
-      const float my = coll_bin(p.y, kOffY[g], cs, gm1);
-      const float4* grid = d.cgrid + (size_t)g * G2;
-      float total = 0.f, gx = 0.f, gy = 0.f;
-      for (int dx = -1; dx <= 1; ++dx)
-        for (int dy = -1; dy <= 1; ++dy) {
-          const float ncx = __fadd_rn(mx, (float)dx), ncy = __fadd_rn(my, (float)dy);
-          if (ncx < 0.f || ncx >= Gf || ncy < 0.f || ncy >= Gf) continue;
-          const float4 cd = __ldg(&grid[(int)ncy * G + (int)ncx]);
-          const float cnt = cd.w;
-          if (cnt < 0.5f) continue;
-          float ec = cnt, spx = cd.x, spy = cd.y, ss = cd.z;
-          if (dx == 0 && dy == 0) {
-            ec = __fsub_rn(cnt, 1.0f);
-            spx = __fsub_rn(spx, p.x); spy = __fsub_rn(spy, p.y); ss = __fsub_rn(ss, csz);
-          }
-          if (ec < 0.5f) continue;
-          total = __fadd_rn(total, ec);
-          const float avx = __fdiv_rn(spx, ec), avy = __fdiv_rn(spy, ec);
-          const float avs = __fdiv_rn(ss, ec);
-          const float oR = __fadd_rn(cr > 0.f ? cr : __fmul_rn(avs, 0.5f), pad);
-          const float comb = __fadd_rn(R, oR);
-          const float ddx = __fsub_rn(p.x, avx), ddy = __fsub_rn(p.y, avy);
-          const float dist = __fsqrt_rn(__fadd_rn(__fmul_rn(ddx, ddx), __fmul_rn(ddy, ddy)));
-          if (dist < comb && dist > 0.001f) {
-            const float ov = __fdiv_rn(__fsub_rn(comb, dist), comb);
-            const float soft = __fmul_rn(__fmul_rn(__fsqrt_rn(ov), comb), 0.5f);
-            const float dirx = __fdiv_rn(ddx, dist), diry = __fdiv_rn(ddy, dist);
-            float fo = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(tp.alpha, s.coll_strength), soft), 0.25f), ec);
-            fo = gmin(fo, __fmul_rn(comb, 0.5f));
-            gx = __fadd_rn(gx, __fmul_rn(fo, dirx));
-            gy = __fadd_rn(gy, __fmul_rn(fo, diry));
-          } else if (dist <= 0.001f && ec > 0.f) {
-            const float ang = __fmul_rn(cur, 0.618033988749895f);
-            const float fo = gmin(__fmul_rn(__fmul_rn(__fmul_rn(tp.alpha, s.coll_strength), comb), 0.1f),
-                                  __fmul_rn(comb, 0.3f));
-            float sn, cn;
-            portable_sincos(ang, &sn, &cn);
-            const float fe = __fmul_rn(fo, ec);
-            gx = __fadd_rn(gx, __fmul_rn(fe, cn));
-            gy = __fadd_rn(gy, __fmul_rn(fe, sn));
-          }
-        }
-      if (total > 2.0f) {
-        const float dmp = __fdiv_rn(2.0f, total);
-        gx = __fmul_rn(gx, dmp); gy = __fmul_rn(gy, dmp);
-      }
-      const float maxc = __fmul_rn(R, 0.1f);
-      const float corr = __fsqrt_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)));
-      if (corr > maxc) {
-        const float sc = __fdiv_rn(maxc, corr);
-        gx = __fmul_rn(gx, sc); gy = __fmul_rn(gy, sc);
-      }
-      vx = __fadd_rn(vx, gx);
-      vy = __fadd_rn(vy, gy);
-    }
-  }
-  if (!(f & kPinned)) d.pos[i] = integrate(p, vx, vy, s.friction, s.space);
+  const CollParams cp{s.coll_grid, s.coll_cell, s.coll_radius, s.coll_padding, __fmul_rn(tp.alpha, s.coll_strength)};
+  const float2 v = coll_velocity(d.cgrid, cp, p, d.size[i], i, d.n);
+  if (!(f & kPinned)) d.pos[i] = integrate(p, v.x, v.y, s.friction, s.space);
 }
 
 // --------------------------------------------------------------- clusters --

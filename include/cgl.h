@@ -325,9 +325,10 @@ cgl_status cgl_debug_get_slots(cgl_engine* e, int32_t* out, uint64_t capacity);
  * tick runs every job in the batch.  Each job behaves exactly as a plain
  * engine created with the same config, given the same positions and links,
  * rendered and started at alpha 1 (cgl_create + cgl_set_point_positions +
- * cgl_set_links + cgl_render + cgl_start), stepping the same ticks.  Jobs join
- * and leave between ticks (continuous batching).  Jobs run gravity, many-body
- * and link forces; center and collision need a plain engine. */
+ * cgl_set_links [+ cgl_set_point_sizes] + cgl_render + cgl_start), stepping the
+ * same ticks.  Jobs join and leave between ticks (continuous batching).  Jobs
+ * run gravity, center, many-body, link and collision forces; clusters and the
+ * pointer's interaction need a plain engine. */
 typedef struct cgl_batch cgl_batch;
 
 typedef struct cgl_batch_info {
@@ -352,6 +353,27 @@ cgl_status cgl_batch_destroy(cgl_batch* b);
  * src/index.ts:2164-2169). */
 cgl_status cgl_batch_add(cgl_batch* b, const cgl_config* cfg, const float* xy, uint64_t n_floats, const float* links,
                          uint64_t n_link_floats, uint32_t max_ticks, int32_t stop_below_alpha_min, uint32_t* id);
+/* One job of cgl_batch_add_many: cgl_batch_add's arguments, plus the job's
+ * per-point sizes (Graph.setPointSizes, the collision radii; NULL = none). */
+typedef struct cgl_batch_job {
+  const cgl_config* cfg;
+  const float* xy;
+  uint64_t n_floats;
+  const float* links;
+  uint64_t n_link_floats;
+  const float* sizes;
+  uint64_t n_sizes;
+  uint32_t max_ticks;
+  int32_t stop_below_alpha_min;
+} cgl_batch_job;
+/* Add `count` jobs, each as cgl_batch_add would.  Their host work (positions,
+ * the random draws of the reference's sequential stream, host link lists)
+ * runs on `threads` host threads (0 = one per core) while earlier jobs upload;
+ * the jobs join in order and ids[k] receives job k's id.  On a failure the
+ * jobs before the failing one stay added (*added of them, may be null) and
+ * its status is returned. */
+cgl_status cgl_batch_add_many(cgl_batch* b, uint32_t count, const cgl_batch_job* jobs, uint32_t* ids,
+                              uint32_t threads, uint32_t* added);
 cgl_status cgl_batch_remove(cgl_batch* b, uint32_t id);
 cgl_status cgl_batch_step(cgl_batch* b, uint32_t ticks);
 cgl_status cgl_batch_synchronize(cgl_batch* b);

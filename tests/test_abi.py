@@ -51,6 +51,7 @@ def test_struct_sizes_match_header():
     assert C.sizeof(_abi.Config) == 208
     assert C.sizeof(_abi.State) == 56
     assert C.sizeof(_abi.Layout) == 88
+    assert C.sizeof(_abi.BatchJob) == 64
 
 
 def test_create_without_gpu_fails_loudly():

@@ -108,15 +108,80 @@ def test_jobs_join_and_leave_between_ticks():
             assert same_bits(b.get_point_positions(jid), _alone(pos, links, fields, 6))
 
 
-def test_batch_rejects_center_and_collision():
+def _alone_sized(pos, links, fields, ticks, sizes=None):
+    from graph_gb300.engine import Engine
+    e = Engine(**fields)
+    e.set_point_positions(pos)
+    if links is not None:
+        e.set_links(links)
+    if sizes is not None:
+        e.set_point_sizes(sizes)
+    e.render()
+    e.start(1.0)
+    e.step(ticks)
+    out = e.get_point_positions()
+    e.close()
+    return out
+
+
+def test_batch_center_and_collision_equal_alone():
+    # ForceCenter and ForceCollision per job, beside jobs without them, in one launch per tick
+    from graph_gb300.batch import Batch
+    rng = np.random.default_rng(31)
+    base = _jobs(3)
+    cases = []
+    for k, (pos, links, fields) in enumerate(base[3:9]):
+        n = pos.size // 2
+        sizes = rng.uniform(2, 14, size=n).astype(np.float32) if k % 2 else None
+        if sizes is not None:
+            sizes[::17] = np.nan                       # NaN -> pointDefaultSize
+        extra = [dict(simulation_center=0.4), dict(simulation_collision=0.6),
+                 dict(simulation_center=0.3, simulation_collision=0.5, simulation_collision_radius=3.0)][k % 3]
+        cases.append((pos, links, dict(fields, **extra, random_seed=500 + k), sizes))
+    pos = base[6][0].copy()
+    pos[40:80] = np.nan                                # absent points stay out of centroids and grids
+    cases.append((pos, base[6][1], dict(base[6][2], simulation_center=0.5, simulation_collision=0.4, random_seed=599),
+                  None))
+    cases += [(p, l, f, None) for p, l, f in base[:3]]
+    ticks = 9
+    with Batch() as b:
+        ids = [b.add(p, l, sizes=sz, **f) for p, l, f, sz in cases]
+        assert b.info().kernels_per_tick > 12
+        b.step(ticks)
+        for (p, l, f, sz), jid in zip(cases, ids):
+            got = b.get_point_positions(jid)
+            want = _alone_sized(p, l, f, ticks, sz)
+            assert same_bits(got, want), (f, first_mismatch(got, want))
+
+
+@pytest.mark.parametrize("stream", [_abi.RANDOM_REFERENCE, _abi.RANDOM_COUNTER])
+def test_add_many_equals_add(stream):
+    from graph_gb300.batch import Batch
+    jobs = [(p, l, dict(f, random_stream=stream, device_ingest_min_links=1000.0)) for p, l, f in _jobs(4)]
+    with Batch() as one, Batch() as many:
+        ids1 = [one.add(p, l, **f) for p, l, f in jobs]
+        ids2 = many.add_many([dict(positions=p, links=l, **f) for p, l, f in jobs], threads=4)
+        assert len(ids2) == len(jobs)
+        one.step(6)
+        many.step(6)
+        for a, c in zip(ids1, ids2):
+            assert same_bits(one.get_point_positions(a), many.get_point_positions(c))
+            assert one.state(a).rng_draws == many.state(c).rng_draws
+
+
+def test_add_many_stops_at_a_bad_job():
     from graph_gb300.batch import Batch
     from graph_gb300._calls import StatusError
-    pos = generators.uniform_positions(100, 0, 4096, 1)
+    jobs = _jobs(5)[3:7]
+    specs = [dict(positions=p, links=l, **f) for p, l, f in jobs]
+    specs.insert(2, dict(positions=np.zeros(0, np.float32), links=None, random_seed=1))   # no points
     with Batch() as b:
         with pytest.raises(StatusError):
-            b.add(pos, None, simulation_center=0.5)
-        with pytest.raises(StatusError):
-            b.add(pos, None, simulation_collision=0.5)
+            b.add_many(specs, threads=3)
+        assert b.info().jobs == 2
+        b.step(3)
+        for jid, (p, l, f) in zip(range(2), jobs[:2]):
+            assert same_bits(b.get_point_positions(jid), _alone(p, l, f, 3))
 
 
 def test_batch_budget_refuses_admission():
