@@ -617,7 +617,7 @@ def run_batch(args):
     b.step(args.ticks)
     b.synchronize()
     t2 = time.perf_counter()
-    out_batch = [b.get_point_positions(i) for i in ids]
+    out_batch = b.get_positions_many(ids)
     t3 = time.perf_counter()
     info = b.info()
     batch = {"ingest_s": t1 - t0, "simulate_s": t2 - t1, "readback_s": t3 - t2}

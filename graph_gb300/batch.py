@@ -25,6 +25,8 @@ def _declare(lib):
                                   C.POINTER(C.c_uint32)]
     lib.cgl_batch_add_many.argtypes = [B, C.c_uint32, C.POINTER(_abi.BatchJob), C.POINTER(C.c_uint32), C.c_uint32,
                                        C.POINTER(C.c_uint32)]
+    lib.cgl_batch_get_positions_many.argtypes = [B, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_void_p),
+                                                 C.POINTER(C.c_uint64)]
     lib.cgl_batch_remove.argtypes = [B, C.c_uint32]
     lib.cgl_batch_step.argtypes = [B, C.c_uint32]
     lib.cgl_batch_synchronize.argtypes = [B]
@@ -34,7 +36,7 @@ def _declare(lib):
     lib.cgl_batch_last_error.argtypes = [B]
     lib.cgl_batch_last_error.restype = C.c_char_p
     for fn in ("create", "destroy", "add", "add_many", "remove", "step", "synchronize", "get_point_positions",
-               "get_state", "get_info"):
+               "get_positions_many", "get_state", "get_info"):
         getattr(lib, "cgl_batch_" + fn).restype = C.c_int
     lib._batch_declared = True
 
@@ -122,6 +124,16 @@ class Batch:
         self._check("get_point_positions", self._lib.cgl_batch_get_point_positions(self._h, int(job), _fptr(out),
                                                                                    out.size))
         return out
+
+    def get_positions_many(self, jobs):
+        """Positions of several jobs with one device-to-host copy; a list of arrays in job order."""
+        jobs = list(jobs)
+        outs = [np.empty(2 * self._n[j], dtype=np.float32) for j in jobs]
+        ids = (C.c_uint32 * len(jobs))(*jobs)
+        ptrs = (C.c_void_p * len(jobs))(*[o.ctypes.data for o in outs])
+        caps = (C.c_uint64 * len(jobs))(*[o.size for o in outs])
+        self._check("get_positions_many", self._lib.cgl_batch_get_positions_many(self._h, len(jobs), ids, ptrs, caps))
+        return outs
 
     def state(self, job):
         s = _abi.State()

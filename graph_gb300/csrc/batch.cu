@@ -113,6 +113,8 @@ struct cgl_batch {
   bool any_center = false, any_collision = false;
   uint32_t n_tiles = 0, n_heavy_in = 0, n_heavy_out = 0, slots_cap = 0;
   BatchTick* h_ticks = nullptr;
+  float2* h_stage = nullptr;   // pinned read-back staging of the point arena
+  uint64_t stage_cap = 0;
   cudaGraphExec_t graph = nullptr;
   bool dirty = true;
   BatchView view{};
@@ -700,7 +702,7 @@ cgl_status commit_job(cgl_batch* b, HostJob& h, uint32_t* id) {
     if (j.m_out)
       JCU(cudaMemcpyAsync((uint4*)b->ent.p + j.e_out, h.cout_.ent.data(), j.m_out * 16, cudaMemcpyHostToDevice, s));
   }
-  JCU(cudaStreamSynchronize(s));
+  if (dev_links) JCU(cudaStreamSynchronize(s));   // the temporaries' kernels; pageable uploads are staged at the call
 #undef JCU
   GraphDesc& D = j.desc;
   D.p_off = (uint32_t)j.p_off;
@@ -726,6 +728,7 @@ cgl_status commit_job(cgl_batch* b, HostJob& h, uint32_t* id) {
   D.link_r1 = (float)cfg->simulation_link_dist_random_variation_range[1];
   D.fx = h.fx;
   D.center = (float)cfg->simulation_center;
+  D.level_guard = D.csf >= 2.0f && D.space <= 33554432.0f;   // 2^25
   D.coll_off = (uint32_t)j.coll_off;
   b->jobs[g] = std::move(j);
   b->dirty = true;
@@ -757,7 +760,7 @@ cgl_status cgl_batch_create(int32_t device, double hbm_budget_bytes, cgl_batch**
     return CGL_CUDA_ERROR;
   }
   cgl_status st;
-  if ((st = grow(b, b->big_count, 16, 0, 0)) || (st = grow(b, b->tick_ctr, 4, 0, 0)) ||
+  if ((st = grow(b, b->big_count, 32, 0, 0)) || (st = grow(b, b->tick_ctr, 4, 0, 0)) ||
       (st = reserve_cells(b, 1024)) || (st = reserve_points(b, 1024))) {
     cgl_batch_destroy(b);
     return st;
@@ -780,6 +783,7 @@ cgl_status cgl_batch_destroy(cgl_batch* b) {
   for (Buf* x : all)
     if (x->p) cudaFree(x->p);
   if (b->h_ticks) cudaFreeHost(b->h_ticks);
+  if (b->h_stage) cudaFreeHost(b->h_stage);
   for (int k = 0; k < 2; ++k) {
     if (b->fork[k]) cudaEventDestroy(b->fork[k]);
     if (b->join[k]) cudaEventDestroy(b->join[k]);
@@ -925,6 +929,45 @@ cgl_status cgl_batch_get_point_positions(cgl_batch* b, uint32_t id, float* out, 
   if (cudaSetDevice(b->device) != cudaSuccess) return bfail(b, CGL_CUDA_ERROR, "cudaSetDevice");
   BCU(cudaMemcpyAsync(out, (float2*)b->pos.p + j.p_off, j.n * 8, cudaMemcpyDeviceToHost, b->stream));
   BCU(cudaStreamSynchronize(b->stream));
+  return CGL_OK;
+}
+
+cgl_status cgl_batch_get_positions_many(cgl_batch* b, uint32_t count, const uint32_t* ids, float* const* outs,
+                                        const uint64_t* capacity_floats) {
+  if (!b || (count && (!ids || !outs || !capacity_floats))) return CGL_INVALID_ARG;
+  b->err.clear();
+  for (uint32_t k = 0; k < count; ++k) {
+    if (ids[k] >= b->jobs.size() || !b->jobs[ids[k]].used) return bfail(b, CGL_INVALID_ARG, "job %u: no such job", ids[k]);
+    const Job& j = b->jobs[ids[k]];
+    if (!outs[k] || capacity_floats[k] < 2 * j.n)
+      return bfail(b, CGL_INVALID_ARG, "job %u: output holds %llu floats, need %llu", ids[k],
+                   (unsigned long long)capacity_floats[k], (unsigned long long)(2 * j.n));
+  }
+  if (count == 0) return CGL_OK;
+  if (cudaSetDevice(b->device) != cudaSuccess) return bfail(b, CGL_CUDA_ERROR, "cudaSetDevice");
+  // the used point arena in one copy, then each job's range on host threads
+  const uint64_t hwm = b->pts.hwm;
+  if (hwm > b->stage_cap) {
+    if (b->h_stage) cudaFreeHost(b->h_stage);
+    b->h_stage = nullptr;
+    b->stage_cap = 0;
+    BCU(cudaMallocHost((void**)&b->h_stage, hwm * sizeof(float2)));
+    b->stage_cap = hwm;
+  }
+  BCU(cudaMemcpyAsync(b->h_stage, b->pos.p, hwm * sizeof(float2), cudaMemcpyDeviceToHost, b->stream));
+  BCU(cudaStreamSynchronize(b->stream));
+  const unsigned nt = std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), count);
+  std::atomic<uint32_t> next{0};
+  auto worker = [&]() {
+    for (uint32_t k; (k = next.fetch_add(1)) < count;) {
+      const Job& j = b->jobs[ids[k]];
+      std::memcpy(outs[k], b->h_stage + j.p_off, j.n * sizeof(float2));
+    }
+  };
+  std::vector<std::thread> pool;
+  for (unsigned t = 1; t < nt; ++t) pool.emplace_back(worker);
+  worker();
+  for (auto& t : pool) t.join();
   return CGL_OK;
 }
 

@@ -41,6 +41,7 @@ struct GraphDesc {
   float link_spring, link_distance, link_r0, link_r1;
   FixedScale fx;
   float center;                // simulationCenter (kGCenter)
+  int32_t level_guard;         // finest cell >= 2 units, space <= 2^25 (the plain engine's level_guard)
   // collision (kGCollision): four coll_grid^2 grids from cell coll_off of the collision arena
   uint32_t coll_off;
   int32_t coll_grid;
@@ -68,7 +69,8 @@ struct BatchView {
   uint32_t* scan2;
   uint32_t* big_list;          // [2 x cell arena] CTA cells, then warp cells: those above
                                // kWarpSmallCell from the front, the others from the back
-  uint32_t* big_count;         // [4] CTA cells, heavy and light warp cells, warp-cell ticket
+  uint32_t* big_count;         // [8] CTA cells, heavy and light warp cells, warp-cell ticket, then [4] = 1
+                               // when a binned point lies outside its graph's space (zeroed each tick)
   long long* big_sx;
   long long* big_sy;
   uint32_t* big_ns;

@@ -25,11 +25,17 @@ __device__ __forceinline__ uint32_t level_base(int l) {
 }
 
 // ---------------------------------------------------------------- prepass --
+constexpr uint32_t kBatchOutside = 4;   // big_count word: a binned point outside its space
+
 __device__ __forceinline__ void kb_bin(const BatchView& v, const GraphDesc& D, uint32_t P, float2 p) {
   const int cx = cell_index(p.x, D.csf, D.gf), cy = cell_index(p.y, D.csf, D.gf);
   const uint32_t key = D.cell_off + (uint32_t)(cy * D.gf + cx);
   v.key[P] = key;
   v.rank[P] = atomicAdd(&v.counts[key], 1u);
+  const bool outside = !(p.x >= 0.f && p.x <= D.space && p.y >= 0.f && p.y <= D.space);
+  const unsigned am = __activemask();
+  if (__ballot_sync(am, outside) && (threadIdx.x & 31) == (unsigned)(__ffs(am) - 1))
+    atomicOr(&v.big_count[kBatchOutside], 1u);
 }
 
 // Adds each `live` lane's exact (x, y, 1) into its graph's centroid sums; all
@@ -449,7 +455,9 @@ __global__ void __launch_bounds__(kBlock) kb_coarse(BatchView v) {
 
 // --------------------------------------------------------------- manybody --
 // FAST: the repulsion quotients come from the reciprocals (quotient_by_recip(k)).
-template <bool FAST>
+// GUARDED: the level terms without the range flag (the job's level_guard and
+// no binned point of the batch outside its space this tick).
+template <bool FAST, bool GUARDED = false>
 __device__ __forceinline__ void kb_manybody_point(const BatchView& v, const GraphDesc& D, uint32_t j, uint32_t P,
                                                   float2 p, float k) {
   const int gf = D.gf, L = D.levels;
@@ -460,7 +468,7 @@ __device__ __forceinline__ void kb_manybody_point(const BatchView& v, const Grap
 #pragma unroll 1
   for (int l = 0; l < L; ++l) {   // force-level.frag:70-95
     const int sh = L - 1 - l;
-    vel = add2(vel, level_terms<FAST>(rec + level_base(l), 4 << l, fcx >> sh, fcy >> sh, p, k, pu), pu);
+    vel = add2(vel, level_terms<FAST, FAST, GUARDED>(rec + level_base(l), 4 << l, fcx >> sh, fcy >> sh, p, k, pu), pu);
   }
   // near field (force-nearfield.frag:199-263)
   const float2 rj = v.jitter[P];
@@ -485,8 +493,9 @@ __global__ void __launch_bounds__(kBlock) kb_manybody(BatchView v) {
   const BatchTick tp = tick_of(v, g);
   const float2 p = v.sorted_pos[j];
   const float k = __fmul_rn(tp.alpha, D.repulsion);
-  if (quotient_by_recip(k)) kb_manybody_point<true>(v, D, j, P, p, k);
-  else kb_manybody_point<false>(v, D, j, P, p, k);
+  if (!quotient_by_recip(k)) kb_manybody_point<false>(v, D, j, P, p, k);
+  else if (D.level_guard && __ldg(&v.big_count[kBatchOutside]) == 0) kb_manybody_point<true, true>(v, D, j, P, p, k);
+  else kb_manybody_point<true>(v, D, j, P, p, k);
 }
 
 // ------------------------------------------------------------------- link --
@@ -596,7 +605,7 @@ inline uint32_t blocks(uint32_t n) { return (n + kBlock - 1) / kBlock; }
 }  // namespace
 
 void batch_launch_tick(const BatchView& v, cudaStream_t st, cudaStream_t side, cudaEvent_t* fork, cudaEvent_t* join) {
-  cudaMemsetAsync(v.big_count, 0, 4 * sizeof(uint32_t), st);
+  cudaMemsetAsync(v.big_count, 0, 8 * sizeof(uint32_t), st);
   if (v.any_center) cudaMemsetAsync(v.centroid, 0, 3 * sizeof(long long) * (size_t)v.slots, st);
   if (v.point_hwm) kb_prepass<<<blocks(v.point_hwm), kBlock, 0, st>>>(v);
   if (v.any_center && v.point_hwm) kb_center<<<blocks(v.point_hwm), kBlock, 0, st>>>(v);

@@ -558,11 +558,17 @@ __global__ void k_cells(DeviceView d, SimScalars s) {
 // the same for every point of a pass, so each launch runs one of the two).
 
 // Level l's sum for the point in finest cell (fcx, fcy).
-template <bool FAST, bool UNCHECKED = FAST>
+template <bool FAST, bool UNCHECKED = FAST, bool GUARDED = false>
 __device__ __forceinline__ float2 level_sum(const DeviceView& d, int L, int l, int fcx, int fcy, float2 p, float k,
                                             PairUnits pu) {
   const int sh = L - 1 - l;
-  return level_terms<FAST, UNCHECKED>(d.rec + d.level_off[l], 4 << l, fcx >> sh, fcy >> sh, p, k, pu);
+  return level_terms<FAST, UNCHECKED, GUARDED>(d.rec + d.level_off[l], 4 << l, fcx >> sh, fcy >> sh, p, k, pu);
+}
+
+// The level guard of a pass (SimScalars::level_guard) holds this tick: no
+// binned point lies outside the space.
+__device__ __forceinline__ bool level_guard_holds(const DeviceView& d, const SimScalars& s) {
+  return s.level_guard && __ldg(&d.big_count[kOutsideFlag]) == 0;
 }
 
 // force-nearfield.frag:151-157 (jitter, step clamp) and the update.
@@ -577,8 +583,9 @@ __device__ __forceinline__ void finish_point(const DeviceView& d, const SimScala
   if (!(d.flags[i] & kPinned)) d.pos[i] = integrate(p, vel.x, vel.y, s.friction, s.space);
 }
 
-// One point, all of its terms in order on one thread.
-template <bool FAST>
+// One point, all of its terms in order on one thread (GUARDED: the level
+// terms without the range flag, level_guard_holds).
+template <bool FAST, bool GUARDED = false>
 __device__ __forceinline__ void manybody_point(const DeviceView& d, const SimScalars& s, uint32_t j, float k) {
   const uint32_t i = d.sorted_idx[j];
   const float2 p = d.sorted_pos[j];
@@ -587,7 +594,7 @@ __device__ __forceinline__ void manybody_point(const DeviceView& d, const SimSca
   const PairUnits pu = s.units;
   float2 vel = make_float2(0.f, 0.f);
 #pragma unroll 1
-  for (int l = 0; l < L; ++l) vel = add2(vel, level_sum<FAST>(d, L, l, fcx, fcy, p, k, pu), pu);
+  for (int l = 0; l < L; ++l) vel = add2(vel, level_sum<FAST, FAST, GUARDED>(d, L, l, fcx, fcy, p, k, pu), pu);
   const float2 rj = d.jitter[i];
   const float2 nf = near_terms<FAST>(d.rec + d.level_off[L - 1], d.cell_start, d.sorted_pos, gf, fcx, fcy, j, p, rj, k, pu);
   finish_point(d, s, i, p, rj, vel, nf, pu);
@@ -602,7 +609,7 @@ __device__ __forceinline__ void manybody_point(const DeviceView& d, const SimSca
 // do not fill the GPU with one thread per point.
 constexpr int kSplitPoints = kBlock / 16;
 
-template <bool FAST>
+template <bool FAST, bool GUARDED>
 __device__ __forceinline__ void manybody_split(const DeviceView& d, const SimScalars& s, float k,
                                                float2 (&lvs)[kSplitPoints][8], float2 (&nfs)[kSplitPoints][9],
                                                bool (&nfa)[kSplitPoints][9]) {
@@ -619,7 +626,7 @@ __device__ __forceinline__ void manybody_split(const DeviceView& d, const SimSca
     const float2 p = d.sorted_pos[j];
     const int fcx = cell_index(p.x, s.csf, gf), fcy = cell_index(p.y, s.csf, gf);
     if (level_role) {
-      if (part < L) lvs[pt][part] = level_sum<FAST, false>(d, L, part, fcx, fcy, p, k, pu);
+      if (part < L) lvs[pt][part] = level_sum<FAST, GUARDED, GUARDED>(d, L, part, fcx, fcy, p, k, pu);
     } else {
       const float2 rj = d.jitter[i];
       const float4* fine = d.rec + d.level_off[L - 1];
@@ -651,8 +658,9 @@ __global__ void __launch_bounds__(kBlock) k_manybody_split(DeviceView d, SimScal
   __shared__ bool nfa[kSplitPoints][9];
   const TickParams tp = tick_params(d);
   const float k = __fmul_rn(tp.alpha, s.repulsion);
-  if (quotient_by_recip(k)) manybody_split<true>(d, s, k, lvs, nfs, nfa);
-  else manybody_split<false>(d, s, k, lvs, nfs, nfa);
+  if (!quotient_by_recip(k)) manybody_split<false, false>(d, s, k, lvs, nfs, nfa);
+  else if (level_guard_holds(d, s)) manybody_split<true, true>(d, s, k, lvs, nfs, nfa);
+  else manybody_split<true, false>(d, s, k, lvs, nfs, nfa);
 }
 
 // Two points of one finest cell per thread (manybody_duo.cuh): every result
@@ -729,8 +737,9 @@ __global__ void __launch_bounds__(kBlock, 6) k_manybody(DeviceView d, SimScalars
   const uint32_t total = d.cell_start[s.gf * s.gf];
   if (j >= total) return;
   const float k = __fmul_rn(tp.alpha, s.repulsion);
-  if (quotient_by_recip(k)) manybody_point<true>(d, s, j, k);
-  else manybody_point<false>(d, s, j, k);
+  if (!quotient_by_recip(k)) manybody_point<false>(d, s, j, k);
+  else if (level_guard_holds(d, s)) manybody_point<true, true>(d, s, j, k);
+  else manybody_point<true>(d, s, j, k);
 }
 
 // ------------------------------------------------------------------- link --

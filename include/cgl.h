@@ -378,6 +378,12 @@ cgl_status cgl_batch_remove(cgl_batch* b, uint32_t id);
 cgl_status cgl_batch_step(cgl_batch* b, uint32_t ticks);
 cgl_status cgl_batch_synchronize(cgl_batch* b);
 cgl_status cgl_batch_get_point_positions(cgl_batch* b, uint32_t id, float* out_xy, uint64_t capacity_floats);
+/* The positions of `count` jobs at once: outs[k] (host memory, capacity_floats[k]
+ * floats, at least 2 x points) receives job ids[k]'s [x0,y0,x1,y1,...].  One
+ * device-to-host copy of the batch's point arena through a pinned staging
+ * buffer kept by the batch; synchronises the batch's stream. */
+cgl_status cgl_batch_get_positions_many(cgl_batch* b, uint32_t count, const uint32_t* ids, float* const* outs,
+                                        const uint64_t* capacity_floats);
 cgl_status cgl_batch_get_state(cgl_batch* b, uint32_t id, cgl_state* out);
 cgl_status cgl_batch_get_info(cgl_batch* b, cgl_batch_info* out);
 const char* cgl_batch_last_error(cgl_batch* b);

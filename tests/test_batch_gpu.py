@@ -66,10 +66,12 @@ def test_batch_equals_each_job_alone():
         assert info.jobs == len(jobs)
         b.step(5)
         b.step(ticks - 5)
-        for (pos, links, fields), jid in zip(jobs, ids):
+        many = b.get_positions_many(ids[::-1])[::-1]
+        for (pos, links, fields), jid, got2 in zip(jobs, ids, many):
             got = b.get_point_positions(jid)
             want = _alone(pos, links, fields, ticks)
             assert same_bits(got, want), (fields, first_mismatch(got, want))
+            assert same_bits(got2, want)
             assert b.state(jid).tick == ticks
 
 
