@@ -26,6 +26,7 @@
 #include "batch.cuh"
 #include "ingest.h"
 #include "ingest_device.cuh"
+#include "kernels.cuh"
 
 using namespace cgl;
 
@@ -88,6 +89,15 @@ struct Job {
   uint32_t max_ticks = 0;
   bool stop_below_min = false;
   std::vector<uint32_t> heavy_in, heavy_out;   // local
+  // the lists as rows (CSR) in the row and entry arenas: every row when the
+  // device builds them, else only for a direction with long lists (the light
+  // rows are read from the warp layout)
+  uint64_t rows_n[2] = {0, 0}, ents_n[2] = {0, 0};
+  // the light rows by warps (GraphDesc::lr, lw, ln, nw), both directions in one
+  // range of each arena: rows, warp offsets, entries
+  uint64_t lr_off = 0, lrs = 0, lw_off = 0, lws = 0, ln_off = 0, lns = 0;
+  uint32_t nw[2] = {0, 0};
+  uint64_t lane_ents[2] = {0, 0};
   GraphDesc desc{};
 };
 
@@ -100,19 +110,23 @@ struct cgl_batch {
   cudaStream_t stream = nullptr, side = nullptr;
   cudaEvent_t fork[2] = {}, join[2] = {}, params_copied = nullptr;
   bool params_pending = false;
-  Arena pts, cells, recs, accs, rows, ents, colls;
+  Arena pts, cells, recs, accs, rows, ents, colls, lrows, lwoffs, lanes_a;
   std::vector<Job> jobs;
   size_t dev_bytes = 0;
   // point arena
   Buf gid, pos, pos_alt, flags, jitter, key, rank, sorted_idx, sorted_pos;
   // cell arena
-  Buf counts, cell_start, cell_gid, big_list, big_sx, big_sy, big_ns, scan1, scan2;
+  Buf counts, cell_start, cell_gid, big_list, big_sx, big_sy, big_ns, scan_status, scan_seq;
   Buf big_count, tick_ctr;
   Buf rec, acc, rowptr, ent, desc, tiles, heavy_in, heavy_out, ticks;
   Buf size, cgrid_acc, cgrid, coll_gid, centroid;   // collision and center
+  Buf lrow, lwoff, lanes, lwork[2];                   // light rows by warps
+  uint32_t n_lwork[2] = {0, 0};
   bool any_center = false, any_collision = false;
   uint32_t n_tiles = 0, n_heavy_in = 0, n_heavy_out = 0, slots_cap = 0;
   BatchTick* h_ticks = nullptr;
+  uint32_t* h_error = nullptr;   // host-mapped error word (BatchView::error_word)
+  uint32_t* d_error = nullptr;
   float2* h_stage = nullptr;   // pinned read-back staging of the point arena
   uint64_t stage_cap = 0;
   cudaGraphExec_t graph = nullptr;
@@ -181,6 +195,17 @@ cgl_status grow(cgl_batch* b, Buf& x, size_t bytes, size_t keep, int fill) {
   return CGL_OK;
 }
 
+// After a synchronisation: a device wait that gave up (error_word) is
+// reported once, as a CUDA error of the call that found it.
+cgl_status batch_device_error(cgl_batch* b) {
+  if (!b->h_error) return CGL_OK;
+  const uint32_t bits = *(volatile uint32_t*)b->h_error;
+  if (!bits) return CGL_OK;
+  *(volatile uint32_t*)b->h_error = 0;
+  return bfail(b, CGL_CUDA_ERROR, "a device wait gave up (error bits 0x%x): the last ticks' cell scan is not valid",
+               bits);
+}
+
 uint64_t grown(uint64_t cap, uint64_t need) { return std::max<uint64_t>(need, cap + cap / 2 + 1024); }
 
 cgl_status reserve_points(cgl_batch* b, uint64_t cap) {
@@ -201,12 +226,12 @@ cgl_status reserve_cells(cgl_batch* b, uint64_t cap) {
   if (cap <= b->cells.cap) return CGL_OK;
   const uint64_t keep = b->cells.hwm;
   cgl_status st;
-  const uint64_t n1 = cap / 1024 + 2, n2 = n1 / 1024 + 2;
+  const uint64_t chunks = batch_scan_blocks((uint32_t)std::min<uint64_t>(cap, 0xFFFFFFFFull)) + 1;
   if ((st = grow(b, b->counts, cap * 4, keep * 4, 0)) || (st = grow(b, b->cell_start, (cap + 1) * 4, 0, 0)) ||
       (st = grow(b, b->cell_gid, cap * 4, keep * 4, 0xFF)) || (st = grow(b, b->big_list, 2 * cap * 4, 0, -1)) ||
       (st = grow(b, b->big_sx, cap * 8, 0, -1)) || (st = grow(b, b->big_sy, cap * 8, 0, -1)) ||
-      (st = grow(b, b->big_ns, cap * 4, 0, -1)) || (st = grow(b, b->scan1, n1 * 4, 0, -1)) ||
-      (st = grow(b, b->scan2, n2 * 4, 0, -1)))
+      (st = grow(b, b->big_ns, cap * 4, 0, -1)) || (st = grow(b, b->scan_status, chunks * 8, 0, 0)) ||
+      (st = grow(b, b->scan_seq, 8, 0, 0)))
     return st;
   b->cells.cap = cap;
   return CGL_OK;
@@ -243,8 +268,9 @@ void refresh_view(cgl_batch* b) {
   v.sorted_pos = (float2*)b->sorted_pos.p;
   v.counts = (uint32_t*)b->counts.p;
   v.cell_start = (uint32_t*)b->cell_start.p;
-  v.scan1 = (uint32_t*)b->scan1.p;
-  v.scan2 = (uint32_t*)b->scan2.p;
+  v.scan_status = (unsigned long long*)b->scan_status.p;
+  v.scan_seq = (unsigned long long*)b->scan_seq.p;
+  v.error_word = b->d_error;
   v.big_list = (uint32_t*)b->big_list.p;
   v.big_count = (uint32_t*)b->big_count.p;
   v.big_sx = (long long*)b->big_sx.p;
@@ -256,6 +282,13 @@ void refresh_view(cgl_batch* b) {
   v.n_tiles = b->n_tiles;
   v.rowptr = (const uint32_t*)b->rowptr.p;
   v.ent = (const uint4*)b->ent.p;
+  v.lrow = (const uint32_t*)b->lrow.p;
+  v.lwoff = (const uint32_t*)b->lwoff.p;
+  v.lanes = (const uint4*)b->lanes.p;
+  for (int d = 0; d < 2; ++d) {
+    v.lwork[d] = (const uint2*)b->lwork[d].p;
+    v.n_lwork[d] = b->n_lwork[d];
+  }
   v.heavy_in = (const uint32_t*)b->heavy_in.p;
   v.n_heavy_in = b->n_heavy_in;
   v.heavy_out = (const uint32_t*)b->heavy_out.p;
@@ -280,6 +313,7 @@ cgl_status rebuild_tables(cgl_batch* b) {
   std::vector<GraphDesc> descs(slots);
   std::vector<uint2> tiles;
   std::vector<uint32_t> hin, hout;
+  std::vector<uint2> lwork[2];
   b->any_center = b->any_collision = false;
   for (size_t g = 0; g < slots; ++g) {
     const Job& j = b->jobs[g];
@@ -293,6 +327,8 @@ cgl_status rebuild_tables(cgl_batch* b) {
     }
     for (uint32_t p : j.heavy_in) hin.push_back((uint32_t)j.p_off + p);
     for (uint32_t p : j.heavy_out) hout.push_back((uint32_t)j.p_off + p);
+    for (int d = 0; d < 2; ++d)
+      for (uint32_t w = 0; w < j.nw[d]; w += kLinkWarpsPerBlock) lwork[d].push_back(make_uint2((uint32_t)g, w));
   }
   cgl_status st;
   if ((st = grow(b, b->desc, std::max<size_t>(slots, 1) * sizeof(GraphDesc), 0, 0))) return st;
@@ -300,6 +336,12 @@ cgl_status rebuild_tables(cgl_batch* b) {
   if ((st = grow(b, b->heavy_in, std::max<size_t>(hin.size(), 1) * 4, 0, -1))) return st;
   if ((st = grow(b, b->heavy_out, std::max<size_t>(hout.size(), 1) * 4, 0, -1))) return st;
   if ((st = grow(b, b->centroid, std::max<size_t>(slots, 1) * 3 * sizeof(long long), 0, 0))) return st;
+  for (int d = 0; d < 2; ++d) {
+    if ((st = grow(b, b->lwork[d], std::max<size_t>(lwork[d].size(), 1) * sizeof(uint2), 0, -1))) return st;
+    if (!lwork[d].empty())
+      BCU(cudaMemcpyAsync(b->lwork[d].p, lwork[d].data(), lwork[d].size() * sizeof(uint2), cudaMemcpyHostToDevice,
+                          b->stream));
+  }
   if (slots) BCU(cudaMemcpyAsync(b->desc.p, descs.data(), slots * sizeof(GraphDesc), cudaMemcpyHostToDevice, b->stream));
   if (!tiles.empty())
     BCU(cudaMemcpyAsync(b->tiles.p, tiles.data(), tiles.size() * sizeof(uint2), cudaMemcpyHostToDevice, b->stream));
@@ -316,6 +358,7 @@ cgl_status rebuild_tables(cgl_batch* b) {
   b->n_tiles = (uint32_t)tiles.size();
   b->n_heavy_in = (uint32_t)hin.size();
   b->n_heavy_out = (uint32_t)hout.size();
+  for (int d = 0; d < 2; ++d) b->n_lwork[d] = (uint32_t)lwork[d].size();
   refresh_view(b);
   return CGL_OK;
 }
@@ -325,6 +368,9 @@ cgl_status prepare(cgl_batch* b) {
   cgl_status st = rebuild_tables(b);
   if (st) return st;
   if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+  // the scan's status words and tickets start from zero together (its chunk count may have changed)
+  if (b->scan_status.p) BCU(cudaMemsetAsync(b->scan_status.p, 0, b->scan_status.bytes, b->stream));
+  if (b->scan_seq.p) BCU(cudaMemsetAsync(b->scan_seq.p, 0, b->scan_seq.bytes, b->stream));
   cudaGraph_t g = nullptr;
   BCU(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   batch_launch_tick(b->view, b->stream, b->side, b->fork, b->join);
@@ -362,10 +408,13 @@ void release(cgl_batch* b, Job& j) {
   b->cells.release(j.cell_off, j.cells);
   b->recs.release(j.rec_off, j.recs);
   b->accs.release(j.acc_off, j.accs);
-  b->rows.release(j.rp_in, j.n + 1);
-  b->rows.release(j.rp_out, j.n + 1);
-  b->ents.release(j.e_in, j.m_in);
-  b->ents.release(j.e_out, j.m_out);
+  b->rows.release(j.rp_in, j.rows_n[0]);
+  b->rows.release(j.rp_out, j.rows_n[1]);
+  b->ents.release(j.e_in, j.ents_n[0]);
+  b->ents.release(j.e_out, j.ents_n[1]);
+  b->lrows.release(j.lr_off, j.lrs);
+  b->lwoffs.release(j.lw_off, j.lws);
+  b->lanes_a.release(j.ln_off, j.lns);
   b->colls.release(j.coll_off, j.coll_cells);
 }
 
@@ -394,8 +443,67 @@ struct HostJob {
   ingest::Rng rng_links;       // the stream where the link draws start
   std::vector<float> draws;    // reference stream, device build: 2m rest-length draws
   ingest::Csr cin, cout_;      // host build
+  std::vector<uint32_t> lrow, lwoff;   // host build: the light rows by warps, incoming then outgoing
+  std::vector<uint4> lanes;
   std::vector<float> sizes;    // collision: resolved point sizes
 };
+
+// The light rows of one direction by warps (GraphDesc::lr, lw, ln): rows
+// order[nh..n) in that order (every point in index order when there are no
+// lists), warp w's 32 lists interleaved by lane from woff[w], each padded with
+// absent entries to the warp's first (longest) list.  Appended to the vectors;
+// returns the warps.
+uint32_t host_warp_layout(const ingest::Csr& c, uint32_t n, uint32_t nh, std::vector<uint32_t>& lrow,
+                          std::vector<uint32_t>& woff, std::vector<uint4>& lanes, uint64_t* lane_ents) {
+  const uint32_t nw = (n - nh + 31) / 32;
+  const bool lists = !c.order.empty();
+  auto row = [&](uint32_t t) { return lists ? c.order[t] : t; };
+  auto len = [&](uint32_t p) { return c.rowptr[p + 1] - c.rowptr[p]; };
+  const size_t r0 = lrow.size(), w0 = woff.size(), l0 = lanes.size();
+  lrow.resize(r0 + 32ull * nw, kNoPoint);
+  woff.resize(w0 + nw + 1);
+  uint64_t total = 0;
+  for (uint32_t w = 0; w < nw; ++w) {
+    woff[w0 + w] = (uint32_t)total;
+    total += 32ull * len(row(nh + 32 * w));
+  }
+  woff[w0 + nw] = (uint32_t)total;
+  lanes.resize(l0 + total, make_uint4(kAbsentTarget, 0u, 0u, 0u));
+  for (uint32_t t = 0; t < n - nh; ++t) {
+    const uint32_t p = row(nh + t);
+    lrow[r0 + t] = p;
+    const uint32_t e0 = c.rowptr[p], m = len(p);
+    uint4* col = lanes.data() + l0 + woff[w0 + t / 32] + (t & 31);
+    for (uint32_t k = 0; k < m; ++k) col[32 * (size_t)k] = c.ent[e0 + k];
+  }
+  *lane_ents = total;
+  return nw;
+}
+
+// A job whose lists the host built: their sizes, long lists and warp layout.
+// Rows are kept as CSR only for a direction with long lists.
+void host_links_layout(HostJob& h) {
+  Job& j = h.j;
+  j.m_in = h.cin.ent.size();
+  j.m_out = h.cout_.ent.size();
+  j.heavy_in = h.cin.heavy;
+  j.heavy_out = h.cout_.heavy;
+  h.lrow.clear();
+  h.lwoff.clear();
+  h.lanes.clear();
+  j.nw[0] = host_warp_layout(h.cin, (uint32_t)j.n, (uint32_t)j.heavy_in.size(), h.lrow, h.lwoff, h.lanes,
+                             &j.lane_ents[0]);
+  j.nw[1] = host_warp_layout(h.cout_, (uint32_t)j.n, (uint32_t)j.heavy_out.size(), h.lrow, h.lwoff, h.lanes,
+                             &j.lane_ents[1]);
+  for (int d = 0; d < 2; ++d) {
+    const bool heavy = !(d == 0 ? j.heavy_in : j.heavy_out).empty();
+    j.rows_n[d] = heavy ? j.n + 1 : 0;
+    j.ents_n[d] = heavy ? (d == 0 ? j.m_in : j.m_out) : 0;
+  }
+  j.lrs = 32ull * (j.nw[0] + j.nw[1]);
+  j.lws = (uint64_t)j.nw[0] + 1 + j.nw[1] + 1;
+  j.lns = j.lane_ents[0] + j.lane_ents[1];
+}
 
 cgl_status prep_fail(HostJob& h, cgl_status st, const char* fmt, ...) {
   char buf[512];
@@ -437,7 +545,7 @@ cgl_status prepare_job(const cgl_batch_job& in, HostJob& h) {
   const ingest::Grid grid = ingest::grid_for(j.n);
   j.gf = grid.gf;
   j.levels = grid.levels;
-  j.tile = std::min(16, j.gf);
+  j.tile = std::min(32, j.gf);   // kb_cells: 2 x 2 cells per thread
   // the jitter draws come first (ForceManyBody.create), then the link draws
   const uint64_t T = (uint64_t)std::ceil(std::sqrt((double)j.n));
   h.dev_jitter = j.rng.counter && !(cfg->device_ingest_min_links > (double)j.n);
@@ -461,13 +569,12 @@ cgl_status prepare_job(const cgl_batch_job& in, HostJob& h) {
       j.rng.ctr += 2 * m;
     }
     j.m_in = j.m_out = m;
+    j.rows_n[0] = j.rows_n[1] = j.n + 1;
+    j.ents_n[0] = j.ents_n[1] = m;
   } else {
     if (h.has_links) ingest::build_links(in.links, j.E, j.n, nullptr, h.absent, j.rng, h.cin, h.cout_);
     else { h.cin.rowptr.assign(j.n + 1, 0); h.cout_.rowptr.assign(j.n + 1, 0); }
-    j.m_in = h.cin.ent.size();
-    j.m_out = h.cout_.ent.size();
-    j.heavy_in = h.cin.heavy;
-    j.heavy_out = h.cout_.heavy;
+    host_links_layout(h);
   }
   j.stages = 0;
   if (cfg->simulation_gravity != 0 && (mask & CGL_STAGE_GRAVITY)) j.stages |= kGGravity;
@@ -529,6 +636,8 @@ cgl_status commit_job(cgl_batch* b, HostJob& h, uint32_t* id) {
   float* d_draws = nullptr;
   uint32_t *d_valid = nullptr, *d_len_in = nullptr, *d_len_out = nullptr, *d_tmp = nullptr, *d_stats = nullptr;
   uint32_t *d_kin = nullptr, *d_kout = nullptr, *d_vin = nullptr, *d_vout = nullptr;
+  uint32_t* d_ord[2] = {nullptr, nullptr};   // rows by list length
+  uint32_t* d_wo[2] = {nullptr, nullptr};    // warp layout offsets
   if (dev_links) {
     d_links = tmp.get<float2>(j.E);
     d_valid = tmp.get<uint32_t>(j.E + 1);
@@ -549,10 +658,7 @@ cgl_status commit_job(cgl_batch* b, HostJob& h, uint32_t* id) {
     // stream (it draws the same 2m values prepare_job drew)
     j.rng = h.rng_links;
     ingest::build_links(h.links, j.E, j.n, nullptr, h.absent, j.rng, h.cin, h.cout_);
-    j.m_in = h.cin.ent.size();
-    j.m_out = h.cout_.ent.size();
-    j.heavy_in = h.cin.heavy;
-    j.heavy_out = h.cout_.heavy;
+    host_links_layout(h);
   }
   uint32_t dev_stats[4] = {0, 0, 0, 0};
   if (dev_links) {
@@ -573,6 +679,33 @@ cgl_status commit_job(cgl_batch* b, HostJob& h, uint32_t* id) {
     BCU(cudaMemcpyAsync(dev_stats, d_stats, 16, cudaMemcpyDeviceToHost, s));
     BCU(cudaStreamSynchronize(s));
     if (dev_m != h.m) return bfail(b, CGL_CUDA_ERROR, "link count %u on the device, %u on the host", dev_m, h.m);
+    // each direction's rows by list length, longest first (the long lists are
+    // its first stats[1] / stats[3]), and the warp layout's offsets: sizes
+    // known before the arena ranges are taken
+    uint32_t lane_tot[2] = {0, 0};
+    for (int d = 0; d < 2; ++d) {
+      const uint32_t nh = dev_stats[2 * d + 1];
+      j.nw[d] = (N32 - nh + 31) / 32;
+      d_ord[d] = tmp.get<uint32_t>(j.n);
+      d_wo[d] = tmp.get<uint32_t>(j.nw[d] + 1);
+      if (!d_ord[d] || !d_wo[d]) return bfail(b, CGL_OOM, "link warp layout: no device memory for its temporaries");
+      uint32_t* len = d == 0 ? d_len_in : d_len_out;
+      dingest::len_keys(len, N32, d_stats + 2 * d, d_kout, d_ord[d], s);
+      dingest::sort_pairs(d_kout, d_ord[d], N32, dingest::key_bits(dev_stats[2 * d]), d_tmp, s);
+      batch_warp_lengths(d_ord[d], len, nh, N32, d_wo[d], s);
+      dingest::scan_exclusive(d_wo[d], j.nw[d] + 1, d_tmp, s);
+      BCU(cudaMemcpyAsync(&lane_tot[d], d_wo[d] + j.nw[d], 4, cudaMemcpyDeviceToHost, s));
+      std::vector<uint32_t>& hv = d == 0 ? j.heavy_in : j.heavy_out;
+      hv.resize(nh);
+      if (nh) BCU(cudaMemcpyAsync(hv.data(), d_ord[d], nh * 4, cudaMemcpyDeviceToHost, s));
+    }
+    BCU(cudaGetLastError());
+    BCU(cudaStreamSynchronize(s));
+    j.lane_ents[0] = lane_tot[0];
+    j.lane_ents[1] = lane_tot[1];
+    j.lrs = 32ull * (j.nw[0] + j.nw[1]);
+    j.lws = (uint64_t)j.nw[0] + 1 + j.nw[1] + 1;
+    j.lns = j.lane_ents[0] + j.lane_ents[1];
   }
   // arena ranges (grow the arenas when full)
   cgl_status st;
@@ -586,9 +719,12 @@ cgl_status commit_job(cgl_batch* b, HostJob& h, uint32_t* id) {
     else if (kind == 3) s2 = grow(b, b->acc, cap * 3 * sizeof(long long), a.hwm * 3 * sizeof(long long), 0);
     else if (kind == 4) s2 = grow(b, b->rowptr, cap * 4, a.hwm * 4, -1);
     else if (kind == 5) s2 = grow(b, b->ent, cap * sizeof(uint4), a.hwm * sizeof(uint4), -1);
-    else s2 = reserve_colls(b, cap);
+    else if (kind == 6) s2 = reserve_colls(b, cap);
+    else if (kind == 7) s2 = grow(b, b->lrow, cap * 4, a.hwm * 4, -1);
+    else if (kind == 8) s2 = grow(b, b->lwoff, cap * 4, a.hwm * 4, -1);
+    else s2 = grow(b, b->lanes, cap * sizeof(uint4), a.hwm * sizeof(uint4), -1);
     if (s2) return s2;
-    if (kind >= 2 && kind <= 5) a.cap = cap;
+    if ((kind >= 2 && kind <= 5) || kind >= 7) a.cap = cap;
     b->dirty = true;
     return a.alloc(n, off) ? CGL_OK : bfail(b, CGL_OOM, "arena allocation failed");
   };
@@ -596,9 +732,10 @@ cgl_status commit_job(cgl_batch* b, HostJob& h, uint32_t* id) {
   struct Want { Arena* a; uint64_t n; uint64_t* off; int kind; };
   const Want wants[] = {{&b->pts, j.n, &j.p_off, 0},        {&b->cells, j.cells, &j.cell_off, 1},
                         {&b->recs, j.recs, &j.rec_off, 2},   {&b->accs, j.accs, &j.acc_off, 3},
-                        {&b->rows, j.n + 1, &j.rp_in, 4},    {&b->rows, j.n + 1, &j.rp_out, 4},
-                        {&b->ents, j.m_in, &j.e_in, 5},      {&b->ents, j.m_out, &j.e_out, 5},
-                        {&b->colls, j.coll_cells, &j.coll_off, 6}};
+                        {&b->rows, j.rows_n[0], &j.rp_in, 4}, {&b->rows, j.rows_n[1], &j.rp_out, 4},
+                        {&b->ents, j.ents_n[0], &j.e_in, 5}, {&b->ents, j.ents_n[1], &j.e_out, 5},
+                        {&b->colls, j.coll_cells, &j.coll_off, 6}, {&b->lrows, j.lrs, &j.lr_off, 7},
+                        {&b->lwoffs, j.lws, &j.lw_off, 8},   {&b->lanes_a, j.lns, &j.ln_off, 9}};
   int taken = 0;
   st = CGL_OK;
   for (const Want& w : wants) {
@@ -606,7 +743,8 @@ cgl_status commit_job(cgl_batch* b, HostJob& h, uint32_t* id) {
     ++taken;
   }
   if (!st && (b->pts.hwm > 0xFFFFFF00ull || b->cells.hwm > 0xFFFFFF00ull || b->ents.hwm > 0xFFFFFF00ull ||
-              b->colls.hwm > 0xFFFFFF00ull))
+              b->colls.hwm > 0xFFFFFF00ull || b->lrows.hwm > 0xFFFFFF00ull || b->lwoffs.hwm > 0xFFFFFF00ull ||
+              b->lanes_a.hwm > 0xFFFFFF00ull))
     st = bfail(b, CGL_OOM, "arena index space (32 bits) exhausted");
   if (st) {
     for (int k = 0; k < taken; ++k) wants[k].a->release(*wants[k].off, wants[k].n);
@@ -625,18 +763,7 @@ cgl_status commit_job(cgl_batch* b, HostJob& h, uint32_t* id) {
                    cudaGetErrorString(_e));                                                          \
     }                                                                                                \
   } while (0)
-  // upload: absolute indices for rows and neighbours
-  std::vector<uint32_t> rp_in, rp_out;
-  if (!dev_links) {
-    rp_in.resize(j.n + 1);
-    rp_out.resize(j.n + 1);
-    for (uint64_t i = 0; i <= j.n; ++i) {
-      rp_in[i] = (uint32_t)(j.e_in + h.cin.rowptr[i]);
-      rp_out[i] = (uint32_t)(j.e_out + h.cout_.rowptr[i]);
-    }
-    for (auto& e : h.cin.ent) if (e.x != kAbsentTarget) e.x += (uint32_t)j.p_off;
-    for (auto& e : h.cout_.ent) if (e.x != kAbsentTarget) e.x += (uint32_t)j.p_off;
-  }
+  // rows, entries and neighbours stay graph-local (the kernels add the job's offsets)
   std::vector<uint8_t> flags(j.n);
   for (uint64_t i = 0; i < j.n; ++i) flags[i] = h.absent[i] ? kAbsent : 0;
   const uint32_t g = [&]() {
@@ -674,33 +801,36 @@ cgl_status commit_job(cgl_batch* b, HostJob& h, uint32_t* id) {
     dingest::sort_pairs(d_kout, d_vout, M, row_bits, d_tmp, s);
     const uint64_t links_base = h.rng_links.ctr;
     dingest::fill_csr(d_kin, d_vin, M, d_links, true, d_len_in, d_len_out, nullptr, flags_j, d_draws, j.rng.seed,
-                      links_base, (uint32_t)j.p_off, (uint4*)b->ent.p + j.e_in, s);
+                      links_base, 0u, (uint4*)b->ent.p + j.e_in, s);
     dingest::fill_csr(d_kout, d_vout, M, d_links, false, d_len_in, d_len_out, nullptr, flags_j,
-                      d_draws ? d_draws + M : nullptr, j.rng.seed, links_base + M, (uint32_t)j.p_off,
-                      (uint4*)b->ent.p + j.e_out, s);
-    // the long lists (rows by length, longest first; the first stats[1] / stats[3])
-    j.heavy_in.resize(dev_stats[1]);
-    j.heavy_out.resize(dev_stats[3]);
-    for (int dir = 0; dir < 2; ++dir) {
-      std::vector<uint32_t>& hv = dir == 0 ? j.heavy_in : j.heavy_out;
-      if (hv.empty()) continue;
-      dingest::len_keys(dir == 0 ? d_len_in : d_len_out, N32, d_stats + 2 * dir, d_kin, d_vin, s);
-      dingest::sort_pairs(d_kin, d_vin, N32, dingest::key_bits(dev_stats[2 * dir]), d_tmp, s);
-      JCU(cudaMemcpyAsync(hv.data(), d_vin, hv.size() * 4, cudaMemcpyDeviceToHost, s));
+                      d_draws ? d_draws + M : nullptr, j.rng.seed, links_base + M, 0u, (uint4*)b->ent.p + j.e_out, s);
+    // row pointers (exclusive scan of the lengths), then the light rows by warps from them
+    for (int d = 0; d < 2; ++d) {
+      uint32_t* len = d == 0 ? d_len_in : d_len_out;
+      uint32_t* rp = (uint32_t*)b->rowptr.p + (d == 0 ? j.rp_in : j.rp_out);
+      dingest::scan_exclusive(len, N32 + 1, d_tmp, s);
+      dingest::copy_u32(len, rp, N32 + 1, s);
+      const uint32_t nh = dev_stats[2 * d + 1];
+      uint32_t* woff = (uint32_t*)b->lwoff.p + j.lw_off + (d == 0 ? 0 : j.nw[0] + 1);
+      JCU(cudaMemcpyAsync(woff, d_wo[d], ((size_t)j.nw[d] + 1) * 4, cudaMemcpyDeviceToDevice, s));
+      batch_warp_rows(d_ord[d], nh, N32, (uint32_t*)b->lrow.p + j.lr_off + (d == 0 ? 0 : 32ull * j.nw[0]), s);
+      if (j.lane_ents[d])
+        launch_fill_lanes(d_ord[d], rp, (const uint4*)b->ent.p + (d == 0 ? j.e_in : j.e_out), nh, N32, woff,
+                          (uint4*)b->lanes.p + j.ln_off + (d == 0 ? 0 : j.lane_ents[0]), s);
     }
-    // row pointers: exclusive scan of the lengths, offset by the entry range
-    dingest::scan_exclusive(d_len_in, N32 + 1, d_tmp, s);
-    dingest::copy_u32(d_len_in, (uint32_t*)b->rowptr.p + j.rp_in, N32 + 1, s, (uint32_t)j.e_in);
-    dingest::scan_exclusive(d_len_out, N32 + 1, d_tmp, s);
-    dingest::copy_u32(d_len_out, (uint32_t*)b->rowptr.p + j.rp_out, N32 + 1, s, (uint32_t)j.e_out);
     JCU(cudaGetLastError());
   } else {
-    JCU(cudaMemcpyAsync((uint32_t*)b->rowptr.p + j.rp_in, rp_in.data(), (j.n + 1) * 4, cudaMemcpyHostToDevice, s));
-    JCU(cudaMemcpyAsync((uint32_t*)b->rowptr.p + j.rp_out, rp_out.data(), (j.n + 1) * 4, cudaMemcpyHostToDevice, s));
-    if (j.m_in)
+    if (j.rows_n[0]) {
+      JCU(cudaMemcpyAsync((uint32_t*)b->rowptr.p + j.rp_in, h.cin.rowptr.data(), (j.n + 1) * 4, cudaMemcpyHostToDevice, s));
       JCU(cudaMemcpyAsync((uint4*)b->ent.p + j.e_in, h.cin.ent.data(), j.m_in * 16, cudaMemcpyHostToDevice, s));
-    if (j.m_out)
+    }
+    if (j.rows_n[1]) {
+      JCU(cudaMemcpyAsync((uint32_t*)b->rowptr.p + j.rp_out, h.cout_.rowptr.data(), (j.n + 1) * 4, cudaMemcpyHostToDevice, s));
       JCU(cudaMemcpyAsync((uint4*)b->ent.p + j.e_out, h.cout_.ent.data(), j.m_out * 16, cudaMemcpyHostToDevice, s));
+    }
+    JCU(cudaMemcpyAsync((uint32_t*)b->lrow.p + j.lr_off, h.lrow.data(), j.lrs * 4, cudaMemcpyHostToDevice, s));
+    JCU(cudaMemcpyAsync((uint32_t*)b->lwoff.p + j.lw_off, h.lwoff.data(), j.lws * 4, cudaMemcpyHostToDevice, s));
+    if (j.lns) JCU(cudaMemcpyAsync((uint4*)b->lanes.p + j.ln_off, h.lanes.data(), j.lns * 16, cudaMemcpyHostToDevice, s));
   }
   if (dev_links) JCU(cudaStreamSynchronize(s));   // the temporaries' kernels; pageable uploads are staged at the call
 #undef JCU
@@ -713,6 +843,16 @@ cgl_status commit_job(cgl_batch* b, HostJob& h, uint32_t* id) {
   D.acc_cells = (uint32_t)j.accs;
   D.rp_in = (uint32_t)j.rp_in;
   D.rp_out = (uint32_t)j.rp_out;
+  D.e_in = (uint32_t)j.e_in;
+  D.e_out = (uint32_t)j.e_out;
+  D.lr[0] = (uint32_t)j.lr_off;
+  D.lr[1] = (uint32_t)(j.lr_off + 32ull * j.nw[0]);
+  D.lw[0] = (uint32_t)j.lw_off;
+  D.lw[1] = (uint32_t)(j.lw_off + j.nw[0] + 1);
+  D.ln[0] = (uint32_t)j.ln_off;
+  D.ln[1] = (uint32_t)(j.ln_off + j.lane_ents[0]);
+  D.nw[0] = j.nw[0];
+  D.nw[1] = j.nw[1];
   D.gf = j.gf;
   D.levels = j.levels;
   D.tile = j.tile;
@@ -754,11 +894,14 @@ cgl_status cgl_batch_create(int32_t device, double hbm_budget_bytes, cgl_batch**
     if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming);
   }
   if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&b->params_copied, cudaEventDisableTiming);
+  if (ce == cudaSuccess) ce = cudaHostAlloc((void**)&b->h_error, sizeof(uint32_t), cudaHostAllocMapped);
+  if (ce == cudaSuccess) ce = cudaHostGetDevicePointer((void**)&b->d_error, b->h_error, 0);
   if (ce != cudaSuccess) {
     cudaGetLastError();
     cgl_batch_destroy(b);
     return CGL_CUDA_ERROR;
   }
+  *b->h_error = 0;
   cgl_status st;
   if ((st = grow(b, b->big_count, 32, 0, 0)) || (st = grow(b, b->tick_ctr, 4, 0, 0)) ||
       (st = reserve_cells(b, 1024)) || (st = reserve_points(b, 1024))) {
@@ -777,12 +920,14 @@ cgl_status cgl_batch_destroy(cgl_batch* b) {
   if (b->graph) cudaGraphExecDestroy(b->graph);
   Buf* all[] = {&b->gid, &b->pos, &b->pos_alt, &b->flags, &b->jitter, &b->key, &b->rank, &b->sorted_idx,
                 &b->sorted_pos, &b->counts, &b->cell_start, &b->cell_gid, &b->big_list, &b->big_sx, &b->big_sy,
-                &b->big_ns, &b->scan1, &b->scan2, &b->big_count, &b->tick_ctr, &b->rec, &b->acc, &b->rowptr,
+                &b->big_ns, &b->scan_status, &b->scan_seq, &b->big_count, &b->tick_ctr, &b->rec, &b->acc, &b->rowptr,
                 &b->ent, &b->desc, &b->tiles, &b->heavy_in, &b->heavy_out, &b->ticks, &b->size, &b->cgrid_acc,
-                &b->cgrid, &b->coll_gid, &b->centroid};
+                &b->cgrid, &b->coll_gid, &b->centroid, &b->lrow, &b->lwoff, &b->lanes, &b->lwork[0],
+                &b->lwork[1]};
   for (Buf* x : all)
     if (x->p) cudaFree(x->p);
   if (b->h_ticks) cudaFreeHost(b->h_ticks);
+  if (b->h_error) cudaFreeHost(b->h_error);
   if (b->h_stage) cudaFreeHost(b->h_stage);
   for (int k = 0; k < 2; ++k) {
     if (b->fork[k]) cudaEventDestroy(b->fork[k]);
@@ -918,7 +1063,7 @@ cgl_status cgl_batch_step(cgl_batch* b, uint32_t ticks) {
 cgl_status cgl_batch_synchronize(cgl_batch* b) {
   if (!b) return CGL_INVALID_ARG;
   BCU(cudaStreamSynchronize(b->stream));
-  return CGL_OK;
+  return batch_device_error(b);
 }
 
 cgl_status cgl_batch_get_point_positions(cgl_batch* b, uint32_t id, float* out, uint64_t cap) {
@@ -929,7 +1074,7 @@ cgl_status cgl_batch_get_point_positions(cgl_batch* b, uint32_t id, float* out, 
   if (cudaSetDevice(b->device) != cudaSuccess) return bfail(b, CGL_CUDA_ERROR, "cudaSetDevice");
   BCU(cudaMemcpyAsync(out, (float2*)b->pos.p + j.p_off, j.n * 8, cudaMemcpyDeviceToHost, b->stream));
   BCU(cudaStreamSynchronize(b->stream));
-  return CGL_OK;
+  return batch_device_error(b);
 }
 
 cgl_status cgl_batch_get_positions_many(cgl_batch* b, uint32_t count, const uint32_t* ids, float* const* outs,
@@ -968,7 +1113,7 @@ cgl_status cgl_batch_get_positions_many(cgl_batch* b, uint32_t count, const uint
   for (unsigned t = 1; t < nt; ++t) pool.emplace_back(worker);
   worker();
   for (auto& t : pool) t.join();
-  return CGL_OK;
+  return batch_device_error(b);
 }
 
 cgl_status cgl_batch_get_state(cgl_batch* b, uint32_t id, cgl_state* s) {
@@ -989,6 +1134,10 @@ cgl_status cgl_batch_get_state(cgl_batch* b, uint32_t id, cgl_state* s) {
 cgl_status cgl_batch_get_info(cgl_batch* b, cgl_batch_info* out) {
   if (!b || !out) return CGL_INVALID_ARG;
   std::memset(out, 0, sizeof(*out));
+  if (b->dirty) {   // the tables the next tick runs with (its kernel count)
+    const cgl_status st = rebuild_tables(b);
+    if (st) return st;
+  }
   for (const Job& j : b->jobs) {
     if (!j.used) continue;
     out->jobs++;

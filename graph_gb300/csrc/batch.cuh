@@ -15,6 +15,11 @@
 namespace cgl {
 
 constexpr uint32_t kNoGraph = 0xFFFFFFFFu;
+constexpr uint32_t kNoPoint = 0xFFFFFFFFu;
+constexpr uint32_t kLinkWarpsPerBlock = 8;   // light-row link pass: warps of one graph per block
+constexpr int kScanSub = 4;                  // scan: sub-chunks of kBlock x 4 cells per block
+constexpr int kChunk = 1024 * kScanSub;      // scan: cells per block
+constexpr uint32_t kBatchErrorScan = 1;      // error_word bit: a scan block's look-back gave up waiting
 
 // Per graph per tick: the f32 alpha uniform, the peel seed, and whether the
 // graph advances this tick (a graph that reached its tick budget, or whose
@@ -34,7 +39,14 @@ struct GraphDesc {
   uint32_t rec_off;            // level records: level l at rec_off + base(l)
   uint32_t acc_off;            // integer sums of the levels coarser than the cell-kernel tile
   uint32_t acc_cells;          // cells of those levels
-  uint32_t rp_in, rp_out;      // rowptr arena offsets (n + 1 entries each, absolute entry indices)
+  uint32_t rp_in, rp_out;      // rowptr arena offsets (n + 1 entries each, graph-local entry indices)
+  uint32_t e_in, e_out;        // entry arena offsets of the two directions' lists
+  // The light rows (lists of at most kHeavyDegree links) by warps, per
+  // direction d: warp w's 32 rows are graph-local points at lrow[lr[d] + 32 w ..]
+  // (kNoPoint: none), its entries lanes[ln[d] + lwoff[lw[d] + w] .. ln[d] +
+  // lwoff[lw[d] + w + 1]), entry k of lane l at 32 k + l, each list padded with
+  // absent entries to its warp's longest; rows by list length, longest first.
+  uint32_t lr[2], lw[2], ln[2], nw[2];
   int32_t gf, levels, tile;
   uint32_t stages;             // kG* forces this graph runs
   float space, csf, friction, gravity, repulsion;
@@ -65,8 +77,9 @@ struct BatchView {
   float2* sorted_pos;
   uint32_t* counts;            // [cell arena], zeroed by the scan
   uint32_t* cell_start;        // [cell arena + 1]
-  uint32_t* scan1;             // scan partials per 1024 cells, then per 1024^2
-  uint32_t* scan2;
+  unsigned long long* scan_status;   // one-pass scan: status word per chunk of kChunk cells
+  unsigned long long* scan_seq;      // its chunk tickets, counted up across ticks (zeroed with scan_status)
+  uint32_t* error_word;        // host-mapped: kBatchError* bits raised by a device wait that gave up
   uint32_t* big_list;          // [2 x cell arena] CTA cells, then warp cells: those above
                                // kWarpSmallCell from the front, the others from the back
   uint32_t* big_count;         // [8] CTA cells, heavy and light warp cells, warp-cell ticket, then [4] = 1
@@ -79,7 +92,12 @@ struct BatchView {
   const uint2* tiles;          // (graph, tile) work list of the cell kernel
   uint32_t n_tiles;
   const uint32_t* rowptr;
-  const uint4* ent;            // neighbour = absolute arena point index or kAbsentTarget
+  const uint4* ent;            // neighbour = graph-local point index or kAbsentTarget
+  const uint32_t* lrow;        // light rows by warps (GraphDesc::lr, lw, ln, nw)
+  const uint32_t* lwoff;
+  const uint4* lanes;
+  const uint2* lwork[2];       // (graph, first warp) of each block of the light-row link pass, per direction
+  uint32_t n_lwork[2];
   const uint32_t* heavy_in;    // absolute points with long incoming lists
   uint32_t n_heavy_in;
   const uint32_t* heavy_out;
@@ -97,6 +115,15 @@ struct BatchView {
   uint32_t coll_hwm;           // collision cells in use
   int any_center, any_collision;   // some job runs the force (its kernels are launched)
 };
+
+// Light rows by warps on the device (batch_kernels.cu): woff[w] = 32 x the
+// length of row order[nh + 32 w] (w < nw), 0 at nw; lrow[t] = order[nh + t]
+// (t < n - nh), kNoPoint up to 32 nw.
+void batch_warp_lengths(const uint32_t* order, const uint32_t* len, uint32_t nh, uint32_t n, uint32_t* woff,
+                        cudaStream_t st);
+void batch_warp_rows(const uint32_t* order, uint32_t nh, uint32_t n, uint32_t* lrow, cudaStream_t st);
+
+uint32_t batch_scan_blocks(uint32_t cells);   // blocks of the one-pass scan over `cells` cells
 
 void batch_launch_tick(const BatchView& v, cudaStream_t st, cudaStream_t side, cudaEvent_t* fork, cudaEvent_t* join);
 uint32_t batch_kernels_per_tick(const BatchView& v);

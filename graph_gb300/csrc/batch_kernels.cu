@@ -13,7 +13,6 @@
 namespace cgl {
 namespace {
 
-constexpr int kChunk = 1024;   // scan: cells per block (kBlock threads x 4)
 
 __device__ __forceinline__ const BatchTick& tick_of(const BatchView& v, uint32_t g) {
   return v.ticks[(size_t)(*v.tick_ctr) * v.slots + g];
@@ -140,68 +139,65 @@ __global__ void __launch_bounds__(kBlock) kb_center(BatchView v) {
 }
 
 // ------------------------------------------------------------------- scan --
-// Three-level exclusive scan of the cell histogram over the used cell arena.
-__global__ void __launch_bounds__(kBlock) kb_scan_reduce(const uint32_t* in, uint32_t n, uint32_t* out) {
-  const uint32_t base = blockIdx.x * kChunk;
-  uint32_t sum = 0;
+// The cell histogram's exclusive scan over the used cell arena in one pass
+// (device_util.cuh's look-back): cell starts, the histogram zeroed for the
+// next tick, the dense cells listed.  A block scans kChunk cells as kScanSub
+// coalesced sub-chunks of kBlock x 4 (one look-back per block: more bytes in
+// flight per wait).  cell_hwm is a multiple of 64 (every range is a
+// power-of-two grid of at least 8 x 8), so a thread's four cells of a
+// sub-chunk are all inside or all outside.
+__global__ void __launch_bounds__(kBlock) kb_scan(BatchView v) {
+  __shared__ unsigned long long s_seq, s_prefix;
+  if (threadIdx.x == 0) s_seq = atomicAdd(v.scan_seq, 1ull);
+  __syncthreads();
+  const uint32_t n = v.cell_hwm, nb = gridDim.x;
+  const uint32_t vb = (uint32_t)(s_seq % nb);
+  const unsigned long long parity = ((s_seq / nb) & 1ull) << 63;
+  uint4 x[kScanSub];
+  unsigned long long off[kScanSub], tot[kScanSub];
+  unsigned long long total = 0;
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const uint32_t c = base + k * kBlock + threadIdx.x;
-    if (c < n) sum += in[c];
+  for (int k = 0; k < kScanSub; ++k) {
+    const uint32_t base = vb * kChunk + k * (kBlock * 4) + threadIdx.x * 4;
+    x[k] = base < n ? reinterpret_cast<const uint4*>(v.counts)[base >> 2] : make_uint4(0u, 0u, 0u, 0u);
   }
-  uint32_t total;
-  block_exclusive_scan(sum, &total);
-  if (threadIdx.x == 0) out[blockIdx.x] = total;
-}
-
-// Exclusive scan of `n` values in chunks of kChunk, plus the chunk offsets
-// `off` (nullptr: none); the grand total goes to total_out when non-null.
-__global__ void __launch_bounds__(kBlock) kb_scan_down(uint32_t* vals, uint32_t n, const uint32_t* off,
-                                                       uint32_t* out, uint32_t* total_out) {
-  const uint32_t base = blockIdx.x * kChunk + threadIdx.x * 4;
-  uint32_t x[4];
-  uint32_t run = 0;
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    x[k] = base + k < n ? vals[base + k] : 0;
-    run += x[k];
+  for (int k = 0; k < kScanSub; ++k) {
+    off[k] = block_exclusive_scan64((unsigned long long)x[k].x + x[k].y + x[k].z + x[k].w, &tot[k]);
+    total += tot[k];
   }
-  uint32_t total;
-  uint32_t o = block_exclusive_scan(run, &total) + (off ? off[blockIdx.x] : 0);
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    if (base + k < n) out[base + k] = o;
-    o += x[k];
-  }
-  if (total_out && threadIdx.x == 0) *total_out = total;
-}
-
-// Last level: cell starts, histogram zeroed, dense cells listed.
-__global__ void __launch_bounds__(kBlock) kb_scan_cells(BatchView v, const uint32_t* off) {
-  const uint32_t n = v.cell_hwm;
-  const uint32_t base = blockIdx.x * kChunk + threadIdx.x * 4;
-  uint32_t x[4];
-  uint32_t run = 0;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    x[k] = base + k < n ? v.counts[base + k] : 0;
-    run += x[k];
-  }
-  uint32_t total;
-  uint32_t o = block_exclusive_scan(run, &total) + off[blockIdx.x];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const uint32_t c = base + k;
-    if (c < n) {
-      v.cell_start[c] = o;
-      v.counts[c] = 0;
-      if (x[k] > kBigCell) v.big_list[atomicAdd(&v.big_count[0], 1u)] = c;
-      else if (x[k] > kWarpSmallCell) v.big_list[n + atomicAdd(&v.big_count[1], 1u)] = c;
-      else if (x[k] > kSmallCell) v.big_list[2 * n - 1 - atomicAdd(&v.big_count[2], 1u)] = c;
+  if (threadIdx.x < 32) {
+    unsigned long long prefix = 0;
+    if (vb == 0) {
+      if (threadIdx.x == 0) st_relaxed_u64(&v.scan_status[0], parity | kScanInclusive | total);
+    } else {
+      if (threadIdx.x == 0) st_relaxed_u64(&v.scan_status[vb], parity | kScanTotal | total);
+      prefix = scan_look_back(v.scan_status, vb, parity, v.error_word, kBatchErrorScan);
+      if (threadIdx.x == 0) st_relaxed_u64(&v.scan_status[vb], parity | kScanInclusive | ((prefix + total) & kScanValue));
     }
-    o += x[k];
+    if (threadIdx.x == 0) s_prefix = prefix;
   }
-  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == kBlock - 1) v.cell_start[n] = o;
+  __syncthreads();
+  unsigned long long run = s_prefix;
+#pragma unroll
+  for (int k = 0; k < kScanSub; ++k) {
+    const uint32_t base = vb * kChunk + k * (kBlock * 4) + threadIdx.x * 4;
+    if (base < n) {
+      const uint32_t o0 = (uint32_t)(run + off[k]), o1 = o0 + x[k].x, o2 = o1 + x[k].y, o3 = o2 + x[k].z;
+      reinterpret_cast<uint4*>(v.cell_start)[base >> 2] = make_uint4(o0, o1, o2, o3);
+      reinterpret_cast<uint4*>(v.counts)[base >> 2] = make_uint4(0u, 0u, 0u, 0u);
+      const uint32_t cnt[4] = {x[k].x, x[k].y, x[k].z, x[k].w};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const uint32_t c = base + q;
+        if (cnt[q] > kBigCell) v.big_list[atomicAdd(&v.big_count[0], 1u)] = c;
+        else if (cnt[q] > kWarpSmallCell) v.big_list[n + atomicAdd(&v.big_count[1], 1u)] = c;
+        else if (cnt[q] > kSmallCell) v.big_list[2 * n - 1 - atomicAdd(&v.big_count[2], 1u)] = c;
+      }
+    }
+    run += tot[k];
+  }
+  if (vb == nb - 1 && threadIdx.x == 0) v.cell_start[n] = (uint32_t)(s_prefix + total);
 }
 
 // ---------------------------------------------------------------- scatter --
@@ -338,9 +334,60 @@ __global__ void __launch_bounds__(kBlock) kb_bigcells(BatchView v) {
   }
 }
 
-// One CTA per (graph, tile) of the work list; thread per finest cell of the
-// tile; levels inside the tile by shared-memory reduction, coarser levels by
-// integer atomics finished in kb_coarse.
+// One finest cell: its exact sums (from kb_bigcells for a dense cell, else
+// from its points), its near-field slots moved to the head of its segment
+// [b, e) (build-nearfield-slots.vert), its record (calculate-level.vert).
+__device__ __forceinline__ void kb_finest_cell(const BatchView& v, const GraphDesc& D, uint32_t seed, uint32_t c,
+                                               uint32_t lc, uint32_t b, uint32_t e, long long& ax, long long& ay) {
+  ax = 0;
+  ay = 0;
+  int ns = 0;
+  if (e - b > kSmallCell) {
+    ax = v.big_sx[c];
+    ay = v.big_sy[c];
+    ns = (int)v.big_ns[c];
+  } else if (e > b) {
+    unsigned long long best[kSlots];
+    uint32_t at[kSlots];
+#pragma unroll
+    for (int q = 0; q < kSlots; ++q) { best[q] = ~0ull; at[q] = 0; }
+    for (uint32_t j = b; j < e; ++j) {
+      const float2 p = v.sorted_pos[j];
+      ax += to_fixed(p.x, D.fx);
+      ay += to_fixed(p.y, D.fx);
+      top8_insert(best, at, local_key(v.sorted_idx[j], D.p_off, seed), j);
+    }
+#pragma unroll
+    for (int q = 0; q < kSlots; ++q) ns += best[q] != ~0ull;
+    kb_move_head(v, b, ns, at);
+  }
+  float4 r = make_float4(0.f, 0.f, 0.f, (float)ns);
+  if (e > b) {
+    const float cf = (float)(e - b);
+    r.x = __fdiv_rn(from_fixed(ax, D.fx), cf);
+    r.y = __fdiv_rn(from_fixed(ay, D.fx), cf);
+    r.z = cf;
+  }
+  v.rec[D.rec_off + level_base(D.levels - 1) + lc] = r;
+}
+
+__device__ __forceinline__ float4 level_record(long long sx, long long sy, long long n, const FixedScale& fx) {
+  float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (n > 0) {
+    const float cf = (float)n;
+    r.x = __fdiv_rn(from_fixed(sx, fx), cf);
+    r.y = __fdiv_rn(from_fixed(sy, fx), cf);
+    r.z = cf;
+  }
+  return r;
+}
+
+// One CTA per (graph, tile) of the work list.  A tile is T x T finest cells
+// (T = GraphDesc::tile <= 32); each thread takes a 2 x 2 quad of them, whose
+// sums make one cell of the next level in registers; the levels above, inside
+// the tile, by shared-memory reduction; coarser levels by integer atomics
+// finished in kb_coarse.  A quad's four cell starts are six loads issued
+// together, so a sparse graph's mostly empty cells cost little beyond them.
 __global__ void __launch_bounds__(kBlock) kb_cells(BatchView v) {
   __shared__ long long smx[kBlock], smy[kBlock], smn[kBlock];
   const uint2 wk = v.tiles[blockIdx.x];
@@ -348,75 +395,51 @@ __global__ void __launch_bounds__(kBlock) kb_cells(BatchView v) {
   const GraphDesc& D = v.desc[g];
   const BatchTick tp = tick_of(v, g);
   if (!tp.active || !(D.stages & kGManybody)) return;
-  const int T = D.tile;
-  const int tiles_row = D.gf / T;
+  const int T = D.tile, Q = T >> 1, gf = D.gf, L = D.levels;
+  const int tiles_row = gf / T;
   const int tile_x = (int)wk.y % tiles_row, tile_y = (int)wk.y / tiles_row;
-  const bool live = (int)threadIdx.x < T * T;
-  const int tx = (int)threadIdx.x % T, ty = (int)threadIdx.x / T;
-  const int cx = tile_x * T + tx, cy = tile_y * T + ty;
-  const uint32_t lc = (uint32_t)(cy * D.gf + cx);
-  const uint32_t c = D.cell_off + lc;
-  long long ax = 0, ay = 0, cnt = 0;
+  const bool live = (int)threadIdx.x < Q * Q;
+  const int qx = (int)threadIdx.x % Q, qy = (int)threadIdx.x / Q;
+  long long sx = 0, sy = 0, sn = 0;
   if (live) {
-    const uint32_t b = v.cell_start[c], e = v.cell_start[c + 1];
-    cnt = e - b;
-    int ns = 0;
-    if (e - b > kSmallCell) {
-      ax = v.big_sx[c];
-      ay = v.big_sy[c];
-      ns = (int)v.big_ns[c];
-    } else {
-      unsigned long long best[kSlots];
-      uint32_t at[kSlots];
-#pragma unroll
-      for (int q = 0; q < kSlots; ++q) { best[q] = ~0ull; at[q] = 0; }
-      for (uint32_t j = b; j < e; ++j) {
-        const float2 p = v.sorted_pos[j];
-        ax += to_fixed(p.x, D.fx);
-        ay += to_fixed(p.y, D.fx);
-        top8_insert(best, at, local_key(v.sorted_idx[j], D.p_off, tp.seed_bits), j);
-      }
-#pragma unroll
-      for (int q = 0; q < kSlots; ++q) ns += best[q] != ~0ull;
-      kb_move_head(v, b, ns, at);
-    }
-    float4 r = make_float4(0.f, 0.f, 0.f, (float)ns);
-    if (cnt > 0) {
-      const float cf = (float)cnt;
-      r.x = __fdiv_rn(from_fixed(ax, D.fx), cf);
-      r.y = __fdiv_rn(from_fixed(ay, D.fx), cf);
-      r.z = cf;
-    }
-    v.rec[D.rec_off + level_base(D.levels - 1) + lc] = r;
+    const int cx = tile_x * T + 2 * qx, cy = tile_y * T + 2 * qy;
+    const uint32_t l0 = (uint32_t)(cy * gf + cx), l1 = l0 + (uint32_t)gf;
+    const uint32_t c0 = D.cell_off + l0, c1 = D.cell_off + l1;
+    const uint32_t a0 = v.cell_start[c0], a1 = v.cell_start[c0 + 1], a2 = v.cell_start[c0 + 2];
+    const uint32_t b0 = v.cell_start[c1], b1 = v.cell_start[c1 + 1], b2 = v.cell_start[c1 + 2];
+    long long x, y;
+    kb_finest_cell(v, D, tp.seed_bits, c0, l0, a0, a1, x, y);
+    sx += x; sy += y;
+    kb_finest_cell(v, D, tp.seed_bits, c0 + 1, l0 + 1, a1, a2, x, y);
+    sx += x; sy += y;
+    kb_finest_cell(v, D, tp.seed_bits, c1, l1, b0, b1, x, y);
+    sx += x; sy += y;
+    kb_finest_cell(v, D, tp.seed_bits, c1 + 1, l1 + 1, b1, b2, x, y);
+    sx += x; sy += y;
+    sn = (long long)(a2 - a0) + (long long)(b2 - b0);
+    const int G = gf >> 1;   // level L - 2
+    v.rec[D.rec_off + level_base(L - 2) + (tile_y * Q + qy) * G + tile_x * Q + qx] = level_record(sx, sy, sn, D.fx);
   }
-  smx[threadIdx.x] = ax; smy[threadIdx.x] = ay; smn[threadIdx.x] = cnt;
+  smx[threadIdx.x] = sx; smy[threadIdx.x] = sy; smn[threadIdx.x] = sn;
   __syncthreads();
-  int gsz = T;
-  int lv = D.levels - 1;
+  int gsz = Q;
+  int lv = L - 2;
   while (gsz > 1 && lv > 0) {
     gsz >>= 1;
     --lv;
     long long vx = 0, vy = 0, vn = 0;
-    const bool active = live && tx < gsz && ty < gsz;
+    const bool active = live && qx < gsz && qy < gsz;
     if (active) {
-      const int i00 = (2 * ty) * T + 2 * tx;
-      vx = smx[i00] + smx[i00 + 1] + smx[i00 + T] + smx[i00 + T + 1];
-      vy = smy[i00] + smy[i00 + 1] + smy[i00 + T] + smy[i00 + T + 1];
-      vn = smn[i00] + smn[i00 + 1] + smn[i00 + T] + smn[i00 + T + 1];
+      const int i00 = (2 * qy) * Q + 2 * qx;
+      vx = smx[i00] + smx[i00 + 1] + smx[i00 + Q] + smx[i00 + Q + 1];
+      vy = smy[i00] + smy[i00 + 1] + smy[i00 + Q] + smy[i00 + Q + 1];
+      vn = smn[i00] + smn[i00 + 1] + smn[i00 + Q] + smn[i00 + Q + 1];
     }
     __syncthreads();
     if (active) {
-      smx[ty * T + tx] = vx; smy[ty * T + tx] = vy; smn[ty * T + tx] = vn;
+      smx[qy * Q + qx] = vx; smy[qy * Q + qx] = vy; smn[qy * Q + qx] = vn;
       const int G = 4 << lv;
-      const int gx = tile_x * gsz + tx, gy = tile_y * gsz + ty;
-      float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (vn > 0) {
-        const float cf = (float)vn;
-        r.x = __fdiv_rn(from_fixed(vx, D.fx), cf);
-        r.y = __fdiv_rn(from_fixed(vy, D.fx), cf);
-        r.z = cf;
-      }
-      v.rec[D.rec_off + level_base(lv) + gy * G + gx] = r;
+      v.rec[D.rec_off + level_base(lv) + (tile_y * gsz + qy) * G + tile_x * gsz + qx] = level_record(vx, vy, vn, D.fx);
     }
     __syncthreads();
   }
@@ -499,55 +522,131 @@ __global__ void __launch_bounds__(kBlock) kb_manybody(BatchView v) {
 }
 
 // ------------------------------------------------------------------- link --
-// Graphs that do not run this pass (no links, masked, or inactive) copy their
-// positions through, so the ping-pong buffers stay consistent.
-__global__ void __launch_bounds__(kBlock) kb_link(BatchView v, int direction, const float2* __restrict__ src,
-                                                  float2* __restrict__ dst, const uint32_t* __restrict__ rows,
-                                                  uint32_t nrows) {
+// ForceLink.run (ForceLink/index.ts:221-263), force-spring.ts:38-96, as
+// k_link: one list per thread, springs strictly in list order.  Graphs that
+// do not run this pass (no links, masked, or inactive) copy their positions
+// through, so the ping-pong buffers stay consistent.
+struct LinkScalars {
+  float sa, span, r0, dist;
+};
+
+__device__ __forceinline__ LinkScalars link_scalars(const GraphDesc& D, const BatchTick& tp) {
+  return LinkScalars{__fmul_rn(D.link_spring, tp.alpha), __fsub_rn(D.link_r1, D.link_r0), D.link_r0, D.link_distance};
+}
+
+__device__ __forceinline__ void batch_spring(const LinkScalars& ls, const uint4 en, const float2 pp, const float2 q,
+                                             float2& vel, const PairUnits& pu) {
+  float dd = __fadd_rn(__fmul_rn(__uint_as_float(en.y), ls.span), ls.r0);
+  dd = __fmul_rn(dd, ls.dist);
+  spring_step(pp, vel, q, dd, __fmul_rn(dd, 0.99f), ls.sa, __uint_as_float(en.w), __uint_as_float(en.z), pu);
+}
+
+// The long lists (more than kHeavyDegree links): rows[t] is an arena point.
+__global__ void __launch_bounds__(kBlock) kb_link_heavy(BatchView v, int direction, const float2* __restrict__ src,
+                                                        float2* __restrict__ dst, const uint32_t* __restrict__ rows,
+                                                        uint32_t nrows) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nrows) return;
-  const uint32_t P = rows ? rows[t] : t;
+  const uint32_t P = rows[t];
   const uint32_t g = v.gid[P];
   if (g == kNoGraph) return;
   const GraphDesc& D = v.desc[g];
   const BatchTick tp = tick_of(v, g);
-  const uint32_t i = P - D.p_off;
-  const uint32_t rp = (direction == 0 ? D.rp_in : D.rp_out) + i;
-  const uint32_t e0 = v.rowptr[rp], e1 = v.rowptr[rp + 1];
-  if (!rows && e1 - e0 > kHeavyDegree) return;
   const float2 pp = src[P];
   const uint32_t stage = direction == 0 ? kGLinkIn : kGLinkOut;
   const uint8_t f = v.flags[P];
   if (!tp.active || !(D.stages & stage) || (f & kAbsent)) { dst[P] = pp; return; }
-  const float sa = __fmul_rn(D.link_spring, tp.alpha);
+  const uint32_t rp = (direction == 0 ? D.rp_in : D.rp_out) + (P - D.p_off);
+  const uint4* ent = v.ent + (direction == 0 ? D.e_in : D.e_out);
+  const uint32_t e0 = v.rowptr[rp], e1 = v.rowptr[rp + 1];
+  const float2* gsrc = src + D.p_off;
+  const LinkScalars ls = link_scalars(D, tp);
   const PairUnits pu = v.units;
-  const float span = __fsub_rn(D.link_r1, D.link_r0);
   float2 vel = make_float2(0.f, 0.f);
-  auto spring = [&](const uint4 en, const float2 q) {
-    float dd = __fadd_rn(__fmul_rn(__uint_as_float(en.y), span), D.link_r0);
-    dd = __fmul_rn(dd, D.link_distance);
-    spring_step(pp, vel, q, dd, __fmul_rn(dd, 0.99f), sa, __uint_as_float(en.w), __uint_as_float(en.z), pu);
-  };
-
   constexpr int kLinkBatch = 4;
   uint32_t at = e0;
   for (; at + kLinkBatch <= e1; at += kLinkBatch) {
     uint4 en[kLinkBatch];
     float2 q[kLinkBatch];
 #pragma unroll
-    for (int u = 0; u < kLinkBatch; ++u) en[u] = __ldg(&v.ent[at + u]);
+    for (int u = 0; u < kLinkBatch; ++u) en[u] = __ldg(&ent[at + u]);
 #pragma unroll
-    for (int u = 0; u < kLinkBatch; ++u) q[u] = en[u].x != kAbsentTarget ? __ldg(&src[en[u].x]) : make_float2(0.f, 0.f);
+    for (int u = 0; u < kLinkBatch; ++u) q[u] = en[u].x != kAbsentTarget ? __ldg(&gsrc[en[u].x]) : make_float2(0.f, 0.f);
 #pragma unroll
     for (int u = 0; u < kLinkBatch; ++u)
-      if (en[u].x != kAbsentTarget) spring(en[u], q[u]);
+      if (en[u].x != kAbsentTarget) batch_spring(ls, en[u], pp, q[u], vel, pu);
   }
   for (; at < e1; ++at) {
-    const uint4 en = __ldg(&v.ent[at]);
+    const uint4 en = __ldg(&ent[at]);
     if (en.x == kAbsentTarget) continue;
-    spring(en, __ldg(&src[en.x]));
+    batch_spring(ls, en, pp, __ldg(&gsrc[en.x]), vel, pu);
   }
   dst[P] = (f & kPinned) ? pp : integrate(pp, vel.x, vel.y, D.friction, D.space);
+}
+
+// The light rows by warps (GraphDesc::lr, lw, ln, nw): a block takes
+// kLinkWarpsPerBlock warps of one graph from the work list; a warp's lanes walk
+// lists of nearly the same length, and entry k of all 32 lists is one
+// coalesced 512-byte load.
+__global__ void __launch_bounds__(kBlock) kb_link_warps(BatchView v, int direction, const float2* __restrict__ src,
+                                                        float2* __restrict__ dst) {
+  const uint2 wk = v.lwork[direction][blockIdx.x];
+  const uint32_t g = wk.x;
+  const GraphDesc& D = v.desc[g];
+  const uint32_t w = wk.y + (threadIdx.x >> 5);
+  if (w >= D.nw[direction]) return;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t i = __ldg(&v.lrow[D.lr[direction] + 32 * w + lane]);
+  if (i == kNoPoint) return;
+  const uint32_t P = D.p_off + i;
+  const BatchTick tp = tick_of(v, g);
+  const float2 pp = src[P];
+  const uint32_t stage = direction == 0 ? kGLinkIn : kGLinkOut;
+  const uint8_t f = v.flags[P];
+  if (!tp.active || !(D.stages & stage) || (f & kAbsent)) { dst[P] = pp; return; }
+  const uint32_t* wo = v.lwoff + D.lw[direction] + w;
+  const uint32_t o0 = __ldg(&wo[0]), cnt = (__ldg(&wo[1]) - o0) >> 5;
+  const uint4* col = v.lanes + D.ln[direction] + o0 + lane;
+  const float2* gsrc = src + D.p_off;
+  const LinkScalars ls = link_scalars(D, tp);
+  const PairUnits pu = v.units;
+  float2 vel = make_float2(0.f, 0.f);
+  constexpr int kLinkBatch = 4;
+  uint32_t at = 0;
+  for (; at + kLinkBatch <= cnt; at += kLinkBatch) {
+    uint4 en[kLinkBatch];
+    float2 q[kLinkBatch];
+#pragma unroll
+    for (int u = 0; u < kLinkBatch; ++u) en[u] = __ldg(&col[32 * (at + u)]);
+#pragma unroll
+    for (int u = 0; u < kLinkBatch; ++u) q[u] = en[u].x != kAbsentTarget ? __ldg(&gsrc[en[u].x]) : make_float2(0.f, 0.f);
+#pragma unroll
+    for (int u = 0; u < kLinkBatch; ++u)
+      if (en[u].x != kAbsentTarget) batch_spring(ls, en[u], pp, q[u], vel, pu);
+  }
+  for (; at < cnt; ++at) {
+    const uint4 en = __ldg(&col[32 * at]);
+    if (en.x == kAbsentTarget) continue;
+    batch_spring(ls, en, pp, __ldg(&gsrc[en.x]), vel, pu);
+  }
+  dst[P] = (f & kPinned) ? pp : integrate(pp, vel.x, vel.y, D.friction, D.space);
+}
+
+__global__ void __launch_bounds__(kBlock) kb_warp_lengths(const uint32_t* __restrict__ order,
+                                                          const uint32_t* __restrict__ len, uint32_t nh, uint32_t n,
+                                                          uint32_t* __restrict__ woff) {
+  const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t nw = (n - nh + 31) / 32;
+  if (w > nw) return;
+  woff[w] = w < nw ? 32 * len[order[nh + 32 * w]] : 0u;   // a warp's first row has its longest list
+}
+
+__global__ void __launch_bounds__(kBlock) kb_warp_rows(const uint32_t* __restrict__ order, uint32_t nh, uint32_t n,
+                                                       uint32_t* __restrict__ lrow) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t nw = (n - nh + 31) / 32;
+  if (t >= 32 * nw) return;
+  lrow[t] = t < n - nh ? order[nh + t] : kNoPoint;
 }
 
 // -------------------------------------------------------------- collision --
@@ -609,15 +708,7 @@ void batch_launch_tick(const BatchView& v, cudaStream_t st, cudaStream_t side, c
   if (v.any_center) cudaMemsetAsync(v.centroid, 0, 3 * sizeof(long long) * (size_t)v.slots, st);
   if (v.point_hwm) kb_prepass<<<blocks(v.point_hwm), kBlock, 0, st>>>(v);
   if (v.any_center && v.point_hwm) kb_center<<<blocks(v.point_hwm), kBlock, 0, st>>>(v);
-  if (v.cell_hwm) {
-    const uint32_t n1 = (v.cell_hwm + kChunk - 1) / kChunk;   // partials of 1024 cells
-    const uint32_t n2 = (n1 + kChunk - 1) / kChunk;           // partials of 1024^2 cells (<= 1024)
-    kb_scan_reduce<<<n1, kBlock, 0, st>>>(v.counts, v.cell_hwm, v.scan1);
-    kb_scan_reduce<<<n2, kBlock, 0, st>>>(v.scan1, n1, v.scan2);
-    kb_scan_down<<<1, kBlock, 0, st>>>(v.scan2, n2, nullptr, v.scan2, nullptr);
-    kb_scan_down<<<n2, kBlock, 0, st>>>(v.scan1, n1, v.scan2, v.scan1, nullptr);
-    kb_scan_cells<<<n1, kBlock, 0, st>>>(v, v.scan1);
-  }
+  if (v.cell_hwm) kb_scan<<<batch_scan_blocks(v.cell_hwm), kBlock, 0, st>>>(v);
   if (v.point_hwm) kb_scatter<<<blocks(v.point_hwm), kBlock, 0, st>>>(v);
   kb_bigcells<<<8 * sm_count(), kBlock, 0, st>>>(v);   // as k_bigcells: 8 blocks per SM
   if (v.n_tiles) kb_cells<<<v.n_tiles, kBlock, 0, st>>>(v);
@@ -631,10 +722,10 @@ void batch_launch_tick(const BatchView& v, cudaStream_t st, cudaStream_t side, c
     if (nh) {
       cudaEventRecord(fork[dir], st);
       cudaStreamWaitEvent(side, fork[dir], 0);
-      kb_link<<<blocks(nh), kBlock, 0, side>>>(v, dir, src, dst, heavy, nh);
+      kb_link_heavy<<<blocks(nh), kBlock, 0, side>>>(v, dir, src, dst, heavy, nh);
       cudaEventRecord(join[dir], side);
     }
-    if (v.point_hwm) kb_link<<<blocks(v.point_hwm), kBlock, 0, st>>>(v, dir, src, dst, nullptr, v.point_hwm);
+    if (v.n_lwork[dir]) kb_link_warps<<<v.n_lwork[dir], kBlock, 0, st>>>(v, dir, src, dst);
     if (nh) cudaStreamWaitEvent(st, join[dir], 0);
   }
   if (v.any_collision && v.point_hwm) {   // after the links, as in runSimulationStep (src/index.ts:2068-2078)
@@ -645,9 +736,23 @@ void batch_launch_tick(const BatchView& v, cudaStream_t st, cudaStream_t side, c
   kb_tick_end<<<1, 1, 0, st>>>(v);
 }
 
+uint32_t batch_scan_blocks(uint32_t cells) { return (cells + kChunk - 1) / kChunk; }
+
+void batch_warp_lengths(const uint32_t* order, const uint32_t* len, uint32_t nh, uint32_t n, uint32_t* woff,
+                        cudaStream_t st) {
+  const uint32_t nw = (n - nh + 31) / 32;
+  kb_warp_lengths<<<blocks(nw + 1), kBlock, 0, st>>>(order, len, nh, n, woff);
+}
+
+void batch_warp_rows(const uint32_t* order, uint32_t nh, uint32_t n, uint32_t* lrow, cudaStream_t st) {
+  const uint32_t nw = (n - nh + 31) / 32;
+  if (nw) kb_warp_rows<<<blocks(32 * nw), kBlock, 0, st>>>(order, nh, n, lrow);
+}
+
 uint32_t batch_kernels_per_tick(const BatchView& v) {
-  uint32_t k = 1 + 1 + 1 + 1 + 1 + 2;   // prepass, scatter, big cells, coarse, manybody, link x2
-  if (v.cell_hwm) k += 5;
+  uint32_t k = 1 + 1 + 1 + 1 + 1;       // prepass, scatter, big cells, coarse, manybody
+  k += (v.n_lwork[0] > 0) + (v.n_lwork[1] > 0);
+  if (v.cell_hwm) k += 1;
   if (v.n_tiles) k += 1;
   k += (v.n_heavy_in > 0) + (v.n_heavy_out > 0);
   if (v.any_center) k += 1;

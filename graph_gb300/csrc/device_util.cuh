@@ -80,6 +80,61 @@ static __device__ unsigned long long block_exclusive_scan64(unsigned long long v
   return before + x - v;
 }
 
+// Single-pass scans (decoupled look-back, Merrill and Garland 2016): each
+// block takes the next chunk in the order blocks start (a ticket), so every
+// chunk before its own belongs to a block that has already started.  The block publishes
+// its chunk's total, then warp 0 walks back over the status words of the
+// chunks before it, adding totals until it meets a chunk whose inclusive
+// prefix is known; the block then publishes its own inclusive prefix.  A
+// status word holds the value in its low 60 bits, a flag for "total" or
+// "inclusive prefix", and the parity of the pass (the ticket / blocks), so a
+// word left from the previous tick never reads as current.
+constexpr unsigned long long kScanTotal = 1ull << 61, kScanInclusive = 1ull << 62, kScanParity = 1ull << 63;
+constexpr unsigned long long kScanValue = (1ull << 60) - 1;
+constexpr uint32_t kScanPollLimit = 1u << 20;   // ~0.1 s of polls: far beyond any wait on a started block
+
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// The exclusive prefix of chunk `vb` (> 0) from the status words of chunks
+// [0, vb); warp 0 of the block, every lane gets it.  A wait that outlasts
+// kScanPollLimit polls sets `error_bit` in *error and returns what it has.
+static __device__ unsigned long long scan_look_back(const unsigned long long* status, uint32_t vb,
+                                                    unsigned long long parity, uint32_t* error, uint32_t error_bit) {
+  const int lane = threadIdx.x & 31;
+  unsigned long long prefix = 0;
+  int end = (int)vb;   // this round looks at chunks end - 1 - lane
+  for (uint32_t polls = 0;;) {
+    const int i = end - 1 - lane;
+    const unsigned long long w = i >= 0 ? ld_relaxed_u64(&status[i]) : (parity | kScanInclusive);
+    const bool current = (w & kScanParity) == parity && (w & (kScanTotal | kScanInclusive));
+    const unsigned ready = __ballot_sync(0xffffffffu, current);
+    const unsigned incl = __ballot_sync(0xffffffffu, current && (w & kScanInclusive));
+    // the lanes up to and including the nearest chunk with an inclusive prefix
+    const unsigned need = incl ? (incl ^ (incl - 1u)) : 0xffffffffu;
+    if ((ready & need) == need) {
+      unsigned long long x = ((need >> lane) & 1u) ? (w & kScanValue) : 0ull;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+      prefix += x;
+      if (incl) return prefix;
+      end -= 32;
+      continue;
+    }
+    if (++polls > kScanPollLimit) {
+      if (lane == 0) atomicOr(error, error_bit);
+      return prefix;
+    }
+    __nanosleep(64);
+  }
+}
+
 // Insert (hash bits, index) into a sorted list of the 8 smallest DISTINCT
 // hashes, each kept with its lowest index (the peel's tie rule,
 // build-nearfield-slots.vert:146-162); `at` tracks segment positions.

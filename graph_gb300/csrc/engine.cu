@@ -39,6 +39,8 @@ struct cgl_engine {
   int device = 0;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
+  uint32_t* h_error = nullptr;   // host-mapped error word (DeviceView::error_word)
+  uint32_t* d_error = nullptr;
 
   // staged input (copied at set_*, applied at render)
   bool have_pos_input = false, have_link_input = false, have_strength = false, have_sizes = false;
@@ -138,6 +140,16 @@ cgl_status fail(cgl_engine* e, cgl_status st, const char* fmt, ...) {
                   #call, cudaGetErrorString(_err), __FILE__, __LINE__);                       \
   } while (0)
 
+// After a synchronisation: a device wait that gave up (error_word) is
+// reported once, as a CUDA error of the call that found it.
+cgl_status device_error(cgl_engine* e) {
+  const uint32_t bits = *(volatile uint32_t*)e->h_error;
+  if (!bits) return CGL_OK;
+  *(volatile uint32_t*)e->h_error = 0;
+  return fail(e, CGL_CUDA_ERROR, "a device wait gave up (error bits 0x%x): the last ticks' cell scan is not valid",
+              bits);
+}
+
 cgl_status dev_reserve(cgl_engine* e, DevBuf& b, size_t bytes, bool zero) {
   if (bytes == 0) bytes = 16;
   if (b.bytes >= bytes) {
@@ -221,8 +233,9 @@ void refresh_view(cgl_engine* e) {
   d.pos_s = (float2*)e->b_pos_s.p;
   d.bin_state = (uint32_t*)e->b_bin_state.p;
   d.pair_list = (uint32_t*)e->b_pair_list.p;
-  d.scan_ticket = (uint32_t*)e->b_tickets.p;
-  d.cells_ticket = d.scan_ticket ? d.scan_ticket + 1 : nullptr;
+  d.scan_seq = (unsigned long long*)e->b_tickets.p;
+  d.cells_ticket = e->b_tickets.p ? (uint32_t*)e->b_tickets.p + 2 : nullptr;
+  d.error_word = e->d_error;
   d.big_list = (uint32_t*)e->b_big_list.p;
   d.big_count = (uint32_t*)e->b_big_count.p;
   d.big_sx = (long long*)e->b_big_sx.p;
@@ -757,7 +770,8 @@ cgl_status build_graph(cgl_engine* e, double alpha, uint64_t N, uint64_t E) {
       const uint32_t cells = (uint32_t)(e->Gf * e->Gf);
       if ((st = dev_reserve(e, e->b_counts, cells * sizeof(uint32_t), true))) return st;
       if ((st = dev_reserve(e, e->b_cell_start, (cells + 1) * sizeof(uint32_t), false))) return st;
-      if ((st = dev_reserve(e, e->b_block_sums, (scan_blocks(cells) + 1) * sizeof(unsigned long long), false)))
+      // the scan's status words and tickets start from zero together
+      if ((st = dev_reserve(e, e->b_block_sums, (scan_blocks(cells) + 1) * sizeof(unsigned long long), true)))
         return st;
       if ((st = dev_reserve(e, e->b_pair_start, (cells + 1) * sizeof(uint32_t), true))) return st;
       if ((st = dev_reserve(e, e->b_pair_list, std::max<size_t>(n, 1) * sizeof(uint32_t), false))) return st;
@@ -919,15 +933,19 @@ cgl_status cgl_create(const cgl_config* cfg, cgl_engine** out) {
   if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking);
   if (ce == cudaSuccess) ce = cudaMallocHost((void**)&e->h_params, kParamChunk * sizeof(TickParams));
   if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->params_copied, cudaEventDisableTiming);
+  if (ce == cudaSuccess) ce = cudaHostAlloc((void**)&e->h_error, sizeof(uint32_t), cudaHostAllocMapped);
+  if (ce == cudaSuccess) ce = cudaHostGetDevicePointer((void**)&e->d_error, e->h_error, 0);
   if (ce != cudaSuccess) {
     cudaGetLastError();
     static thread_local std::string create_err;
     create_err = cudaGetErrorString(ce);
     if (e->own_stream) cudaStreamDestroy(e->own_stream);
     if (e->h_params) cudaFreeHost(e->h_params);
+    if (e->h_error) cudaFreeHost(e->h_error);
     delete e;
     return ce == cudaErrorMemoryAllocation ? CGL_OOM : CGL_CUDA_ERROR;
   }
+  *e->h_error = 0;
   e->stream = e->own_stream;
   cgl_status st;
   if ((st = dev_reserve(e, e->b_params, kParamChunk * sizeof(TickParams), true)) ||
@@ -948,6 +966,7 @@ cgl_status cgl_destroy(cgl_engine* e) {
   dev_free_all(e);
   if (e->params_copied) cudaEventDestroy(e->params_copied);
   if (e->h_params) cudaFreeHost(e->h_params);
+  if (e->h_error) cudaFreeHost(e->h_error);
   if (e->own_stream) cudaStreamDestroy(e->own_stream);
   delete e;
   return CGL_OK;
@@ -1294,7 +1313,7 @@ cgl_status cgl_get_point_positions(cgl_engine* e, float* out, uint64_t cap) {
   if (!e->N) return CGL_OK;
   CU(cudaMemcpyAsync(out, e->b_pos.p, e->N * sizeof(float2), cudaMemcpyDeviceToHost, e->stream));
   CU(cudaStreamSynchronize(e->stream));
-  return CGL_OK;
+  return device_error(e);
 }
 
 cgl_status cgl_get_state(cgl_engine* e, cgl_state* s) {
@@ -1331,7 +1350,7 @@ cgl_status cgl_set_stream(cgl_engine* e, void* cuda_stream) {
 cgl_status cgl_synchronize(cgl_engine* e) {
   CHECK_E(e);
   CU(cudaStreamSynchronize(e->stream));
-  return CGL_OK;
+  return device_error(e);
 }
 
 cgl_status cgl_profile_stages(cgl_engine* e, uint32_t ticks, double* ms_out) {

@@ -198,77 +198,71 @@ __device__ __forceinline__ unsigned long long scan_word(uint32_t count) {
   return PAIRS ? ((unsigned long long)((count + 1) >> 1) << 32) | count : count;
 }
 
+// Exclusive scan of the cell histogram into cell_start (and, with PAIRS,
+// pair_start), the histogram zeroed for the next tick, the dense cells listed.
 template <bool PAIRS>
-__global__ void __launch_bounds__(kBlock) k_scan_reduce(DeviceView d, uint32_t cells) {
-  const uint32_t base = blockIdx.x * kScanChunk;
-  unsigned long long sum = 0;
-#pragma unroll
-  for (int k = 0; k < kScanItems; ++k) {
-    uint32_t c = base + k * kBlock + threadIdx.x;
-    if (c < cells) sum += scan_word<PAIRS>(d.counts[c]);
-  }
+__global__ void __launch_bounds__(kBlock) k_scan(DeviceView d, uint32_t cells) {
+  __shared__ unsigned long long s_seq, s_prefix;
+  __shared__ uint32_t s_lists[6];   // dense cells of this block per list, then each list's base
+  if (threadIdx.x == 0) s_seq = atomicAdd(d.scan_seq, 1ull);
+  if (threadIdx.x < 3) s_lists[threadIdx.x] = 0;
+  __syncthreads();
+  const uint32_t nb = gridDim.x;
+  const uint32_t vb = (uint32_t)(s_seq % nb);
+  const unsigned long long parity = ((s_seq / nb) & 1ull) << 63;
+  // cells is a multiple of 64 (a power-of-two grid of at least 8 x 8) and
+  // base of 4: a thread's four cells are all inside or all outside
+  const uint32_t base = vb * kScanChunk + threadIdx.x * kScanItems;
+  const bool inside = base < cells;
+  uint4 v = make_uint4(0u, 0u, 0u, 0u);
+  if (inside) v = reinterpret_cast<const uint4*>(d.counts)[base >> 2];
+  const unsigned long long w0 = scan_word<PAIRS>(v.x), w1 = scan_word<PAIRS>(v.y), w2 = scan_word<PAIRS>(v.z),
+                           w3 = scan_word<PAIRS>(v.w);
   unsigned long long total;
-  block_exclusive_scan64(sum, &total);
-  __shared__ bool last;
-  if (threadIdx.x == 0) {
-    d.block_sums[blockIdx.x] = total;
-    __threadfence();
-    last = atomicAdd(d.scan_ticket, 1u) == gridDim.x - 1;
+  unsigned long long off = block_exclusive_scan64(w0 + w1 + w2 + w3, &total);
+  if (threadIdx.x < 32) {
+    unsigned long long prefix = 0;
+    if (vb == 0) {
+      if (threadIdx.x == 0) st_relaxed_u64(&d.block_sums[0], parity | kScanInclusive | total);
+    } else {
+      if (threadIdx.x == 0) st_relaxed_u64(&d.block_sums[vb], parity | kScanTotal | total);
+      prefix = scan_look_back(d.block_sums, vb, parity, d.error_word, kErrorScan);
+      if (threadIdx.x == 0) st_relaxed_u64(&d.block_sums[vb], parity | kScanInclusive | ((prefix + total) & kScanValue));
+    }
+    if (threadIdx.x == 0) s_prefix = prefix;
   }
   __syncthreads();
-  if (!last) return;
-  // Last block: exclusive scan of the block totals (gridDim.x <= kScanChunk).
-  __threadfence();
-  unsigned long long v[kScanItems];
-  unsigned long long run = 0;
+  off += s_prefix;
+  if (inside) {
+    const unsigned long long o1 = off + w0, o2 = o1 + w1, o3 = o2 + w2;
+    reinterpret_cast<uint4*>(d.cell_start)[base >> 2] = make_uint4((uint32_t)off, (uint32_t)o1, (uint32_t)o2, (uint32_t)o3);
+    if (PAIRS)
+      reinterpret_cast<uint4*>(d.pair_start)[base >> 2] =
+          make_uint4((uint32_t)(off >> 32), (uint32_t)(o1 >> 32), (uint32_t)(o2 >> 32), (uint32_t)(o3 >> 32));
+    reinterpret_cast<uint4*>(d.counts)[base >> 2] = make_uint4(0u, 0u, 0u, 0u);   // ready for the next tick
+  }
+  // the dense cells' list entries: a slot in the block's share of each list
+  // (shared-memory atomics), then one global atomic per list and block
+  const uint32_t cnt[4] = {v.x, v.y, v.z, v.w};
+  int cls[4];
+  uint32_t slot[4];
 #pragma unroll
   for (int k = 0; k < kScanItems; ++k) {
-    uint32_t b = threadIdx.x * kScanItems + k;
-    v[k] = b < gridDim.x ? __ldcg(&d.block_sums[b]) : 0;
-    run += v[k];
+    cls[k] = cnt[k] > kBigCell ? 0 : cnt[k] > kWarpSmallCell ? 1 : cnt[k] > kSmallCell ? 2 : 3;
+    slot[k] = cls[k] < 3 ? atomicAdd(&s_lists[cls[k]], 1u) : 0u;
   }
-  unsigned long long grand;
-  unsigned long long off = block_exclusive_scan64(run, &grand);
+  __syncthreads();
+  if (threadIdx.x < 3 && s_lists[threadIdx.x]) s_lists[3 + threadIdx.x] = atomicAdd(&d.big_count[threadIdx.x], s_lists[threadIdx.x]);
+  __syncthreads();
 #pragma unroll
   for (int k = 0; k < kScanItems; ++k) {
-    uint32_t b = threadIdx.x * kScanItems + k;
-    if (b < gridDim.x) d.block_sums[b] = off;
-    off += v[k];
+    const uint32_t c = base + k;
+    if (cls[k] == 0) d.big_list[s_lists[3] + slot[k]] = c;
+    else if (cls[k] == 1) d.big_list[cells + s_lists[4] + slot[k]] = c;
+    else if (cls[k] == 2) d.big_list[2 * cells - 1 - (s_lists[5] + slot[k])] = c;
   }
-  if (threadIdx.x == 0) {
-    d.block_sums[gridDim.x] = grand;
-    *d.scan_ticket = 0;
-  }
-}
-
-template <bool PAIRS>
-__global__ void __launch_bounds__(kBlock) k_scan_down(DeviceView d, uint32_t cells) {
-  const uint32_t base = blockIdx.x * kScanChunk + threadIdx.x * kScanItems;
-  uint32_t v[kScanItems];
-  unsigned long long run = 0;
-#pragma unroll
-  for (int k = 0; k < kScanItems; ++k) {
-    uint32_t c = base + k;
-    v[k] = c < cells ? d.counts[c] : 0;
-    run += scan_word<PAIRS>(v[k]);
-  }
-  unsigned long long total;
-  unsigned long long off = block_exclusive_scan64(run, &total) + __ldcg(&d.block_sums[blockIdx.x]);
-#pragma unroll
-  for (int k = 0; k < kScanItems; ++k) {
-    uint32_t c = base + k;
-    if (c < cells) {
-      d.cell_start[c] = (uint32_t)off;
-      if (PAIRS) d.pair_start[c] = (uint32_t)(off >> 32);
-      d.counts[c] = 0;   // histogram ready for the next tick
-      if (v[k] > kBigCell) d.big_list[atomicAdd(&d.big_count[0], 1u)] = c;
-      else if (v[k] > kWarpSmallCell) d.big_list[cells + atomicAdd(&d.big_count[1], 1u)] = c;
-      else if (v[k] > kSmallCell) d.big_list[2 * cells - 1 - atomicAdd(&d.big_count[2], 1u)] = c;
-    }
-    off += scan_word<PAIRS>(v[k]);
-  }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    const unsigned long long g = __ldcg(&d.block_sums[gridDim.x]);
+  if (vb == nb - 1 && threadIdx.x == 0) {
+    const unsigned long long g = s_prefix + total;
     d.cell_start[cells] = (uint32_t)g;
     if (PAIRS) d.pair_start[cells] = (uint32_t)(g >> 32);
   }
@@ -751,7 +745,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_manybody(DeviceView d, SimScalars
 constexpr int kHubChunk = kBlock - 32;
 struct HubStage {
   float4 a[2][kHubChunk];   // neighbour x, y, rest length d, 0.99 d
-  float4 b[2][kHubChunk];   // strength, bias, absent flag, -
+  float4 b[2][kHubChunk];   // strength, bias, absent flag, rcp.approx(0.99 d)
 };
 
 // Stages link at + (thread - 32); returns kStagedAbsent when its target is
@@ -766,7 +760,8 @@ __device__ __forceinline__ int hub_fill(HubStage& st, int buf, uint32_t at, uint
   const float2 q = absent ? make_float2(0.f, 0.f) : __ldg(&src[en.x]);
   const float dd = __fmul_rn(__fadd_rn(__fmul_rn(__uint_as_float(en.y), span), r0), dist);
   st.a[buf][k] = make_float4(q.x, q.y, dd, __fmul_rn(dd, 0.99f));
-  st.b[buf][k] = make_float4(__uint_as_float(en.w), __uint_as_float(en.z), absent ? 1.f : 0.f, 0.f);
+  st.b[buf][k] = make_float4(__uint_as_float(en.w), __uint_as_float(en.z), absent ? 1.f : 0.f,
+                             rcp_estimate(__fmul_rn(dd, 0.99f)));
   return (absent ? kStagedAbsent : 0) | (__uint_as_float(en.w) != 1.0f ? kStagedStrength : 0);
 }
 
@@ -781,14 +776,14 @@ __device__ __forceinline__ bool hub_chunk_fast(const float4* A, const float4* B,
     for (int k = 0; k < kHubChunk; ++k) {
       const float4 a = A[k];
       const float4 b = B[k];
-      spring_step_fast<UNIT_STRENGTH>(pp, vel, make_float2(a.x, a.y), a.z, a.w, sa, b.x, b.y, pu, out);
+      spring_step_fast<UNIT_STRENGTH>(pp, vel, make_float2(a.x, a.y), a.z, a.w, b.w, sa, b.x, b.y, pu, out);
     }
   } else {
 #pragma unroll 4
     for (uint32_t k = 0; k < len; ++k) {
       const float4 a = A[k];
       const float4 b = B[k];
-      spring_step_fast<UNIT_STRENGTH>(pp, vel, make_float2(a.x, a.y), a.z, a.w, sa, b.x, b.y, pu, out);
+      spring_step_fast<UNIT_STRENGTH>(pp, vel, make_float2(a.x, a.y), a.z, a.w, b.w, sa, b.x, b.y, pu, out);
     }
   }
   return out;
@@ -1131,13 +1126,8 @@ void launch_center(const DeviceView& d, const SimScalars& s, bool bin, cudaStrea
 void launch_scan(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
   const uint32_t cells = (uint32_t)(s.gf * s.gf);
   const uint32_t nb = scan_blocks(cells);
-  if (s.pairs) {
-    k_scan_reduce<true><<<nb, kBlock, 0, st>>>(d, cells);
-    k_scan_down<true><<<nb, kBlock, 0, st>>>(d, cells);
-  } else {
-    k_scan_reduce<false><<<nb, kBlock, 0, st>>>(d, cells);
-    k_scan_down<false><<<nb, kBlock, 0, st>>>(d, cells);
-  }
+  if (s.pairs) k_scan<true><<<nb, kBlock, 0, st>>>(d, cells);
+  else k_scan<false><<<nb, kBlock, 0, st>>>(d, cells);
 }
 
 void launch_scatter(const DeviceView& d, const SimScalars& s, cudaStream_t st) {

@@ -28,7 +28,8 @@ struct DeviceView {
   float2* sorted_pos;         // positions in the same order (snapshot for the many-body pass) [n]
   uint32_t* counts;           // finest-cell histogram [G^2] (zeroed by the scan)
   uint32_t* cell_start;       // exclusive scan [G^2 + 1]
-  unsigned long long* block_sums;  // scan partials: (count, pairs) packed as low and high 32 bits
+  unsigned long long* block_sums;  // scan status per chunk: (count, pairs) packed as low and high 32
+                                   // bits of a 60-bit value, with its flags (kernels.cu, k_scan)
   uint32_t* idx_s;            // binning in the previous cell order: the point at position j [n]
   float2* pos_s;              // and its position after the prepass [n]
   uint32_t* bin_state;        // [0] = 1 once sorted_idx holds a cell order of the live points (zeroed at
@@ -36,7 +37,8 @@ struct DeviceView {
   uint32_t* pair_start;       // exclusive scan of ceil(count / 2) per finest cell [G^2 + 1]
   uint32_t* pair_list;        // per pair of one cell's consecutive sorted positions (j, j + 1): j,
                               // with the top bit set when j is the cell's last point alone [<= n]
-  uint32_t* scan_ticket;      // last-block ticket of the scan
+  unsigned long long* scan_seq;   // scan chunk tickets, counted up across ticks (zeroed with block_sums)
+  uint32_t* error_word;       // host-mapped: kError* bits raised by a device wait that gave up
   float4* rec;                // cell records of all levels (cx, cy, count, nslot)
   uint32_t level_off[10];     // offset of level l in rec
   long long* acc;             // coarse-level integer sums (x, y, count) per cell, levels < tile level
@@ -107,6 +109,7 @@ struct SimScalars {
                               // then in [1, 2^52] whenever every binned point lies in [0, space]
   int any_pinned;             // some live point is pinned
 };
+constexpr uint32_t kErrorScan = 1;     // error_word bit: a scan block's look-back gave up waiting
 constexpr uint32_t kOutsideFlag = 4;   // big_count word of the outside-the-space flag
 constexpr uint32_t kSingleBit = 0x80000000u;
 
