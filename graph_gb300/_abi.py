@@ -106,6 +106,7 @@ class Layout(C.Structure):
 MANYBODY_ONE_POINT = 0
 MANYBODY_SPLIT = 1
 MANYBODY_TWO_POINTS = 2
+CGL_ERROR_SCAN = 1          # error bit of a one-pass cell scan whose bounded wait gave up
 
 
 # Reference defaults (src/variables.ts:10,15,19,69-82,147-148) mapped to C field names.

@@ -1340,6 +1340,32 @@ cgl_status cgl_random_draws(const char* seed_text, uint64_t n, double* out) {
   return CGL_OK;
 }
 
+cgl_status cgl_check_wait_limit(int32_t device, uint32_t* error_bits) {
+  if (!error_bits) return CGL_INVALID_ARG;
+  *error_bits = 0;
+  if (cudaSetDevice(device) != cudaSuccess) { cudaGetLastError(); return CGL_CUDA_ERROR; }
+  unsigned long long* status = nullptr;
+  uint32_t *h_err = nullptr, *d_err = nullptr;
+  cudaStream_t st = nullptr;
+  cudaError_t ce = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  if (ce == cudaSuccess) ce = cudaMalloc((void**)&status, 2 * sizeof(unsigned long long));
+  if (ce == cudaSuccess) ce = cudaMemsetAsync(status, 0, 2 * sizeof(unsigned long long), st);
+  if (ce == cudaSuccess) ce = cudaHostAlloc((void**)&h_err, sizeof(uint32_t), cudaHostAllocMapped);
+  if (ce == cudaSuccess) ce = cudaHostGetDevicePointer((void**)&d_err, h_err, 0);
+  if (ce == cudaSuccess) {
+    *h_err = 0;
+    launch_wait_limit(status, d_err, st);
+    ce = cudaGetLastError();
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    if (ce == cudaSuccess) *error_bits = *(volatile uint32_t*)h_err;
+  }
+  if (status) cudaFree(status);
+  if (h_err) cudaFreeHost(h_err);
+  if (st) cudaStreamDestroy(st);
+  if (ce != cudaSuccess) { cudaGetLastError(); return CGL_CUDA_ERROR; }
+  return CGL_OK;
+}
+
 cgl_status cgl_set_stream(cgl_engine* e, void* cuda_stream) {
   CHECK_E(e);
   CU(cudaStreamSynchronize(e->stream));

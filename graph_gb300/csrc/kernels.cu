@@ -1123,6 +1123,17 @@ void launch_center(const DeviceView& d, const SimScalars& s, bool bin, cudaStrea
   else k_center<false><<<nb, kBlock, 0, st>>>(d, s);
 }
 
+namespace {
+// Chunk 1 looks back at chunk 0, whose status word nothing sets (all zero).
+__global__ void k_wait_limit(const unsigned long long* status, uint32_t* error) {
+  if (threadIdx.x < 32) (void)scan_look_back(status, 1u, 0ull, error, kErrorScan);
+}
+}  // namespace
+
+void launch_wait_limit(const unsigned long long* status, uint32_t* error, cudaStream_t st) {
+  k_wait_limit<<<1, 32, 0, st>>>(status, error);
+}
+
 void launch_scan(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
   const uint32_t cells = (uint32_t)(s.gf * s.gf);
   const uint32_t nb = scan_blocks(cells);

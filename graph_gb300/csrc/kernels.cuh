@@ -119,6 +119,8 @@ enum PrepassMode : uint32_t { kPreGravity = 1, kPreCentroid = 2, kPreBin = 4 };
 void launch_prepass(const DeviceView& d, const SimScalars& s, uint32_t mode, cudaStream_t st);
 void launch_center(const DeviceView& d, const SimScalars& s, bool bin, cudaStream_t st);
 void launch_scan(const DeviceView& d, const SimScalars& s, cudaStream_t st);
+// The scans' bounded look-back against a status array nothing sets (2 words, zeroed).
+void launch_wait_limit(const unsigned long long* status, uint32_t* error, cudaStream_t st);
 void launch_scatter(const DeviceView& d, const SimScalars& s, cudaStream_t st);
 void launch_cells(const DeviceView& d, const SimScalars& s, cudaStream_t st);
 void launch_manybody(const DeviceView& d, const SimScalars& s, cudaStream_t st);

@@ -52,6 +52,8 @@ def load_library(build_if_missing: bool = True):
     lib.cgl_levels_noalloc.restype = C.c_int
     lib.cgl_random_draws.argtypes = [C.c_char_p, C.c_uint64, C.POINTER(C.c_double)]
     lib.cgl_random_draws.restype = C.c_int
+    lib.cgl_check_wait_limit.argtypes = [C.c_int32, C.POINTER(C.c_uint32)]
+    lib.cgl_check_wait_limit.restype = C.c_int
     _abi.declare(lib, "cgl")
     _LIB = lib
     return lib

@@ -277,6 +277,14 @@ const char* cgl_last_error(cgl_engine* e);
  * reproduce the draws.  seed_text is UTF-8. */
 cgl_status cgl_random_draws(const char* seed_text, uint64_t n, double* out);
 
+/* The bounded wait of the one-pass cell scans, run alone on `device`: one
+ * block looks back at a chunk whose status nothing ever sets, gives up after
+ * its poll limit (about a second) and raises its error bit, as a scan block
+ * does before the engine reports CGL_CUDA_ERROR.  *error_bits receives the
+ * bits raised (CGL_ERROR_SCAN expected); the context stays usable. */
+enum { CGL_ERROR_SCAN = 1 };
+cgl_status cgl_check_wait_limit(int32_t device, uint32_t* error_bits);
+
 /* Run the engine's kernels on a caller-owned cudaStream_t (NULL = engine's own). */
 cgl_status cgl_set_stream(cgl_engine* e, void* cuda_stream);
 /* Block until all queued work on the engine stream finished. */
