@@ -114,7 +114,7 @@ struct cgl_batch {
   std::vector<Job> jobs;
   size_t dev_bytes = 0;
   // point arena
-  Buf gid, pos, pos_alt, flags, jitter, key, rank, sorted_idx, sorted_pos;
+  Buf gid, pos, pos_alt, flags, jitter, key, rank, sorted_idx, sorted_pos, sib_list;
   // cell arena
   Buf counts, cell_start, cell_gid, big_list, big_sx, big_sy, big_ns, scan_status, scan_seq;
   Buf big_count, tick_ctr;
@@ -216,7 +216,8 @@ cgl_status reserve_points(cgl_batch* b, uint64_t cap) {
       (st = grow(b, b->pos_alt, cap * 8, keep * 8, -1)) || (st = grow(b, b->flags, cap, keep, 0)) ||
       (st = grow(b, b->jitter, cap * 8, keep * 8, -1)) || (st = grow(b, b->key, cap * 4, 0, -1)) ||
       (st = grow(b, b->rank, cap * 4, 0, -1)) || (st = grow(b, b->sorted_idx, cap * 4, 0, -1)) ||
-      (st = grow(b, b->sorted_pos, cap * 8, 0, -1)) || (st = grow(b, b->size, cap * 4, keep * 4, 0)))
+      (st = grow(b, b->sorted_pos, cap * 8, 0, -1)) || (st = grow(b, b->size, cap * 4, keep * 4, 0)) ||
+      (st = grow(b, b->sib_list, cap * 8, 0, -1)))
     return st;
   b->pts.cap = cap;
   return CGL_OK;
@@ -266,6 +267,7 @@ void refresh_view(cgl_batch* b) {
   v.rank = (uint32_t*)b->rank.p;
   v.sorted_idx = (uint32_t*)b->sorted_idx.p;
   v.sorted_pos = (float2*)b->sorted_pos.p;
+  v.sib_list = (uint2*)b->sib_list.p;
   v.counts = (uint32_t*)b->counts.p;
   v.cell_start = (uint32_t*)b->cell_start.p;
   v.scan_status = (unsigned long long*)b->scan_status.p;
@@ -918,7 +920,7 @@ cgl_status cgl_batch_destroy(cgl_batch* b) {
   cudaSetDevice(b->device);
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->graph) cudaGraphExecDestroy(b->graph);
-  Buf* all[] = {&b->gid, &b->pos, &b->pos_alt, &b->flags, &b->jitter, &b->key, &b->rank, &b->sorted_idx,
+  Buf* all[] = {&b->sib_list, &b->gid, &b->pos, &b->pos_alt, &b->flags, &b->jitter, &b->key, &b->rank, &b->sorted_idx,
                 &b->sorted_pos, &b->counts, &b->cell_start, &b->cell_gid, &b->big_list, &b->big_sx, &b->big_sy,
                 &b->big_ns, &b->scan_status, &b->scan_seq, &b->big_count, &b->tick_ctr, &b->rec, &b->acc, &b->rowptr,
                 &b->ent, &b->desc, &b->tiles, &b->heavy_in, &b->heavy_out, &b->ticks, &b->size, &b->cgrid_acc,

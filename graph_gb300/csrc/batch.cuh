@@ -20,6 +20,8 @@ constexpr uint32_t kLinkWarpsPerBlock = 8;   // light-row link pass: warps of on
 constexpr int kScanSub = 4;                  // scan: sub-chunks of kBlock x 4 cells per block
 constexpr int kChunk = 1024 * kScanSub;      // scan: cells per block
 constexpr uint32_t kBatchErrorScan = 1;      // error_word bit: a scan block's look-back gave up waiting
+constexpr uint32_t kBatchOutside = 4;        // big_count word: a binned point outside its space
+constexpr uint32_t kBatchSibs = 5;           // big_count word: the many-body pass's work items this tick
 
 // Per graph per tick: the f32 alpha uniform, the peel seed, and whether the
 // graph advances this tick (a graph that reached its tick budget, or whose
@@ -83,7 +85,10 @@ struct BatchView {
   uint32_t* big_list;          // [2 x cell arena] CTA cells, then warp cells: those above
                                // kWarpSmallCell from the front, the others from the back
   uint32_t* big_count;         // [8] CTA cells, heavy and light warp cells, warp-cell ticket, then [4] = 1
-                               // when a binned point lies outside its graph's space (zeroed each tick)
+                               // when a binned point lies outside its graph's space, [5] the many-body
+                               // pass's work items (zeroed each tick)
+  uint2* sib_list;             // [point arena] many-body work items: sorted positions (jA, jB), jB = kNoPoint
+                               // when jA is alone; the points of one parent cell (kb_cells)
   long long* big_sx;
   long long* big_sy;
   uint32_t* big_ns;

@@ -7,6 +7,7 @@
 // are graph-local, so a graph advances exactly as it would alone.
 #include "batch.cuh"
 #include "collision.cuh"
+#include "manybody_duo.cuh"
 #include "device_util.cuh"
 #include "warp_cells.cuh"
 
@@ -24,7 +25,6 @@ __device__ __forceinline__ uint32_t level_base(int l) {
 }
 
 // ---------------------------------------------------------------- prepass --
-constexpr uint32_t kBatchOutside = 4;   // big_count word: a binned point outside its space
 
 __device__ __forceinline__ void kb_bin(const BatchView& v, const GraphDesc& D, uint32_t P, float2 p) {
   const int cx = cell_index(p.x, D.csf, D.gf), cy = cell_index(p.y, D.csf, D.gf);
@@ -382,6 +382,32 @@ __device__ __forceinline__ float4 level_record(long long sx, long long sy, long 
   return r;
 }
 
+// The many-body pass's work items of one parent cell: its points are the
+// sorted positions [a0, a2) (the upper two children) then [b0, b2) (the lower
+// two), taken two at a time in that order, the last alone when their number
+// is odd.  Items are appended with one atomic per warp.  Called by all 32
+// lanes of the warp (lanes without a parent cell pass empty ranges).
+__device__ __forceinline__ void sib_items(const BatchView& v, uint32_t a0, uint32_t a2, uint32_t b0, uint32_t b2) {
+  const uint32_t n0 = a2 - a0, n = n0 + (b2 - b0);
+  const uint32_t items = (n + 1) >> 1;
+  const int lane = threadIdx.x & 31;
+  uint32_t incl = items;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  uint32_t base = 0;
+  if (lane == 31 && incl) base = atomicAdd(&v.big_count[kBatchSibs], incl);
+  base = __shfl_sync(0xffffffffu, base, 31) + incl - items;
+  for (uint32_t t = 0; t < items; ++t) {
+    const uint32_t i0 = 2 * t, i1 = i0 + 1;
+    const uint32_t jA = i0 < n0 ? a0 + i0 : b0 + (i0 - n0);
+    const uint32_t jB = i1 >= n ? kNoPoint : i1 < n0 ? a0 + i1 : b0 + (i1 - n0);
+    v.sib_list[base + t] = make_uint2(jA, jB);
+  }
+}
+
 // One CTA per (graph, tile) of the work list.  A tile is T x T finest cells
 // (T = GraphDesc::tile <= 32); each thread takes a 2 x 2 quad of them, whose
 // sums make one cell of the next level in registers; the levels above, inside
@@ -401,12 +427,17 @@ __global__ void __launch_bounds__(kBlock) kb_cells(BatchView v) {
   const bool live = (int)threadIdx.x < Q * Q;
   const int qx = (int)threadIdx.x % Q, qy = (int)threadIdx.x / Q;
   long long sx = 0, sy = 0, sn = 0;
+  uint32_t a0 = 0, a2 = 0, b0 = 0, b2 = 0;   // the quad's points: [a0, a2) and [b0, b2)
   if (live) {
     const int cx = tile_x * T + 2 * qx, cy = tile_y * T + 2 * qy;
     const uint32_t l0 = (uint32_t)(cy * gf + cx), l1 = l0 + (uint32_t)gf;
     const uint32_t c0 = D.cell_off + l0, c1 = D.cell_off + l1;
-    const uint32_t a0 = v.cell_start[c0], a1 = v.cell_start[c0 + 1], a2 = v.cell_start[c0 + 2];
-    const uint32_t b0 = v.cell_start[c1], b1 = v.cell_start[c1 + 1], b2 = v.cell_start[c1 + 2];
+    a0 = v.cell_start[c0];
+    const uint32_t a1 = v.cell_start[c0 + 1];
+    a2 = v.cell_start[c0 + 2];
+    b0 = v.cell_start[c1];
+    const uint32_t b1 = v.cell_start[c1 + 1];
+    b2 = v.cell_start[c1 + 2];
     long long x, y;
     kb_finest_cell(v, D, tp.seed_bits, c0, l0, a0, a1, x, y);
     sx += x; sy += y;
@@ -420,6 +451,7 @@ __global__ void __launch_bounds__(kBlock) kb_cells(BatchView v) {
     const int G = gf >> 1;   // level L - 2
     v.rec[D.rec_off + level_base(L - 2) + (tile_y * Q + qy) * G + tile_x * Q + qx] = level_record(sx, sy, sn, D.fx);
   }
+  sib_items(v, a0, a2, b0, b2);   // every lane of the warp (empty ranges outside the tile)
   smx[threadIdx.x] = sx; smy[threadIdx.x] = sy; smn[threadIdx.x] = sn;
   __syncthreads();
   int gsz = Q;
@@ -477,6 +509,25 @@ __global__ void __launch_bounds__(kBlock) kb_coarse(BatchView v) {
 }
 
 // --------------------------------------------------------------- manybody --
+// The near field (force-nearfield.frag:199-263) of the point at sorted
+// position j, added to its level velocity, and the update.
+template <bool FAST>
+__device__ __forceinline__ void kb_finish_point(const BatchView& v, const GraphDesc& D, uint32_t j, uint32_t P, float2 p,
+                                                int fcx, int fcy, float2 vel, float k) {
+  const PairUnits pu = v.units;
+  const float4* fine = v.rec + D.rec_off + level_base(D.levels - 1);
+  const float2 rj = v.jitter[P];
+  float2 nf = near_terms<FAST>(fine, v.cell_start + D.cell_off, v.sorted_pos, D.gf, fcx, fcy, j, p, rj, k, pu);
+  nf = add2(nf, mul2(nf, rj, pu), pu);
+  const float max_step = __fmul_rn(2.0f, D.csf);
+  const float2 nsq = mul2(nf, nf, pu);
+  const float speed = __fsqrt_rn(__fadd_rn(nsq.x, nsq.y));
+  if (speed > max_step) nf = mul2(nf, splat(__fdiv_rn(max_step, speed)), pu);
+  vel = add2(vel, nf, pu);
+  if (!(v.flags[P] & kPinned)) v.pos[P] = integrate(p, vel.x, vel.y, D.friction, D.space);
+}
+
+// One point (force-level.frag:70-95 for every level, then the near field).
 // FAST: the repulsion quotients come from the reciprocals (quotient_by_recip(k)).
 // GUARDED: the level terms without the range flag (the job's level_guard and
 // no binned point of the batch outside its space this tick).
@@ -489,36 +540,76 @@ __device__ __forceinline__ void kb_manybody_point(const BatchView& v, const Grap
   const float4* rec = v.rec + D.rec_off;
   float2 vel = make_float2(0.f, 0.f);
 #pragma unroll 1
-  for (int l = 0; l < L; ++l) {   // force-level.frag:70-95
+  for (int l = 0; l < L; ++l) {
     const int sh = L - 1 - l;
     vel = add2(vel, level_terms<FAST, FAST, GUARDED>(rec + level_base(l), 4 << l, fcx >> sh, fcy >> sh, p, k, pu), pu);
   }
-  // near field (force-nearfield.frag:199-263)
-  const float2 rj = v.jitter[P];
-  float2 nf = near_terms<FAST>(rec + level_base(L - 1), v.cell_start + D.cell_off, v.sorted_pos, gf, fcx, fcy, j, p, rj,
-                               k, pu);
-  nf = add2(nf, mul2(nf, rj, pu), pu);
-  const float max_step = __fmul_rn(2.0f, D.csf);
-  const float2 nsq = mul2(nf, nf, pu);
-  const float speed = __fsqrt_rn(__fadd_rn(nsq.x, nsq.y));
-  if (speed > max_step) nf = mul2(nf, splat(__fdiv_rn(max_step, speed)), pu);
-  vel = add2(vel, nf, pu);
-  if (!(v.flags[P] & kPinned)) v.pos[P] = integrate(p, vel.x, vel.y, D.friction, D.space);
+  kb_finish_point<FAST>(v, D, j, P, p, fcx, fcy, vel, k);
 }
 
-__global__ void __launch_bounds__(kBlock) kb_manybody(BatchView v) {
-  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t total = v.cell_start[v.cell_hwm];
-  if (j >= total) return;
-  const uint32_t P = v.sorted_idx[j];
-  const uint32_t g = v.gid[P];
+// Two points of one parent cell (sorted positions jA, jB; the same finest
+// cell or sibling cells) on f32x2 lanes (manybody_duo.cuh): the levels above
+// the finest are the same cells for both, the finest level is one walk over
+// the shared 6x6 block that each point takes outside its own 3x3
+// (level_terms_duo_sibs); each lane is the one-point chain, in its order, so
+// each result is bit for bit kb_manybody_point's.  A level with a length
+// outside the in-range sequences is summed again per point with the tested
+// terms; the near fields are per point.  `single`: jA alone.
+template <bool GUARD>
+__device__ __forceinline__ void kb_manybody_sibs(const BatchView& v, const GraphDesc& D, uint32_t jA, uint32_t jB,
+                                                 bool single, float k) {
+  const uint32_t PA = v.sorted_idx[jA], PB = v.sorted_idx[jB];
+  const float2 pA = v.sorted_pos[jA], pB = v.sorted_pos[jB];
+  const int gf = D.gf, L = D.levels;
+  const int ax = cell_index(pA.x, D.csf, gf), ay = cell_index(pA.y, D.csf, gf);
+  const int bx = cell_index(pB.x, D.csf, gf), by = cell_index(pB.y, D.csf, gf);
+  const PairUnits pu = v.units;
+  const float4* rec = v.rec + D.rec_off;
+  const Duo P = {make_float2(pA.x, pB.x), make_float2(pA.y, pB.y)};
+  Duo vel = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll 1
+  for (int l = 0; l < L; ++l) {
+    const int sh = L - 1 - l;
+    const float4* lv = rec + level_base(l);
+    const int G = 4 << l;
+    bool out = false;
+    Duo w = sh ? level_terms_duo<!GUARD>(lv, G, ax >> sh, ay >> sh, P, k, pu, out)
+               : level_terms_duo_sibs<!GUARD>(lv, G, ax, ay, bx, by, P, k, pu, out);
+    if (!GUARD && out) {   // a length outside the sequences: each point's level with the tested terms
+      const float2 a = level_terms<true, false>(lv, G, ax >> sh, ay >> sh, pA, k, pu);
+      const float2 b = level_terms<true, false>(lv, G, bx >> sh, by >> sh, pB, k, pu);
+      w.x = make_float2(a.x, b.x);
+      w.y = make_float2(a.y, b.y);
+    }
+    vel.x = add2(vel.x, w.x, pu);
+    vel.y = add2(vel.y, w.y, pu);
+  }
+  kb_finish_point<true>(v, D, jA, PA, pA, ax, ay, make_float2(vel.x.x, vel.y.x), k);
+  if (!single) kb_finish_point<true>(v, D, jB, PB, pB, bx, by, make_float2(vel.x.y, vel.y.y), k);
+}
+
+// One work item per thread: up to two points of one parent cell (sib_list,
+// written by kb_cells; big_count[kBatchSibs] items this tick).  Four blocks
+// per SM, as the plain engine's two-point pass.
+__global__ void __launch_bounds__(kBlock, 4) kb_manybody(BatchView v) {
+  const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= __ldg(&v.big_count[kBatchSibs])) return;
+  const uint2 it = v.sib_list[w];
+  const bool single = it.y == kNoPoint;
+  const uint32_t jA = it.x, jB = single ? it.x : it.y;
+  const uint32_t PA = v.sorted_idx[jA];
+  const uint32_t g = v.gid[PA];
   const GraphDesc& D = v.desc[g];
   const BatchTick tp = tick_of(v, g);
-  const float2 p = v.sorted_pos[j];
   const float k = __fmul_rn(tp.alpha, D.repulsion);
-  if (!quotient_by_recip(k)) kb_manybody_point<false>(v, D, j, P, p, k);
-  else if (D.level_guard && __ldg(&v.big_count[kBatchOutside]) == 0) kb_manybody_point<true, true>(v, D, j, P, p, k);
-  else kb_manybody_point<true>(v, D, j, P, p, k);
+  if (!quotient_by_recip(k)) {   // quotients outside the reciprocal method's range: one point at a time
+    kb_manybody_point<false>(v, D, jA, PA, v.sorted_pos[jA], k);
+    if (!single) kb_manybody_point<false>(v, D, jB, v.sorted_idx[jB], v.sorted_pos[jB], k);
+  } else if (D.level_guard && __ldg(&v.big_count[kBatchOutside]) == 0) {
+    kb_manybody_sibs<true>(v, D, jA, jB, single, k);
+  } else {
+    kb_manybody_sibs<false>(v, D, jA, jB, single, k);
+  }
 }
 
 // ------------------------------------------------------------------- link --
@@ -715,7 +806,7 @@ void batch_launch_tick(const BatchView& v, cudaStream_t st, cudaStream_t side, c
   kb_bigcells<<<8 * sm_count(), kBlock, 0, st>>>(v);   // as k_bigcells: 8 blocks per SM
   if (v.n_tiles) kb_cells<<<v.n_tiles, kBlock, 0, st>>>(v);
   if (v.slots) kb_coarse<<<v.slots, kBlock, 0, st>>>(v);
-  if (v.point_hwm) kb_manybody<<<blocks(v.point_hwm), kBlock, 0, st>>>(v);
+  if (v.point_hwm) kb_manybody<<<blocks(v.point_hwm), kBlock, 0, st>>>(v);   // items <= points
   for (int dir = 0; dir < 2; ++dir) {
     const float2* src = dir == 0 ? v.pos : v.pos_alt;
     float2* dst = dir == 0 ? v.pos_alt : v.pos;

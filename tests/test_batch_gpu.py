@@ -224,3 +224,30 @@ def test_batch_device_and_host_ingest_match_oracle(dmin):
     orc.step(4)
     want = orc.get_point_positions()
     assert same_bits(got, want), first_mismatch(got, want)
+
+
+def test_sibling_pairs_in_awkward_jobs():
+    # the many-body pass takes two points of one parent cell per thread: cells under 2 units (range
+    # flags and the tested re-sums), coincident stacks, a dense job, absent points, odd counts
+    from graph_gb300.batch import Batch
+    rng = np.random.default_rng(44)
+    jobs = []
+    pos = rng.uniform(0, 256, size=2 * 20000).astype(np.float32)                 # finest cells 0.5 units
+    jobs.append((pos, generators.erdos_renyi(20000, 4, 1), dict(space_size=256.0, random_seed=11)))
+    stacks = rng.uniform(100, 900, size=(40, 2))
+    pos = stacks[rng.integers(0, 40, 6000)].astype(np.float32).reshape(-1)          # coincident points
+    jobs.append((pos, None, dict(space_size=1024.0, random_seed=12)))
+    pos = rng.uniform(0, 2048, size=2 * 100000).astype(np.float32)                  # ~0.4 points a cell
+    pos[2 * rng.integers(0, 100000, 500)] = np.nan                                  # absent points
+    jobs.append((pos, generators.barabasi_albert(100000, 3, 2), dict(space_size=2048.0, random_seed=13)))
+    pos = rng.normal(1024, 30, size=2 * 90000).clip(0, 2048).astype(np.float32)    # dense, clustered
+    jobs.append((pos, None, dict(space_size=2048.0, random_seed=14, simulation_repulsion=0.7)))
+    jobs.append((rng.uniform(0, 512, size=2 * 3).astype(np.float32), None, dict(space_size=512.0, random_seed=15)))
+    ticks = 6
+    with Batch() as b:
+        ids = [b.add(p, l, **f) for p, l, f in jobs]
+        b.step(ticks)
+        got = b.get_positions_many(ids)
+    for (p, l, f), g in zip(jobs, got):
+        want = _alone(p, l, f, ticks)
+        assert same_bits(g, want), (f, first_mismatch(g, want))
