@@ -738,14 +738,21 @@ __global__ void __launch_bounds__(kBlock, 6) k_manybody(DeviceView d, SimScalars
 
 // ------------------------------------------------------------------- link --
 // Hub rows: a list of thousands of links is one strictly sequential chain
-// (each spring reads the velocity the previous one left).  One CTA per hub:
-// warps 1..7 gather the next kHubChunk links (entry, neighbour position,
-// rest length) into one shared buffer while lane 0 of warp 0 runs the chain
-// over the other, so the chain never waits on a global load.
+// (each spring reads the velocity the previous one left).  One CTA per hub, in
+// rounds of kHubChunk links: in round c lane 0 of warp 0 runs the chain over
+// chunk c from shared memory, recording the velocity before each link, while
+// warps 1..7 stage chunk c + 1 (entry, neighbour position, rest length) and
+// check chunk c - 1 link by link (spring_chain_check), so neither the loads
+// nor the checks sit on the chain.  Three buffers rotate.  A chunk whose check
+// fails runs again with the correctly rounded springs from its recorded
+// starting velocity, and so does the chunk that followed it.
 constexpr int kHubChunk = kBlock - 32;
+constexpr int kHubBufs = 3;
 struct HubStage {
-  float4 a[2][kHubChunk];   // neighbour x, y, rest length d, 0.99 d
-  float4 b[2][kHubChunk];   // strength, bias, absent flag, rcp.approx(0.99 d)
+  float4 a[kHubBufs][kHubChunk];   // neighbour x, y, rest length d, 0.99 d
+  float4 b[kHubBufs][kHubChunk];   // strength, bias, absent flag, rcp.approx(0.99 d)
+  float2 v[kHubBufs][kHubChunk];   // velocity before each link, when the chunk ran on the fast chain
+  int fast[kHubBufs];              // the chunk ran on the fast chain (its check is due)
 };
 
 // Stages link at + (thread - 32); returns kStagedAbsent when its target is
@@ -765,28 +772,39 @@ __device__ __forceinline__ int hub_fill(HubStage& st, int buf, uint32_t at, uint
   return (absent ? kStagedAbsent : 0) | (__uint_as_float(en.w) != 1.0f ? kStagedStrength : 0);
 }
 
-// The fast chain over one staged chunk without absent targets (a full chunk
-// with a constant trip count); returns spring_step_fast's flag.
+// The fast chain over one staged chunk without absent targets, recording the
+// velocity before each link (a full chunk with a constant trip count).
 template <bool UNIT_STRENGTH>
-__device__ __forceinline__ bool hub_chunk_fast(const float4* A, const float4* B, uint32_t len, float2 pp, float2& vel,
-                                               float sa, PairUnits pu) {
-  bool out = false;
+__device__ __forceinline__ void hub_chunk_chain(const float4* A, const float4* B, float2* V, uint32_t len, float2 pp,
+                                                float2& vel, float sa, PairUnits pu) {
   if (len == (uint32_t)kHubChunk) {
 #pragma unroll 4
     for (int k = 0; k < kHubChunk; ++k) {
       const float4 a = A[k];
       const float4 b = B[k];
-      spring_step_fast<UNIT_STRENGTH>(pp, vel, make_float2(a.x, a.y), a.z, a.w, b.w, sa, b.x, b.y, pu, out);
+      V[k] = vel;
+      spring_chain_step<UNIT_STRENGTH>(pp, vel, make_float2(a.x, a.y), a.z, a.w, b.w, sa, b.x, b.y, pu);
     }
   } else {
 #pragma unroll 4
     for (uint32_t k = 0; k < len; ++k) {
       const float4 a = A[k];
       const float4 b = B[k];
-      spring_step_fast<UNIT_STRENGTH>(pp, vel, make_float2(a.x, a.y), a.z, a.w, b.w, sa, b.x, b.y, pu, out);
+      V[k] = vel;
+      spring_chain_step<UNIT_STRENGTH>(pp, vel, make_float2(a.x, a.y), a.z, a.w, b.w, sa, b.x, b.y, pu);
     }
   }
-  return out;
+}
+
+// The correctly rounded springs over one staged chunk (absent targets skipped).
+__device__ __forceinline__ void hub_chunk_exact(const float4* A, const float4* B, uint32_t len, float2 pp, float2& vel,
+                                                float sa, PairUnits pu) {
+  for (uint32_t k = 0; k < len; ++k) {
+    const float4 a = A[k];
+    const float4 b = B[k];
+    if (b.z != 0.f) continue;
+    spring_step(pp, vel, make_float2(a.x, a.y), a.z, a.w, sa, b.x, b.y, pu);
+  }
 }
 
 // Blocks [0, nhub) take the hub rows rows[0..nhub) (longest first, so the
@@ -815,39 +833,50 @@ __global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, con
     }
     const uint32_t e0 = rowptr[p], e1 = rowptr[p + 1];
     const uint32_t chunks = (e1 - e0 + kHubChunk - 1) / kHubChunk;
+    auto chunk_len = [&](uint32_t c) { return min((uint32_t)kHubChunk, e1 - e0 - c * kHubChunk); };
     int staged = 0;
     if (threadIdx.x >= 32) staged = hub_fill(hub, 0, e0, e1, ent, src, span, s.link_r0, s.link_distance);
-    int absent = __syncthreads_or(staged & kStagedAbsent);       // some target of the chunk is absent
-    int strengths = __syncthreads_or(staged & kStagedStrength);  // some strength of the chunk is not 1
+    int absent = __syncthreads_or(staged & kStagedAbsent);       // some target of chunk c is absent
+    int strengths = __syncthreads_or(staged & kStagedStrength);  // some strength of chunk c is not 1
     float2 vel = make_float2(0.f, 0.f);
-    for (uint32_t c = 0; c < chunks; ++c) {
-      const int buf = c & 1;
+    // round c: chain over chunk c, staging of chunk c + 1, check of chunk c - 1
+    for (uint32_t c = 0; c <= chunks; ++c) {
+      const int buf = c % kHubBufs, prev = (c + kHubBufs - 1) % kHubBufs;
       int next = 0;
+      bool bad = false;
       if (threadIdx.x >= 32) {
         if (c + 1 < chunks)
-          next = hub_fill(hub, buf ^ 1, e0 + (c + 1) * kHubChunk, e1, ent, src, span, s.link_r0, s.link_distance);
-      } else if (threadIdx.x == 0) {
-        const uint32_t len = min((uint32_t)kHubChunk, e1 - e0 - c * kHubChunk);
-        const float4* A = hub.a[buf];
-        const float4* B = hub.b[buf];
-        bool exact = absent != 0;
-        if (!absent) {   // no per-link branch: the chain runs back to back
-          const float2 v0 = vel;
-          const bool out = strengths ? hub_chunk_fast<false>(A, B, len, pp, vel, sa, pu)
-                                     : hub_chunk_fast<true>(A, B, len, pp, vel, sa, pu);
-          if (out) { vel = v0; exact = true; }
+          next = hub_fill(hub, (c + 1) % kHubBufs, e0 + (c + 1) * kHubChunk, e1, ent, src, span, s.link_r0,
+                          s.link_distance);
+        const uint32_t k = threadIdx.x - 32;
+        if (c > 0 && hub.fast[prev] && k < chunk_len(c - 1)) {
+          const float4 a = hub.a[prev][k];
+          bad = !spring_chain_check(pp, hub.v[prev][k], make_float2(a.x, a.y), a.z, a.w, hub.b[prev][k].w, pu);
         }
-        if (exact) {   // absent targets, or operands outside the in-range sequences
-          for (uint32_t k = 0; k < len; ++k) {
-            const float4 a = A[k];
-            const float4 b = B[k];
-            if (b.z != 0.f) continue;
-            spring_step(pp, vel, make_float2(a.x, a.y), a.z, a.w, sa, b.x, b.y, pu);
-          }
+      } else if (threadIdx.x == 0 && c < chunks) {
+        const uint32_t len = chunk_len(c);
+        if (absent) {   // absent targets: the correctly rounded springs, skipping them
+          hub_chunk_exact(hub.a[buf], hub.b[buf], len, pp, vel, sa, pu);
+          hub.fast[buf] = 0;
+        } else {        // no per-link branch: the chain runs back to back
+          if (strengths) hub_chunk_chain<false>(hub.a[buf], hub.b[buf], hub.v[buf], len, pp, vel, sa, pu);
+          else hub_chunk_chain<true>(hub.a[buf], hub.b[buf], hub.v[buf], len, pp, vel, sa, pu);
+          hub.fast[buf] = 1;
         }
       }
       absent = __syncthreads_or(next & kStagedAbsent);
       strengths = __syncthreads_or(next & kStagedStrength);
+      if (__syncthreads_or(bad)) {   // chunk c - 1 left the sequences: it and chunk c again, exactly
+        if (threadIdx.x == 0) {
+          vel = hub.v[prev][0];
+          hub_chunk_exact(hub.a[prev], hub.b[prev], chunk_len(c - 1), pp, vel, sa, pu);
+          if (c < chunks) {
+            hub_chunk_exact(hub.a[buf], hub.b[buf], chunk_len(c), pp, vel, sa, pu);
+            hub.fast[buf] = 0;
+          }
+        }
+        __syncthreads();
+      }
     }
     if (threadIdx.x == 0) dst[p] = (f & kPinned) ? pp : integrate(pp, vel.x, vel.y, s.friction, s.space);
     return;

@@ -177,6 +177,29 @@ def test_springs_outside_the_in_range_sequences():
         _assert_same(eng, orc, ("short springs", t))
 
 
+def test_springs_outside_the_sequences_in_later_chunks():
+    # The hub chain runs a chunk while the chunk before it is checked: a chunk
+    # that fails its check runs again with the correctly rounded springs, and
+    # so does the chunk after it.  Here the failing links sit in a middle chunk
+    # and in the last one (the check of the last chunk comes after the chain
+    # has ended), and two failing chunks follow each other.
+    n = 1600
+    rng = np.random.default_rng(35)
+    pos = rng.uniform(1000, 1400, size=2 * n).astype(np.float32)
+    hub = pos[0:2].copy()
+    for lo, hi in ((700, 712), (900, 906), (1120, 1126), (n - 8, n)):
+        pos[2 * lo:2 * hi] = (hub[None, :] + rng.uniform(-0.3, 0.3, size=(hi - lo, 2))).reshape(-1).astype(np.float32)
+    pos[2 * 1300:2 * 1302] = np.tile(hub, 2)                                         # on top of the hub
+    star = np.stack([np.zeros(n - 1), np.arange(1, n)], axis=1)
+    links = np.concatenate([star, rng.integers(1, n, size=(800, 2))]).astype(np.float32).reshape(-1)
+    eng, orc = make_pair(pos, links, dict(random_seed=35, simulation_link_distance=0.3))
+    assert eng.layout().max_degree_in > 256 or eng.layout().max_degree_out > 256
+    for t in range(4):
+        eng.step(1)
+        orc.step(1)
+        _assert_same(eng, orc, ("later chunks", t))
+
+
 def test_level_terms_under_one_unit():
     # Space 32 and a 128-cell finest grid: cells 0.25 units wide, so level
     # centroids within one unit of a point are common and those levels are
