@@ -41,6 +41,8 @@ struct cgl_engine {
   cudaStream_t stream = nullptr;
   uint32_t* h_error = nullptr;   // host-mapped error word (DeviceView::error_word)
   uint32_t* d_error = nullptr;
+  cudaStream_t side = nullptr;   // the outgoing hub chains beside the collision sums
+  cudaEvent_t fork = nullptr, join = nullptr;
 
   // staged input (copied at set_*, applied at render)
   bool have_pos_input = false, have_link_input = false, have_strength = false, have_sizes = false;
@@ -100,6 +102,7 @@ struct cgl_engine {
   DevBuf b_big_list, b_big_count, b_big_sx, b_big_sy, b_big_ns;
   DevBuf b_params, b_tick_ctr;
   DevBuf b_rowptr_in, b_rowptr_out, b_ent_in, b_ent_out, b_heavy_in, b_heavy_out;
+  DevBuf b_hub_out;   // 1 for the points whose outgoing list runs on a hub CTA
   DevBuf b_woff_in, b_woff_out, b_lane_ent_in, b_lane_ent_out;   // light rows by warps (kernels.cuh)
   uint32_t n_heavy_in = 0, n_heavy_out = 0;
   DevBuf b_size, b_cgrid_acc, b_cgrid;
@@ -188,7 +191,7 @@ void dev_free_all(cgl_engine* e) {
                    &e->b_tickets, &e->b_rec, &e->b_acc, &e->b_centroid, &e->b_params, &e->b_tick_ctr,
                    &e->b_rowptr_in, &e->b_rowptr_out, &e->b_ent_in, &e->b_ent_out, &e->b_size,
                    &e->b_cgrid_acc, &e->b_cgrid, &e->b_big_list, &e->b_big_count,
-                   &e->b_big_sx, &e->b_big_sy, &e->b_big_ns, &e->b_heavy_in, &e->b_heavy_out,
+                   &e->b_big_sx, &e->b_big_sy, &e->b_big_ns, &e->b_heavy_in, &e->b_heavy_out, &e->b_hub_out,
                    &e->b_cl_of, &e->b_cl_coeff, &e->b_cl_custom, &e->b_cl_acc, &e->b_texture,
                    &e->b_woff_in, &e->b_woff_out, &e->b_lane_ent_in, &e->b_lane_ent_out, &e->b_pair_start,
                    &e->b_pair_list, &e->b_idx_s, &e->b_pos_s, &e->b_bin_state};
@@ -335,6 +338,12 @@ cgl_status enqueue_tick(cgl_engine* e, cudaStream_t st, cudaEvent_t* ev) {
   auto mark = [&](int stage, int which) {
     if (ev) cudaEventRecord(ev[2 * stage + which], st);
   };
+  // With collision right after the link passes (no cluster pass between), the
+  // outgoing pass's hub chains run on a second stream while its light rows and
+  // then the collision sums of every other point run on this one; the hubs'
+  // points are summed once their chains end.  Not in a stage profile (ev).
+  const bool overlap =
+      p.link_in && p.link_out && p.coll && !p.clus && p.mb && !ev && d.n_heavy_out > 0 && e->b_hub_out.p;
   if (p.cent) CU(cudaMemsetAsync(d.centroid, 0, 3 * sizeof(long long), st));
   if (p.mb) CU(cudaMemsetAsync(d.big_count, 0, 8 * sizeof(uint32_t), st));
   uint32_t mode = 0;
@@ -358,7 +367,19 @@ cgl_status enqueue_tick(cgl_engine* e, cudaStream_t st, cudaEvent_t* ev) {
     if (p.link_in) launch_link(d, s, 0, false, st);
     mark(6, 1);
     mark(7, 0);
-    if (p.link_out) launch_link(d, s, 1, p.link_in, st);
+    if (p.link_out && !overlap) launch_link(d, s, 1, p.link_in, st);
+    if (overlap) {
+      CU(cudaEventRecord(e->fork, st));
+      CU(cudaStreamWaitEvent(e->side, e->fork, 0));
+      launch_link(d, s, 1, p.link_in, e->side, kLinkHubs);
+      CU(cudaEventRecord(e->join, e->side));
+      launch_link(d, s, 1, p.link_in, st, kLinkLight);
+      launch_collision_sums(d, s, d.sorted_idx, (uint32_t)e->live, (const uint8_t*)e->b_hub_out.p, st);
+      CU(cudaStreamWaitEvent(st, e->join, 0));
+      launch_collision_sums(d, s, d.heavy_out, d.n_heavy_out, nullptr, st);
+      launch_collision_convert(d, s, st);
+      launch_collision_force(d, s, d.sorted_idx, (uint32_t)e->live, st);
+    }
     mark(7, 1);
     if (!(p.link_in && p.link_out))
       CU(cudaMemcpyAsync(d.pos, d.pos_alt, e->N * sizeof(float2), cudaMemcpyDeviceToDevice, st));
@@ -372,7 +393,7 @@ cgl_status enqueue_tick(cgl_engine* e, cudaStream_t st, cudaEvent_t* ev) {
     launch_cluster_force(d, s, st);
     mark(10, 1);
   }
-  if (p.coll) {
+  if (p.coll && !overlap) {
     // the many-body pass left every live point in sorted_idx, grouped by cell
     const uint32_t* order = p.mb ? d.sorted_idx : nullptr;
     mark(8, 0); launch_collision_grid(d, s, order, (uint32_t)e->live, st); mark(8, 1);
@@ -426,7 +447,8 @@ cgl_status prepare_tick(cgl_engine* e) {
   cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
   if (st) { if (g) cudaGraphDestroy(g); return st; }
   if (ce != cudaSuccess) return fail(e, CGL_CUDA_ERROR, "graph capture: %s", cudaGetErrorString(ce));
-  ce = cudaGraphInstantiate(&e->graph, g, 0);
+  // node priorities as captured: the hub chains' stream goes first (enqueue_tick)
+  ce = cudaGraphInstantiate(&e->graph, g, cudaGraphInstantiateFlagUseNodePriority);
   cudaGraphDestroy(g);
   if (ce != cudaSuccess) { e->graph = nullptr; return fail(e, CGL_CUDA_ERROR, "graph instantiate: %s", cudaGetErrorString(ce)); }
   e->graph_dirty = false;
@@ -847,6 +869,12 @@ cgl_status build_graph(cgl_engine* e, double alpha, uint64_t N, uint64_t E) {
     CU(cudaStreamSynchronize(e->stream));
     }
     if ((st = build_link_warps(e))) return st;
+    // the points whose outgoing list runs on a hub CTA (the collision sums of
+    // the other points need not wait for those chains)
+    if ((st = dev_reserve(e, e->b_hub_out, std::max<size_t>(n, 1), true))) return st;
+    launch_mark_hubs((const uint32_t*)e->b_heavy_out.p, e->n_heavy_out, (uint8_t*)e->b_hub_out.p, e->stream);
+    CU(cudaGetLastError());
+    CU(cudaStreamSynchronize(e->stream));
   }
   if (e->clusters_dirty || pos_changed) {
     // Clusters.create (Clusters/index.ts:54-100), src/index.ts:1668
@@ -933,6 +961,13 @@ cgl_status cgl_create(const cgl_config* cfg, cgl_engine** out) {
   if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking);
   if (ce == cudaSuccess) ce = cudaMallocHost((void**)&e->h_params, kParamChunk * sizeof(TickParams));
   if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->params_copied, cudaEventDisableTiming);
+  if (ce == cudaSuccess) {   // the hub chains' stream first in line for the SMs: the longest chain starts at once
+    int lo = 0, hi = 0;
+    ce = cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    if (ce == cudaSuccess) ce = cudaStreamCreateWithPriority(&e->side, cudaStreamNonBlocking, hi);
+  }
+  if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming);
+  if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->join, cudaEventDisableTiming);
   if (ce == cudaSuccess) ce = cudaHostAlloc((void**)&e->h_error, sizeof(uint32_t), cudaHostAllocMapped);
   if (ce == cudaSuccess) ce = cudaHostGetDevicePointer((void**)&e->d_error, e->h_error, 0);
   if (ce != cudaSuccess) {
@@ -940,6 +975,9 @@ cgl_status cgl_create(const cgl_config* cfg, cgl_engine** out) {
     static thread_local std::string create_err;
     create_err = cudaGetErrorString(ce);
     if (e->own_stream) cudaStreamDestroy(e->own_stream);
+    if (e->side) cudaStreamDestroy(e->side);
+    if (e->fork) cudaEventDestroy(e->fork);
+    if (e->join) cudaEventDestroy(e->join);
     if (e->h_params) cudaFreeHost(e->h_params);
     if (e->h_error) cudaFreeHost(e->h_error);
     delete e;
@@ -967,6 +1005,9 @@ cgl_status cgl_destroy(cgl_engine* e) {
   if (e->params_copied) cudaEventDestroy(e->params_copied);
   if (e->h_params) cudaFreeHost(e->h_params);
   if (e->h_error) cudaFreeHost(e->h_error);
+  if (e->side) cudaStreamDestroy(e->side);
+  if (e->fork) cudaEventDestroy(e->fork);
+  if (e->join) cudaEventDestroy(e->join);
   if (e->own_stream) cudaStreamDestroy(e->own_stream);
   delete e;
   return CGL_OK;

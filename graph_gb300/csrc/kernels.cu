@@ -815,16 +815,19 @@ __global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, con
                                                  const uint4* __restrict__ ent, const uint32_t* __restrict__ woff,
                                                  const uint4* __restrict__ lane_ent, const float2* __restrict__ src,
                                                  float2* __restrict__ dst, const uint32_t* __restrict__ rows,
-                                                 uint32_t nrows, uint32_t nhub) {
+                                                 uint32_t nrows, uint32_t nhub, uint32_t block0) {
   // ForceLink.run (ForceLink/index.ts:221-263), force-spring.ts:38-96
+  // block0: the first block's place in the whole pass (a launch of the light
+  // rows alone starts at nhub)
+  const uint32_t bx = blockIdx.x + block0;
   extern __shared__ float4 hub_smem[];   // a HubStage when nhub > 0, else nothing
   HubStage& hub = *reinterpret_cast<HubStage*>(hub_smem);
   const TickParams tp = tick_params(d);
   const float sa = __fmul_rn(s.link_spring, tp.alpha);
   const PairUnits pu = s.units;
   const float span = __fsub_rn(s.link_r1, s.link_r0);
-  if (blockIdx.x < nhub) {
-    const uint32_t p = rows[blockIdx.x];
+  if (bx < nhub) {
+    const uint32_t p = rows[bx];
     const float2 pp = src[p];
     const uint8_t f = d.flags[p];
     if (f & kAbsent) {
@@ -881,7 +884,7 @@ __global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, con
     if (threadIdx.x == 0) dst[p] = (f & kPinned) ? pp : integrate(pp, vel.x, vel.y, s.friction, s.space);
     return;
   }
-  const uint32_t t = nhub + (blockIdx.x - nhub) * kBlock + threadIdx.x;
+  const uint32_t t = nhub + (bx - nhub) * kBlock + threadIdx.x;
   if (t >= nrows) return;
   const uint32_t p = rows[t];
   const float2 pp = src[p];
@@ -957,14 +960,16 @@ __global__ void __launch_bounds__(kBlock) k_fill_lanes(const uint32_t* __restric
 // Points are taken in `order` (the many-body pass's cell order) when given,
 // so the lanes of a warp fall into a few grid cells.
 __global__ void __launch_bounds__(kBlock) k_coll_grid(DeviceView d, SimScalars s, const uint32_t* __restrict__ order,
-                                                      uint32_t count) {
-  // build-grid.vert:28-62 for the 4 offsets (ForceCollision/index.ts:19-24)
+                                                      uint32_t count, const uint8_t* __restrict__ skip) {
+  // build-grid.vert:28-62 for the 4 offsets (ForceCollision/index.ts:19-24);
+  // points marked in `skip` are left to another launch (integer sums: the
+  // grids do not depend on the order in which points are added)
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t i = 0;
   bool live = t < count;
   if (live) {
     i = order ? order[t] : t;
-    live = !(d.flags[i] & kAbsent);
+    live = !(d.flags[i] & kAbsent) && !(skip && skip[i]);
   }
   if (!__any_sync(0xffffffffu, live)) return;   // warp-uniform
   float2 p = make_float2(0.f, 0.f);
@@ -1211,7 +1216,8 @@ void launch_manybody(const DeviceView& d, const SimScalars& s, cudaStream_t st) 
   }
 }
 
-void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool swap_back, cudaStream_t st) {
+void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool swap_back, cudaStream_t st,
+                 int part) {
   if (!d.n) return;
   const uint32_t* rp = direction == 0 ? d.rowptr_in : d.rowptr_out;
   const uint4* en = direction == 0 ? d.ent_in : d.ent_out;
@@ -1221,8 +1227,27 @@ void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool s
   const uint4* lane_ent = direction == 0 ? d.lane_ent_in : d.lane_ent_out;
   const float2* src = swap_back ? d.pos_alt : d.pos;
   float2* dst = swap_back ? d.pos : d.pos_alt;
-  const uint32_t nb = nhub + blocks_for(d.n - nhub);
-  k_link<<<nb, kBlock, nhub ? sizeof(HubStage) : 0, st>>>(d, s, rp, en, woff, lane_ent, src, dst, order, d.n, nhub);
+  const uint32_t nlight = blocks_for(d.n - nhub);
+  if (part == kLinkHubs) {
+    if (nhub) k_link<<<nhub, kBlock, sizeof(HubStage), st>>>(d, s, rp, en, woff, lane_ent, src, dst, order, d.n, nhub, 0u);
+  } else if (part == kLinkLight) {
+    if (nlight) k_link<<<nlight, kBlock, 0, st>>>(d, s, rp, en, woff, lane_ent, src, dst, order, d.n, nhub, nhub);
+  } else {
+    k_link<<<nhub + nlight, kBlock, nhub ? sizeof(HubStage) : 0, st>>>(d, s, rp, en, woff, lane_ent, src, dst, order,
+                                                                      d.n, nhub, 0u);
+  }
+}
+
+namespace {
+__global__ void __launch_bounds__(kBlock) k_mark_hubs(const uint32_t* __restrict__ order, uint32_t nhub,
+                                                      uint8_t* __restrict__ mark) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nhub) mark[order[t]] = 1;
+}
+}  // namespace
+
+void launch_mark_hubs(const uint32_t* order, uint32_t nhub, uint8_t* mark, cudaStream_t st) {
+  if (nhub) k_mark_hubs<<<blocks_for(nhub), kBlock, 0, st>>>(order, nhub, mark);
 }
 
 void launch_warp_lengths(const uint32_t* order, const uint32_t* rowptr, uint32_t nhub, uint32_t n, uint32_t* woff,
@@ -1250,13 +1275,22 @@ void launch_cluster_force(const DeviceView& d, const SimScalars& s, cudaStream_t
   if (nb) k_cluster_force<<<nb, kBlock, 0, st>>>(d, s);
 }
 
-void launch_collision_grid(const DeviceView& d, const SimScalars& s, const uint32_t* order, uint32_t count,
-                           cudaStream_t st) {
+void launch_collision_sums(const DeviceView& d, const SimScalars& s, const uint32_t* order, uint32_t count,
+                           const uint8_t* skip, cudaStream_t st) {
   if (!order) count = d.n;
   const uint32_t nb = blocks_for(count);
-  if (nb) k_coll_grid<<<nb, kBlock, 0, st>>>(d, s, order, count);
+  if (nb) k_coll_grid<<<nb, kBlock, 0, st>>>(d, s, order, count, skip);
+}
+
+void launch_collision_convert(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
   const uint32_t cells = 4u * (uint32_t)(s.coll_grid * s.coll_grid);
   k_coll_convert<<<blocks_for(cells), kBlock, 0, st>>>(d, s);
+}
+
+void launch_collision_grid(const DeviceView& d, const SimScalars& s, const uint32_t* order, uint32_t count,
+                           cudaStream_t st) {
+  launch_collision_sums(d, s, order, count, nullptr, st);
+  launch_collision_convert(d, s, st);
 }
 
 void launch_collision_force(const DeviceView& d, const SimScalars& s, const uint32_t* order, uint32_t count,

@@ -126,7 +126,13 @@ void launch_cells(const DeviceView& d, const SimScalars& s, cudaStream_t st);
 void launch_manybody(const DeviceView& d, const SimScalars& s, cudaStream_t st);
 // direction 0 = incoming (reads pos, writes pos_alt), 1 = outgoing (pos_alt -> pos)
 // The first n_heavy_* rows of the order each get a CTA of their own.
-void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool swap_back, cudaStream_t st);
+// A link pass: all of it (kLinkAll), or its hub CTAs or its light rows alone
+// (the two halves write disjoint points and may run on two streams).
+enum { kLinkAll = 0, kLinkHubs = 1, kLinkLight = 2 };
+void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool swap_back, cudaStream_t st,
+                 int part = kLinkAll);
+// mark[order[t]] = 1 for t < nhub (the points whose list runs on a hub CTA)
+void launch_mark_hubs(const uint32_t* order, uint32_t nhub, uint8_t* mark, cudaStream_t st);
 // The warp layout of one direction's light rows (woff, lane_ent above):
 // warp_lengths writes 32 x the longest list of each of the nw warps to
 // woff[0 .. nw) and 0 to woff[nw] (an exclusive scan then gives the offsets);
@@ -139,6 +145,12 @@ void launch_fill_lanes(const uint32_t* order, const uint32_t* rowptr, const uint
 // pass, `count` of them), or nullptr to take all points in index order.
 void launch_collision_grid(const DeviceView& d, const SimScalars& s, const uint32_t* order, uint32_t count,
                            cudaStream_t st);
+// launch_collision_grid in two steps: the integer grid sums of the points in
+// `order` not marked in `skip` (nullptr: all), then their conversion to the
+// grids once every point is summed.
+void launch_collision_sums(const DeviceView& d, const SimScalars& s, const uint32_t* order, uint32_t count,
+                           const uint8_t* skip, cudaStream_t st);
+void launch_collision_convert(const DeviceView& d, const SimScalars& s, cudaStream_t st);
 void launch_collision_force(const DeviceView& d, const SimScalars& s, const uint32_t* order, uint32_t count,
                             cudaStream_t st);
 // Sums of each cluster's live points (cluster_acc must be zero on entry).

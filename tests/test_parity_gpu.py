@@ -156,6 +156,26 @@ def test_hub_lists():
         _assert_same(eng, orc, ("hub", t))
 
 
+def test_hub_lists_with_collision():
+    # collision right after the link passes: the outgoing hub chains run on a
+    # second stream while the other points' collision sums are taken, and the
+    # hubs' points are summed once their chains end
+    n = 4000
+    rng = np.random.default_rng(23)
+    pos = rng.uniform(800, 1300, size=2 * n).astype(np.float32)
+    out_star = np.stack([np.zeros(n - 1), np.arange(1, n)], axis=1)          # point 0: a long list each way
+    in_star = np.stack([np.arange(2, 1400), np.full(1398, 1)], axis=1)
+    links = np.concatenate([out_star, in_star, rng.integers(0, n, size=(6000, 2))]).astype(np.float32).reshape(-1)
+    sizes = rng.uniform(2, 10, size=n).astype(np.float32)
+    eng, orc = make_pair(pos, links, dict(random_seed=23, simulation_collision=0.6, simulation_link_distance=4.0),
+                         sizes=sizes)
+    assert eng.layout().max_degree_in > 256 and eng.layout().max_degree_out > 256
+    for t in range(5):
+        eng.step(1)
+        orc.step(1)
+        _assert_same(eng, orc, ("hubs and collision", t))
+
+
 def test_springs_outside_the_in_range_sequences():
     # A hub whose list holds neighbours on top of it and well under one unit
     # away, with rest lengths under one unit: springs of length 0 and below 1
