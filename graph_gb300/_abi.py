@@ -62,6 +62,7 @@ class Config(C.Structure):
         ("random_stream", C.c_int32),
         ("rescale_positions", C.c_int32),
         ("random_seed_text", C.c_char_p),
+        ("manybody_kernel", C.c_int32),
     ]
 
 
@@ -100,9 +101,11 @@ class Layout(C.Structure):
         ("device_bytes", C.c_uint64),
         ("kernels_per_tick", C.c_uint32),
         ("manybody_kernel", C.c_uint32),
+        ("manybody_tuned", C.c_uint32),
     ]
 
 
+MANYBODY_AUTO = -1
 MANYBODY_ONE_POINT = 0
 MANYBODY_SPLIT = 1
 MANYBODY_TWO_POINTS = 2
@@ -140,6 +143,7 @@ DEFAULTS = dict(
     random_stream=RANDOM_REFERENCE,
     rescale_positions=-1,
     random_seed_text=None,
+    manybody_kernel=-1,
 )
 
 # Reference config keys (camelCase, src/config.ts) -> C field names.

@@ -43,6 +43,14 @@ struct cgl_engine {
   uint32_t* d_error = nullptr;
   cudaStream_t side = nullptr;   // the outgoing hub chains beside the collision sums
   cudaEvent_t fork = nullptr, join = nullptr;
+  // many-body kernel tuning (cfg.manybody_kernel == CGL_MANYBODY_AUTO): the
+  // candidates run two ticks each, timed, and the fastest is kept
+  int mb_choice = -1;            // the kernel in use; -1: the size rule
+  bool mb_tuned = false;
+  std::vector<int> tune_cands;
+  uint32_t tune_next = 0;        // timed ticks so far
+  float tune_ms[3][2] = {};
+  cudaEvent_t tune_ev[2] = {nullptr, nullptr};
 
   // staged input (copied at set_*, applied at render)
   bool have_pos_input = false, have_link_input = false, have_strength = false, have_sizes = false;
@@ -273,6 +281,22 @@ void refresh_view(cgl_engine* e) {
   d.n_clusters = e->n_clusters;
 }
 
+uint32_t device_sms() {
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms > 0 ? (uint32_t)sms : 1u;
+}
+
+// Without timing: two points of a cell per thread once the cells hold one
+// point on average and the graph fills the GPU with one thread per point; a
+// point over 16 threads below that size; else a thread per point.
+int size_rule_kernel(const cgl_engine* e) {
+  const uint64_t full = 2ull * 256 * device_sms();
+  if (e->Gf > 0 && e->live >= (uint64_t)e->Gf * e->Gf && e->N >= full) return kManybodyTwoPoints;
+  return e->N < full ? kManybodySplit : kManybodyOnePoint;
+}
+
 SimScalars make_scalars(const cgl_engine* e) {
   SimScalars s{};
   s.space = (float)e->adjusted_space;
@@ -297,12 +321,11 @@ SimScalars make_scalars(const cgl_engine* e) {
   s.fx = e->fx;
   s.units = PairUnits{1.0f, -0.0f};
   s.cluster = (float)e->cfg.simulation_cluster;
-  // two points of a cell per thread once the cells hold one point on average
-  // and the graph fills the GPU with one thread per point
-  int dev = 0, sms = 1;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  s.pairs = e->Gf > 0 && e->live >= (uint64_t)e->Gf * e->Gf && e->N >= 2ull * 256 * (uint64_t)sms;
+  // the many-body kernel: the configured one, else the one the tuner kept
+  // for this graph, else the size rule
+  const int32_t forced = e->cfg.manybody_kernel;
+  s.mb_kernel = forced >= 0 ? forced : e->mb_choice >= 0 ? e->mb_choice : size_rule_kernel(e);
+  s.pairs = s.mb_kernel == kManybodyTwoPoints;
   s.level_guard = s.csf >= 2.0f && s.space <= 33554432.0f;   // 2^25
   s.any_pinned = e->any_pinned;
   return s;
@@ -484,7 +507,74 @@ TickParams host_tick(cgl_engine* e, bool draws_seed) {
   return tp;
 }
 
+// The many-body kernels a graph is timed with: a thread per point always; a
+// point over 16 threads while the graph is under four GPU-fulls of 512
+// points a SM; two points of a cell per thread from half a point a cell.
+std::vector<int> tune_candidates(const cgl_engine* e) {
+  std::vector<int> c{kManybodyOnePoint};
+  if (e->N < 4ull * 2 * 256 * device_sms()) c.push_back(kManybodySplit);
+  if (e->Gf > 0 && 2 * e->live >= (uint64_t)e->Gf * e->Gf) c.push_back(kManybodyTwoPoints);
+  return c;
+}
+
+bool tuning(const cgl_engine* e, const cudaEvent_t* ev) {
+  return e->cfg.manybody_kernel == CGL_MANYBODY_AUTO && !e->mb_tuned && e->use_graph && !ev && plan_tick(e).mb;
+}
+
+// One tick of the tuning: the next candidate's graph, timed with events.
+// *ran: whether a tick ran (with a single candidate there is nothing to time).
+cgl_status tune_tick(cgl_engine* e, bool* ran) {
+  *ran = false;
+  if (e->tune_cands.empty()) {
+    e->tune_cands = tune_candidates(e);
+    e->tune_next = 0;
+    if (e->tune_cands.size() == 1) {   // nothing to choose
+      e->mb_choice = e->tune_cands[0];
+      e->mb_tuned = true;
+      e->graph_dirty = true;
+      return CGL_OK;
+    }
+  }
+  const uint32_t idx = e->tune_next / 2;
+  if (e->mb_choice != e->tune_cands[idx]) {
+    e->mb_choice = e->tune_cands[idx];
+    e->graph_dirty = true;
+  }
+  cgl_status st = prepare_tick(e);
+  if (st) return st;
+  if (e->params_pending) { CU(cudaEventSynchronize(e->params_copied)); e->params_pending = false; }
+  e->h_params[0] = host_tick(e, plan_tick(e).mb);
+  CU(cudaMemcpyAsync(e->b_params.p, e->h_params, sizeof(TickParams), cudaMemcpyHostToDevice, e->stream));
+  CU(cudaEventRecord(e->params_copied, e->stream));
+  e->params_pending = true;
+  CU(cudaMemsetAsync(e->b_tick_ctr.p, 0, sizeof(uint32_t), e->stream));
+  if (mouse_active(e)) launch_pointer_force(e);
+  CU(cudaEventRecord(e->tune_ev[0], e->stream));
+  CU(cudaGraphLaunch(e->graph, e->stream));
+  CU(cudaEventRecord(e->tune_ev[1], e->stream));
+  CU(cudaEventSynchronize(e->tune_ev[1]));
+  float ms = 0.f;
+  CU(cudaEventElapsedTime(&ms, e->tune_ev[0], e->tune_ev[1]));
+  e->tune_ms[idx][e->tune_next % 2] = ms;
+  *ran = true;
+  if (++e->tune_next == 2 * e->tune_cands.size()) {
+    size_t best = 0;
+    for (size_t k = 1; k < e->tune_cands.size(); ++k)
+      if (std::min(e->tune_ms[k][0], e->tune_ms[k][1]) < std::min(e->tune_ms[best][0], e->tune_ms[best][1])) best = k;
+    if (e->mb_choice != e->tune_cands[best]) e->graph_dirty = true;
+    e->mb_choice = e->tune_cands[best];
+    e->mb_tuned = true;
+  }
+  return CGL_OK;
+}
+
 cgl_status run_ticks(cgl_engine* e, uint32_t ticks, cudaEvent_t* ev, double* stage_ms) {
+  while (ticks > 0 && tuning(e, ev)) {   // a graph's first ticks time the many-body kernels
+    bool ran = false;
+    cgl_status st = tune_tick(e, &ran);
+    if (st) return st;
+    if (ran) --ticks;
+  }
   if (ticks == 0) return CGL_OK;
   cgl_status st = prepare_tick(e);
   if (st) return st;
@@ -780,6 +870,11 @@ cgl_status build_graph(cgl_engine* e, double alpha, uint64_t N, uint64_t E) {
     // ForceManyBody.create (ForceManyBody/index.ts:124-185): pyramid sizes and
     // the jitter texture (2 draws per texel of pointsTextureSize^2, :133-138)
     e->mb_ready = false;
+    // a new point set: its many-body kernel is timed again
+    e->mb_choice = -1;
+    e->mb_tuned = false;
+    e->tune_cands.clear();
+    e->tune_next = 0;
     if (e->T) {
       const ingest::Grid grid = ingest::grid_for(e->N);
       e->Gf = grid.gf;
@@ -942,10 +1037,13 @@ void cgl_config_defaults(cgl_config* c) {
   c->random_stream = CGL_RANDOM_REFERENCE;
   c->rescale_positions = -1;
   c->random_seed_text = nullptr;
+  c->manybody_kernel = CGL_MANYBODY_AUTO;
 }
 
 cgl_status cgl_create(const cgl_config* cfg, cgl_engine** out) {
   if (!cfg || !out) return CGL_INVALID_ARG;
+  if (cfg->manybody_kernel < CGL_MANYBODY_AUTO || cfg->manybody_kernel > CGL_MANYBODY_TWO_POINTS)
+    return CGL_INVALID_ARG;
   *out = nullptr;
   cgl_engine* e = new cgl_engine();
   e->cfg = *cfg;
@@ -967,6 +1065,8 @@ cgl_status cgl_create(const cgl_config* cfg, cgl_engine** out) {
     if (ce == cudaSuccess) ce = cudaStreamCreateWithPriority(&e->side, cudaStreamNonBlocking, hi);
   }
   if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e->tune_ev[0]);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e->tune_ev[1]);
   if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->join, cudaEventDisableTiming);
   if (ce == cudaSuccess) ce = cudaHostAlloc((void**)&e->h_error, sizeof(uint32_t), cudaHostAllocMapped);
   if (ce == cudaSuccess) ce = cudaHostGetDevicePointer((void**)&e->d_error, e->h_error, 0);
@@ -978,6 +1078,7 @@ cgl_status cgl_create(const cgl_config* cfg, cgl_engine** out) {
     if (e->side) cudaStreamDestroy(e->side);
     if (e->fork) cudaEventDestroy(e->fork);
     if (e->join) cudaEventDestroy(e->join);
+    for (cudaEvent_t x : e->tune_ev) if (x) cudaEventDestroy(x);
     if (e->h_params) cudaFreeHost(e->h_params);
     if (e->h_error) cudaFreeHost(e->h_error);
     delete e;
@@ -1008,6 +1109,7 @@ cgl_status cgl_destroy(cgl_engine* e) {
   if (e->side) cudaStreamDestroy(e->side);
   if (e->fork) cudaEventDestroy(e->fork);
   if (e->join) cudaEventDestroy(e->join);
+  for (cudaEvent_t x : e->tune_ev) if (x) cudaEventDestroy(x);
   if (e->own_stream) cudaStreamDestroy(e->own_stream);
   delete e;
   return CGL_OK;
@@ -1024,6 +1126,8 @@ cgl_status cgl_destroy(cgl_engine* e) {
 cgl_status cgl_set_config(cgl_engine* e, const cgl_config* cfg) {
   CHECK_E(e);
   if (!cfg) return CGL_INVALID_ARG;
+  if (cfg->manybody_kernel < CGL_MANYBODY_AUTO || cfg->manybody_kernel > CGL_MANYBODY_TWO_POINTS)
+    return fail(e, CGL_INVALID_ARG, "manybody_kernel %d: not a CGL_MANYBODY_* value", cfg->manybody_kernel);
   const cgl_config prev = e->cfg;
   e->cfg = *cfg;
   e->cfg.has_random_seed = prev.has_random_seed;   // init-only (src/index.ts:1720-1724)
@@ -1453,19 +1557,18 @@ cgl_status cgl_get_layout(cgl_engine* e, cgl_layout* o) {
   o->collision_cell_size = e->ccell;
   o->device_bytes = e->dev_bytes;
   if (e->mb_ready && e->N) {
-    int dev = 0, sms = 1;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    o->manybody_kernel = make_scalars(e).pairs ? CGL_MANYBODY_TWO_POINTS
-                         : e->N < 2ull * 256 * (uint64_t)sms ? CGL_MANYBODY_SPLIT : CGL_MANYBODY_ONE_POINT;
+    o->manybody_kernel = (uint32_t)make_scalars(e).mb_kernel;
+    o->manybody_tuned = e->mb_tuned && e->cfg.manybody_kernel == CGL_MANYBODY_AUTO;
   }
   const TickPlan p = plan_tick(e);
   uint32_t k = 1;                                      // tick end
   if (p.grav || p.cent || p.mb) k += 1;                // prepass
   if (p.cent) k += 1;
-  if (p.mb) k += 6;                                    // scan (2), scatter, big cells, cells, manybody
+  if (p.mb) k += 5;                                    // scan, scatter, big cells, cells, manybody
   k += (uint32_t)p.link_in + (uint32_t)p.link_out;
   if (p.coll) k += 3;                                  // grid, convert, force
+  // the outgoing hub chains beside the collision sums: two link launches, two sums
+  if (p.link_in && p.link_out && p.coll && !p.clus && p.mb && e->n_heavy_out > 0) k += 2;
   if (p.clus) k += 1 + (uint32_t)p.clus_sum;           // sums, pull + update
   o->kernels_per_tick = k;
   return CGL_OK;

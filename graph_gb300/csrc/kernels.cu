@@ -1209,7 +1209,7 @@ void launch_manybody(const DeviceView& d, const SimScalars& s, cudaStream_t st) 
     const uint32_t items = (uint32_t)(((uint64_t)d.n + (uint64_t)s.gf * s.gf) / 2 + 1);
     if (s.level_guard) k_manybody_duo<true><<<blocks_for(items), kBlock, 0, st>>>(d, s);
     else k_manybody_duo<false><<<blocks_for(items), kBlock, 0, st>>>(d, s);
-  } else if (d.n < 2u * kBlock * sm_count()) {
+  } else if (s.mb_kernel == kManybodySplit) {
     k_manybody_split<<<(d.n + kSplitPoints - 1) / kSplitPoints, kBlock, 0, st>>>(d, s);
   } else {
     k_manybody<<<blocks_for(d.n), kBlock, 0, st>>>(d, s);

@@ -104,7 +104,8 @@ struct SimScalars {
   PairUnits units;            // {1, -0}: operands of the paired sums and products
   float cluster;              // simulationCluster
   int pairs;                  // the many-body pass takes two points of a cell per thread (k_manybody_duo);
-                              // the scan and scatter then build the pair list
+                              // the binning passes then also build its work list
+  int mb_kernel;              // CGL_MANYBODY_* (include/cgl.h): the many-body pass's kernel
   int level_guard;            // finest cell >= 2 units and space <= 2^25: a level term's length is
                               // then in [1, 2^52] whenever every binned point lies in [0, space]
   int any_pinned;             // some live point is pinned
@@ -114,6 +115,7 @@ constexpr uint32_t kOutsideFlag = 4;   // big_count word of the outside-the-spac
 constexpr uint32_t kSingleBit = 0x80000000u;
 
 
+enum : int { kManybodyOnePoint = 0, kManybodySplit = 1, kManybodyTwoPoints = 2 };   // CGL_MANYBODY_*
 enum PrepassMode : uint32_t { kPreGravity = 1, kPreCentroid = 2, kPreBin = 4 };
 
 void launch_prepass(const DeviceView& d, const SimScalars& s, uint32_t mode, cudaStream_t st);

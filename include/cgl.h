@@ -105,6 +105,9 @@ typedef struct cgl_config {
   const char* random_seed_text;              /* with has_random_seed: randomSeed as text (UTF-8), for string seeds
                                                 and non-integer numbers (the reference seeds with String(seed));
                                                 NULL = random_seed in decimal.  Copied at cgl_create; init-only */
+  int32_t manybody_kernel;                   /* CGL_MANYBODY_AUTO (default): the engine times its many-body
+                                                kernels on a graph's first ticks and keeps the fastest; or one
+                                                CGL_MANYBODY_* kernel.  Every kernel gives the same results */
 } cgl_config;
 
 typedef struct cgl_state {
@@ -314,11 +317,13 @@ typedef struct cgl_layout {
   uint64_t device_bytes;       /* device memory held by the handle */
   uint32_t kernels_per_tick;   /* kernel launches one tick makes with the current data and config */
   uint32_t manybody_kernel;    /* CGL_MANYBODY_*: how the many-body pass spreads points over threads */
+  uint32_t manybody_tuned;     /* 1 once manybody_kernel was chosen by timing this graph's ticks */
 } cgl_layout;
 enum {
+  CGL_MANYBODY_AUTO = -1,       /* cgl_config.manybody_kernel: time the candidates, keep the fastest */
   CGL_MANYBODY_ONE_POINT = 0,   /* a thread per point */
-  CGL_MANYBODY_SPLIT = 1,       /* small graphs: a point's terms over 16 threads */
-  CGL_MANYBODY_TWO_POINTS = 2   /* two points of one finest cell per thread (cells of >= 1 point on average) */
+  CGL_MANYBODY_SPLIT = 1,       /* a point's terms over 16 threads (small graphs) */
+  CGL_MANYBODY_TWO_POINTS = 2   /* two points of one finest cell per thread (dense graphs) */
 };
 cgl_status cgl_get_layout(cgl_engine* e, cgl_layout* out);
 

@@ -48,9 +48,9 @@ def test_config_defaults_match_reference(engine_lib):
 
 def test_struct_sizes_match_header():
     # natural C layout: doubles and uint64 aligned to 8
-    assert C.sizeof(_abi.Config) == 208
+    assert C.sizeof(_abi.Config) == 216
     assert C.sizeof(_abi.State) == 56
-    assert C.sizeof(_abi.Layout) == 88
+    assert C.sizeof(_abi.Layout) == 96
     assert C.sizeof(_abi.BatchJob) == 64
 
 
@@ -76,4 +76,12 @@ def test_layout_names_the_many_body_kernels():
     for name, value in (("CGL_MANYBODY_ONE_POINT", 0), ("CGL_MANYBODY_SPLIT", 1), ("CGL_MANYBODY_TWO_POINTS", 2)):
         assert re.search(r"%s = %d" % (name, value), src)
     assert (_abi.MANYBODY_ONE_POINT, _abi.MANYBODY_SPLIT, _abi.MANYBODY_TWO_POINTS) == (0, 1, 2)
-    assert [f for f, _ in _abi.Layout._fields_][-1] == "manybody_kernel"
+    assert [f for f, _ in _abi.Layout._fields_][-2:] == ["manybody_kernel", "manybody_tuned"]
+
+
+def test_create_rejects_an_unknown_manybody_kernel(engine_lib):
+    # checked before any device call, so it runs without a GPU
+    for bad in (-2, 3, 99):
+        cfg = _abi.make_config(manybody_kernel=bad)
+        h = C.c_void_p()
+        assert engine_lib.cgl_create(C.byref(cfg), C.byref(h)) == _abi.CGL_INVALID_ARG

@@ -62,7 +62,7 @@ def test_two_points_per_thread_matches_oracle(kind):
     pos_kind = "uniform" if kind in ("small_space", "full_tick") else kind
     pos = _positions(pos_kind, space)
     links = generators.erdos_renyi(N, 4, 7) if not mb_only else None
-    fields = dict(space_size=space, random_seed=5, **extra)
+    fields = dict(space_size=space, random_seed=5, manybody_kernel=_abi.MANYBODY_TWO_POINTS, **extra)
     if mb_only:
         fields["stage_mask"] = _abi.STAGE_MANYBODY | (_abi.STAGE_GRAVITY if "simulation_gravity" not in extra else 0)
     pinned = None
@@ -83,10 +83,49 @@ def test_two_points_per_thread_matches_oracle(kind):
     assert np.array_equal(eng.slots(), orc.slots())
 
 
-def test_sparse_graphs_keep_one_point_per_thread():
+def test_size_rule_and_tuning():
+    # before a graph's first ticks the size rule names the kernel; with
+    # CGL_MANYBODY_AUTO the first ticks time the candidates (two ticks each) and
+    # keep the fastest; a configured kernel is used as given
     pos = generators.uniform_positions(120_000, 0, 8192, 3)   # 0.46 points per finest cell
     eng, orc = make_pair(pos, None, dict(space_size=8192.0, random_seed=3))
     assert eng.layout().manybody_kernel == _abi.MANYBODY_ONE_POINT
+    assert eng.layout().manybody_tuned == 0
+    for t in range(7):
+        eng.step(1)
+        orc.step(1)
+        a, b = eng.get_point_positions(), orc.get_point_positions()
+        assert same_bits(a, b), (t, first_mismatch(a, b))
+    lay = eng.layout()
+    assert lay.manybody_tuned == 1
+    assert lay.manybody_kernel in (_abi.MANYBODY_ONE_POINT, _abi.MANYBODY_SPLIT)
     small = generators.uniform_positions(5000, 0, 4096, 3)
     e2, _ = make_pair(small, None, dict(random_seed=3))
     assert e2.layout().manybody_kernel == _abi.MANYBODY_SPLIT
+    e3, _ = make_pair(small, None, dict(random_seed=3, manybody_kernel=_abi.MANYBODY_TWO_POINTS))
+    e3.step(3)
+    assert e3.layout().manybody_kernel == _abi.MANYBODY_TWO_POINTS and e3.layout().manybody_tuned == 0
+
+
+@pytest.mark.parametrize("kind", ["sparse", "dense"])
+def test_every_kernel_gives_the_same_layout(kind):
+    # the tuner may pick any of the three kernels: each is the same arithmetic
+    n = 100_000
+    rng = np.random.default_rng(77)
+    if kind == "sparse":
+        pos = rng.uniform(0, 8192, size=2 * n).astype(np.float32)           # 0.4 points per finest cell
+    else:
+        pos = rng.normal(4096, 600, size=2 * n).clip(0, 8192).astype(np.float32)
+    links = generators.erdos_renyi(n, 4, 77)
+    runs = []
+    for kernel in (_abi.MANYBODY_ONE_POINT, _abi.MANYBODY_SPLIT, _abi.MANYBODY_TWO_POINTS):
+        eng, orc = make_pair(pos, links, dict(space_size=8192.0, random_seed=7, manybody_kernel=kernel))
+        eng.step(3)
+        assert eng.layout().manybody_kernel == kernel
+        runs.append(eng.get_point_positions())
+        if kernel == _abi.MANYBODY_ONE_POINT:
+            orc.step(3)
+            want = orc.get_point_positions()
+            assert same_bits(runs[0], want), first_mismatch(runs[0], want)
+    for got in runs[1:]:
+        assert same_bits(got, runs[0]), first_mismatch(got, runs[0])
