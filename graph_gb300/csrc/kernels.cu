@@ -748,6 +748,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_manybody(DeviceView d, SimScalars
 // starting velocity, and so does the chunk that followed it.
 constexpr int kHubChunk = kBlock - 32;
 constexpr int kHubBufs = 3;
+constexpr uint32_t kHubInlineChunks = 8;   // lists of up to 8 chunks (1,792 links) check on the chain thread
 struct HubStage {
   float4 a[kHubBufs][kHubChunk];   // neighbour x, y, rest length d, 0.99 d
   float4 b[kHubBufs][kHubChunk];   // strength, bias, absent flag, rcp.approx(0.99 d)
@@ -796,6 +797,21 @@ __device__ __forceinline__ void hub_chunk_chain(const float4* A, const float4* B
   }
 }
 
+// The fast chain over one staged chunk with its checks on the chain thread;
+// returns whether one failed.
+template <bool UNIT_STRENGTH>
+__device__ __forceinline__ bool hub_chunk_checked(const float4* A, const float4* B, uint32_t len, float2 pp,
+                                                  float2& vel, float sa, PairUnits pu) {
+  bool out = false;
+#pragma unroll 4
+  for (uint32_t k = 0; k < len; ++k) {
+    const float4 a = A[k];
+    const float4 b = B[k];
+    spring_chain_step_checked<UNIT_STRENGTH>(pp, vel, make_float2(a.x, a.y), a.z, a.w, b.w, sa, b.x, b.y, pu, out);
+  }
+  return out;
+}
+
 // The correctly rounded springs over one staged chunk (absent targets skipped).
 __device__ __forceinline__ void hub_chunk_exact(const float4* A, const float4* B, uint32_t len, float2 pp, float2& vel,
                                                 float sa, PairUnits pu) {
@@ -842,6 +858,32 @@ __global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, con
     int absent = __syncthreads_or(staged & kStagedAbsent);       // some target of chunk c is absent
     int strengths = __syncthreads_or(staged & kStagedStrength);  // some strength of chunk c is not 1
     float2 vel = make_float2(0.f, 0.f);
+    if (chunks <= kHubInlineChunks) {
+      // a short list: two buffers, the checks on the chain thread (a round of
+      // checks after the chain would cost more than it saves)
+      for (uint32_t c = 0; c < chunks; ++c) {
+        const int buf = c & 1;
+        int next = 0;
+        if (threadIdx.x >= 32) {
+          if (c + 1 < chunks)
+            next = hub_fill(hub, buf ^ 1, e0 + (c + 1) * kHubChunk, e1, ent, src, span, s.link_r0, s.link_distance);
+        } else if (threadIdx.x == 0) {
+          const uint32_t len = chunk_len(c);
+          bool exact = absent != 0;
+          if (!absent) {
+            const float2 v0 = vel;
+            const bool out = strengths ? hub_chunk_checked<false>(hub.a[buf], hub.b[buf], len, pp, vel, sa, pu)
+                                       : hub_chunk_checked<true>(hub.a[buf], hub.b[buf], len, pp, vel, sa, pu);
+            if (out) { vel = v0; exact = true; }
+          }
+          if (exact) hub_chunk_exact(hub.a[buf], hub.b[buf], len, pp, vel, sa, pu);
+        }
+        absent = __syncthreads_or(next & kStagedAbsent);
+        strengths = __syncthreads_or(next & kStagedStrength);
+      }
+      if (threadIdx.x == 0) dst[p] = (f & kPinned) ? pp : integrate(pp, vel.x, vel.y, s.friction, s.space);
+      return;
+    }
     // round c: chain over chunk c, staging of chunk c + 1, check of chunk c - 1
     for (uint32_t c = 0; c <= chunks; ++c) {
       const int buf = c % kHubBufs, prev = (c + kHubBufs - 1) % kHubBufs;

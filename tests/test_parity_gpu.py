@@ -202,8 +202,9 @@ def test_springs_outside_the_sequences_in_later_chunks():
     # that fails its check runs again with the correctly rounded springs, and
     # so does the chunk after it.  Here the failing links sit in a middle chunk
     # and in the last one (the check of the last chunk comes after the chain
-    # has ended), and two failing chunks follow each other.
-    n = 1600
+    # has ended), and two failing chunks follow each other.  2,399 links: more
+    # than the lists whose checks stay on the chain thread.
+    n = 2400
     rng = np.random.default_rng(35)
     pos = rng.uniform(1000, 1400, size=2 * n).astype(np.float32)
     hub = pos[0:2].copy()
