@@ -71,6 +71,7 @@ if _reference_arm(sys.argv[1:]) and int(os.environ.get("WORLD_SIZE", "1")) > 1:
 from graph_gb300 import _abi, generators, replicas  # noqa: E402
 
 METRIC = "point-iterations/s"
+MANYBODY_NAMES = {0: "one point per thread", 1: "a point over 16 threads", 2: "two points of a cell per thread"}
 UNIT = "point-iter/s"
 
 
@@ -355,6 +356,9 @@ def main():
     ap.add_argument("--save-positions", default=None, help="write the final positions (.npy) for profiling runs")
     ap.add_argument("--positions-from", default=None, help="start from saved positions (.npy) instead of the seeded ones")
     ap.add_argument("--quick", action="store_true", help="timed ticks only: no stage profile, e2e or CPU baseline")
+    ap.add_argument("--manybody-kernel", default="auto", choices=["auto", "one", "split", "two"],
+                    help="the many-body kernel (auto: timed on the first ticks); a profiler's replay distorts "
+                         "that timing, so profiled runs name the kernel the unprofiled run keeps")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -393,7 +397,9 @@ def main():
         pos = np.load(args.positions_from).astype(np.float32)
         desc += " (evolved positions from %s)" % os.path.basename(args.positions_from)
     from graph_gb300.engine import Engine
-    eng = Engine(**dict(fields, device=local_rank))
+    kernel = {"auto": _abi.MANYBODY_AUTO, "one": _abi.MANYBODY_ONE_POINT, "split": _abi.MANYBODY_SPLIT,
+              "two": _abi.MANYBODY_TWO_POINTS}[args.manybody_kernel]
+    eng = Engine(**dict(fields, device=local_rank, manybody_kernel=kernel))
     eng.set_point_positions(pos)
     eng.set_links(links)
     if sizes is not None:
@@ -428,10 +434,15 @@ def main():
     ms = replicas.max_over_ranks(ms, device="cuda")
     live_all = replicas.sum_over_ranks(live, device="cuda")
     value = live_all * args.steps / (ms / 1e3)
+    tuned = eng.layout()
+    mb_kernel = {"kernel": MANYBODY_NAMES.get(int(tuned.manybody_kernel), "?"),
+                 "chosen_by": "timing of the first ticks" if tuned.manybody_tuned else
+                 ("--manybody-kernel" if args.manybody_kernel != "auto" else "size rule")}
     if args.quick:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "steps": args.steps,
-                              "ms_per_step": ms / args.steps, "quick": True, "config": {"workload": desc}}))
+                              "ms_per_step": ms / args.steps, "quick": True,
+                              "config": {"workload": desc, "manybody_kernel": mb_kernel}}))
         if args.save_positions and rank == 0:
             np.save(args.save_positions, eng.get_point_positions())
         eng.close()
@@ -500,7 +511,8 @@ def main():
                        "levels": int(lay.levels), "step": "one simulation tick (Graph.step)",
                        "l2": "inputs larger than L2 (per-tick working set ~%d MB > 129 MB)"
                              % int((29 * live + 24 * 2 * m + 60 * live) / 1e6),
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "manybody_kernel": mb_kernel},
             "roofline": roofline,
             "tick_roofline": {"bytes_model": "112 N + 48 E + 107 C_f" + (" + 144 N + 128 C_c" if coll_on else ""),
                               "bytes": tb, "achieved": tick_gbs, "peak": peak, "unit": "GB/s",

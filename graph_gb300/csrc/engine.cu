@@ -44,12 +44,12 @@ struct cgl_engine {
   cudaStream_t side = nullptr;   // the outgoing hub chains beside the collision sums
   cudaEvent_t fork = nullptr, join = nullptr;
   // many-body kernel tuning (cfg.manybody_kernel == CGL_MANYBODY_AUTO): the
-  // candidates run two ticks each, timed, and the fastest is kept
+  // candidates run kTuneTicks ticks each, timed, and the fastest is kept
   int mb_choice = -1;            // the kernel in use; -1: the size rule
   bool mb_tuned = false;
   std::vector<int> tune_cands;
   uint32_t tune_next = 0;        // timed ticks so far
-  float tune_ms[3][2] = {};
+  float tune_ms[3][3] = {};
   cudaEvent_t tune_ev[2] = {nullptr, nullptr};
 
   // staged input (copied at set_*, applied at render)
@@ -521,6 +521,13 @@ bool tuning(const cgl_engine* e, const cudaEvent_t* ev) {
   return e->cfg.manybody_kernel == CGL_MANYBODY_AUTO && !e->mb_tuned && e->use_graph && !ev && plan_tick(e).mb;
 }
 
+// Ticks per candidate; the first after a candidate's graph is built carries
+// its first launch and is not counted.  A candidate replaces the size rule's
+// kernel only when it is kTuneMargin faster: two kernels within the margin
+// are kept as the rule has them, not swapped on timing noise.
+constexpr uint32_t kTuneTicks = 3;
+constexpr float kTuneMargin = 0.97f;
+
 // One tick of the tuning: the next candidate's graph, timed with events.
 // *ran: whether a tick ran (with a single candidate there is nothing to time).
 cgl_status tune_tick(cgl_engine* e, bool* ran) {
@@ -535,7 +542,7 @@ cgl_status tune_tick(cgl_engine* e, bool* ran) {
       return CGL_OK;
     }
   }
-  const uint32_t idx = e->tune_next / 2;
+  const uint32_t idx = e->tune_next / kTuneTicks;
   if (e->mb_choice != e->tune_cands[idx]) {
     e->mb_choice = e->tune_cands[idx];
     e->graph_dirty = true;
@@ -555,14 +562,19 @@ cgl_status tune_tick(cgl_engine* e, bool* ran) {
   CU(cudaEventSynchronize(e->tune_ev[1]));
   float ms = 0.f;
   CU(cudaEventElapsedTime(&ms, e->tune_ev[0], e->tune_ev[1]));
-  e->tune_ms[idx][e->tune_next % 2] = ms;
+  e->tune_ms[idx][e->tune_next % kTuneTicks] = ms;
   *ran = true;
-  if (++e->tune_next == 2 * e->tune_cands.size()) {
-    size_t best = 0;
-    for (size_t k = 1; k < e->tune_cands.size(); ++k)
-      if (std::min(e->tune_ms[k][0], e->tune_ms[k][1]) < std::min(e->tune_ms[best][0], e->tune_ms[best][1])) best = k;
-    if (e->mb_choice != e->tune_cands[best]) e->graph_dirty = true;
-    e->mb_choice = e->tune_cands[best];
+  if (++e->tune_next == kTuneTicks * e->tune_cands.size()) {
+    auto best_of = [&](size_t k) { return std::min(e->tune_ms[k][1], e->tune_ms[k][2]); };   // [0]: first launch
+    const int rule = size_rule_kernel(e);
+    size_t pick = 0, fastest = 0;
+    for (size_t k = 0; k < e->tune_cands.size(); ++k) {
+      if (e->tune_cands[k] == rule) pick = k;
+      if (best_of(k) < best_of(fastest)) fastest = k;
+    }
+    if (best_of(fastest) < kTuneMargin * best_of(pick)) pick = fastest;
+    if (e->mb_choice != e->tune_cands[pick]) e->graph_dirty = true;
+    e->mb_choice = e->tune_cands[pick];
     e->mb_tuned = true;
   }
   return CGL_OK;
