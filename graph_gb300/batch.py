@@ -73,9 +73,11 @@ class Batch:
         self._n[gid.value] = xy.size // 2
         return gid.value
 
-    def add_many(self, jobs, threads=0):
+    def add_many(self, jobs, threads=0, until_full=False):
         """Add jobs (dicts of add()'s arguments) with their host work on `threads` host threads
-        (0 = one per core); returns their ids in order."""
+        (0 = one per core); returns their ids in order.  until_full: a job refused for device
+        memory (CGL_OOM) ends the call without an error, and the ids of the jobs added before it
+        are returned."""
         keep = []
         arr = (_abi.BatchJob * len(jobs))()
         for k, jb in enumerate(jobs):
@@ -106,6 +108,8 @@ class Batch:
         st = self._lib.cgl_batch_add_many(self._h, len(jobs), arr, ids, int(threads), C.byref(added))
         for k in range(added.value):
             self._n[ids[k]] = int(arr[k].n_floats) // 2
+        if until_full and st == _abi.CGL_OOM:
+            return [ids[k] for k in range(added.value)]
         self._check("add_many", st)
         return [ids[k] for k in range(len(jobs))]
 

@@ -48,6 +48,7 @@ class LayoutService:
         self.queue = collections.deque()
         self.running = {}
         self.done = []
+        self._full = False   # the last admission was refused for memory and no job has retired since
 
     def submit(self, key, positions, links, fields, max_ticks=1000, arrival=None):
         r = Request(key, positions, links, fields, max_ticks, self.clock() if arrival is None else arrival)
@@ -55,18 +56,26 @@ class LayoutService:
         return r
 
     def _admit(self):
-        while self.queue:
-            r = self.queue[0]
-            try:
-                r.job = self.batch.add(r.positions, r.links, max_ticks=r.max_ticks, stop_below_alpha_min=True,
-                                       **r.fields)
-            except StatusError as e:
-                if e.status == _abi.CGL_OOM and self.running:
-                    return            # wait for running jobs to free memory
-                raise
-            r.admitted = self.clock()
+        """Admit queued jobs in arrival order while memory allows: one call for all of them, which
+        prepares them (positions, random draws, link lists) on the host's cores at once.  A job
+        refused for memory waits, with those behind it, for running jobs to retire (nothing is tried
+        again until one has); with none running the refusal is final."""
+        if not self.queue or self._full:
+            return
+        reqs = list(self.queue)
+        jobs = [dict(positions=r.positions, links=r.links, max_ticks=r.max_ticks, stop_below_alpha_min=True,
+                     **r.fields) for r in reqs]
+        ids = self.batch.add_many(jobs, until_full=True)
+        if not ids and not self.running:   # the head job alone does not fit: it never will
+            raise StatusError("cgl_batch_add_many", _abi.CGL_OOM,
+                              "the job at the head of the queue exceeds the device-memory budget")
+        self._full = len(ids) < len(reqs)
+        now = self.clock()
+        for r, job in zip(reqs, ids):
+            r.job = job
+            r.admitted = now
             self.queue.popleft()
-            self.running[r.job] = r
+            self.running[job] = r
 
     def step_round(self):
         """Admit what fits, advance every running job one round, retire finished ones."""
@@ -90,6 +99,7 @@ class LayoutService:
             r.result = self.batch.get_point_positions(job)
             r.finished = self.clock()
             self.batch.remove(job)
+            self._full = False
             self.done.append(r)
         return len(finished)
 

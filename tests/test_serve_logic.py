@@ -33,6 +33,18 @@ class FakeBatch:
         self.added.append(job)
         return job
 
+    def add_many(self, jobs, threads=0, until_full=False):
+        self.calls = getattr(self, "calls", 0) + 1
+        ids = []
+        for jb in jobs:
+            try:
+                ids.append(self.add(**jb))
+            except StatusError as e:
+                if until_full and e.status == _abi.CGL_OOM:
+                    return ids
+                raise
+        return ids
+
     def remove(self, job):
         self.used -= self.jobs.pop(job)["n"]
         self.removed.append(job)
@@ -126,3 +138,15 @@ def test_a_job_that_can_never_fit_is_refused(service):
     with pytest.raises(StatusError) as e:
         service.step_round()
     assert e.value.status == _abi.CGL_OOM
+
+
+def test_a_full_batch_is_not_asked_again_until_a_job_retires(service):
+    service.submit("a", points(80), None, {}, max_ticks=30)
+    service.submit("b", points(40), None, {}, max_ticks=10)
+    service.step_round()                 # a admitted, b refused for memory
+    assert service.batch.calls == 1 and len(service.queue) == 1
+    service.step_round()                 # nothing retired: no second attempt
+    assert service.batch.calls == 1
+    service.step_round()                 # a retires at tick 30 ...
+    service.step_round()                 # ... and b is admitted on the next round
+    assert service.batch.calls == 2 and not service.queue
