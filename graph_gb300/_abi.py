@@ -102,6 +102,8 @@ class Layout(C.Structure):
         ("kernels_per_tick", C.c_uint32),
         ("manybody_kernel", C.c_uint32),
         ("manybody_tuned", C.c_uint32),
+        ("early_hubs", C.c_uint32),
+        ("early_points", C.c_uint32),
     ]
 
 

@@ -77,6 +77,7 @@ struct BatchView {
   uint32_t* rank;
   uint32_t* sorted_idx;        // absolute arena point indices, grouped by cell
   float2* sorted_pos;
+  uint32_t* inv;               // null: a batch keeps no sorted-position map (no early pass)
   uint32_t* counts;            // [cell arena], zeroed by the scan
   uint32_t* cell_start;        // [cell arena + 1]
   unsigned long long* scan_status;   // one-pass scan: status word per chunk of kChunk cells

@@ -41,7 +41,8 @@ struct cgl_engine {
   cudaStream_t stream = nullptr;
   uint32_t* h_error = nullptr;   // host-mapped error word (DeviceView::error_word)
   uint32_t* d_error = nullptr;
-  cudaStream_t side = nullptr;   // the outgoing hub chains beside the collision sums
+  cudaStream_t side = nullptr;   // the early hubs' chains beside the many-body pass; the outgoing hub
+                                 // chains beside the collision sums
   cudaEvent_t fork = nullptr, join = nullptr;
   // many-body kernel tuning (cfg.manybody_kernel == CGL_MANYBODY_AUTO): the
   // candidates run kTuneTicks ticks each, timed, and the fastest is kept
@@ -113,6 +114,10 @@ struct cgl_engine {
   DevBuf b_hub_out;   // 1 for the points whose outgoing list runs on a hub CTA
   DevBuf b_woff_in, b_woff_out, b_lane_ent_in, b_lane_ent_out;   // light rows by warps (kernels.cuh)
   uint32_t n_heavy_in = 0, n_heavy_out = 0;
+  // early hubs (DeviceView::n_early_hubs): their points and link targets
+  DevBuf b_early_pts, b_inv;
+  uint32_t n_early_hubs = 0, n_early_pts = 0;
+  std::vector<uint8_t> early;   // kEarly per point (empty: none)
   DevBuf b_size, b_cgrid_acc, b_cgrid;
   DevBuf b_cl_of, b_cl_coeff, b_cl_custom, b_cl_acc;
   DevBuf b_texture;                        // staging for pageable texture read-back
@@ -202,7 +207,7 @@ void dev_free_all(cgl_engine* e) {
                    &e->b_big_sx, &e->b_big_sy, &e->b_big_ns, &e->b_heavy_in, &e->b_heavy_out, &e->b_hub_out,
                    &e->b_cl_of, &e->b_cl_coeff, &e->b_cl_custom, &e->b_cl_acc, &e->b_texture,
                    &e->b_woff_in, &e->b_woff_out, &e->b_lane_ent_in, &e->b_lane_ent_out, &e->b_pair_start,
-                   &e->b_pair_list, &e->b_idx_s, &e->b_pos_s, &e->b_bin_state};
+                   &e->b_pair_list, &e->b_idx_s, &e->b_pos_s, &e->b_bin_state, &e->b_early_pts, &e->b_inv};
   for (DevBuf* b : all) {
     if (b->p) cudaFree(b->p);
     b->p = nullptr;
@@ -267,6 +272,10 @@ void refresh_view(cgl_engine* e) {
   d.heavy_out = (const uint32_t*)e->b_heavy_out.p;
   d.n_heavy_in = e->n_heavy_in;
   d.n_heavy_out = e->n_heavy_out;
+  d.early_pts = (const uint32_t*)e->b_early_pts.p;
+  d.n_early_pts = e->n_early_pts;
+  d.n_early_hubs = e->n_early_hubs;
+  d.inv = e->n_early_hubs ? (uint32_t*)e->b_inv.p : nullptr;
   d.woff_in = (const uint32_t*)e->b_woff_in.p;
   d.lane_ent_in = (const uint4*)e->b_lane_ent_in.p;
   d.woff_out = (const uint32_t*)e->b_woff_out.p;
@@ -356,8 +365,13 @@ TickPlan plan_tick(const cgl_engine* e) {
 // Enqueue one tick.  ev (optional) = 2 events per stage for profiling.
 cgl_status enqueue_tick(cgl_engine* e, cudaStream_t st, cudaEvent_t* ev) {
   const TickPlan p = plan_tick(e);
-  const SimScalars s = make_scalars(e);
   const DeviceView& d = e->view;
+  // With early hubs, their points take their many-body terms first; their
+  // incoming chains then run on a second stream beside the rest of the
+  // many-body pass and of the incoming pass.  Not in a stage profile (ev).
+  const bool early = p.mb && p.link_in && !ev && d.n_early_hubs > 0 && d.n_early_pts > 0 && d.inv;
+  SimScalars s = make_scalars(e);
+  s.skip_early = early;
   auto mark = [&](int stage, int which) {
     if (ev) cudaEventRecord(ev[2 * stage + which], st);
   };
@@ -383,11 +397,21 @@ cgl_status enqueue_tick(cgl_engine* e, cudaStream_t st, cudaEvent_t* ev) {
     mark(2, 0); launch_scan(d, s, st); mark(2, 1);
     mark(3, 0); launch_scatter(d, s, st); mark(3, 1);
     mark(4, 0); launch_cells(d, s, st); mark(4, 1);
-    mark(5, 0); launch_manybody(d, s, st); mark(5, 1);
+    mark(5, 0);
+    if (early) {
+      launch_manybody_early(d, s, st);
+      CU(cudaEventRecord(e->fork, st));
+      CU(cudaStreamWaitEvent(e->side, e->fork, 0));
+      launch_link(d, s, 0, false, e->side, kLinkEarlyHubs);
+      CU(cudaEventRecord(e->join, e->side));
+    }
+    launch_manybody(d, s, st);
+    mark(5, 1);
   }
   if (p.link_in || p.link_out) {
     mark(6, 0);
-    if (p.link_in) launch_link(d, s, 0, false, st);
+    if (p.link_in) launch_link(d, s, 0, false, st, early ? kLinkAfterEarly : kLinkAll);
+    if (early) CU(cudaStreamWaitEvent(st, e->join, 0));
     mark(6, 1);
     mark(7, 0);
     if (p.link_out && !overlap) launch_link(d, s, 1, p.link_in, st);
@@ -776,6 +800,94 @@ cgl_status build_link_warps(cgl_engine* e) {
   return rc;
 }
 
+// Device flags from the pinned, absent and early marks.
+cgl_status upload_flags(cgl_engine* e) {
+  if (!e->N) return CGL_OK;
+  const bool with_early = e->early.size() == e->N;
+  std::vector<uint8_t> flags(e->N);
+  for (uint64_t i = 0; i < e->N; ++i)
+    flags[i] = (e->pinned[i] ? kPinned : 0) | (e->absent[i] ? kAbsent : 0) | (with_early && e->early[i] ? kEarly : 0);
+  CU(cudaMemcpyAsync(e->b_flags.p, flags.data(), e->N, cudaMemcpyHostToDevice, e->stream));
+  CU(cudaStreamSynchronize(e->stream));
+  return CGL_OK;
+}
+
+// Early hubs: the leading incoming lists (longest first) of at least
+// kEarlyMinLinks links and a quarter of the longest, while their links total
+// at most an eighth of the points.  Their chains need the many-body results of
+// their own points and link targets only; those run first, and the chains
+// then start beside the rest of the many-body pass instead of after it.
+constexpr uint32_t kEarlyCandidates = 64;
+constexpr uint32_t kEarlyMinLinks = 4096;
+
+cgl_status build_early(cgl_engine* e) {
+  e->n_early_hubs = e->n_early_pts = 0;
+  e->early.clear();
+  const uint32_t n = (uint32_t)e->N;
+  const uint32_t m = std::min(e->n_heavy_in, kEarlyCandidates);
+  cgl_status rc = CGL_OK;
+  if (m && e->T) {
+    DevBuf t_spans;
+    if ((rc = dev_reserve(e, t_spans, m * sizeof(uint2), false))) return rc;
+    std::vector<uint2> spans(m);
+    std::vector<uint32_t> hubs(m);
+    launch_hub_spans((const uint32_t*)e->b_heavy_in.p, (const uint32_t*)e->b_rowptr_in.p, m, (uint2*)t_spans.p,
+                     e->stream);
+    cudaError_t err = cudaGetLastError();
+    if (err == cudaSuccess)
+      err = cudaMemcpyAsync(spans.data(), t_spans.p, m * sizeof(uint2), cudaMemcpyDeviceToHost, e->stream);
+    if (err == cudaSuccess)
+      err = cudaMemcpyAsync(hubs.data(), e->b_heavy_in.p, m * sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(e->stream);
+    dev_release(e, t_spans);
+    if (err != cudaSuccess) return fail(e, CGL_CUDA_ERROR, "early hubs: %s", cudaGetErrorString(err));
+    const uint32_t len0 = spans[0].y - spans[0].x;
+    const uint32_t least = std::max(kEarlyMinLinks, len0 / 4);
+    uint64_t total = 0;
+    uint32_t k = 0;
+    for (; k < m; ++k) {
+      const uint32_t len = spans[k].y - spans[k].x;
+      if (len < least || total + len > n / 8) break;
+      total += len;
+    }
+    if (k) {
+      std::vector<uint4> ent(total);
+      size_t at = 0;
+      for (uint32_t t = 0; t < k && err == cudaSuccess; ++t) {
+        const uint32_t len = spans[t].y - spans[t].x;
+        err = cudaMemcpyAsync(ent.data() + at, (const uint4*)e->b_ent_in.p + spans[t].x, len * sizeof(uint4),
+                              cudaMemcpyDeviceToHost, e->stream);
+        at += len;
+      }
+      if (err == cudaSuccess) err = cudaStreamSynchronize(e->stream);
+      if (err != cudaSuccess) return fail(e, CGL_CUDA_ERROR, "early hubs: %s", cudaGetErrorString(err));
+      e->early.assign(n, 0);
+      for (uint32_t t = 0; t < k; ++t)
+        if (!e->absent[hubs[t]]) e->early[hubs[t]] = 1;
+      for (const uint4& en : ent)
+        if (en.x < n && !e->absent[en.x]) e->early[en.x] = 1;
+      std::vector<uint32_t> pts;
+      for (uint32_t i = 0; i < n; ++i)
+        if (e->early[i]) pts.push_back(i);
+      if ((rc = dev_reserve(e, e->b_early_pts, std::max<size_t>(pts.size(), 1) * sizeof(uint32_t), false)) ||
+          (rc = dev_reserve(e, e->b_inv, (size_t)n * sizeof(uint32_t), false))) {
+        e->early.clear();
+        return rc;
+      }
+      if (!pts.empty())
+        CU(cudaMemcpyAsync(e->b_early_pts.p, pts.data(), pts.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                           e->stream));
+      e->n_early_hubs = k;
+      e->n_early_pts = (uint32_t)pts.size();
+    }
+  }
+  if (!e->n_early_hubs) {
+    dev_release(e, e->b_early_pts);
+    dev_release(e, e->b_inv);
+  }
+  return upload_flags(e);
+}
+
 cgl_status apply_pinned(cgl_engine* e) {
   // Points.updatePinnedStatus (Points/index.ts:1264-1277) -> device flags
   e->pinned.assign(e->N, 0);
@@ -787,11 +899,7 @@ cgl_status apply_pinned(cgl_engine* e) {
   if (any != e->any_pinned) e->graph_dirty = true;   // the tick kernels take it as a constant
   e->any_pinned = any;
   if (!e->N) return CGL_OK;
-  std::vector<uint8_t> flags(e->N);
-  for (uint64_t i = 0; i < e->N; ++i) flags[i] = (e->pinned[i] ? kPinned : 0) | (e->absent[i] ? kAbsent : 0);
-  CU(cudaMemcpyAsync(e->b_flags.p, flags.data(), e->N, cudaMemcpyHostToDevice, e->stream));
-  CU(cudaStreamSynchronize(e->stream));
-  return CGL_OK;
+  return upload_flags(e);
 }
 
 // A render that fails part way (a refused or failed allocation, a CUDA error)
@@ -809,6 +917,8 @@ void forget_graph(cgl_engine* e) {
   e->entries = 0;
   e->max_deg_in = e->max_deg_out = 0;
   e->n_heavy_in = e->n_heavy_out = 0;
+  e->n_early_hubs = e->n_early_pts = 0;
+  e->early.clear();
   e->mb_ready = false;
   e->collision_ready = false;
   e->point_clusters = e->cluster_positions = false;
@@ -841,6 +951,10 @@ cgl_status build_graph(cgl_engine* e, double alpha, uint64_t N, uint64_t E) {
   const bool pos_changed = e->pos_dirty;
   const bool links_changed = e->links_dirty || pos_changed;
   cgl_status st;
+  if (links_changed) {   // the early hubs are chosen again from the new lists
+    e->n_early_hubs = e->n_early_pts = 0;
+    e->early.clear();
+  }
   if (pos_changed) e->N = N;
   e->E = E;
   e->has_strength = e->have_strength && e->in_strength.size() == E;
@@ -982,6 +1096,7 @@ cgl_status build_graph(cgl_engine* e, double alpha, uint64_t N, uint64_t E) {
     launch_mark_hubs((const uint32_t*)e->b_heavy_out.p, e->n_heavy_out, (uint8_t*)e->b_hub_out.p, e->stream);
     CU(cudaGetLastError());
     CU(cudaStreamSynchronize(e->stream));
+    if ((st = build_early(e))) return st;
   }
   if (e->clusters_dirty || pos_changed) {
     // Clusters.create (Clusters/index.ts:54-100), src/index.ts:1668
@@ -1582,7 +1697,11 @@ cgl_status cgl_get_layout(cgl_engine* e, cgl_layout* o) {
   // the outgoing hub chains beside the collision sums: two link launches, two sums
   if (p.link_in && p.link_out && p.coll && !p.clus && p.mb && e->n_heavy_out > 0) k += 2;
   if (p.clus) k += 1 + (uint32_t)p.clus_sum;           // sums, pull + update
+  // the early points' many-body terms and the early hubs' chains
+  if (p.mb && p.link_in && e->n_early_hubs > 0 && e->n_early_pts > 0) k += 2;
   o->kernels_per_tick = k;
+  o->early_hubs = e->n_early_hubs;
+  o->early_points = e->n_early_pts;
   return CGL_OK;
 }
 

@@ -299,6 +299,7 @@ __global__ void __launch_bounds__(kBlock) k_scatter(DeviceView d, uint32_t cells
   const uint32_t dst = b + r;
   d.sorted_idx[dst] = i;
   d.sorted_pos[dst] = p;
+  if (d.inv) d.inv[i] = dst;
   if (PAIRS && !(r & 1u)) {
     const uint32_t m = d.cell_start[k + 1] - b;
     d.pair_list[d.pair_start[k] + (r >> 1)] = dst | (r + 1 == m ? kSingleBit : 0u);
@@ -318,6 +319,7 @@ __device__ __forceinline__ void move_slots_to_head(const DeviceView& d, uint32_t
         const float2 p0 = d.sorted_pos[tq], p1 = d.sorted_pos[pq];
         d.sorted_idx[tq] = i1; d.sorted_pos[tq] = p1;
         d.sorted_idx[pq] = i0; d.sorted_pos[pq] = p0;
+        if (d.inv) { d.inv[i1] = tq; d.inv[i0] = pq; }
 #pragma unroll
         for (int r = q + 1; r < kSlots; ++r)
           if (at[r] == tq) at[r] = pq;
@@ -565,22 +567,26 @@ __device__ __forceinline__ bool level_guard_holds(const DeviceView& d, const Sim
   return s.level_guard && __ldg(&d.big_count[kOutsideFlag]) == 0;
 }
 
-// force-nearfield.frag:151-157 (jitter, step clamp) and the update.
+// force-nearfield.frag:151-157 (jitter, step clamp) and the update.  The
+// point is left alone when the early pass (early) writes it this tick.
 __device__ __forceinline__ void finish_point(const DeviceView& d, const SimScalars& s, uint32_t i, float2 p, float2 rj,
-                                             float2 vel, float2 nf, PairUnits pu) {
+                                             float2 vel, float2 nf, PairUnits pu, bool early = false) {
   nf = add2(nf, mul2(nf, rj, pu), pu);
   const float max_step = __fmul_rn(2.0f, s.csf);
   const float2 nsq = mul2(nf, nf, pu);
   const float speed = __fsqrt_rn(__fadd_rn(nsq.x, nsq.y));
   if (speed > max_step) nf = mul2(nf, splat(__fdiv_rn(max_step, speed)), pu);
   vel = add2(vel, nf, pu);
-  if (!(d.flags[i] & kPinned)) d.pos[i] = integrate(p, vel.x, vel.y, s.friction, s.space);
+  const uint8_t f = d.flags[i];
+  if (!(f & kPinned) && (early || !(s.skip_early && (f & kEarly))))
+    d.pos[i] = integrate(p, vel.x, vel.y, s.friction, s.space);
 }
 
 // One point, all of its terms in order on one thread (GUARDED: the level
 // terms without the range flag, level_guard_holds).
 template <bool FAST, bool GUARDED = false>
-__device__ __forceinline__ void manybody_point(const DeviceView& d, const SimScalars& s, uint32_t j, float k) {
+__device__ __forceinline__ void manybody_point(const DeviceView& d, const SimScalars& s, uint32_t j, float k,
+                                               bool early = false) {
   const uint32_t i = d.sorted_idx[j];
   const float2 p = d.sorted_pos[j];
   const int gf = s.gf, L = s.levels;
@@ -591,7 +597,7 @@ __device__ __forceinline__ void manybody_point(const DeviceView& d, const SimSca
   for (int l = 0; l < L; ++l) vel = add2(vel, level_sum<FAST, FAST, GUARDED>(d, L, l, fcx, fcy, p, k, pu), pu);
   const float2 rj = d.jitter[i];
   const float2 nf = near_terms<FAST>(d.rec + d.level_off[L - 1], d.cell_start, d.sorted_pos, gf, fcx, fcy, j, p, rj, k, pu);
-  finish_point(d, s, i, p, rj, vel, nf, pu);
+  finish_point(d, s, i, p, rj, vel, nf, pu, early);
 }
 
 // Small graphs: each point's level sums and near-field cells are independent
@@ -734,6 +740,22 @@ __global__ void __launch_bounds__(kBlock, 6) k_manybody(DeviceView d, SimScalars
   if (!quotient_by_recip(k)) manybody_point<false>(d, s, j, k);
   else if (level_guard_holds(d, s)) manybody_point<true, true>(d, s, j, k);
   else manybody_point<true>(d, s, j, k);
+}
+
+// The early points (the early hubs and their incoming link targets), a thread
+// each, at their sorted positions: the terms of manybody_point, so each result
+// is the one the whole pass gives that point.  The whole pass then skips them
+// (SimScalars::skip_early), and the early hubs' chains start on them while it
+// runs.
+__global__ void __launch_bounds__(kBlock) k_manybody_early(DeviceView d, SimScalars s) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= d.n_early_pts) return;
+  const TickParams tp = tick_params(d);
+  const float k = __fmul_rn(tp.alpha, s.repulsion);
+  const uint32_t j = d.inv[d.early_pts[t]];
+  if (!quotient_by_recip(k)) manybody_point<false>(d, s, j, k, true);
+  else if (level_guard_holds(d, s)) manybody_point<true, true>(d, s, j, k, true);
+  else manybody_point<true>(d, s, j, k, true);
 }
 
 // ------------------------------------------------------------------- link --
@@ -1258,6 +1280,10 @@ void launch_manybody(const DeviceView& d, const SimScalars& s, cudaStream_t st) 
   }
 }
 
+void launch_manybody_early(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
+  if (d.n_early_pts) k_manybody_early<<<blocks_for(d.n_early_pts), kBlock, 0, st>>>(d, s);
+}
+
 void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool swap_back, cudaStream_t st,
                  int part) {
   if (!d.n) return;
@@ -1270,8 +1296,16 @@ void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool s
   const float2* src = swap_back ? d.pos_alt : d.pos;
   float2* dst = swap_back ? d.pos : d.pos_alt;
   const uint32_t nlight = blocks_for(d.n - nhub);
+  const uint32_t early = direction == 0 ? std::min(d.n_early_hubs, nhub) : 0u;
   if (part == kLinkHubs) {
     if (nhub) k_link<<<nhub, kBlock, sizeof(HubStage), st>>>(d, s, rp, en, woff, lane_ent, src, dst, order, d.n, nhub, 0u);
+  } else if (part == kLinkEarlyHubs) {
+    if (early) k_link<<<early, kBlock, sizeof(HubStage), st>>>(d, s, rp, en, woff, lane_ent, src, dst, order, d.n, nhub, 0u);
+  } else if (part == kLinkAfterEarly) {
+    const uint32_t nb = nhub - early + nlight;
+    if (nb)
+      k_link<<<nb, kBlock, nhub > early ? sizeof(HubStage) : 0, st>>>(d, s, rp, en, woff, lane_ent, src, dst, order,
+                                                                       d.n, nhub, early);
   } else if (part == kLinkLight) {
     if (nlight) k_link<<<nlight, kBlock, 0, st>>>(d, s, rp, en, woff, lane_ent, src, dst, order, d.n, nhub, nhub);
   } else {
@@ -1290,6 +1324,19 @@ __global__ void __launch_bounds__(kBlock) k_mark_hubs(const uint32_t* __restrict
 
 void launch_mark_hubs(const uint32_t* order, uint32_t nhub, uint8_t* mark, cudaStream_t st) {
   if (nhub) k_mark_hubs<<<blocks_for(nhub), kBlock, 0, st>>>(order, nhub, mark);
+}
+
+namespace {
+__global__ void __launch_bounds__(kBlock) k_hub_spans(const uint32_t* __restrict__ order,
+                                                      const uint32_t* __restrict__ rowptr, uint32_t m,
+                                                      uint2* __restrict__ spans) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < m) spans[t] = make_uint2(rowptr[order[t]], rowptr[order[t] + 1]);
+}
+}  // namespace
+
+void launch_hub_spans(const uint32_t* order, const uint32_t* rowptr, uint32_t m, uint2* spans, cudaStream_t st) {
+  if (m) k_hub_spans<<<blocks_for(m), kBlock, 0, st>>>(order, rowptr, m, spans);
 }
 
 void launch_warp_lengths(const uint32_t* order, const uint32_t* rowptr, uint32_t nhub, uint32_t n, uint32_t* woff,

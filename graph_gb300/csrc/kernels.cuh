@@ -19,7 +19,7 @@ struct DeviceView {
   uint32_t n;                 // points (original index space)
   float2* pos;                // current positions [n]
   float2* pos_alt;            // ping-pong target of the link passes [n]
-  const uint8_t* flags;       // kPinned | kAbsent [n]
+  const uint8_t* flags;       // kPinned | kAbsent | kEarly [n]
   const float2* jitter;       // per-point random vector (ForceManyBody/index.ts:133-138) [n]
   uint32_t* key;              // finest cell of each point, kNoCell if absent [n] (of position j when
                               // bin_state[1]: see idx_s)
@@ -63,6 +63,13 @@ struct DeviceView {
   const uint32_t* heavy_in;   // all points by incoming list length, longest first;
   const uint32_t* heavy_out;  // the first n_heavy_* have lists longer than kHeavyDegree
   uint32_t n_heavy_in, n_heavy_out;
+  // Early hubs: the first n_early_hubs rows of heavy_in (the longest incoming
+  // lists) run their chains beside the many-body pass.  Their points and link
+  // targets (early_pts, kEarly in flags) take their many-body terms in a pass
+  // of their own first; inv then holds each live point's sorted position.
+  const uint32_t* early_pts;
+  uint32_t n_early_pts, n_early_hubs;
+  uint32_t* inv;              // sorted position of each live point [n]; null without early hubs
   // The rows after the first n_heavy_* of the order, by warps of 32: warp w's
   // entries at lane_ent[woff[w] .. woff[w + 1]), entry k of lane l at
   // 32 k + l, each lane's list padded to its warp's longest with absent entries.
@@ -109,6 +116,7 @@ struct SimScalars {
   int level_guard;            // finest cell >= 2 units and space <= 2^25: a level term's length is
                               // then in [1, 2^52] whenever every binned point lies in [0, space]
   int any_pinned;             // some live point is pinned
+  int skip_early;             // this tick runs k_manybody_early: the many-body pass leaves kEarly points to it
 };
 constexpr uint32_t kErrorScan = 1;     // error_word bit: a scan block's look-back gave up waiting
 constexpr uint32_t kOutsideFlag = 4;   // big_count word of the outside-the-space flag
@@ -126,15 +134,20 @@ void launch_wait_limit(const unsigned long long* status, uint32_t* error, cudaSt
 void launch_scatter(const DeviceView& d, const SimScalars& s, cudaStream_t st);
 void launch_cells(const DeviceView& d, const SimScalars& s, cudaStream_t st);
 void launch_manybody(const DeviceView& d, const SimScalars& s, cudaStream_t st);
+// The many-body terms of the early points alone (DeviceView::early_pts).
+void launch_manybody_early(const DeviceView& d, const SimScalars& s, cudaStream_t st);
 // direction 0 = incoming (reads pos, writes pos_alt), 1 = outgoing (pos_alt -> pos)
 // The first n_heavy_* rows of the order each get a CTA of their own.
 // A link pass: all of it (kLinkAll), or its hub CTAs or its light rows alone
-// (the two halves write disjoint points and may run on two streams).
-enum { kLinkAll = 0, kLinkHubs = 1, kLinkLight = 2 };
+// (the two halves write disjoint points and may run on two streams); or the
+// early hubs' CTAs (the first n_early_hubs) and then the rest of the pass.
+enum { kLinkAll = 0, kLinkHubs = 1, kLinkLight = 2, kLinkEarlyHubs = 3, kLinkAfterEarly = 4 };
 void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool swap_back, cudaStream_t st,
                  int part = kLinkAll);
 // mark[order[t]] = 1 for t < nhub (the points whose list runs on a hub CTA)
 void launch_mark_hubs(const uint32_t* order, uint32_t nhub, uint8_t* mark, cudaStream_t st);
+// spans[t] = (rowptr[order[t]], rowptr[order[t] + 1]) for t < m
+void launch_hub_spans(const uint32_t* order, const uint32_t* rowptr, uint32_t m, uint2* spans, cudaStream_t st);
 // The warp layout of one direction's light rows (woff, lane_ent above):
 // warp_lengths writes 32 x the longest list of each of the nw warps to
 // woff[0 .. nw) and 0 to woff[nw] (an exclusive scan then gives the offsets);

@@ -58,10 +58,12 @@ __device__ __forceinline__ void warp_finish_cell(const V& d, uint32_t c, uint32_
   if (in_head) {
     d.sorted_idx[h] = take_idx;
     d.sorted_pos[h] = take_pos;
+    if (d.inv) d.inv[take_idx] = h;
   }
   if (displaced) {
     d.sorted_idx[dest] = disp_idx;
     d.sorted_pos[dest] = disp_pos;
+    if (d.inv) d.inv[disp_idx] = dest;
   }
   if (lane == 0) {
     d.big_sx[c] = ax;

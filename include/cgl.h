@@ -318,6 +318,8 @@ typedef struct cgl_layout {
   uint32_t kernels_per_tick;   /* kernel launches one tick makes with the current data and config */
   uint32_t manybody_kernel;    /* CGL_MANYBODY_*: how the many-body pass spreads points over threads */
   uint32_t manybody_tuned;     /* 1 once manybody_kernel was chosen by timing this graph's ticks */
+  uint32_t early_hubs;         /* longest incoming lists whose chains start beside the many-body pass */
+  uint32_t early_points;       /* their points and link targets, whose many-body terms run first */
 } cgl_layout;
 enum {
   CGL_MANYBODY_AUTO = -1,       /* cgl_config.manybody_kernel: time the candidates, keep the fastest */
