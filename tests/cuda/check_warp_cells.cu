@@ -25,6 +25,7 @@ struct View {
   long long* big_sx;
   long long* big_sy;
   uint32_t* big_ns;
+  uint32_t* inv = nullptr;   // no sorted-position map here
 };
 
 constexpr uint32_t kSeed = 0x2545F491u;
