@@ -118,6 +118,7 @@ struct cgl_engine {
   DevBuf b_early_pts, b_inv;
   uint32_t n_early_hubs = 0, n_early_pts = 0;
   std::vector<uint8_t> early;   // kEarly per point (empty: none)
+  int32_t early_limit = -1;     // at most this many early hubs (cgl_debug_set_early_hubs); -1: the rule
   DevBuf b_size, b_cgrid_acc, b_cgrid;
   DevBuf b_cl_of, b_cl_coeff, b_cl_custom, b_cl_acc;
   DevBuf b_texture;                        // staging for pageable texture read-back
@@ -824,7 +825,8 @@ cgl_status build_early(cgl_engine* e) {
   e->n_early_hubs = e->n_early_pts = 0;
   e->early.clear();
   const uint32_t n = (uint32_t)e->N;
-  const uint32_t m = std::min(e->n_heavy_in, kEarlyCandidates);
+  uint32_t m = std::min(e->n_heavy_in, kEarlyCandidates);
+  if (e->early_limit >= 0) m = std::min(m, (uint32_t)e->early_limit);
   cgl_status rc = CGL_OK;
   if (m && e->T) {
     DevBuf t_spans;
@@ -874,11 +876,31 @@ cgl_status build_early(cgl_engine* e) {
         e->early.clear();
         return rc;
       }
-      if (!pts.empty())
-        CU(cudaMemcpyAsync(e->b_early_pts.p, pts.data(), pts.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
-                           e->stream));
+      const uint32_t np = (uint32_t)pts.size();
+      if (np) {
+        CU(cudaMemcpyAsync(e->b_early_pts.p, pts.data(), np * sizeof(uint32_t), cudaMemcpyHostToDevice, e->stream));
+        // by finest cell of their positions now: the early pass then walks them
+        // in (roughly) the order the cells hold them
+        DevBuf t_keys, t_tmp;
+        if ((rc = dev_reserve(e, t_keys, np * sizeof(uint32_t), false)) ||
+            (rc = dev_reserve(e, t_tmp, dingest::sort_temp_words(np) * sizeof(uint32_t), false))) {
+          dev_release(e, t_keys);
+          e->early.clear();
+          return rc;
+        }
+        const SimScalars s = make_scalars(e);
+        launch_cell_keys((const float2*)e->b_pos.p, (const uint32_t*)e->b_early_pts.p, np, s.csf, s.gf,
+                         (uint32_t*)t_keys.p, e->stream);
+        dingest::sort_pairs((uint32_t*)t_keys.p, (uint32_t*)e->b_early_pts.p, np,
+                            dingest::key_bits((uint64_t)e->Gf * e->Gf), (uint32_t*)t_tmp.p, e->stream);
+        err = cudaGetLastError();
+        if (err == cudaSuccess) err = cudaStreamSynchronize(e->stream);
+        dev_release(e, t_keys);
+        dev_release(e, t_tmp);
+        if (err != cudaSuccess) return fail(e, CGL_CUDA_ERROR, "early points: %s", cudaGetErrorString(err));
+      }
       e->n_early_hubs = k;
-      e->n_early_pts = (uint32_t)pts.size();
+      e->n_early_pts = np;
     }
   }
   if (!e->n_early_hubs) {
@@ -1713,6 +1735,19 @@ cgl_status cgl_debug_get_cells(cgl_engine* e, uint32_t level, float* out, uint64
   CU(cudaMemcpyAsync(out, (float4*)e->b_rec.p + e->level_off[level], cells * sizeof(float4), cudaMemcpyDeviceToHost,
                      e->stream));
   CU(cudaStreamSynchronize(e->stream));
+  return CGL_OK;
+}
+
+cgl_status cgl_debug_set_early_hubs(cgl_engine* e, int32_t max_hubs) {
+  CHECK_E(e);
+  if (max_hubs < -1) return fail(e, CGL_INVALID_ARG, "max_hubs %d", max_hubs);
+  e->early_limit = max_hubs;
+  if (e->N && !e->links_dirty && !e->pos_dirty) {
+    const cgl_status st = build_early(e);
+    if (st) return st;
+  }
+  refresh_view(e);
+  e->graph_dirty = true;
   return CGL_OK;
 }
 

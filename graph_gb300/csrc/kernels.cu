@@ -1339,6 +1339,21 @@ void launch_hub_spans(const uint32_t* order, const uint32_t* rowptr, uint32_t m,
   if (m) k_hub_spans<<<blocks_for(m), kBlock, 0, st>>>(order, rowptr, m, spans);
 }
 
+namespace {
+__global__ void __launch_bounds__(kBlock) k_cell_keys(const float2* __restrict__ pos, const uint32_t* __restrict__ pts,
+                                                      uint32_t m, float csf, int gf, uint32_t* __restrict__ keys) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  const float2 p = pos[pts[t]];
+  keys[t] = (uint32_t)cell_index(p.y, csf, gf) * (uint32_t)gf + (uint32_t)cell_index(p.x, csf, gf);
+}
+}  // namespace
+
+void launch_cell_keys(const float2* pos, const uint32_t* pts, uint32_t m, float csf, int gf, uint32_t* keys,
+                      cudaStream_t st) {
+  if (m) k_cell_keys<<<blocks_for(m), kBlock, 0, st>>>(pos, pts, m, csf, gf, keys);
+}
+
 void launch_warp_lengths(const uint32_t* order, const uint32_t* rowptr, uint32_t nhub, uint32_t n, uint32_t* woff,
                          cudaStream_t st) {
   const uint32_t nw = (n - nhub + 31) / 32;

@@ -148,6 +148,9 @@ void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool s
 void launch_mark_hubs(const uint32_t* order, uint32_t nhub, uint8_t* mark, cudaStream_t st);
 // spans[t] = (rowptr[order[t]], rowptr[order[t] + 1]) for t < m
 void launch_hub_spans(const uint32_t* order, const uint32_t* rowptr, uint32_t m, uint2* spans, cudaStream_t st);
+// keys[t] = the finest cell (row-major) of pos[pts[t]] for t < m
+void launch_cell_keys(const float2* pos, const uint32_t* pts, uint32_t m, float csf, int gf, uint32_t* keys,
+                      cudaStream_t st);
 // The warp layout of one direction's light rows (woff, lane_ent above):
 // warp_lengths writes 32 x the longest list of each of the nw warps to
 // woff[0 .. nw) and 0 to woff[nw] (an exclusive scan then gives the offsets);

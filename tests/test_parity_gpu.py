@@ -210,6 +210,16 @@ def test_early_hubs():
         orc.step(1)
         _assert_same(eng, orc, ("early hubs, new pins", t))
     _assert_cells_and_slots(eng, orc)
+    eng.set_early_hubs(0)                      # every chain after the many-body pass again
+    assert eng.layout().early_hubs == 0
+    eng.step(2)
+    orc.step(2)
+    _assert_same(eng, orc, "early hubs off")
+    eng.set_early_hubs(1)
+    assert eng.layout().early_hubs == 1
+    eng.step(2)
+    orc.step(2)
+    _assert_same(eng, orc, "one early hub")
 
 
 def test_springs_outside_the_in_range_sequences():
