@@ -104,6 +104,7 @@ class Layout(C.Structure):
         ("manybody_tuned", C.c_uint32),
         ("early_hubs", C.c_uint32),
         ("early_points", C.c_uint32),
+        ("leading_out_hubs", C.c_uint32),
     ]
 
 

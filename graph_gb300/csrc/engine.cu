@@ -117,6 +117,7 @@ struct cgl_engine {
   // early hubs (DeviceView::n_early_hubs): their points and link targets
   DevBuf b_early_pts, b_inv;
   uint32_t n_early_hubs = 0, n_early_pts = 0;
+  uint32_t n_first_out = 0;     // leading outgoing hubs (DeviceView::n_first_out)
   std::vector<uint8_t> early;   // kEarly per point (empty: none)
   int32_t early_limit = -1;     // at most this many early hubs (cgl_debug_set_early_hubs); -1: the rule
   DevBuf b_size, b_cgrid_acc, b_cgrid;
@@ -276,6 +277,7 @@ void refresh_view(cgl_engine* e) {
   d.early_pts = (const uint32_t*)e->b_early_pts.p;
   d.n_early_pts = e->n_early_pts;
   d.n_early_hubs = e->n_early_hubs;
+  d.n_first_out = e->n_first_out;
   d.inv = e->n_early_hubs ? (uint32_t*)e->b_inv.p : nullptr;
   d.woff_in = (const uint32_t*)e->b_woff_in.p;
   d.lane_ent_in = (const uint4*)e->b_lane_ent_in.p;
@@ -403,7 +405,7 @@ cgl_status enqueue_tick(cgl_engine* e, cudaStream_t st, cudaEvent_t* ev) {
       launch_manybody_early(d, s, st);
       CU(cudaEventRecord(e->fork, st));
       CU(cudaStreamWaitEvent(e->side, e->fork, 0));
-      launch_link(d, s, 0, false, e->side, kLinkEarlyHubs);
+      launch_link(d, s, 0, false, e->side, kLinkFirstHubs);
       CU(cudaEventRecord(e->join, e->side));
     }
     launch_manybody(d, s, st);
@@ -411,22 +413,32 @@ cgl_status enqueue_tick(cgl_engine* e, cudaStream_t st, cudaEvent_t* ev) {
   }
   if (p.link_in || p.link_out) {
     mark(6, 0);
-    if (p.link_in) launch_link(d, s, 0, false, st, early ? kLinkAfterEarly : kLinkAll);
+    if (p.link_in) launch_link(d, s, 0, false, st, early ? kLinkAfterFirst : kLinkAll);
     if (early) CU(cudaStreamWaitEvent(st, e->join, 0));
     mark(6, 1);
     mark(7, 0);
-    if (p.link_out && !overlap) launch_link(d, s, 1, p.link_in, st);
-    if (overlap) {
-      CU(cudaEventRecord(e->fork, st));
-      CU(cudaStreamWaitEvent(e->side, e->fork, 0));
-      launch_link(d, s, 1, p.link_in, e->side, kLinkHubs);
-      CU(cudaEventRecord(e->join, e->side));
-      launch_link(d, s, 1, p.link_in, st, kLinkLight);
-      launch_collision_sums(d, s, d.sorted_idx, (uint32_t)e->live, (const uint8_t*)e->b_hub_out.p, st);
-      CU(cudaStreamWaitEvent(st, e->join, 0));
-      launch_collision_sums(d, s, d.heavy_out, d.n_heavy_out, nullptr, st);
-      launch_collision_convert(d, s, st);
-      launch_collision_force(d, s, d.sorted_idx, (uint32_t)e->live, st);
+    if (p.link_out) {
+      // The leading outgoing hubs on the second stream, an SM each, beside the
+      // rest of the pass; with the overlap all hub CTAs go there when no list
+      // leads, beside the light rows.
+      const bool first_out = !ev && d.n_first_out > 0;
+      const bool split = first_out || overlap;
+      if (split) {
+        CU(cudaEventRecord(e->fork, st));
+        CU(cudaStreamWaitEvent(e->side, e->fork, 0));
+        launch_link(d, s, 1, p.link_in, e->side, first_out ? kLinkFirstHubs : kLinkHubs);
+        CU(cudaEventRecord(e->join, e->side));
+      }
+      launch_link(d, s, 1, p.link_in, st, first_out ? kLinkAfterFirst : overlap ? kLinkLight : kLinkAll);
+      if (overlap) {
+        launch_collision_sums(d, s, d.sorted_idx, (uint32_t)e->live, (const uint8_t*)e->b_hub_out.p, st);
+        CU(cudaStreamWaitEvent(st, e->join, 0));
+        launch_collision_sums(d, s, d.heavy_out, d.n_heavy_out, nullptr, st);
+        launch_collision_convert(d, s, st);
+        launch_collision_force(d, s, d.sorted_idx, (uint32_t)e->live, st);
+      } else if (split) {
+        CU(cudaStreamWaitEvent(st, e->join, 0));
+      }
     }
     mark(7, 1);
     if (!(p.link_in && p.link_out))
@@ -813,95 +825,119 @@ cgl_status upload_flags(cgl_engine* e) {
   return CGL_OK;
 }
 
-// Early hubs: the leading incoming lists (longest first) of at least
-// kEarlyMinLinks links and a quarter of the longest, while their links total
-// at most an eighth of the points.  Their chains need the many-body results of
-// their own points and link targets only; those run first, and the chains
-// then start beside the rest of the many-body pass instead of after it.
-constexpr uint32_t kEarlyCandidates = 64;
-constexpr uint32_t kEarlyMinLinks = 4096;
+// Leading hubs: the first lists of a direction's order (longest first) of at
+// least kLeadMinLinks links and a quarter of the longest, at most
+// kLeadCandidates of them (or the test hook's limit).  Their chains each run
+// on an SM of their own on the second stream.  Incoming (early hubs): while
+// their links total at most an eighth of the points.  Their chains need the
+// many-body results of their own points and link targets only; those run
+// first, and the chains then start beside the rest of the many-body pass
+// instead of after it.  Outgoing: their chains run beside the other lists of
+// the pass.
+constexpr uint32_t kLeadCandidates = 32;
+constexpr uint32_t kLeadMinLinks = 4096;
+
+// spans (rowptr[p], rowptr[p + 1]) and points p of the leading hubs of a
+// direction; returns their count (0 when none qualifies).
+cgl_status leading_hubs(cgl_engine* e, int dir, uint64_t max_total, std::vector<uint2>& spans,
+                        std::vector<uint32_t>& hubs, uint32_t* count) {
+  *count = 0;
+  const uint32_t nheavy = dir == 0 ? e->n_heavy_in : e->n_heavy_out;
+  const uint32_t* order = (const uint32_t*)(dir == 0 ? e->b_heavy_in.p : e->b_heavy_out.p);
+  const uint32_t* rowptr = (const uint32_t*)(dir == 0 ? e->b_rowptr_in.p : e->b_rowptr_out.p);
+  uint32_t m = std::min(nheavy, kLeadCandidates);
+  if (e->early_limit >= 0) m = std::min(m, (uint32_t)e->early_limit);
+  if (!m) return CGL_OK;
+  DevBuf t_spans;
+  cgl_status rc;
+  if ((rc = dev_reserve(e, t_spans, m * sizeof(uint2), false))) return rc;
+  spans.resize(m);
+  hubs.resize(m);
+  launch_hub_spans(order, rowptr, m, (uint2*)t_spans.p, e->stream);
+  cudaError_t err = cudaGetLastError();
+  if (err == cudaSuccess)
+    err = cudaMemcpyAsync(spans.data(), t_spans.p, m * sizeof(uint2), cudaMemcpyDeviceToHost, e->stream);
+  if (err == cudaSuccess)
+    err = cudaMemcpyAsync(hubs.data(), order, m * sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(e->stream);
+  dev_release(e, t_spans);
+  if (err != cudaSuccess) return fail(e, CGL_CUDA_ERROR, "leading hubs: %s", cudaGetErrorString(err));
+  const uint32_t least = std::max(kLeadMinLinks, (spans[0].y - spans[0].x) / 4);
+  uint64_t total = 0;
+  uint32_t k = 0;
+  for (; k < m; ++k) {
+    const uint32_t len = spans[k].y - spans[k].x;
+    if (len < least || total + len > max_total) break;
+    total += len;
+  }
+  *count = k;
+  return CGL_OK;
+}
 
 cgl_status build_early(cgl_engine* e) {
-  e->n_early_hubs = e->n_early_pts = 0;
+  e->n_early_hubs = e->n_early_pts = e->n_first_out = 0;
   e->early.clear();
   const uint32_t n = (uint32_t)e->N;
-  uint32_t m = std::min(e->n_heavy_in, kEarlyCandidates);
-  if (e->early_limit >= 0) m = std::min(m, (uint32_t)e->early_limit);
   cgl_status rc = CGL_OK;
-  if (m && e->T) {
-    DevBuf t_spans;
-    if ((rc = dev_reserve(e, t_spans, m * sizeof(uint2), false))) return rc;
-    std::vector<uint2> spans(m);
-    std::vector<uint32_t> hubs(m);
-    launch_hub_spans((const uint32_t*)e->b_heavy_in.p, (const uint32_t*)e->b_rowptr_in.p, m, (uint2*)t_spans.p,
-                     e->stream);
-    cudaError_t err = cudaGetLastError();
-    if (err == cudaSuccess)
-      err = cudaMemcpyAsync(spans.data(), t_spans.p, m * sizeof(uint2), cudaMemcpyDeviceToHost, e->stream);
-    if (err == cudaSuccess)
-      err = cudaMemcpyAsync(hubs.data(), e->b_heavy_in.p, m * sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream);
-    if (err == cudaSuccess) err = cudaStreamSynchronize(e->stream);
-    dev_release(e, t_spans);
-    if (err != cudaSuccess) return fail(e, CGL_CUDA_ERROR, "early hubs: %s", cudaGetErrorString(err));
-    const uint32_t len0 = spans[0].y - spans[0].x;
-    const uint32_t least = std::max(kEarlyMinLinks, len0 / 4);
+  std::vector<uint2> spans;
+  std::vector<uint32_t> hubs;
+  uint32_t k = 0;
+  if (e->T && (rc = leading_hubs(e, 1, ~0ull, spans, hubs, &k))) return rc;
+  e->n_first_out = k;
+  k = 0;
+  if (e->T && (rc = leading_hubs(e, 0, n / 8, spans, hubs, &k))) return rc;
+  if (k) {
     uint64_t total = 0;
-    uint32_t k = 0;
-    for (; k < m; ++k) {
-      const uint32_t len = spans[k].y - spans[k].x;
-      if (len < least || total + len > n / 8) break;
-      total += len;
+    for (uint32_t t = 0; t < k; ++t) total += spans[t].y - spans[t].x;
+    std::vector<uint4> ent(total);
+    size_t at = 0;
+    cudaError_t err = cudaSuccess;
+    for (uint32_t t = 0; t < k && err == cudaSuccess; ++t) {
+      const uint32_t len = spans[t].y - spans[t].x;
+      err = cudaMemcpyAsync(ent.data() + at, (const uint4*)e->b_ent_in.p + spans[t].x, len * sizeof(uint4),
+                            cudaMemcpyDeviceToHost, e->stream);
+      at += len;
     }
-    if (k) {
-      std::vector<uint4> ent(total);
-      size_t at = 0;
-      for (uint32_t t = 0; t < k && err == cudaSuccess; ++t) {
-        const uint32_t len = spans[t].y - spans[t].x;
-        err = cudaMemcpyAsync(ent.data() + at, (const uint4*)e->b_ent_in.p + spans[t].x, len * sizeof(uint4),
-                              cudaMemcpyDeviceToHost, e->stream);
-        at += len;
-      }
-      if (err == cudaSuccess) err = cudaStreamSynchronize(e->stream);
-      if (err != cudaSuccess) return fail(e, CGL_CUDA_ERROR, "early hubs: %s", cudaGetErrorString(err));
-      e->early.assign(n, 0);
-      for (uint32_t t = 0; t < k; ++t)
-        if (!e->absent[hubs[t]]) e->early[hubs[t]] = 1;
-      for (const uint4& en : ent)
-        if (en.x < n && !e->absent[en.x]) e->early[en.x] = 1;
-      std::vector<uint32_t> pts;
-      for (uint32_t i = 0; i < n; ++i)
-        if (e->early[i]) pts.push_back(i);
-      if ((rc = dev_reserve(e, e->b_early_pts, std::max<size_t>(pts.size(), 1) * sizeof(uint32_t), false)) ||
-          (rc = dev_reserve(e, e->b_inv, (size_t)n * sizeof(uint32_t), false))) {
+    if (err == cudaSuccess) err = cudaStreamSynchronize(e->stream);
+    if (err != cudaSuccess) return fail(e, CGL_CUDA_ERROR, "early hubs: %s", cudaGetErrorString(err));
+    e->early.assign(n, 0);
+    for (uint32_t t = 0; t < k; ++t)
+      if (!e->absent[hubs[t]]) e->early[hubs[t]] = 1;
+    for (const uint4& en : ent)
+      if (en.x < n && !e->absent[en.x]) e->early[en.x] = 1;
+    std::vector<uint32_t> pts;
+    for (uint32_t i = 0; i < n; ++i)
+      if (e->early[i]) pts.push_back(i);
+    if ((rc = dev_reserve(e, e->b_early_pts, std::max<size_t>(pts.size(), 1) * sizeof(uint32_t), false)) ||
+        (rc = dev_reserve(e, e->b_inv, (size_t)n * sizeof(uint32_t), false))) {
+      e->early.clear();
+      return rc;
+    }
+    const uint32_t np = (uint32_t)pts.size();
+    if (np) {
+      CU(cudaMemcpyAsync(e->b_early_pts.p, pts.data(), np * sizeof(uint32_t), cudaMemcpyHostToDevice, e->stream));
+      // by finest cell of their positions now: the early pass then walks them
+      // in (roughly) the order the cells hold them
+      DevBuf t_keys, t_tmp;
+      if ((rc = dev_reserve(e, t_keys, np * sizeof(uint32_t), false)) ||
+          (rc = dev_reserve(e, t_tmp, dingest::sort_temp_words(np) * sizeof(uint32_t), false))) {
+        dev_release(e, t_keys);
         e->early.clear();
         return rc;
       }
-      const uint32_t np = (uint32_t)pts.size();
-      if (np) {
-        CU(cudaMemcpyAsync(e->b_early_pts.p, pts.data(), np * sizeof(uint32_t), cudaMemcpyHostToDevice, e->stream));
-        // by finest cell of their positions now: the early pass then walks them
-        // in (roughly) the order the cells hold them
-        DevBuf t_keys, t_tmp;
-        if ((rc = dev_reserve(e, t_keys, np * sizeof(uint32_t), false)) ||
-            (rc = dev_reserve(e, t_tmp, dingest::sort_temp_words(np) * sizeof(uint32_t), false))) {
-          dev_release(e, t_keys);
-          e->early.clear();
-          return rc;
-        }
-        const SimScalars s = make_scalars(e);
-        launch_cell_keys((const float2*)e->b_pos.p, (const uint32_t*)e->b_early_pts.p, np, s.csf, s.gf,
-                         (uint32_t*)t_keys.p, e->stream);
-        dingest::sort_pairs((uint32_t*)t_keys.p, (uint32_t*)e->b_early_pts.p, np,
-                            dingest::key_bits((uint64_t)e->Gf * e->Gf), (uint32_t*)t_tmp.p, e->stream);
-        err = cudaGetLastError();
-        if (err == cudaSuccess) err = cudaStreamSynchronize(e->stream);
-        dev_release(e, t_keys);
-        dev_release(e, t_tmp);
-        if (err != cudaSuccess) return fail(e, CGL_CUDA_ERROR, "early points: %s", cudaGetErrorString(err));
-      }
-      e->n_early_hubs = k;
-      e->n_early_pts = np;
+      const SimScalars s = make_scalars(e);
+      launch_cell_keys((const float2*)e->b_pos.p, (const uint32_t*)e->b_early_pts.p, np, s.csf, s.gf,
+                       (uint32_t*)t_keys.p, e->stream);
+      dingest::sort_pairs((uint32_t*)t_keys.p, (uint32_t*)e->b_early_pts.p, np,
+                          dingest::key_bits((uint64_t)e->Gf * e->Gf), (uint32_t*)t_tmp.p, e->stream);
+      err = cudaGetLastError();
+      if (err == cudaSuccess) err = cudaStreamSynchronize(e->stream);
+      dev_release(e, t_keys);
+      dev_release(e, t_tmp);
+      if (err != cudaSuccess) return fail(e, CGL_CUDA_ERROR, "early points: %s", cudaGetErrorString(err));
     }
+    e->n_early_hubs = k;
+    e->n_early_pts = np;
   }
   if (!e->n_early_hubs) {
     dev_release(e, e->b_early_pts);
@@ -939,7 +975,7 @@ void forget_graph(cgl_engine* e) {
   e->entries = 0;
   e->max_deg_in = e->max_deg_out = 0;
   e->n_heavy_in = e->n_heavy_out = 0;
-  e->n_early_hubs = e->n_early_pts = 0;
+  e->n_early_hubs = e->n_early_pts = e->n_first_out = 0;
   e->early.clear();
   e->mb_ready = false;
   e->collision_ready = false;
@@ -973,8 +1009,8 @@ cgl_status build_graph(cgl_engine* e, double alpha, uint64_t N, uint64_t E) {
   const bool pos_changed = e->pos_dirty;
   const bool links_changed = e->links_dirty || pos_changed;
   cgl_status st;
-  if (links_changed) {   // the early hubs are chosen again from the new lists
-    e->n_early_hubs = e->n_early_pts = 0;
+  if (links_changed) {   // the leading hubs are chosen again from the new lists
+    e->n_early_hubs = e->n_early_pts = e->n_first_out = 0;
     e->early.clear();
   }
   if (pos_changed) e->N = N;
@@ -1721,9 +1757,13 @@ cgl_status cgl_get_layout(cgl_engine* e, cgl_layout* o) {
   if (p.clus) k += 1 + (uint32_t)p.clus_sum;           // sums, pull + update
   // the early points' many-body terms and the early hubs' chains
   if (p.mb && p.link_in && e->n_early_hubs > 0 && e->n_early_pts > 0) k += 2;
+  // the leading outgoing hubs apart from the rest of their pass (counted above with the overlap)
+  const bool overlap = p.link_in && p.link_out && p.coll && !p.clus && p.mb && e->n_heavy_out > 0;
+  if (p.link_out && e->n_first_out > 0 && !overlap) k += 1;
   o->kernels_per_tick = k;
   o->early_hubs = e->n_early_hubs;
   o->early_points = e->n_early_pts;
+  o->leading_out_hubs = e->n_first_out;
   return CGL_OK;
 }
 

@@ -26,6 +26,8 @@
 // captured CUDA graph serves every tick.  Outside the tick: the pointer's
 // repulsion and drag passes (force-mouse.frag, drag-point.frag) and the
 // renderer's position texture.
+#include <atomic>
+
 #include "device_util.cuh"
 #include "collision.cuh"
 #include "kernels.cuh"
@@ -1284,6 +1286,33 @@ void launch_manybody_early(const DeviceView& d, const SimScalars& s, cudaStream_
   if (d.n_early_pts) k_manybody_early<<<blocks_for(d.n_early_pts), kBlock, 0, st>>>(d, s);
 }
 
+// The leading hubs' CTAs ask for all the shared memory a CTA may have, so no
+// other CTA shares their SM: the chain thread then issues without the
+// many-body warps beside it (each CTA also holds 1 KB of the SM's 228 KB).
+// sizeof(HubStage) where the device does not allow that much.  Set once per
+// device (the attribute is per device; concurrent first calls set the same).
+static size_t hub_exclusive_smem() {
+  constexpr int kDevices = 64;
+  static std::atomic<size_t> bytes[kDevices];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kDevices) {
+    cudaGetLastError();
+    return sizeof(HubStage);
+  }
+  size_t b = bytes[dev].load(std::memory_order_relaxed);
+  if (!b) {
+    int optin = 0;
+    b = sizeof(HubStage);
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess &&
+        (size_t)optin > b &&
+        cudaFuncSetAttribute(k_link, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) == cudaSuccess)
+      b = (size_t)optin;
+    cudaGetLastError();   // a refused attribute leaves no error behind
+    bytes[dev].store(b, std::memory_order_relaxed);
+  }
+  return b;
+}
+
 void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool swap_back, cudaStream_t st,
                  int part) {
   if (!d.n) return;
@@ -1296,12 +1325,13 @@ void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool s
   const float2* src = swap_back ? d.pos_alt : d.pos;
   float2* dst = swap_back ? d.pos : d.pos_alt;
   const uint32_t nlight = blocks_for(d.n - nhub);
-  const uint32_t early = direction == 0 ? std::min(d.n_early_hubs, nhub) : 0u;
+  const uint32_t early = std::min(direction == 0 ? d.n_early_hubs : d.n_first_out, nhub);
   if (part == kLinkHubs) {
     if (nhub) k_link<<<nhub, kBlock, sizeof(HubStage), st>>>(d, s, rp, en, woff, lane_ent, src, dst, order, d.n, nhub, 0u);
-  } else if (part == kLinkEarlyHubs) {
-    if (early) k_link<<<early, kBlock, sizeof(HubStage), st>>>(d, s, rp, en, woff, lane_ent, src, dst, order, d.n, nhub, 0u);
-  } else if (part == kLinkAfterEarly) {
+  } else if (part == kLinkFirstHubs) {
+    if (early)
+      k_link<<<early, kBlock, hub_exclusive_smem(), st>>>(d, s, rp, en, woff, lane_ent, src, dst, order, d.n, nhub, 0u);
+  } else if (part == kLinkAfterFirst) {
     const uint32_t nb = nhub - early + nlight;
     if (nb)
       k_link<<<nb, kBlock, nhub > early ? sizeof(HubStage) : 0, st>>>(d, s, rp, en, woff, lane_ent, src, dst, order,

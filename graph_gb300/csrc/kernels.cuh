@@ -63,12 +63,14 @@ struct DeviceView {
   const uint32_t* heavy_in;   // all points by incoming list length, longest first;
   const uint32_t* heavy_out;  // the first n_heavy_* have lists longer than kHeavyDegree
   uint32_t n_heavy_in, n_heavy_out;
-  // Early hubs: the first n_early_hubs rows of heavy_in (the longest incoming
-  // lists) run their chains beside the many-body pass.  Their points and link
-  // targets (early_pts, kEarly in flags) take their many-body terms in a pass
-  // of their own first; inv then holds each live point's sorted position.
+  // Leading hubs run on an SM each on a second stream.  Incoming (early hubs):
+  // the first n_early_hubs rows of heavy_in run their chains beside the
+  // many-body pass.  Their points and link targets (early_pts, kEarly in
+  // flags) take their many-body terms in a pass of their own first; inv then
+  // holds each live point's sorted position.  Outgoing: the first n_first_out
+  // rows of heavy_out run beside the rest of the pass.
   const uint32_t* early_pts;
-  uint32_t n_early_pts, n_early_hubs;
+  uint32_t n_early_pts, n_early_hubs, n_first_out;
   uint32_t* inv;              // sorted position of each live point [n]; null without early hubs
   // The rows after the first n_heavy_* of the order, by warps of 32: warp w's
   // entries at lane_ent[woff[w] .. woff[w + 1]), entry k of lane l at
@@ -140,8 +142,9 @@ void launch_manybody_early(const DeviceView& d, const SimScalars& s, cudaStream_
 // The first n_heavy_* rows of the order each get a CTA of their own.
 // A link pass: all of it (kLinkAll), or its hub CTAs or its light rows alone
 // (the two halves write disjoint points and may run on two streams); or the
-// early hubs' CTAs (the first n_early_hubs) and then the rest of the pass.
-enum { kLinkAll = 0, kLinkHubs = 1, kLinkLight = 2, kLinkEarlyHubs = 3, kLinkAfterEarly = 4 };
+// leading hubs' CTAs (n_early_hubs incoming, n_first_out outgoing), an SM
+// each, and then the rest of the pass.
+enum { kLinkAll = 0, kLinkHubs = 1, kLinkLight = 2, kLinkFirstHubs = 3, kLinkAfterFirst = 4 };
 void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool swap_back, cudaStream_t st,
                  int part = kLinkAll);
 // mark[order[t]] = 1 for t < nhub (the points whose list runs on a hub CTA)

@@ -117,7 +117,7 @@ class Engine(EngineCalls):
         return self._call("synchronize")
 
     def set_early_hubs(self, max_hubs):
-        """Test hook: at most max_hubs early hubs (0: none, -1: the engine's rule)."""
+        """Test hook: at most max_hubs leading hubs each way (0: none, -1: the engine's rule)."""
         return self._call("debug_set_early_hubs", int(max_hubs))
 
     def profile_stages(self, ticks):

@@ -320,6 +320,7 @@ typedef struct cgl_layout {
   uint32_t manybody_tuned;     /* 1 once manybody_kernel was chosen by timing this graph's ticks */
   uint32_t early_hubs;         /* longest incoming lists whose chains start beside the many-body pass */
   uint32_t early_points;       /* their points and link targets, whose many-body terms run first */
+  uint32_t leading_out_hubs;   /* longest outgoing lists whose chains run on an SM each beside the rest */
 } cgl_layout;
 enum {
   CGL_MANYBODY_AUTO = -1,       /* cgl_config.manybody_kernel: time the candidates, keep the fastest */
@@ -334,9 +335,10 @@ cgl_status cgl_get_layout(cgl_engine* e, cgl_layout* out);
 cgl_status cgl_debug_get_cells(cgl_engine* e, uint32_t level, float* out, uint64_t capacity_floats);
 /* finest level: 8 point indices per cell in slot (hash) order, -1 = empty slot. */
 cgl_status cgl_debug_get_slots(cgl_engine* e, int32_t* out, uint64_t capacity);
-/* At most max_hubs early hubs (cgl_layout.early_hubs) from now on: 0 runs every
- * incoming chain after the many-body pass, -1 restores the engine's rule.  The
- * results do not change; the hook exists to compare and time the two orders. */
+/* At most max_hubs leading hubs each way (cgl_layout.early_hubs,
+ * leading_out_hubs) from now on: 0 runs every chain with the rest of its pass
+ * (the incoming ones after the many-body pass), -1 restores the engine's rule.
+ * The results do not change; the hook exists to compare and time the orders. */
 cgl_status cgl_debug_set_early_hubs(cgl_engine* e, int32_t max_hubs);
 
 /* --- Batched engine (no counterpart in the reference) -----------------------

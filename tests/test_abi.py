@@ -76,8 +76,8 @@ def test_layout_names_the_many_body_kernels():
     for name, value in (("CGL_MANYBODY_ONE_POINT", 0), ("CGL_MANYBODY_SPLIT", 1), ("CGL_MANYBODY_TWO_POINTS", 2)):
         assert re.search(r"%s = %d" % (name, value), src)
     assert (_abi.MANYBODY_ONE_POINT, _abi.MANYBODY_SPLIT, _abi.MANYBODY_TWO_POINTS) == (0, 1, 2)
-    assert [f for f, _ in _abi.Layout._fields_][-4:] == ["manybody_kernel", "manybody_tuned", "early_hubs",
-                                                         "early_points"]
+    assert [f for f, _ in _abi.Layout._fields_][-5:] == ["manybody_kernel", "manybody_tuned", "early_hubs",
+                                                         "early_points", "leading_out_hubs"]
 
 
 def test_create_rejects_an_unknown_manybody_kernel(engine_lib):

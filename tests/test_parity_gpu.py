@@ -177,12 +177,14 @@ def test_hub_lists_with_collision():
 
 
 def test_early_hubs():
-    # Incoming lists of 12,000 and 5,000 links (past the early threshold: at
+    # Incoming lists of 12,000 and 5,000 links (past the leading threshold: at
     # least 4,096 links and a quarter of the longest) start their chains beside
     # the many-body pass, after a many-body pass over their points and link
-    # targets; a list of 3,000 links stays with the rest of the pass.  Some
-    # targets are absent, some early points pinned (and unpinned later, which
-    # uploads the point flags again), and collision follows the link passes.
+    # targets; a list of 3,000 links stays with the rest of the pass.  The
+    # outgoing list of 6,000 links runs on its own SM beside the rest of its
+    # pass.  Some targets are absent, some early points pinned (and unpinned
+    # later, which uploads the point flags again), and collision follows the
+    # link passes.
     n = 150_000
     rng = np.random.default_rng(41)
     pos = rng.uniform(500, 3500, size=2 * n).astype(np.float32)
@@ -199,6 +201,7 @@ def test_early_hubs():
     eng, orc = make_pair(pos, links, fields, sizes=sizes, pinned=[1, 7, 30_001, 1, 99_999])
     lay = eng.layout()
     assert lay.early_hubs == 2 and 16_990 <= lay.early_points <= 17_010   # 17,002 less the absent targets
+    assert lay.leading_out_hubs == 1
     for t in range(4):
         eng.step(1)
         orc.step(1)
@@ -210,13 +213,19 @@ def test_early_hubs():
         orc.step(1)
         _assert_same(eng, orc, ("early hubs, new pins", t))
     _assert_cells_and_slots(eng, orc)
-    eng.set_early_hubs(0)                      # every chain after the many-body pass again
-    assert eng.layout().early_hubs == 0
+    cfg = _abi.make_config(**dict(fields, simulation_collision=0.0))   # the outgoing pass alone waits for its lead
+    eng.set_config(cfg)
+    orc.set_config(cfg)
+    eng.step(2)
+    orc.step(2)
+    _assert_same(eng, orc, "leading hubs without collision")
+    eng.set_early_hubs(0)                      # every chain with the rest of its pass again
+    assert eng.layout().early_hubs == 0 and eng.layout().leading_out_hubs == 0
     eng.step(2)
     orc.step(2)
     _assert_same(eng, orc, "early hubs off")
     eng.set_early_hubs(1)
-    assert eng.layout().early_hubs == 1
+    assert eng.layout().early_hubs == 1 and eng.layout().leading_out_hubs == 1
     eng.step(2)
     orc.step(2)
     _assert_same(eng, orc, "one early hub")
