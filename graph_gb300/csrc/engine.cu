@@ -119,7 +119,8 @@ struct cgl_engine {
   uint32_t n_early_hubs = 0, n_early_pts = 0;
   uint32_t n_first_out = 0;     // leading outgoing hubs (DeviceView::n_first_out)
   std::vector<uint8_t> early;   // kEarly per point (empty: none)
-  int32_t early_limit = -1;     // at most this many early hubs (cgl_debug_set_early_hubs); -1: the rule
+  int32_t lead_limit[2] = {-1, -1};   // at most this many leading hubs each way (cgl_debug_set_leading_hubs);
+                                      // -1: the rule
   DevBuf b_size, b_cgrid_acc, b_cgrid;
   DevBuf b_cl_of, b_cl_coeff, b_cl_custom, b_cl_acc;
   DevBuf b_texture;                        // staging for pageable texture read-back
@@ -846,7 +847,7 @@ cgl_status leading_hubs(cgl_engine* e, int dir, uint64_t max_total, std::vector<
   const uint32_t* order = (const uint32_t*)(dir == 0 ? e->b_heavy_in.p : e->b_heavy_out.p);
   const uint32_t* rowptr = (const uint32_t*)(dir == 0 ? e->b_rowptr_in.p : e->b_rowptr_out.p);
   uint32_t m = std::min(nheavy, kLeadCandidates);
-  if (e->early_limit >= 0) m = std::min(m, (uint32_t)e->early_limit);
+  if (e->lead_limit[dir] >= 0) m = std::min(m, (uint32_t)e->lead_limit[dir]);
   if (!m) return CGL_OK;
   DevBuf t_spans;
   cgl_status rc;
@@ -1778,10 +1779,11 @@ cgl_status cgl_debug_get_cells(cgl_engine* e, uint32_t level, float* out, uint64
   return CGL_OK;
 }
 
-cgl_status cgl_debug_set_early_hubs(cgl_engine* e, int32_t max_hubs) {
+cgl_status cgl_debug_set_leading_hubs(cgl_engine* e, int32_t max_in, int32_t max_out) {
   CHECK_E(e);
-  if (max_hubs < -1) return fail(e, CGL_INVALID_ARG, "max_hubs %d", max_hubs);
-  e->early_limit = max_hubs;
+  if (max_in < -1 || max_out < -1) return fail(e, CGL_INVALID_ARG, "max_in %d, max_out %d", max_in, max_out);
+  e->lead_limit[0] = max_in;
+  e->lead_limit[1] = max_out;
   if (e->N && !e->links_dirty && !e->pos_dirty) {
     const cgl_status st = build_early(e);
     if (st) return st;

@@ -54,8 +54,8 @@ def load_library(build_if_missing: bool = True):
     lib.cgl_random_draws.restype = C.c_int
     lib.cgl_check_wait_limit.argtypes = [C.c_int32, C.POINTER(C.c_uint32)]
     lib.cgl_check_wait_limit.restype = C.c_int
-    lib.cgl_debug_set_early_hubs.argtypes = [E, C.c_int32]
-    lib.cgl_debug_set_early_hubs.restype = C.c_int
+    lib.cgl_debug_set_leading_hubs.argtypes = [E, C.c_int32, C.c_int32]
+    lib.cgl_debug_set_leading_hubs.restype = C.c_int
     _abi.declare(lib, "cgl")
     _LIB = lib
     return lib
@@ -116,9 +116,10 @@ class Engine(EngineCalls):
     def synchronize(self):
         return self._call("synchronize")
 
-    def set_early_hubs(self, max_hubs):
-        """Test hook: at most max_hubs leading hubs each way (0: none, -1: the engine's rule)."""
-        return self._call("debug_set_early_hubs", int(max_hubs))
+    def set_leading_hubs(self, max_in, max_out=None):
+        """Test hook: at most max_in incoming and max_out (default max_in) outgoing leading hubs
+        (0: none, -1: the engine's rule)."""
+        return self._call("debug_set_leading_hubs", int(max_in), int(max_in if max_out is None else max_out))
 
     def profile_stages(self, ticks):
         out = (C.c_double * _abi.NUM_STAGE_TIMES)()

@@ -219,13 +219,13 @@ def test_early_hubs():
     eng.step(2)
     orc.step(2)
     _assert_same(eng, orc, "leading hubs without collision")
-    eng.set_early_hubs(0)                      # every chain with the rest of its pass again
+    eng.set_leading_hubs(0)                      # every chain with the rest of its pass again
     assert eng.layout().early_hubs == 0 and eng.layout().leading_out_hubs == 0
     eng.step(2)
     orc.step(2)
     _assert_same(eng, orc, "early hubs off")
-    eng.set_early_hubs(1)
-    assert eng.layout().early_hubs == 1 and eng.layout().leading_out_hubs == 1
+    eng.set_leading_hubs(1, 0)
+    assert eng.layout().early_hubs == 1 and eng.layout().leading_out_hubs == 0
     eng.step(2)
     orc.step(2)
     _assert_same(eng, orc, "one early hub")
