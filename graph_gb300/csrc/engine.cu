@@ -827,20 +827,22 @@ cgl_status upload_flags(cgl_engine* e) {
 }
 
 // Leading hubs: the first lists of a direction's order (longest first) of at
-// least kLeadMinLinks links and a quarter of the longest, at most
+// least kLeadMinLinks links and a fraction of the longest, at most
 // kLeadCandidates of them (or the test hook's limit).  Their chains each run
-// on an SM of their own on the second stream.  Incoming (early hubs): while
-// their links total at most an eighth of the points.  Their chains need the
-// many-body results of their own points and link targets only; those run
-// first, and the chains then start beside the rest of the many-body pass
-// instead of after it.  Outgoing: their chains run beside the other lists of
-// the pass.
+// on an SM of their own on the second stream.  Incoming (early hubs): half the
+// longest, while their links total at most an eighth of the points.  Their
+// chains need the many-body results of their own points and link targets
+// only; those run first, and the chains then start beside the rest of the
+// many-body pass instead of after it.  More of them take SMs from that pass
+// (R-MAT 2^23: 24 early hubs, 0.15-0.2 ms a tick slower than 1 to 4).
+// Outgoing: a quarter of the longest; their chains run beside the other lists
+// of the pass (1 to 24 of them time the same there).
 constexpr uint32_t kLeadCandidates = 32;
 constexpr uint32_t kLeadMinLinks = 4096;
 
 // spans (rowptr[p], rowptr[p + 1]) and points p of the leading hubs of a
 // direction; returns their count (0 when none qualifies).
-cgl_status leading_hubs(cgl_engine* e, int dir, uint64_t max_total, std::vector<uint2>& spans,
+cgl_status leading_hubs(cgl_engine* e, int dir, uint32_t fraction, uint64_t max_total, std::vector<uint2>& spans,
                         std::vector<uint32_t>& hubs, uint32_t* count) {
   *count = 0;
   const uint32_t nheavy = dir == 0 ? e->n_heavy_in : e->n_heavy_out;
@@ -863,7 +865,7 @@ cgl_status leading_hubs(cgl_engine* e, int dir, uint64_t max_total, std::vector<
   if (err == cudaSuccess) err = cudaStreamSynchronize(e->stream);
   dev_release(e, t_spans);
   if (err != cudaSuccess) return fail(e, CGL_CUDA_ERROR, "leading hubs: %s", cudaGetErrorString(err));
-  const uint32_t least = std::max(kLeadMinLinks, (spans[0].y - spans[0].x) / 4);
+  const uint32_t least = std::max(kLeadMinLinks, (spans[0].y - spans[0].x) / fraction);
   uint64_t total = 0;
   uint32_t k = 0;
   for (; k < m; ++k) {
@@ -883,10 +885,10 @@ cgl_status build_early(cgl_engine* e) {
   std::vector<uint2> spans;
   std::vector<uint32_t> hubs;
   uint32_t k = 0;
-  if (e->T && (rc = leading_hubs(e, 1, ~0ull, spans, hubs, &k))) return rc;
+  if (e->T && (rc = leading_hubs(e, 1, 4, ~0ull, spans, hubs, &k))) return rc;
   e->n_first_out = k;
   k = 0;
-  if (e->T && (rc = leading_hubs(e, 0, n / 8, spans, hubs, &k))) return rc;
+  if (e->T && (rc = leading_hubs(e, 0, 2, n / 8, spans, hubs, &k))) return rc;
   if (k) {
     uint64_t total = 0;
     for (uint32_t t = 0; t < k; ++t) total += spans[t].y - spans[t].x;

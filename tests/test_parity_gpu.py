@@ -177,22 +177,22 @@ def test_hub_lists_with_collision():
 
 
 def test_early_hubs():
-    # Incoming lists of 12,000 and 5,000 links (past the leading threshold: at
-    # least 4,096 links and a quarter of the longest) start their chains beside
-    # the many-body pass, after a many-body pass over their points and link
+    # Incoming lists of 12,000 and 7,000 links (past the leading threshold: at
+    # least 4,096 links and half the longest) start their chains beside the
+    # many-body pass, after a many-body pass over their points and link
     # targets; a list of 3,000 links stays with the rest of the pass.  The
     # outgoing list of 6,000 links runs on its own SM beside the rest of its
     # pass.  Some targets are absent, some early points pinned (and unpinned
     # later, which uploads the point flags again), and collision follows the
     # link passes.
-    n = 150_000
+    n = 160_000
     rng = np.random.default_rng(41)
     pos = rng.uniform(500, 3500, size=2 * n).astype(np.float32)
     pos[2 * 50:2 * 60] = np.nan                                                 # absent targets of hub 0
     # the incoming list of point p holds the links (p, q)
     hub0 = np.stack([np.zeros(12_000), np.arange(1, 12_001)], axis=1)
     back0 = np.stack([np.arange(20_000, 26_000), np.zeros(6000)], axis=1)
-    hub1 = np.stack([np.ones(5000), np.arange(30_000, 35_000)], axis=1)
+    hub1 = np.stack([np.ones(7000), np.arange(30_000, 37_000)], axis=1)
     hub2 = np.stack([np.full(3000, 2), np.arange(40_000, 43_000)], axis=1)
     links = np.concatenate([hub0, back0, hub1, hub2, rng.integers(0, n, size=(200_000, 2))])
     links = links.astype(np.float32).reshape(-1)
@@ -200,7 +200,7 @@ def test_early_hubs():
     fields = dict(random_seed=41, simulation_collision=0.4, simulation_link_distance=3.0, simulation_gravity=0.25)
     eng, orc = make_pair(pos, links, fields, sizes=sizes, pinned=[1, 7, 30_001, 1, 99_999])
     lay = eng.layout()
-    assert lay.early_hubs == 2 and 16_990 <= lay.early_points <= 17_010   # 17,002 less the absent targets
+    assert lay.early_hubs == 2 and 18_985 <= lay.early_points <= 19_010   # 19,002 less the absent targets
     assert lay.leading_out_hubs == 1
     for t in range(4):
         eng.step(1)
