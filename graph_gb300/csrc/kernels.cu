@@ -189,11 +189,7 @@ __global__ void __launch_bounds__(kBlock) k_center(DeviceView d, SimScalars s) {
 }
 
 // ------------------------------------------------------------------- scan --
-// 4,096 cells a block: a 512^2 grid takes 64 blocks, so the last block's
-// look-back reads at most two rounds of 32 status words (11.4 us with 1,024
-// cells a block and up to eight rounds).
-constexpr int kScanItems = 16;
-constexpr int kScanQuads = kScanItems / 4;
+constexpr int kScanItems = 4;
 constexpr int kScanChunk = kBlock * kScanItems;   // cells per scan block
 
 // A cell's scan word: its count, and with PAIRS the number of work items of
@@ -217,21 +213,15 @@ __global__ void __launch_bounds__(kBlock) k_scan(DeviceView d, uint32_t cells) {
   const uint32_t vb = (uint32_t)(s_seq % nb);
   const unsigned long long parity = ((s_seq / nb) & 1ull) << 63;
   // cells is a multiple of 64 (a power-of-two grid of at least 8 x 8) and
-  // base of 16: a thread's cells are all inside or all outside
+  // base of 4: a thread's four cells are all inside or all outside
   const uint32_t base = vb * kScanChunk + threadIdx.x * kScanItems;
   const bool inside = base < cells;
-  uint32_t cnt[kScanItems];
-#pragma unroll
-  for (int q = 0; q < kScanQuads; ++q) {
-    uint4 v = make_uint4(0u, 0u, 0u, 0u);
-    if (inside) v = reinterpret_cast<const uint4*>(d.counts)[(base >> 2) + q];
-    cnt[4 * q] = v.x; cnt[4 * q + 1] = v.y; cnt[4 * q + 2] = v.z; cnt[4 * q + 3] = v.w;
-  }
-  unsigned long long sum = 0;
-#pragma unroll
-  for (int k = 0; k < kScanItems; ++k) sum += scan_word<PAIRS>(cnt[k]);
+  uint4 v = make_uint4(0u, 0u, 0u, 0u);
+  if (inside) v = reinterpret_cast<const uint4*>(d.counts)[base >> 2];
+  const unsigned long long w0 = scan_word<PAIRS>(v.x), w1 = scan_word<PAIRS>(v.y), w2 = scan_word<PAIRS>(v.z),
+                           w3 = scan_word<PAIRS>(v.w);
   unsigned long long total;
-  unsigned long long off = block_exclusive_scan64(sum, &total);
+  unsigned long long off = block_exclusive_scan64(w0 + w1 + w2 + w3, &total);
   if (threadIdx.x < 32) {
     unsigned long long prefix = 0;
     if (vb == 0) {
@@ -246,26 +236,18 @@ __global__ void __launch_bounds__(kBlock) k_scan(DeviceView d, uint32_t cells) {
   __syncthreads();
   off += s_prefix;
   if (inside) {
-#pragma unroll
-    for (int q = 0; q < kScanQuads; ++q) {
-      unsigned long long o[4];
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        o[k] = off;
-        off += scan_word<PAIRS>(cnt[4 * q + k]);
-      }
-      reinterpret_cast<uint4*>(d.cell_start)[(base >> 2) + q] =
-          make_uint4((uint32_t)o[0], (uint32_t)o[1], (uint32_t)o[2], (uint32_t)o[3]);
-      if (PAIRS)
-        reinterpret_cast<uint4*>(d.pair_start)[(base >> 2) + q] = make_uint4(
-            (uint32_t)(o[0] >> 32), (uint32_t)(o[1] >> 32), (uint32_t)(o[2] >> 32), (uint32_t)(o[3] >> 32));
-      reinterpret_cast<uint4*>(d.counts)[(base >> 2) + q] = make_uint4(0u, 0u, 0u, 0u);   // ready for the next tick
-    }
+    const unsigned long long o1 = off + w0, o2 = o1 + w1, o3 = o2 + w2;
+    reinterpret_cast<uint4*>(d.cell_start)[base >> 2] = make_uint4((uint32_t)off, (uint32_t)o1, (uint32_t)o2, (uint32_t)o3);
+    if (PAIRS)
+      reinterpret_cast<uint4*>(d.pair_start)[base >> 2] =
+          make_uint4((uint32_t)(off >> 32), (uint32_t)(o1 >> 32), (uint32_t)(o2 >> 32), (uint32_t)(o3 >> 32));
+    reinterpret_cast<uint4*>(d.counts)[base >> 2] = make_uint4(0u, 0u, 0u, 0u);   // ready for the next tick
   }
   // the dense cells' list entries: a slot in the block's share of each list
   // (shared-memory atomics), then one global atomic per list and block
-  int cls[kScanItems];
-  uint32_t slot[kScanItems];
+  const uint32_t cnt[4] = {v.x, v.y, v.z, v.w};
+  int cls[4];
+  uint32_t slot[4];
 #pragma unroll
   for (int k = 0; k < kScanItems; ++k) {
     cls[k] = cnt[k] > kBigCell ? 0 : cnt[k] > kWarpSmallCell ? 1 : cnt[k] > kSmallCell ? 2 : 3;
