@@ -117,8 +117,8 @@ class Engine(EngineCalls):
         return self._call("synchronize")
 
     def set_leading_hubs(self, max_in, max_out=None):
-        """Test hook: at most max_in incoming and max_out (default max_in) outgoing leading hubs
-        (0: none, -1: the engine's rule)."""
+        """Test hook: the first max_in incoming and max_out (default max_in) outgoing hub lists
+        lead whatever their lengths (0: none, -1: the engine's rule)."""
         return self._call("debug_set_leading_hubs", int(max_in), int(max_in if max_out is None else max_out))
 
     def profile_stages(self, ticks):

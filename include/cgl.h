@@ -335,11 +335,13 @@ cgl_status cgl_get_layout(cgl_engine* e, cgl_layout* out);
 cgl_status cgl_debug_get_cells(cgl_engine* e, uint32_t level, float* out, uint64_t capacity_floats);
 /* finest level: 8 point indices per cell in slot (hash) order, -1 = empty slot. */
 cgl_status cgl_debug_get_slots(cgl_engine* e, int32_t* out, uint64_t capacity);
-/* At most max_in incoming and max_out outgoing leading hubs
- * (cgl_layout.early_hubs, leading_out_hubs) from now on: 0 runs every chain
- * of that direction with the rest of its pass (the incoming ones after the
- * many-body pass), -1 restores the engine's rule.  The results do not change;
- * the hook exists to compare and time the orders. */
+/* The first max_in incoming and max_out outgoing lists longer than 256 links
+ * lead (cgl_layout.early_hubs, leading_out_hubs) from now on, whatever their
+ * lengths (the early hubs' links still total at most an eighth of the
+ * points): 0 runs every chain of that direction with the rest of its pass
+ * (the incoming ones after the many-body pass), -1 restores the engine's
+ * rule.  The results do not change; the hook exists to compare and time the
+ * orders. */
 cgl_status cgl_debug_set_leading_hubs(cgl_engine* e, int32_t max_in, int32_t max_out);
 
 /* --- Batched engine (no counterpart in the reference) -----------------------
