@@ -76,9 +76,10 @@ __device__ __forceinline__ void coll_accumulate(long long* __restrict__ acc, int
 
 // One grid cell's sums rounded once to f32 (sx, sy, ssize, count), and the
 // integer sums zeroed for the next tick.
+template <bool ZERO = true>
 __device__ __forceinline__ void coll_convert_cell(long long* a, float4* out, const FixedScale& fx) {
   *out = make_float4(from_fixed(a[0], fx), from_fixed(a[1], fx), from_fixed(a[2], fx), (float)a[3]);
-  a[0] = 0; a[1] = 0; a[2] = 0; a[3] = 0;
+  if (ZERO) { a[0] = 0; a[1] = 0; a[2] = 0; a[3] = 0; }
 }
 
 struct CollParams {

@@ -122,6 +122,7 @@ struct cgl_engine {
   int32_t lead_limit[2] = {-1, -1};   // at most this many leading hubs each way (cgl_debug_set_leading_hubs);
                                       // -1: the rule
   DevBuf b_size, b_cgrid_acc, b_cgrid;
+  DevBuf b_coll_mark, b_pos_coll;   // DeviceView::coll_mark, pos_coll
   DevBuf b_cl_of, b_cl_coeff, b_cl_custom, b_cl_acc;
   DevBuf b_texture;                        // staging for pageable texture read-back
   DeviceView view{};
@@ -210,7 +211,8 @@ void dev_free_all(cgl_engine* e) {
                    &e->b_big_sx, &e->b_big_sy, &e->b_big_ns, &e->b_heavy_in, &e->b_heavy_out, &e->b_hub_out,
                    &e->b_cl_of, &e->b_cl_coeff, &e->b_cl_custom, &e->b_cl_acc, &e->b_texture,
                    &e->b_woff_in, &e->b_woff_out, &e->b_lane_ent_in, &e->b_lane_ent_out, &e->b_pair_start,
-                   &e->b_pair_list, &e->b_idx_s, &e->b_pos_s, &e->b_bin_state, &e->b_early_pts, &e->b_inv};
+                   &e->b_pair_list, &e->b_idx_s, &e->b_pos_s, &e->b_bin_state, &e->b_early_pts, &e->b_inv,
+                   &e->b_coll_mark, &e->b_pos_coll};
   for (DevBuf* b : all) {
     if (b->p) cudaFree(b->p);
     b->p = nullptr;
@@ -287,6 +289,8 @@ void refresh_view(cgl_engine* e) {
   d.size = (const float*)e->b_size.p;
   d.cgrid_acc = (long long*)e->b_cgrid_acc.p;
   d.cgrid = (float4*)e->b_cgrid.p;
+  d.coll_mark = (uint32_t*)e->b_coll_mark.p;
+  d.pos_coll = (float2*)e->b_pos_coll.p;
   d.cluster_of = (const uint32_t*)e->b_cl_of.p;
   d.cluster_coeff = (const float*)e->b_cl_coeff.p;
   d.cluster_custom = (const float2*)e->b_cl_custom.p;
@@ -432,11 +436,28 @@ cgl_status enqueue_tick(cgl_engine* e, cudaStream_t st, cudaEvent_t* ev) {
       }
       launch_link(d, s, 1, p.link_in, st, first_out ? kLinkAfterFirst : overlap ? kLinkLight : kLinkAll);
       if (overlap) {
-        launch_collision_sums(d, s, d.sorted_idx, (uint32_t)e->live, (const uint8_t*)e->b_hub_out.p, st);
-        CU(cudaStreamWaitEvent(st, e->join, 0));
-        launch_collision_sums(d, s, d.heavy_out, d.n_heavy_out, nullptr, st);
-        launch_collision_convert(d, s, st);
-        launch_collision_force(d, s, d.sorted_idx, (uint32_t)e->live, st);
+        // the points on the second stream ("late": the leading hubs, else every
+        // hub) are marked in b_hub_out and summed once their chains end
+        const uint8_t* late = (const uint8_t*)e->b_hub_out.p;
+        const uint32_t n_late = first_out ? d.n_first_out : d.n_heavy_out;
+        launch_collision_sums(d, s, d.sorted_idx, (uint32_t)e->live, late, st);
+        if (first_out && d.pos_coll && d.coll_mark) {
+          // every other point's result beside the chains; then the late points'
+          // and those of the points whose windows hold a late point's cell
+          launch_collision_convert(d, s, st, false);
+          launch_collision_force_early(d, s, d.sorted_idx, (uint32_t)e->live, late, st);
+          CU(cudaStreamWaitEvent(st, e->join, 0));
+          launch_collision_sums(d, s, d.heavy_out, n_late, nullptr, st);
+          launch_collision_late(d, s, d.heavy_out, n_late, st);
+          launch_collision_fixup(d, s, late, st);
+          CU(cudaMemsetAsync(d.cgrid_acc, 0, e->b_cgrid_acc.bytes, st));
+          CU(cudaMemsetAsync(d.coll_mark, 0, e->b_coll_mark.bytes, st));
+        } else {
+          CU(cudaStreamWaitEvent(st, e->join, 0));
+          launch_collision_sums(d, s, d.heavy_out, n_late, nullptr, st);
+          launch_collision_convert(d, s, st);
+          launch_collision_force(d, s, d.sorted_idx, (uint32_t)e->live, st);
+        }
       } else if (split) {
         CU(cudaStreamWaitEvent(st, e->join, 0));
       }
@@ -485,6 +506,7 @@ cgl_status collision_create(cgl_engine* e) {
   if ((st = dev_reserve(e, e->b_size, e->N * sizeof(float), false))) return st;
   if ((st = dev_reserve(e, e->b_cgrid_acc, cells * 4 * sizeof(long long), true))) return st;
   if ((st = dev_reserve(e, e->b_cgrid, cells * sizeof(float4), false))) return st;
+  if ((st = dev_reserve(e, e->b_coll_mark, (cells + 31) / 32 * sizeof(uint32_t), true))) return st;
   if (e->N) CU(cudaMemcpyAsync(e->b_size.p, sizes.data(), e->N * sizeof(float), cudaMemcpyHostToDevice, e->stream));
   CU(cudaStreamSynchronize(e->stream));
   e->collision_ready = true;
@@ -948,6 +970,18 @@ cgl_status build_early(cgl_engine* e) {
     dev_release(e, e->b_early_pts);
     dev_release(e, e->b_inv);
   }
+  // the points whose outgoing chains run on the second stream (the leading
+  // hubs, else every hub): their collision sums wait for those chains
+  if ((rc = dev_reserve(e, e->b_hub_out, std::max<size_t>(n, 1), false))) return rc;
+  CU(cudaMemsetAsync(e->b_hub_out.p, 0, std::max<size_t>(n, 1), e->stream));
+  launch_mark_hubs((const uint32_t*)e->b_heavy_out.p, e->n_first_out ? e->n_first_out : e->n_heavy_out,
+                   (uint8_t*)e->b_hub_out.p, e->stream);
+  CU(cudaGetLastError());
+  if (e->n_first_out) {
+    if ((rc = dev_reserve(e, e->b_pos_coll, std::max<size_t>(n, 1) * sizeof(float2), false))) return rc;
+  } else {
+    dev_release(e, e->b_pos_coll);
+  }
   return upload_flags(e);
 }
 
@@ -1153,12 +1187,6 @@ cgl_status build_graph(cgl_engine* e, double alpha, uint64_t N, uint64_t E) {
     CU(cudaStreamSynchronize(e->stream));
     }
     if ((st = build_link_warps(e))) return st;
-    // the points whose outgoing list runs on a hub CTA (the collision sums of
-    // the other points need not wait for those chains)
-    if ((st = dev_reserve(e, e->b_hub_out, std::max<size_t>(n, 1), true))) return st;
-    launch_mark_hubs((const uint32_t*)e->b_heavy_out.p, e->n_heavy_out, (uint8_t*)e->b_hub_out.p, e->stream);
-    CU(cudaGetLastError());
-    CU(cudaStreamSynchronize(e->stream));
     if ((st = build_early(e))) return st;
   }
   if (e->clusters_dirty || pos_changed) {
@@ -1762,9 +1790,11 @@ cgl_status cgl_get_layout(cgl_engine* e, cgl_layout* o) {
   if (p.clus) k += 1 + (uint32_t)p.clus_sum;           // sums, pull + update
   // the early points' many-body terms and the early hubs' chains
   if (p.mb && p.link_in && e->n_early_hubs > 0 && e->n_early_pts > 0) k += 2;
-  // the leading outgoing hubs apart from the rest of their pass (counted above with the overlap)
+  // the leading outgoing hubs apart from the rest of their pass (counted above with the overlap);
+  // with the overlap, the collision results beside their chains: the late cells and the fix-up
   const bool overlap = p.link_in && p.link_out && p.coll && !p.clus && p.mb && e->n_heavy_out > 0;
   if (p.link_out && e->n_first_out > 0 && !overlap) k += 1;
+  if (overlap && e->n_first_out > 0 && e->b_pos_coll.p && e->b_coll_mark.p) k += 2;
   o->kernels_per_tick = k;
   o->early_hubs = e->n_early_hubs;
   o->early_points = e->n_early_pts;

@@ -1044,11 +1044,12 @@ __global__ void __launch_bounds__(kBlock) k_coll_grid(DeviceView d, SimScalars s
   coll_accumulate(d.cgrid_acc, s.coll_grid, s.coll_cell, s.fx, p, sz, live);
 }
 
+template <bool ZERO>
 __global__ void __launch_bounds__(kBlock) k_coll_convert(DeviceView d, SimScalars s) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t total = 4u * (uint32_t)(s.coll_grid * s.coll_grid);
   if (k >= total) return;
-  coll_convert_cell(d.cgrid_acc + 4 * (size_t)k, d.cgrid + k, s.fx);
+  coll_convert_cell<ZERO>(d.cgrid_acc + 4 * (size_t)k, d.cgrid + k, s.fx);
 }
 
 __global__ void __launch_bounds__(kBlock) k_coll_force(DeviceView d, SimScalars s, const uint32_t* __restrict__ order,
@@ -1064,6 +1065,85 @@ __global__ void __launch_bounds__(kBlock) k_coll_force(DeviceView d, SimScalars 
   const CollParams cp{s.coll_grid, s.coll_cell, s.coll_radius, s.coll_padding, __fmul_rn(tp.alpha, s.coll_strength)};
   const float2 v = coll_velocity(d.cgrid, cp, p, d.size[i], i, d.n);
   if (!(f & kPinned)) d.pos[i] = integrate(p, v.x, v.y, s.friction, s.space);
+}
+
+// k_coll_force into pos_coll, every point but the late ones (absent and
+// pinned points copied), from grids that lack the late points.
+__global__ void __launch_bounds__(kBlock) k_coll_force_early(DeviceView d, SimScalars s,
+                                                             const uint32_t* __restrict__ order, uint32_t count,
+                                                             const uint8_t* __restrict__ late) {
+  const TickParams tp = tick_params(d);
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const uint32_t i = order ? order[t] : t;
+  if (late[i]) return;
+  const uint8_t f = d.flags[i];
+  const float2 p = d.pos[i];
+  float2 out = p;
+  if (!(f & (kAbsent | kPinned))) {
+    const CollParams cp{s.coll_grid, s.coll_cell, s.coll_radius, s.coll_padding,
+                        __fmul_rn(tp.alpha, s.coll_strength)};
+    const float2 v = coll_velocity(d.cgrid, cp, p, d.size[i], i, d.n);
+    out = integrate(p, v.x, v.y, s.friction, s.space);
+  }
+  d.pos_coll[i] = out;
+}
+
+// One thread per (late point, grid, cell of its 3x3 window): the window's
+// cells marked; the centre thread converts the late point's cell again from
+// the sums that now hold every point (the same value for late points sharing
+// a cell).
+__global__ void __launch_bounds__(kBlock) k_coll_late(DeviceView d, SimScalars s,
+                                                      const uint32_t* __restrict__ late_list, uint32_t n_late) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_late * 36u) return;
+  const uint32_t i = late_list[t / 36u];
+  if (d.flags[i] & kAbsent) return;
+  const int g = (int)((t / 9u) % 4u), w = (int)(t % 9u);
+  const int G = s.coll_grid;
+  const float gm1 = (float)G - 1.0f;
+  const float2 p = d.pos[i];
+  const int cx = (int)coll_bin(p.x, coll_offset_x(g), s.coll_cell, gm1);
+  const int cy = (int)coll_bin(p.y, coll_offset_y(g), s.coll_cell, gm1);
+  const uint32_t G2 = (uint32_t)(G * G);
+  if (w == 4) {
+    const uint32_t k = (uint32_t)g * G2 + (uint32_t)(cy * G + cx);
+    coll_convert_cell<false>(d.cgrid_acc + 4 * (size_t)k, d.cgrid + k, s.fx);
+  }
+  const int mx = cx + w % 3 - 1, my = cy + w / 3 - 1;
+  if (mx < 0 || mx >= G || my < 0 || my >= G) return;
+  const uint32_t bit = (uint32_t)g * G2 + (uint32_t)(my * G + mx);
+  atomicOr(&d.coll_mark[bit >> 5], 1u << (bit & 31u));
+}
+
+// Every live point's final collision result into pos: pos_coll's, or computed
+// again when the point is late or one of its four cells is marked.
+__global__ void __launch_bounds__(kBlock) k_coll_fixup(DeviceView d, SimScalars s, const uint8_t* __restrict__ late) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n) return;
+  const uint8_t f = d.flags[i];
+  if (f & kAbsent) return;   // absent points keep their (NaN) position
+  const float2 p = d.pos[i];
+  const int G = s.coll_grid;
+  const float gm1 = (float)G - 1.0f;
+  const uint32_t G2 = (uint32_t)(G * G);
+  bool again = late[i] != 0;
+#pragma unroll
+  for (int g = 0; g < 4; ++g) {
+    const int cx = (int)coll_bin(p.x, coll_offset_x(g), s.coll_cell, gm1);
+    const int cy = (int)coll_bin(p.y, coll_offset_y(g), s.coll_cell, gm1);
+    const uint32_t bit = (uint32_t)g * G2 + (uint32_t)(cy * G + cx);
+    again |= (__ldg(&d.coll_mark[bit >> 5]) >> (bit & 31u)) & 1u;
+  }
+  if (!again) {
+    d.pos[i] = d.pos_coll[i];
+    return;
+  }
+  if (f & kPinned) return;
+  const TickParams tp = tick_params(d);
+  const CollParams cp{s.coll_grid, s.coll_cell, s.coll_radius, s.coll_padding, __fmul_rn(tp.alpha, s.coll_strength)};
+  const float2 v = coll_velocity(d.cgrid, cp, p, d.size[i], i, d.n);
+  d.pos[i] = integrate(p, v.x, v.y, s.friction, s.space);
 }
 
 // --------------------------------------------------------------- clusters --
@@ -1416,9 +1496,27 @@ void launch_collision_sums(const DeviceView& d, const SimScalars& s, const uint3
   if (nb) k_coll_grid<<<nb, kBlock, 0, st>>>(d, s, order, count, skip);
 }
 
-void launch_collision_convert(const DeviceView& d, const SimScalars& s, cudaStream_t st) {
+void launch_collision_convert(const DeviceView& d, const SimScalars& s, cudaStream_t st, bool zero) {
   const uint32_t cells = 4u * (uint32_t)(s.coll_grid * s.coll_grid);
-  k_coll_convert<<<blocks_for(cells), kBlock, 0, st>>>(d, s);
+  if (zero) k_coll_convert<true><<<blocks_for(cells), kBlock, 0, st>>>(d, s);
+  else k_coll_convert<false><<<blocks_for(cells), kBlock, 0, st>>>(d, s);
+}
+
+void launch_collision_force_early(const DeviceView& d, const SimScalars& s, const uint32_t* order, uint32_t count,
+                                  const uint8_t* late, cudaStream_t st) {
+  if (!order) count = d.n;
+  const uint32_t nb = blocks_for(count);
+  if (nb) k_coll_force_early<<<nb, kBlock, 0, st>>>(d, s, order, count, late);
+}
+
+void launch_collision_late(const DeviceView& d, const SimScalars& s, const uint32_t* late_list, uint32_t n_late,
+                           cudaStream_t st) {
+  if (n_late) k_coll_late<<<blocks_for(n_late * 36u), kBlock, 0, st>>>(d, s, late_list, n_late);
+}
+
+void launch_collision_fixup(const DeviceView& d, const SimScalars& s, const uint8_t* late, cudaStream_t st) {
+  const uint32_t nb = blocks_for(d.n);
+  if (nb) k_coll_fixup<<<nb, kBlock, 0, st>>>(d, s, late);
 }
 
 void launch_collision_grid(const DeviceView& d, const SimScalars& s, const uint32_t* order, uint32_t count,

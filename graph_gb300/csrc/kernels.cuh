@@ -83,6 +83,10 @@ struct DeviceView {
   const float* size;          // resolved point sizes [n]
   long long* cgrid_acc;       // 4 grids x G_c^2 x (x, y, size, count)
   float4* cgrid;              // 4 grids x G_c^2 (sx, sy, ssize, count)
+  uint32_t* coll_mark;        // a bit per cell of the 4 grids: the 3x3 windows around the late points'
+                              // cells (launch_collision_late); zero between ticks
+  float2* pos_coll;           // collision results computed beside late points [n] (with leading
+                              // outgoing hubs; the chains still read pos_alt)
   // clusters
   const uint32_t* cluster_of;     // cluster of each point, 0xFFFFFFFF if none [n]
   const float* cluster_coeff;     // pull coefficient of each point [n]
@@ -171,9 +175,22 @@ void launch_collision_grid(const DeviceView& d, const SimScalars& s, const uint3
 // grids once every point is summed.
 void launch_collision_sums(const DeviceView& d, const SimScalars& s, const uint32_t* order, uint32_t count,
                            const uint8_t* skip, cudaStream_t st);
-void launch_collision_convert(const DeviceView& d, const SimScalars& s, cudaStream_t st);
+// zero: clear the integer sums after converting (else they stay for later points)
+void launch_collision_convert(const DeviceView& d, const SimScalars& s, cudaStream_t st, bool zero = true);
 void launch_collision_force(const DeviceView& d, const SimScalars& s, const uint32_t* order, uint32_t count,
                             cudaStream_t st);
+// Collision beside late points (chains still running): launch_collision_force
+// of every point not marked `late`, from grids without the late points, into
+// pos_coll.  After the late points' sums: launch_collision_late converts the
+// late points' cells again and marks the 3x3 windows around them in coll_mark;
+// launch_collision_fixup then moves every result into pos, computing again the
+// points that read a marked cell (and the late points).  A point's force reads
+// only its 3x3 windows, so every other result is already the final one.
+void launch_collision_force_early(const DeviceView& d, const SimScalars& s, const uint32_t* order, uint32_t count,
+                                  const uint8_t* late, cudaStream_t st);
+void launch_collision_late(const DeviceView& d, const SimScalars& s, const uint32_t* late_list, uint32_t n_late,
+                           cudaStream_t st);
+void launch_collision_fixup(const DeviceView& d, const SimScalars& s, const uint8_t* late, cudaStream_t st);
 // Sums of each cluster's live points (cluster_acc must be zero on entry).
 void launch_cluster_sum(const DeviceView& d, const SimScalars& s, cudaStream_t st);
 // The cluster pull and the update of every point.

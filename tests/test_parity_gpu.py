@@ -181,27 +181,30 @@ def test_early_hubs():
     # least 4,096 links and half the longest) start their chains beside the
     # many-body pass, after a many-body pass over their points and link
     # targets; a list of 3,000 links stays with the rest of the pass.  The
-    # outgoing list of 6,000 links runs on its own SM beside the rest of its
-    # pass.  Some targets are absent, some early points pinned (and unpinned
-    # later, which uploads the point flags again), and collision follows the
-    # link passes.
+    # outgoing lists of 6,000 and 5,000 links run on SMs of their own beside
+    # the rest of their pass, and the collision results of every other point
+    # are computed beside them (their two points sit 1.5 units apart, so their
+    # collision windows overlap).  Some targets are absent, some early points
+    # pinned (and unpinned later, which uploads the point flags again).
     n = 160_000
     rng = np.random.default_rng(41)
     pos = rng.uniform(500, 3500, size=2 * n).astype(np.float32)
     pos[2 * 50:2 * 60] = np.nan                                                 # absent targets of hub 0
+    pos[6:8] = pos[0:2] + 1.5                                                   # outgoing hub 3 beside hub 0
     # the incoming list of point p holds the links (p, q)
     hub0 = np.stack([np.zeros(12_000), np.arange(1, 12_001)], axis=1)
     back0 = np.stack([np.arange(20_000, 26_000), np.zeros(6000)], axis=1)
     hub1 = np.stack([np.ones(7000), np.arange(30_000, 37_000)], axis=1)
     hub2 = np.stack([np.full(3000, 2), np.arange(40_000, 43_000)], axis=1)
-    links = np.concatenate([hub0, back0, hub1, hub2, rng.integers(0, n, size=(200_000, 2))])
+    back3 = np.stack([np.arange(50_000, 55_000), np.full(5000, 3)], axis=1)
+    links = np.concatenate([hub0, back0, hub1, hub2, back3, rng.integers(0, n, size=(200_000, 2))])
     links = links.astype(np.float32).reshape(-1)
     sizes = rng.uniform(2, 8, size=n).astype(np.float32)
     fields = dict(random_seed=41, simulation_collision=0.4, simulation_link_distance=3.0, simulation_gravity=0.25)
     eng, orc = make_pair(pos, links, fields, sizes=sizes, pinned=[1, 7, 30_001, 1, 99_999])
     lay = eng.layout()
     assert lay.early_hubs == 2 and 18_985 <= lay.early_points <= 19_010   # 19,002 less the absent targets
-    assert lay.leading_out_hubs == 1
+    assert lay.leading_out_hubs == 2
     for t in range(4):
         eng.step(1)
         orc.step(1)
@@ -224,11 +227,19 @@ def test_early_hubs():
     eng.step(2)
     orc.step(2)
     _assert_same(eng, orc, "early hubs off")
-    eng.set_leading_hubs(1, 0)
+    cfg = _abi.make_config(**fields)           # collision again
+    eng.set_config(cfg)
+    orc.set_config(cfg)
+    eng.set_leading_hubs(1, 0)                 # every outgoing chain on the second stream beside the sums
     assert eng.layout().early_hubs == 1 and eng.layout().leading_out_hubs == 0
     eng.step(2)
     orc.step(2)
     _assert_same(eng, orc, "one early hub")
+    eng.set_leading_hubs(0, 1)                 # one late point for the collision results
+    assert eng.layout().early_hubs == 0 and eng.layout().leading_out_hubs == 1
+    eng.step(2)
+    orc.step(2)
+    _assert_same(eng, orc, "one leading outgoing hub")
 
 
 def test_springs_outside_the_in_range_sequences():
