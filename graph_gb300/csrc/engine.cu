@@ -122,7 +122,7 @@ struct cgl_engine {
   int32_t lead_limit[2] = {-1, -1};   // at most this many leading hubs each way (cgl_debug_set_leading_hubs);
                                       // -1: the rule
   DevBuf b_size, b_cgrid_acc, b_cgrid;
-  DevBuf b_coll_mark, b_pos_coll;   // DeviceView::coll_mark, pos_coll
+  DevBuf b_coll_mark, b_pos_coll, b_coll_redo;   // DeviceView::coll_mark, pos_coll, coll_redo
   DevBuf b_cl_of, b_cl_coeff, b_cl_custom, b_cl_acc;
   DevBuf b_texture;                        // staging for pageable texture read-back
   DeviceView view{};
@@ -212,7 +212,7 @@ void dev_free_all(cgl_engine* e) {
                    &e->b_cl_of, &e->b_cl_coeff, &e->b_cl_custom, &e->b_cl_acc, &e->b_texture,
                    &e->b_woff_in, &e->b_woff_out, &e->b_lane_ent_in, &e->b_lane_ent_out, &e->b_pair_start,
                    &e->b_pair_list, &e->b_idx_s, &e->b_pos_s, &e->b_bin_state, &e->b_early_pts, &e->b_inv,
-                   &e->b_coll_mark, &e->b_pos_coll};
+                   &e->b_coll_mark, &e->b_pos_coll, &e->b_coll_redo};
   for (DevBuf* b : all) {
     if (b->p) cudaFree(b->p);
     b->p = nullptr;
@@ -291,6 +291,7 @@ void refresh_view(cgl_engine* e) {
   d.cgrid = (float4*)e->b_cgrid.p;
   d.coll_mark = (uint32_t*)e->b_coll_mark.p;
   d.pos_coll = (float2*)e->b_pos_coll.p;
+  d.coll_redo = (uint32_t*)e->b_coll_redo.p;
   d.cluster_of = (const uint32_t*)e->b_cl_of.p;
   d.cluster_coeff = (const float*)e->b_cl_coeff.p;
   d.cluster_custom = (const float2*)e->b_cl_custom.p;
@@ -441,7 +442,7 @@ cgl_status enqueue_tick(cgl_engine* e, cudaStream_t st, cudaEvent_t* ev) {
         const uint8_t* late = (const uint8_t*)e->b_hub_out.p;
         const uint32_t n_late = first_out ? d.n_first_out : d.n_heavy_out;
         launch_collision_sums(d, s, d.sorted_idx, (uint32_t)e->live, late, st);
-        if (first_out && d.pos_coll && d.coll_mark) {
+        if (first_out && d.pos_coll && d.coll_mark && d.coll_redo) {
           // every other point's result beside the chains; then the late points'
           // and those of the points whose windows hold a late point's cell
           launch_collision_convert(d, s, st, false);
@@ -452,6 +453,7 @@ cgl_status enqueue_tick(cgl_engine* e, cudaStream_t st, cudaEvent_t* ev) {
           launch_collision_fixup(d, s, late, st);
           CU(cudaMemsetAsync(d.cgrid_acc, 0, e->b_cgrid_acc.bytes, st));
           CU(cudaMemsetAsync(d.coll_mark, 0, e->b_coll_mark.bytes, st));
+          CU(cudaMemsetAsync(d.coll_redo, 0, sizeof(uint32_t), st));
         } else {
           CU(cudaStreamWaitEvent(st, e->join, 0));
           launch_collision_sums(d, s, d.heavy_out, n_late, nullptr, st);
@@ -978,9 +980,12 @@ cgl_status build_early(cgl_engine* e) {
                    (uint8_t*)e->b_hub_out.p, e->stream);
   CU(cudaGetLastError());
   if (e->n_first_out) {
-    if ((rc = dev_reserve(e, e->b_pos_coll, std::max<size_t>(n, 1) * sizeof(float2), false))) return rc;
+    if ((rc = dev_reserve(e, e->b_pos_coll, std::max<size_t>(n, 1) * sizeof(float2), false)) ||
+        (rc = dev_reserve(e, e->b_coll_redo, ((size_t)n + 1) * sizeof(uint32_t), true)))
+      return rc;
   } else {
     dev_release(e, e->b_pos_coll);
+    dev_release(e, e->b_coll_redo);
   }
   return upload_flags(e);
 }
@@ -1791,10 +1796,10 @@ cgl_status cgl_get_layout(cgl_engine* e, cgl_layout* o) {
   // the early points' many-body terms and the early hubs' chains
   if (p.mb && p.link_in && e->n_early_hubs > 0 && e->n_early_pts > 0) k += 2;
   // the leading outgoing hubs apart from the rest of their pass (counted above with the overlap);
-  // with the overlap, the collision results beside their chains: the late cells and the fix-up
+  // with the overlap, the collision results beside their chains: the late cells, the fix-up, the redo
   const bool overlap = p.link_in && p.link_out && p.coll && !p.clus && p.mb && e->n_heavy_out > 0;
   if (p.link_out && e->n_first_out > 0 && !overlap) k += 1;
-  if (overlap && e->n_first_out > 0 && e->b_pos_coll.p && e->b_coll_mark.p) k += 2;
+  if (overlap && e->n_first_out > 0 && e->b_pos_coll.p && e->b_coll_mark.p && e->b_coll_redo.p) k += 3;
   o->kernels_per_tick = k;
   o->early_hubs = e->n_early_hubs;
   o->early_points = e->n_early_pts;

@@ -1116,34 +1116,51 @@ __global__ void __launch_bounds__(kBlock) k_coll_late(DeviceView d, SimScalars s
   atomicOr(&d.coll_mark[bit >> 5], 1u << (bit & 31u));
 }
 
-// Every live point's final collision result into pos: pos_coll's, or computed
-// again when the point is late or one of its four cells is marked.
+// Every live point's final collision result into pos: pos_coll's, or, when
+// the point is late or one of its four cells is marked, listed in coll_redo
+// (a warp's entries with one atomic): those points are scattered over the
+// indices (a hub's link targets gather in its cells), so k_coll_redo computes
+// them with every lane busy.
 __global__ void __launch_bounds__(kBlock) k_coll_fixup(DeviceView d, SimScalars s, const uint8_t* __restrict__ late) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.n) return;
-  const uint8_t f = d.flags[i];
-  if (f & kAbsent) return;   // absent points keep their (NaN) position
-  const float2 p = d.pos[i];
-  const int G = s.coll_grid;
-  const float gm1 = (float)G - 1.0f;
-  const uint32_t G2 = (uint32_t)(G * G);
-  bool again = late[i] != 0;
+  bool again = false;
+  if (i < d.n && !(d.flags[i] & kAbsent)) {   // absent points keep their (NaN) position
+    const float2 p = d.pos[i];
+    const int G = s.coll_grid;
+    const float gm1 = (float)G - 1.0f;
+    const uint32_t G2 = (uint32_t)(G * G);
+    again = late[i] != 0;
 #pragma unroll
-  for (int g = 0; g < 4; ++g) {
-    const int cx = (int)coll_bin(p.x, coll_offset_x(g), s.coll_cell, gm1);
-    const int cy = (int)coll_bin(p.y, coll_offset_y(g), s.coll_cell, gm1);
-    const uint32_t bit = (uint32_t)g * G2 + (uint32_t)(cy * G + cx);
-    again |= (__ldg(&d.coll_mark[bit >> 5]) >> (bit & 31u)) & 1u;
+    for (int g = 0; g < 4; ++g) {
+      const int cx = (int)coll_bin(p.x, coll_offset_x(g), s.coll_cell, gm1);
+      const int cy = (int)coll_bin(p.y, coll_offset_y(g), s.coll_cell, gm1);
+      const uint32_t bit = (uint32_t)g * G2 + (uint32_t)(cy * G + cx);
+      again |= (__ldg(&d.coll_mark[bit >> 5]) >> (bit & 31u)) & 1u;
+    }
+    if (!again) d.pos[i] = d.pos_coll[i];
   }
-  if (!again) {
-    d.pos[i] = d.pos_coll[i];
-    return;
-  }
-  if (f & kPinned) return;
+  const unsigned m = __ballot_sync(0xffffffffu, again);
+  if (!m) return;
+  const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(&d.coll_redo[0], (uint32_t)__popc(m));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (again) d.coll_redo[1 + base + (uint32_t)__popc(m & ((1u << lane) - 1u))] = i;
+}
+
+// The listed points' collision results from the complete grids (grid-stride
+// over the device-side count).
+__global__ void __launch_bounds__(kBlock) k_coll_redo(DeviceView d, SimScalars s) {
+  const uint32_t count = d.coll_redo[0];
   const TickParams tp = tick_params(d);
   const CollParams cp{s.coll_grid, s.coll_cell, s.coll_radius, s.coll_padding, __fmul_rn(tp.alpha, s.coll_strength)};
-  const float2 v = coll_velocity(d.cgrid, cp, p, d.size[i], i, d.n);
-  d.pos[i] = integrate(p, v.x, v.y, s.friction, s.space);
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
+    const uint32_t i = d.coll_redo[1 + t];
+    if (d.flags[i] & kPinned) continue;
+    const float2 p = d.pos[i];
+    const float2 v = coll_velocity(d.cgrid, cp, p, d.size[i], i, d.n);
+    d.pos[i] = integrate(p, v.x, v.y, s.friction, s.space);
+  }
 }
 
 // --------------------------------------------------------------- clusters --
@@ -1516,7 +1533,9 @@ void launch_collision_late(const DeviceView& d, const SimScalars& s, const uint3
 
 void launch_collision_fixup(const DeviceView& d, const SimScalars& s, const uint8_t* late, cudaStream_t st) {
   const uint32_t nb = blocks_for(d.n);
-  if (nb) k_coll_fixup<<<nb, kBlock, 0, st>>>(d, s, late);
+  if (!nb) return;
+  k_coll_fixup<<<nb, kBlock, 0, st>>>(d, s, late);
+  k_coll_redo<<<std::min(nb, 8u * sm_count()), kBlock, 0, st>>>(d, s);
 }
 
 void launch_collision_grid(const DeviceView& d, const SimScalars& s, const uint32_t* order, uint32_t count,

@@ -87,6 +87,8 @@ struct DeviceView {
                               // cells (launch_collision_late); zero between ticks
   float2* pos_coll;           // collision results computed beside late points [n] (with leading
                               // outgoing hubs; the chains still read pos_alt)
+  uint32_t* coll_redo;        // [0]: count, then the points whose collision result is computed again
+                              // [1 + n] (launch_collision_fixup); the count is zero between ticks
   // clusters
   const uint32_t* cluster_of;     // cluster of each point, 0xFFFFFFFF if none [n]
   const float* cluster_coeff;     // pull coefficient of each point [n]
@@ -183,9 +185,10 @@ void launch_collision_force(const DeviceView& d, const SimScalars& s, const uint
 // of every point not marked `late`, from grids without the late points, into
 // pos_coll.  After the late points' sums: launch_collision_late converts the
 // late points' cells again and marks the 3x3 windows around them in coll_mark;
-// launch_collision_fixup then moves every result into pos, computing again the
-// points that read a marked cell (and the late points).  A point's force reads
-// only its 3x3 windows, so every other result is already the final one.
+// launch_collision_fixup then moves every result into pos and lists the points
+// that read a marked cell (and the late points) in coll_redo, whose results it
+// computes again.  A point's force reads only its 3x3 windows, so every other
+// result is already the final one.
 void launch_collision_force_early(const DeviceView& d, const SimScalars& s, const uint32_t* order, uint32_t count,
                                   const uint8_t* late, cudaStream_t st);
 void launch_collision_late(const DeviceView& d, const SimScalars& s, const uint32_t* late_list, uint32_t n_late,
