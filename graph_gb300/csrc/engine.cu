@@ -41,6 +41,8 @@ struct cgl_engine {
   cudaStream_t stream = nullptr;
   uint32_t* h_error = nullptr;   // host-mapped error word (DeviceView::error_word)
   uint32_t* d_error = nullptr;
+  cudaStream_t side2 = nullptr;  // the next outgoing hubs' chains (DeviceView::n_next_out)
+  cudaEvent_t join2 = nullptr;
   cudaStream_t side = nullptr;   // the early hubs' chains beside the many-body pass; the outgoing hub
                                  // chains beside the collision sums
   cudaEvent_t fork = nullptr, join = nullptr;
@@ -117,7 +119,7 @@ struct cgl_engine {
   // early hubs (DeviceView::n_early_hubs): their points and link targets
   DevBuf b_early_pts, b_inv;
   uint32_t n_early_hubs = 0, n_early_pts = 0;
-  uint32_t n_first_out = 0;     // leading outgoing hubs (DeviceView::n_first_out)
+  uint32_t n_first_out = 0, n_next_out = 0;   // leading outgoing hubs (DeviceView::n_first_out, n_next_out)
   std::vector<uint8_t> early;   // kEarly per point (empty: none)
   int32_t lead_limit[2] = {-1, -1};   // at most this many leading hubs each way (cgl_debug_set_leading_hubs);
                                       // -1: the rule
@@ -281,6 +283,7 @@ void refresh_view(cgl_engine* e) {
   d.n_early_pts = e->n_early_pts;
   d.n_early_hubs = e->n_early_hubs;
   d.n_first_out = e->n_first_out;
+  d.n_next_out = e->n_next_out;
   d.inv = e->n_early_hubs ? (uint32_t*)e->b_inv.p : nullptr;
   d.woff_in = (const uint32_t*)e->b_woff_in.p;
   d.lane_ent_in = (const uint4*)e->b_lane_ent_in.p;
@@ -428,19 +431,25 @@ cgl_status enqueue_tick(cgl_engine* e, cudaStream_t st, cudaEvent_t* ev) {
       // rest of the pass; with the overlap all hub CTAs go there when no list
       // leads, beside the light rows.
       const bool first_out = !ev && d.n_first_out > 0;
+      const bool next_out = first_out && d.n_next_out > 0;
       const bool split = first_out || overlap;
       if (split) {
         CU(cudaEventRecord(e->fork, st));
         CU(cudaStreamWaitEvent(e->side, e->fork, 0));
         launch_link(d, s, 1, p.link_in, e->side, first_out ? kLinkFirstHubs : kLinkHubs);
         CU(cudaEventRecord(e->join, e->side));
+        if (next_out) {   // the next hubs on a third stream: their chains leave this one to the sums
+          CU(cudaStreamWaitEvent(e->side2, e->fork, 0));
+          launch_link(d, s, 1, p.link_in, e->side2, kLinkNextHubs);
+          CU(cudaEventRecord(e->join2, e->side2));
+        }
       }
       launch_link(d, s, 1, p.link_in, st, first_out ? kLinkAfterFirst : overlap ? kLinkLight : kLinkAll);
       if (overlap) {
         // the points on the second stream ("late": the leading hubs, else every
         // hub) are marked in b_hub_out and summed once their chains end
         const uint8_t* late = (const uint8_t*)e->b_hub_out.p;
-        const uint32_t n_late = first_out ? d.n_first_out : d.n_heavy_out;
+        const uint32_t n_late = first_out ? d.n_first_out + d.n_next_out : d.n_heavy_out;
         launch_collision_sums(d, s, d.sorted_idx, (uint32_t)e->live, late, st);
         if (first_out && d.pos_coll && d.coll_mark && d.coll_redo) {
           // every other point's result beside the chains; then the late points'
@@ -448,6 +457,7 @@ cgl_status enqueue_tick(cgl_engine* e, cudaStream_t st, cudaEvent_t* ev) {
           launch_collision_convert(d, s, st, false);
           launch_collision_force_early(d, s, d.sorted_idx, (uint32_t)e->live, late, st);
           CU(cudaStreamWaitEvent(st, e->join, 0));
+          if (next_out) CU(cudaStreamWaitEvent(st, e->join2, 0));
           launch_collision_sums(d, s, d.heavy_out, n_late, nullptr, st);
           launch_collision_late(d, s, d.heavy_out, n_late, st);
           launch_collision_fixup(d, s, late, st);
@@ -456,12 +466,14 @@ cgl_status enqueue_tick(cgl_engine* e, cudaStream_t st, cudaEvent_t* ev) {
           CU(cudaMemsetAsync(d.coll_redo, 0, sizeof(uint32_t), st));
         } else {
           CU(cudaStreamWaitEvent(st, e->join, 0));
+          if (next_out) CU(cudaStreamWaitEvent(st, e->join2, 0));
           launch_collision_sums(d, s, d.heavy_out, n_late, nullptr, st);
           launch_collision_convert(d, s, st);
           launch_collision_force(d, s, d.sorted_idx, (uint32_t)e->live, st);
         }
       } else if (split) {
         CU(cudaStreamWaitEvent(st, e->join, 0));
+        if (next_out) CU(cudaStreamWaitEvent(st, e->join2, 0));
       }
     }
     mark(7, 1);
@@ -859,8 +871,9 @@ cgl_status upload_flags(cgl_engine* e) {
 // only; those run first, and the chains then start beside the rest of the
 // many-body pass instead of after it.  More of them take SMs from that pass
 // (R-MAT 2^23: 24 early hubs, 0.15-0.2 ms a tick slower than 1 to 4).
-// Outgoing: a quarter of the longest; their chains run beside the other lists
-// of the pass (1 to 24 of them time the same there).
+// Outgoing: half the longest on SMs of their own, then down to a quarter of
+// the longest on a third stream (their SMs shared): the rest of the pass and
+// the collision results of every other point run beside them.
 constexpr uint32_t kLeadCandidates = 32;
 constexpr uint32_t kLeadMinLinks = 4096;
 
@@ -904,15 +917,17 @@ cgl_status leading_hubs(cgl_engine* e, int dir, uint32_t fraction, uint64_t max_
 }
 
 cgl_status build_early(cgl_engine* e) {
-  e->n_early_hubs = e->n_early_pts = e->n_first_out = 0;
+  e->n_early_hubs = e->n_early_pts = e->n_first_out = e->n_next_out = 0;
   e->early.clear();
   const uint32_t n = (uint32_t)e->N;
   cgl_status rc = CGL_OK;
   std::vector<uint2> spans;
   std::vector<uint32_t> hubs;
-  uint32_t k = 0;
-  if (e->T && (rc = leading_hubs(e, 1, 4, ~0ull, spans, hubs, &k))) return rc;
+  uint32_t k = 0, k4 = 0;
+  if (e->T && (rc = leading_hubs(e, 1, 2, ~0ull, spans, hubs, &k))) return rc;
+  if (e->T && (rc = leading_hubs(e, 1, 4, ~0ull, spans, hubs, &k4))) return rc;
   e->n_first_out = k;
+  e->n_next_out = k ? k4 - k : 0;
   k = 0;
   if (e->T && (rc = leading_hubs(e, 0, 2, n / 8, spans, hubs, &k))) return rc;
   if (k) {
@@ -976,8 +991,9 @@ cgl_status build_early(cgl_engine* e) {
   // hubs, else every hub): their collision sums wait for those chains
   if ((rc = dev_reserve(e, e->b_hub_out, std::max<size_t>(n, 1), false))) return rc;
   CU(cudaMemsetAsync(e->b_hub_out.p, 0, std::max<size_t>(n, 1), e->stream));
-  launch_mark_hubs((const uint32_t*)e->b_heavy_out.p, e->n_first_out ? e->n_first_out : e->n_heavy_out,
-                   (uint8_t*)e->b_hub_out.p, e->stream);
+  launch_mark_hubs((const uint32_t*)e->b_heavy_out.p,
+                   e->n_first_out ? e->n_first_out + e->n_next_out : e->n_heavy_out, (uint8_t*)e->b_hub_out.p,
+                   e->stream);
   CU(cudaGetLastError());
   if (e->n_first_out) {
     if ((rc = dev_reserve(e, e->b_pos_coll, std::max<size_t>(n, 1) * sizeof(float2), false)) ||
@@ -1019,7 +1035,7 @@ void forget_graph(cgl_engine* e) {
   e->entries = 0;
   e->max_deg_in = e->max_deg_out = 0;
   e->n_heavy_in = e->n_heavy_out = 0;
-  e->n_early_hubs = e->n_early_pts = e->n_first_out = 0;
+  e->n_early_hubs = e->n_early_pts = e->n_first_out = e->n_next_out = 0;
   e->early.clear();
   e->mb_ready = false;
   e->collision_ready = false;
@@ -1054,7 +1070,7 @@ cgl_status build_graph(cgl_engine* e, double alpha, uint64_t N, uint64_t E) {
   const bool links_changed = e->links_dirty || pos_changed;
   cgl_status st;
   if (links_changed) {   // the leading hubs are chosen again from the new lists
-    e->n_early_hubs = e->n_early_pts = e->n_first_out = 0;
+    e->n_early_hubs = e->n_early_pts = e->n_first_out = e->n_next_out = 0;
     e->early.clear();
   }
   if (pos_changed) e->N = N;
@@ -1286,11 +1302,13 @@ cgl_status cgl_create(const cgl_config* cfg, cgl_engine** out) {
     int lo = 0, hi = 0;
     ce = cudaDeviceGetStreamPriorityRange(&lo, &hi);
     if (ce == cudaSuccess) ce = cudaStreamCreateWithPriority(&e->side, cudaStreamNonBlocking, hi);
+    if (ce == cudaSuccess) ce = cudaStreamCreateWithPriority(&e->side2, cudaStreamNonBlocking, lo);
   }
   if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming);
   if (ce == cudaSuccess) ce = cudaEventCreate(&e->tune_ev[0]);
   if (ce == cudaSuccess) ce = cudaEventCreate(&e->tune_ev[1]);
   if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->join, cudaEventDisableTiming);
+  if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->join2, cudaEventDisableTiming);
   if (ce == cudaSuccess) ce = cudaHostAlloc((void**)&e->h_error, sizeof(uint32_t), cudaHostAllocMapped);
   if (ce == cudaSuccess) ce = cudaHostGetDevicePointer((void**)&e->d_error, e->h_error, 0);
   if (ce != cudaSuccess) {
@@ -1299,8 +1317,10 @@ cgl_status cgl_create(const cgl_config* cfg, cgl_engine** out) {
     create_err = cudaGetErrorString(ce);
     if (e->own_stream) cudaStreamDestroy(e->own_stream);
     if (e->side) cudaStreamDestroy(e->side);
+    if (e->side2) cudaStreamDestroy(e->side2);
     if (e->fork) cudaEventDestroy(e->fork);
     if (e->join) cudaEventDestroy(e->join);
+    if (e->join2) cudaEventDestroy(e->join2);
     for (cudaEvent_t x : e->tune_ev) if (x) cudaEventDestroy(x);
     if (e->h_params) cudaFreeHost(e->h_params);
     if (e->h_error) cudaFreeHost(e->h_error);
@@ -1330,8 +1350,10 @@ cgl_status cgl_destroy(cgl_engine* e) {
   if (e->h_params) cudaFreeHost(e->h_params);
   if (e->h_error) cudaFreeHost(e->h_error);
   if (e->side) cudaStreamDestroy(e->side);
+  if (e->side2) cudaStreamDestroy(e->side2);
   if (e->fork) cudaEventDestroy(e->fork);
   if (e->join) cudaEventDestroy(e->join);
+  if (e->join2) cudaEventDestroy(e->join2);
   for (cudaEvent_t x : e->tune_ev) if (x) cudaEventDestroy(x);
   if (e->own_stream) cudaStreamDestroy(e->own_stream);
   delete e;
@@ -1799,11 +1821,12 @@ cgl_status cgl_get_layout(cgl_engine* e, cgl_layout* o) {
   // with the overlap, the collision results beside their chains: the late cells, the fix-up, the redo
   const bool overlap = p.link_in && p.link_out && p.coll && !p.clus && p.mb && e->n_heavy_out > 0;
   if (p.link_out && e->n_first_out > 0 && !overlap) k += 1;
+  if (p.link_out && e->n_first_out > 0 && e->n_next_out > 0) k += 1;   // the next hubs' launch
   if (overlap && e->n_first_out > 0 && e->b_pos_coll.p && e->b_coll_mark.p && e->b_coll_redo.p) k += 3;
   o->kernels_per_tick = k;
   o->early_hubs = e->n_early_hubs;
   o->early_points = e->n_early_pts;
-  o->leading_out_hubs = e->n_first_out;
+  o->leading_out_hubs = e->n_first_out + e->n_next_out;
   return CGL_OK;
 }
 

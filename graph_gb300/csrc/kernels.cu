@@ -1423,16 +1423,21 @@ void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool s
   float2* dst = swap_back ? d.pos : d.pos_alt;
   const uint32_t nlight = blocks_for(d.n - nhub);
   const uint32_t early = std::min(direction == 0 ? d.n_early_hubs : d.n_first_out, nhub);
+  const uint32_t next = direction == 0 ? 0u : std::min(d.n_next_out, nhub - early);
+  const uint32_t lead = early + next;
   if (part == kLinkHubs) {
     if (nhub) k_link<<<nhub, kBlock, sizeof(HubStage), st>>>(d, s, rp, en, woff, lane_ent, src, dst, order, d.n, nhub, 0u);
   } else if (part == kLinkFirstHubs) {
     if (early)
       k_link<<<early, kBlock, hub_exclusive_smem(), st>>>(d, s, rp, en, woff, lane_ent, src, dst, order, d.n, nhub, 0u);
+  } else if (part == kLinkNextHubs) {
+    if (next)
+      k_link<<<next, kBlock, sizeof(HubStage), st>>>(d, s, rp, en, woff, lane_ent, src, dst, order, d.n, nhub, early);
   } else if (part == kLinkAfterFirst) {
-    const uint32_t nb = nhub - early + nlight;
+    const uint32_t nb = nhub - lead + nlight;
     if (nb)
-      k_link<<<nb, kBlock, nhub > early ? sizeof(HubStage) : 0, st>>>(d, s, rp, en, woff, lane_ent, src, dst, order,
-                                                                       d.n, nhub, early);
+      k_link<<<nb, kBlock, nhub > lead ? sizeof(HubStage) : 0, st>>>(d, s, rp, en, woff, lane_ent, src, dst, order,
+                                                                      d.n, nhub, lead);
   } else if (part == kLinkLight) {
     if (nlight) k_link<<<nlight, kBlock, 0, st>>>(d, s, rp, en, woff, lane_ent, src, dst, order, d.n, nhub, nhub);
   } else {

@@ -68,9 +68,10 @@ struct DeviceView {
   // many-body pass.  Their points and link targets (early_pts, kEarly in
   // flags) take their many-body terms in a pass of their own first; inv then
   // holds each live point's sorted position.  Outgoing: the first n_first_out
-  // rows of heavy_out run beside the rest of the pass.
+  // rows of heavy_out run beside the rest of the pass, and the next
+  // n_next_out on a third stream without SMs of their own.
   const uint32_t* early_pts;
-  uint32_t n_early_pts, n_early_hubs, n_first_out;
+  uint32_t n_early_pts, n_early_hubs, n_first_out, n_next_out;
   uint32_t* inv;              // sorted position of each live point [n]; null without early hubs
   // The rows after the first n_heavy_* of the order, by warps of 32: warp w's
   // entries at lane_ent[woff[w] .. woff[w + 1]), entry k of lane l at
@@ -149,8 +150,9 @@ void launch_manybody_early(const DeviceView& d, const SimScalars& s, cudaStream_
 // A link pass: all of it (kLinkAll), or its hub CTAs or its light rows alone
 // (the two halves write disjoint points and may run on two streams); or the
 // leading hubs' CTAs (n_early_hubs incoming, n_first_out outgoing), an SM
-// each, and then the rest of the pass.
-enum { kLinkAll = 0, kLinkHubs = 1, kLinkLight = 2, kLinkFirstHubs = 3, kLinkAfterFirst = 4 };
+// each, the next outgoing hubs' CTAs (n_next_out), and then the rest of the
+// pass.
+enum { kLinkAll = 0, kLinkHubs = 1, kLinkLight = 2, kLinkFirstHubs = 3, kLinkNextHubs = 4, kLinkAfterFirst = 5 };
 void launch_link(const DeviceView& d, const SimScalars& s, int direction, bool swap_back, cudaStream_t st,
                  int part = kLinkAll);
 // mark[order[t]] = 1 for t < nhub (the points whose list runs on a hub CTA)

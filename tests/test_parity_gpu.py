@@ -181,9 +181,10 @@ def test_early_hubs():
     # least 4,096 links and half the longest) start their chains beside the
     # many-body pass, after a many-body pass over their points and link
     # targets; a list of 3,000 links stays with the rest of the pass.  The
-    # outgoing lists of 6,000 and 5,000 links run on SMs of their own beside
-    # the rest of their pass, and the collision results of every other point
-    # are computed beside them (their two points sit 1.5 units apart, so their
+    # outgoing list of 10,000 links runs on an SM of its own and the one of
+    # 4,500 links (under half the longest) on a third stream, both beside the
+    # rest of their pass, and the collision results of every other point are
+    # computed beside them (their two points sit 1.5 units apart, so their
     # collision windows overlap).  Some targets are absent, some early points
     # pinned (and unpinned later, which uploads the point flags again).
     n = 160_000
@@ -193,10 +194,10 @@ def test_early_hubs():
     pos[6:8] = pos[0:2] + 1.5                                                   # outgoing hub 3 beside hub 0
     # the incoming list of point p holds the links (p, q)
     hub0 = np.stack([np.zeros(12_000), np.arange(1, 12_001)], axis=1)
-    back0 = np.stack([np.arange(20_000, 26_000), np.zeros(6000)], axis=1)
+    back0 = np.stack([np.arange(20_000, 30_000), np.zeros(10_000)], axis=1)
     hub1 = np.stack([np.ones(7000), np.arange(30_000, 37_000)], axis=1)
     hub2 = np.stack([np.full(3000, 2), np.arange(40_000, 43_000)], axis=1)
-    back3 = np.stack([np.arange(50_000, 55_000), np.full(5000, 3)], axis=1)
+    back3 = np.stack([np.arange(50_000, 54_500), np.full(4500, 3)], axis=1)
     links = np.concatenate([hub0, back0, hub1, hub2, back3, rng.integers(0, n, size=(200_000, 2))])
     links = links.astype(np.float32).reshape(-1)
     sizes = rng.uniform(2, 8, size=n).astype(np.float32)
