@@ -10,9 +10,12 @@ seeded.  One step = one simulation tick (Graph.step()) over the whole graph.
          resident in HBM, CUDA events on the engine's stream, max over ranks.
   e2e    the same metric through the C ABI with host buffers: each step is
          cgl_step(1) (uploads the tick's alpha and seed, 8 bytes) followed by
-         cgl_get_point_positions into pinned host memory (8 bytes per point),
-         timed by the host clock (the reference's benchmark story flushes
-         steps with the same readback, repulsion-benchmark.ts:80-86).
+         cgl_enqueue_point_positions into pinned host memory (8 bytes per
+         point, copied beside the next tick; each call returns once the
+         previous tick's copy has landed), timed by the host clock up to the
+         last copy (the reference's benchmark story flushes steps with a
+         readback, repulsion-benchmark.ts:80-86); e2e.synchronous reads back
+         with cgl_get_point_positions after each step instead.
   --impl reference  times the oracle (the CPU restatement of the reference's
          per-tick algorithm; the reference itself is TypeScript/WebGL and
          cannot run here) on all host cores, same workload and metric.
@@ -475,20 +478,28 @@ def main():
     tb = tick_bytes(live, int(lay.links_number), c, int(lay.collision_grid) ** 2 if coll_on else None)
     tick_gbs = tb / (ms / args.steps / 1e3) / 1e9
 
-    # end to end through the C ABI with host buffers
-    pinned = torch.empty(2 * lay.points_number, dtype=torch.float32, pin_memory=True)
-    host = pinned.numpy()
+    # end to end through the C ABI with host buffers: every tick's positions read
+    # back into pinned host memory, beside the next tick (two buffers
+    # alternate; each call returns once the previous tick's copy has landed),
+    # and, for comparison, with the synchronous read-back after each tick
+    bufs = [torch.empty(2 * lay.points_number, dtype=torch.float32, pin_memory=True).numpy() for _ in range(2)]
     e2e_steps = max(10, min(args.steps, 200))
     eng.step(1)
-    eng.get_point_positions_into(host)
+    eng.get_point_positions_into(bufs[0])
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+    for k in range(e2e_steps):
         eng.step(1)
-        eng.get_point_positions_into(host)
+        eng.enqueue_point_positions_into(bufs[k & 1])
+    eng.synchronize()
     e2e_s = replicas.max_over_ranks(time.perf_counter() - t0, device="cuda")
     e2e_value = live_all * e2e_steps / e2e_s
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        eng.step(1)
+        eng.get_point_positions_into(bufs[0])
+    e2e_sync_s = replicas.max_over_ranks(time.perf_counter() - t0, device="cuda")
 
     cpu = None
     approx = None
@@ -524,7 +535,11 @@ def main():
             "cpu_baseline": cpu,
             "approximation_error": approx,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8,
-                    "d2h_bytes_per_step": 8 * int(lay.points_number), "steps": e2e_steps},
+                    "d2h_bytes_per_step": 8 * int(lay.points_number), "steps": e2e_steps,
+                    "read_back": "cgl_enqueue_point_positions after each cgl_step: a device copy, then to "
+                                 "pinned host memory beside the next tick",
+                    "synchronous": {"value": live_all * e2e_steps / e2e_sync_s,
+                                    "read_back": "cgl_get_point_positions after each cgl_step"}},
             "gpu_launches": int(lay.kernels_per_tick) * args.steps,
             "clocks": clk,
         }

@@ -41,6 +41,11 @@ struct cgl_engine {
   cudaStream_t stream = nullptr;
   uint32_t* h_error = nullptr;   // host-mapped error word (DeviceView::error_word)
   uint32_t* d_error = nullptr;
+  // read-back beside the next ticks (cgl_enqueue_point_positions)
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t snap_ready = nullptr, snap_done = nullptr;
+  bool snap_pending = false;
+  DevBuf b_snap;                 // the positions as queued, copied out from here
   cudaStream_t side2 = nullptr;  // the next outgoing hubs' chains (DeviceView::n_next_out)
   cudaEvent_t join2 = nullptr;
   cudaStream_t side = nullptr;   // the early hubs' chains beside the many-body pass; the outgoing hub
@@ -214,7 +219,7 @@ void dev_free_all(cgl_engine* e) {
                    &e->b_cl_of, &e->b_cl_coeff, &e->b_cl_custom, &e->b_cl_acc, &e->b_texture,
                    &e->b_woff_in, &e->b_woff_out, &e->b_lane_ent_in, &e->b_lane_ent_out, &e->b_pair_start,
                    &e->b_pair_list, &e->b_idx_s, &e->b_pos_s, &e->b_bin_state, &e->b_early_pts, &e->b_inv,
-                   &e->b_coll_mark, &e->b_pos_coll, &e->b_coll_redo};
+                   &e->b_coll_mark, &e->b_pos_coll, &e->b_coll_redo, &e->b_snap};
   for (DevBuf* b : all) {
     if (b->p) cudaFree(b->p);
     b->p = nullptr;
@@ -1309,6 +1314,9 @@ cgl_status cgl_create(const cgl_config* cfg, cgl_engine** out) {
   if (ce == cudaSuccess) ce = cudaEventCreate(&e->tune_ev[1]);
   if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->join, cudaEventDisableTiming);
   if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->join2, cudaEventDisableTiming);
+  if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->copy_stream, cudaStreamNonBlocking);
+  if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->snap_ready, cudaEventDisableTiming);
+  if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->snap_done, cudaEventDisableTiming);
   if (ce == cudaSuccess) ce = cudaHostAlloc((void**)&e->h_error, sizeof(uint32_t), cudaHostAllocMapped);
   if (ce == cudaSuccess) ce = cudaHostGetDevicePointer((void**)&e->d_error, e->h_error, 0);
   if (ce != cudaSuccess) {
@@ -1321,6 +1329,9 @@ cgl_status cgl_create(const cgl_config* cfg, cgl_engine** out) {
     if (e->fork) cudaEventDestroy(e->fork);
     if (e->join) cudaEventDestroy(e->join);
     if (e->join2) cudaEventDestroy(e->join2);
+    if (e->copy_stream) cudaStreamDestroy(e->copy_stream);
+    if (e->snap_ready) cudaEventDestroy(e->snap_ready);
+    if (e->snap_done) cudaEventDestroy(e->snap_done);
     for (cudaEvent_t x : e->tune_ev) if (x) cudaEventDestroy(x);
     if (e->h_params) cudaFreeHost(e->h_params);
     if (e->h_error) cudaFreeHost(e->h_error);
@@ -1344,6 +1355,7 @@ cgl_status cgl_destroy(cgl_engine* e) {
   if (!e) return CGL_INVALID_ARG;
   cudaSetDevice(e->device);
   if (e->stream) cudaStreamSynchronize(e->stream);
+  if (e->copy_stream) cudaStreamSynchronize(e->copy_stream);
   if (e->graph) cudaGraphExecDestroy(e->graph);
   dev_free_all(e);
   if (e->params_copied) cudaEventDestroy(e->params_copied);
@@ -1354,6 +1366,9 @@ cgl_status cgl_destroy(cgl_engine* e) {
   if (e->fork) cudaEventDestroy(e->fork);
   if (e->join) cudaEventDestroy(e->join);
   if (e->join2) cudaEventDestroy(e->join2);
+  if (e->copy_stream) cudaStreamDestroy(e->copy_stream);
+  if (e->snap_ready) cudaEventDestroy(e->snap_ready);
+  if (e->snap_done) cudaEventDestroy(e->snap_done);
   for (cudaEvent_t x : e->tune_ev) if (x) cudaEventDestroy(x);
   if (e->own_stream) cudaStreamDestroy(e->own_stream);
   delete e;
@@ -1706,6 +1721,32 @@ cgl_status cgl_get_point_positions(cgl_engine* e, float* out, uint64_t cap) {
   return device_error(e);
 }
 
+cgl_status cgl_enqueue_point_positions(cgl_engine* e, float* out, uint64_t cap) {
+  CHECK_E(e);
+  if (cap < 2 * e->N || (!out && e->N)) return fail(e, CGL_INVALID_ARG, "output holds %llu floats, need %llu",
+                                                      (unsigned long long)cap, (unsigned long long)(2 * e->N));
+  if (!e->N) return CGL_OK;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, out) != cudaSuccess) cudaGetLastError();
+  if (a.type == cudaMemoryTypeUnregistered || (a.type == cudaMemoryTypeDevice && a.device != e->device))
+    return fail(e, CGL_INVALID_ARG, "queued position read-back needs pinned host memory or memory of device %d",
+                e->device);
+  if (e->snap_pending) {   // the previous copy has landed: its buffer is the caller's again, its staging ours
+    CU(cudaEventSynchronize(e->snap_done));
+    e->snap_pending = false;
+  }
+  const size_t bytes = e->N * sizeof(float2);
+  cgl_status st;
+  if ((st = dev_reserve(e, e->b_snap, bytes, false))) return st;
+  CU(cudaMemcpyAsync(e->b_snap.p, e->b_pos.p, bytes, cudaMemcpyDeviceToDevice, e->stream));
+  CU(cudaEventRecord(e->snap_ready, e->stream));
+  CU(cudaStreamWaitEvent(e->copy_stream, e->snap_ready, 0));
+  CU(cudaMemcpyAsync(out, e->b_snap.p, bytes, cudaMemcpyDefault, e->copy_stream));
+  CU(cudaEventRecord(e->snap_done, e->copy_stream));
+  e->snap_pending = true;
+  return device_error(e);
+}
+
 cgl_status cgl_get_state(cgl_engine* e, cgl_state* s) {
   if (!e || !s) return CGL_INVALID_ARG;
   std::memset(s, 0, sizeof(*s));
@@ -1766,6 +1807,10 @@ cgl_status cgl_set_stream(cgl_engine* e, void* cuda_stream) {
 cgl_status cgl_synchronize(cgl_engine* e) {
   CHECK_E(e);
   CU(cudaStreamSynchronize(e->stream));
+  if (e->snap_pending) {
+    CU(cudaEventSynchronize(e->snap_done));
+    e->snap_pending = false;
+  }
   return device_error(e);
 }
 

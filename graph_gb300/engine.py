@@ -54,6 +54,8 @@ def load_library(build_if_missing: bool = True):
     lib.cgl_random_draws.restype = C.c_int
     lib.cgl_check_wait_limit.argtypes = [C.c_int32, C.POINTER(C.c_uint32)]
     lib.cgl_check_wait_limit.restype = C.c_int
+    lib.cgl_enqueue_point_positions.argtypes = [E, C.POINTER(C.c_float), C.c_uint64]
+    lib.cgl_enqueue_point_positions.restype = C.c_int
     lib.cgl_debug_set_leading_hubs.argtypes = [E, C.c_int32, C.c_int32]
     lib.cgl_debug_set_leading_hubs.restype = C.c_int
     _abi.declare(lib, "cgl")
@@ -140,6 +142,13 @@ class Engine(EngineCalls):
     def enqueue_position_texture(self, ptr, capacity_floats):
         """Queue the texture write to device or pinned host memory at `ptr` (done by the next synchronize)."""
         return self._call("enqueue_position_texture", C.c_void_p(ptr), int(capacity_floats))
+
+    def enqueue_point_positions_into(self, out):
+        """Queue the positions' read-back into a pinned host (or device) float32 buffer beside the
+        next ticks; returns once the previously queued read-back has landed."""
+        n = self.layout().points_number
+        assert out.dtype == np.float32 and out.size >= 2 * n
+        return self._call("enqueue_point_positions", out.ctypes.data_as(C.POINTER(C.c_float)), out.size)
 
     def get_point_positions_into(self, out):
         """Read positions into a caller-owned float32 buffer (e.g. pinned host memory)."""

@@ -240,6 +240,14 @@ cgl_status cgl_frame(cgl_engine* e, uint32_t frames, uint32_t* ticks_done);
 /* Graph.getPointPositions() — src/index.ts:1106-1129; absent points read NaN.
  * out_xy holds 2 * points_number floats.  Synchronises the engine stream. */
 cgl_status cgl_get_point_positions(cgl_engine* e, float* out_xy, uint64_t capacity_floats);
+/* The same read-back beside the next ticks: the positions after the work
+ * already queued are copied on the device (2 x 8 bytes a point on the engine
+ * stream), then to out_xy (pinned host or device memory) on a copy stream
+ * while the next ticks run.  It first waits for the copy the previous call
+ * queued to land, so a caller alternating two buffers reads the other one
+ * after each call; cgl_synchronize waits for the last.  Pageable memory:
+ * CGL_INVALID_ARG (use cgl_get_point_positions). */
+cgl_status cgl_enqueue_point_positions(cgl_engine* e, float* out_xy, uint64_t capacity_floats);
 
 /* Graph.getClusterPositions() — src/index.ts:1135-1139, Clusters.getCentroidPositions
  * (Clusters/index.ts:389-423): the centre of mass of each cluster's live points,

@@ -89,3 +89,33 @@ def test_positions_into_pinned_memory():
     assert _same(off.numpy()[2:], want)
     orc.step(2)
     assert _same(want, orc.get_point_positions())
+
+
+def test_queued_point_positions_beside_the_ticks():
+    # cgl_enqueue_point_positions: each call's copy lands by the next call (two
+    # buffers alternate), the last by synchronize; every tick's positions equal
+    # the synchronous read-back's and the oracle's
+    torch = pytest.importorskip("torch")
+    from graph_gb300._calls import StatusError
+    pos, links, fields = scenario("collision")
+    eng, orc = make_pair(pos, links, fields)
+    n = eng.layout().points_number
+    bufs = [torch.empty(2 * n, dtype=torch.float32, pin_memory=True) for _ in range(2)]
+    got = []
+    for k in range(6):
+        eng.step(1)
+        eng.enqueue_point_positions_into(bufs[k % 2].numpy())
+        if k:
+            got.append(bufs[(k - 1) % 2].numpy().copy())   # the previous call's copy has landed
+    eng.synchronize()
+    got.append(bufs[5 % 2].numpy().copy())
+    for k in range(6):
+        orc.step(1)
+        assert _same(got[k], orc.get_point_positions()), k
+    assert _same(got[-1], eng.get_point_positions())
+    with pytest.raises(StatusError):          # pageable memory cannot be copied beside the ticks
+        eng.enqueue_point_positions_into(np.empty(2 * n, dtype=np.float32))
+    import ctypes
+    small = bufs[0].numpy()
+    with pytest.raises(StatusError):          # a buffer short of 2 floats a point
+        eng._call("enqueue_point_positions", small.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), 4)
