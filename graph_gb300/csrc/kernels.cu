@@ -821,19 +821,35 @@ __device__ __forceinline__ void hub_chunk_chain(const float4* A, const float4* B
   }
 }
 
-// The fast chain over one staged chunk with its checks on the chain thread;
-// returns whether one failed.
+// The fast chain over one staged chunk without absent targets, its checks on
+// the chain thread: at the first link whose check fails the chain goes back
+// to that link's starting velocity (recorded in V), takes it with the
+// correctly rounded spring and goes on from the next link, so only the links
+// after it run twice (the whole chunk ran again exactly before).  Every link
+// before a failing one passed its check, so the result is the correctly
+// rounded chain's; each round ends at least one link further on.
 template <bool UNIT_STRENGTH>
-__device__ __forceinline__ bool hub_chunk_checked(const float4* A, const float4* B, uint32_t len, float2 pp,
-                                                  float2& vel, float sa, PairUnits pu) {
-  bool out = false;
+__device__ __forceinline__ void hub_chunk_resumed(const float4* A, const float4* B, float2* V, uint32_t len,
+                                                  float2 pp, float2& vel, float sa, PairUnits pu) {
+  uint32_t k0 = 0;
+  while (k0 < len) {
+    uint32_t bad = len;   // the first link whose check fails
 #pragma unroll 4
-  for (uint32_t k = 0; k < len; ++k) {
-    const float4 a = A[k];
-    const float4 b = B[k];
-    spring_chain_step_checked<UNIT_STRENGTH>(pp, vel, make_float2(a.x, a.y), a.z, a.w, b.w, sa, b.x, b.y, pu, out);
+    for (uint32_t k = k0; k < len; ++k) {
+      const float4 a = A[k];
+      const float4 b = B[k];
+      V[k] = vel;
+      bool out = false;
+      spring_chain_step_checked<UNIT_STRENGTH>(pp, vel, make_float2(a.x, a.y), a.z, a.w, b.w, sa, b.x, b.y, pu, out);
+      bad = (out && bad == len) ? k : bad;
+    }
+    if (bad == len) return;
+    vel = V[bad];
+    const float4 a = A[bad];
+    const float4 b = B[bad];
+    spring_step(pp, vel, make_float2(a.x, a.y), a.z, a.w, sa, b.x, b.y, pu);
+    k0 = bad + 1;
   }
-  return out;
 }
 
 // The correctly rounded springs over one staged chunk (absent targets skipped).
@@ -893,14 +909,9 @@ __global__ void __launch_bounds__(kBlock) k_link(DeviceView d, SimScalars s, con
             next = hub_fill(hub, buf ^ 1, e0 + (c + 1) * kHubChunk, e1, ent, src, span, s.link_r0, s.link_distance);
         } else if (threadIdx.x == 0) {
           const uint32_t len = chunk_len(c);
-          bool exact = absent != 0;
-          if (!absent) {
-            const float2 v0 = vel;
-            const bool out = strengths ? hub_chunk_checked<false>(hub.a[buf], hub.b[buf], len, pp, vel, sa, pu)
-                                       : hub_chunk_checked<true>(hub.a[buf], hub.b[buf], len, pp, vel, sa, pu);
-            if (out) { vel = v0; exact = true; }
-          }
-          if (exact) hub_chunk_exact(hub.a[buf], hub.b[buf], len, pp, vel, sa, pu);
+          if (absent) hub_chunk_exact(hub.a[buf], hub.b[buf], len, pp, vel, sa, pu);
+          else if (strengths) hub_chunk_resumed<false>(hub.a[buf], hub.b[buf], hub.v[buf], len, pp, vel, sa, pu);
+          else hub_chunk_resumed<true>(hub.a[buf], hub.b[buf], hub.v[buf], len, pp, vel, sa, pu);
         }
         absent = __syncthreads_or(next & kStagedAbsent);
         strengths = __syncthreads_or(next & kStagedStrength);
