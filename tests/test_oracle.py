@@ -408,3 +408,57 @@ def test_rescale_defaults_and_dont_rescale():
     off.set_point_positions(pos)
     off.render()
     assert not np.array_equal(off.get_point_positions(), pos)
+
+
+def _collision_cells(xy, grid, cs):
+    """Each point's cell in the four offset grids (force-collision-spatial.frag's
+    binning, f32 like the shader): an (n, 4, 2) array."""
+    xy = xy.reshape(-1, 2).astype(np.float32)
+    cs = np.float32(cs)
+    out = np.empty((xy.shape[0], 4, 2), dtype=np.int64)
+    for g, (ox, oy) in enumerate(((0.0, 0.0), (0.5, 0.0), (0.0, 0.5), (0.5, 0.5))):
+        for a, o in ((0, ox), (1, oy)):
+            off = xy[:, a] + np.float32(o) * cs
+            out[:, g, a] = np.clip(np.floor(off / cs), 0, grid - 1).astype(np.int64)
+    return out
+
+
+def test_collision_result_reads_only_its_windows():
+    # The collision pass alone: moving one point changes only the results of the
+    # points whose 3x3 window, in one of the four offset grids, holds its old or
+    # new cell.  The engine computes every other point's collision result while
+    # the longest outgoing hub chains still run, and afterwards computes again
+    # only the points in those hubs' windows; this is the property it rests on.
+    n = 4000
+    rng = np.random.default_rng(5)
+    pos = rng.uniform(20, 490, size=2 * n).astype(np.float32)
+    sizes = rng.uniform(2, 8, size=n).astype(np.float32)
+    fields = dict(space_size=512, simulation_collision=0.7, stage_mask=_abi.STAGE_COLLISION, random_seed=5)
+
+    def one_tick(xy):
+        o = OracleEngine(_abi.make_config(**fields))
+        o.set_point_positions(xy)
+        o.set_point_sizes(sizes)
+        o.render()
+        o.start(1.0)
+        o.step(1)
+        return o.get_point_positions(), o.layout()
+
+    late = 17
+    moved = pos.copy()
+    moved[2 * late:2 * late + 2] = [400.0, 100.0]
+    a, lay = one_tick(pos)
+    b, _ = one_tick(moved)
+    grid, cs = lay.collision_grid, lay.collision_cell_size
+    cells = _collision_cells(pos, grid, cs)
+    hot = np.concatenate([_collision_cells(pos[2 * late:2 * late + 2], grid, cs),
+                          _collision_cells(moved[2 * late:2 * late + 2], grid, cs)])   # (2, 4, 2)
+    near = (np.abs(cells[:, None, :, :] - hot[None, :, :, :]) <= 1).all(axis=3)      # (n, 2, 4)
+    affected = near.any(axis=(1, 2))
+    affected[late] = True
+    differ = (a.view(np.uint32).reshape(-1, 2) != b.view(np.uint32).reshape(-1, 2)).any(axis=1)
+    assert not (differ & ~affected).any()
+    others = affected.copy()
+    others[late] = False
+    assert (differ & others).any()           # the move does reach the points in its windows
+    assert affected.sum() < n // 10
