@@ -328,7 +328,8 @@ typedef struct cgl_layout {
   uint32_t manybody_tuned;     /* 1 once manybody_kernel was chosen by timing this graph's ticks */
   uint32_t early_hubs;         /* longest incoming lists whose chains start beside the many-body pass */
   uint32_t early_points;       /* their points and link targets, whose many-body terms run first */
-  uint32_t leading_out_hubs;   /* longest outgoing lists whose chains run on an SM each beside the rest */
+  uint32_t leading_out_hubs;   /* longest outgoing lists whose chains run beside the rest of their pass
+                                  (from half the longest on an SM each) */
 } cgl_layout;
 enum {
   CGL_MANYBODY_AUTO = -1,       /* cgl_config.manybody_kernel: time the candidates, keep the fastest */
